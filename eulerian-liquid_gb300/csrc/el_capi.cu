@@ -1,0 +1,630 @@
+// el_capi.cu -- the C ABI (include/eulerian_liquid_gb300.h): contexts, field transfer and the
+// entry points that stand in for the reference's Simulator step methods and fluid:: free
+// functions.  No exception crosses this boundary; every call returns a status code.
+#include <algorithm>
+#include <cstring>
+#include <new>
+
+#include "el_internal.cuh"
+
+namespace el {
+// launchers defined in the kernel translation units
+int advect_any(int dtype, int ni, int nj, int nk, double dx, int comp, void* out, const void* in, const void* vu,
+               const void* vv, const void* vw, const Scalars* dts, double dtv, int trace, int sample,
+               cudaStream_t s);
+int launch_weights(int dtype, int ni, int nj, int nk, const void* solid, void* wu, void* wv, void* ww,
+                   cudaStream_t s);
+int launch_cell_solid(el_ctx* ctx);
+int launch_flags_build(el_ctx* ctx, bool inner32, bool build = true);
+int launch_assign_indices(el_ctx* ctx, int* d_chunks, int* d_total);
+int launch_scatter_pressure(el_ctx* ctx);
+int launch_update_velocity(el_ctx* ctx, const Scalars* s, double dtv);
+int launch_extrapolate(el_ctx* ctx, int field, uint8_t* valid, int layers, bool write_back);
+int launch_masks(el_ctx* ctx, bool gravity, double g, const Scalars* s, double dtv, bool zero);
+int launch_gravity(el_ctx* ctx, double g, const Scalars* s, double dtv);
+int launch_zero_invalid(el_ctx* ctx);
+int launch_time_step(el_ctx* ctx, double cfl, unsigned long long* scratch_max);
+int launch_set_dt(el_ctx* ctx, double dt);
+int launch_emit(el_ctx* ctx, int target, int kind, const double* a, int na);
+int solve_system(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st);
+int setup_solver_storage(el_ctx* ctx, int solver);
+
+int set_error(el_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    return code;
+}
+
+cudaEvent_t prof_event(el_ctx* ctx) {
+    if (ctx->ev_used == ctx->ev_pool.size()) {
+        if (ctx->ev_pool.size() >= 200000) return nullptr;  // cap the record count
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        ctx->ev_pool.push_back(e);
+    }
+    return ctx->ev_pool[ctx->ev_used++];
+}
+
+int check_launch(el_ctx* ctx, const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(ctx, EL_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return EL_OK;
+}
+
+void* ctx_alloc(el_ctx* ctx, size_t bytes) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
+    cudaMemsetAsync(p, 0, std::max<size_t>(bytes, 16), ctx->stream);
+    ctx->allocations.push_back(p);
+    return p;
+}
+
+static size_t field_count(const el_ctx* c, int f) {
+    const size_t ni = c->ni, nj = c->nj, nk = c->nk;
+    switch (f) {
+        case EL_FIELD_U: case EL_FIELD_WEIGHT_U: case EL_FIELD_VALID_U: return (ni + 1) * nj * nk;
+        case EL_FIELD_V: case EL_FIELD_WEIGHT_V: case EL_FIELD_VALID_V: return ni * (nj + 1) * nk;
+        case EL_FIELD_W: case EL_FIELD_WEIGHT_W: case EL_FIELD_VALID_W: return ni * nj * (nk + 1);
+        case EL_FIELD_SOLID_NODAL: return (ni + 1) * (nj + 1) * (nk + 1);
+        default: return ni * nj * nk;
+    }
+}
+
+static size_t field_elem(const el_ctx* c, int f) {
+    if (f >= EL_FIELD_VALID_U && f <= EL_FIELD_VALID_PHI) return 1;
+    if (f == EL_FIELD_INDICES) return 4;
+    return c->esz;
+}
+
+int ensure_projection(el_ctx* ctx) {
+    if (ctx->flags) return EL_OK;
+    const size_t n = (size_t)ctx->ni * ctx->nj * ctx->nk;
+    ctx->flags = (uint8_t*)ctx_alloc(ctx, n);
+    ctx->diag64 = (double*)ctx_alloc(ctx, n * 8);
+    ctx->rhs64 = (double*)ctx_alloc(ctx, n * 8);
+    for (int a = 0; a < 3; ++a) ctx->off[a] = ctx_alloc(ctx, n * ctx->esz);
+    if (!ctx->flags || !ctx->diag64 || !ctx->rhs64 || !ctx->off[0] || !ctx->off[1] || !ctx->off[2])
+        return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "projection buffers");
+    return EL_OK;
+}
+
+int ensure_solver(el_ctx* ctx, int solver) {
+    int st = ensure_projection(ctx);
+    if (st != EL_OK) return st;
+    return setup_solver_storage(ctx, solver);
+}
+
+}  // namespace el
+
+using namespace el;
+
+#define EL_API extern "C" __attribute__((visibility("default")))
+
+#define CHECK_CTX(ctx)                                                              \
+    do {                                                                            \
+        if (!(ctx)) return EL_ERR_INVALID_ARGUMENT;                                 \
+        cudaError_t _se = cudaSetDevice((ctx)->device);                             \
+        if (_se != cudaSuccess) return set_error(ctx, EL_ERR_CUDA, cudaGetErrorString(_se)); \
+    } while (0)
+
+EL_API const char* el_status_string(int status) {
+    switch (status) {
+        case EL_OK: return "ok";
+        case EL_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case EL_ERR_NO_FLUID: return "No fluid";
+        case EL_ERR_NOT_CONVERGED: return "pressure solve did not converge";
+        case EL_ERR_NAN: return "non-finite value";
+        case EL_ERR_CUDA: return "CUDA error";
+        case EL_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case EL_ERR_TIMEOUT: return "device wait timed out";
+        default: return "unknown status";
+    }
+}
+
+EL_API const char* el_ctx_last_error(const el_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+EL_API int el_ctx_create(int ni, int nj, int nk, double dx, int dtype, int device, el_ctx** out) {
+    if (!out) return EL_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (ni < 1 || nj < 1 || nk < 1 || !(dx > 0) || (dtype != EL_F32 && dtype != EL_F64))
+        return EL_ERR_INVALID_ARGUMENT;
+    // the reference indexes with int and refuses sizes that overflow it (array.h:322-325)
+    const long long biggest = (long long)(ni + 1) * (nj + 1) * (nk + 1);
+    if (biggest >= 0x7fffffffLL) return EL_ERR_INVALID_ARGUMENT;
+    if (cudaSetDevice(device) != cudaSuccess) return EL_ERR_CUDA;
+    el_ctx* ctx = new (std::nothrow) el_ctx();
+    if (!ctx) return EL_ERR_OUT_OF_MEMORY;
+    ctx->device = device;
+    ctx->ni = ni;
+    ctx->nj = nj;
+    ctx->nk = nk;
+    ctx->dx = dx;
+    ctx->dtype = dtype;
+    ctx->esz = dtype == EL_F64 ? 8 : 4;
+    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return EL_ERR_CUDA;
+    }
+    ctx->own_stream = true;
+    bool ok = true;
+    for (int f = 0; f < EL_FIELD_COUNT; ++f) {
+        ctx->field_bytes[f] = field_count(ctx, f) * field_elem(ctx, f);
+        ctx->field[f] = ctx_alloc(ctx, ctx->field_bytes[f]);
+        ok = ok && ctx->field[f];
+    }
+    for (int q = 0; q < 4; ++q) {
+        ctx->tmp[q] = ctx_alloc(ctx, ctx->field_bytes[EL_FIELD_PHI + q]);
+        ok = ok && ctx->tmp[q];
+    }
+    size_t biggest_face = 0;
+    for (int f = EL_FIELD_VALID_U; f <= EL_FIELD_VALID_PHI; ++f)
+        biggest_face = std::max(biggest_face, ctx->field_bytes[f]);
+    ctx->valid_tmp = (uint8_t*)ctx_alloc(ctx, biggest_face);
+    ctx->dscal = (Scalars*)ctx_alloc(ctx, 4 * sizeof(Scalars));
+    Geom g = stencil_geom(ni, nj, nk, ctx->num_sms);
+    ctx->max_partials = std::max(g.blocks(), ctx->num_sms * 8) * 2 + 64;
+    ctx->partials = (double*)ctx_alloc(ctx, ctx->max_partials * sizeof(double));
+    ctx->counter = (unsigned*)ctx_alloc(ctx, 64);
+    ok = ok && ctx->valid_tmp && ctx->dscal && ctx->partials && ctx->counter;
+    if (ok && cudaMallocHost(&ctx->hscal, 4 * sizeof(Scalars)) != cudaSuccess) ok = false;
+    if (ok) {
+        // create_grid (simulator.cpp:58-69): valid masks start at 1
+        for (int f = EL_FIELD_VALID_U; f <= EL_FIELD_VALID_PHI; ++f)
+            cudaMemsetAsync(ctx->field[f], 1, ctx->field_bytes[f], ctx->stream);
+        ok = cudaStreamSynchronize(ctx->stream) == cudaSuccess;
+    }
+    if (!ok) {
+        el_ctx_destroy(ctx);
+        return EL_ERR_OUT_OF_MEMORY;
+    }
+    *out = ctx;
+    return EL_OK;
+}
+
+EL_API int el_ctx_destroy(el_ctx* ctx) {
+    if (!ctx) return EL_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (void* p : ctx->allocations) cudaFree(p);
+    for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
+    if (ctx->hscal) cudaFreeHost(ctx->hscal);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return EL_OK;
+}
+
+EL_API int el_ctx_set_stream(el_ctx* ctx, void* stream) {
+    CHECK_CTX(ctx);
+    EL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    if (stream) {
+        ctx->stream = (cudaStream_t)stream;
+        ctx->own_stream = false;
+    } else {
+        EL_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        ctx->own_stream = true;
+    }
+    return EL_OK;
+}
+
+EL_API void* el_ctx_get_stream(el_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+EL_API int el_ctx_sync(el_ctx* ctx) {
+    CHECK_CTX(ctx);
+    EL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return EL_OK;
+}
+
+EL_API int64_t el_ctx_kernel_launches(const el_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+EL_API int el_ctx_profile_begin(el_ctx* ctx, uint32_t class_mask) {
+    CHECK_CTX(ctx);
+    EL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->prof.clear();
+    ctx->ev_used = 0;
+    ctx->prof_mask = class_mask;
+    return EL_OK;
+}
+
+EL_API int el_ctx_profile_end(el_ctx* ctx, el_profile_entry* out) {
+    CHECK_CTX(ctx);
+    if (!out) return EL_ERR_INVALID_ARGUMENT;
+    ctx->prof_mask = 0;
+    EL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int c = 0; c < EL_KC_COUNT; ++c) out[c] = el_profile_entry{0, 0.0, 0.0};
+    for (const auto& r : ctx->prof) {
+        float ms = 0.f;
+        EL_CUDA_TRY(ctx, cudaEventElapsedTime(&ms, r.a, r.b));
+        out[r.cls].launches += 1;
+        out[r.cls].ms += ms;
+        out[r.cls].bytes += r.bytes;
+    }
+    ctx->prof.clear();
+    ctx->ev_used = 0;
+    return EL_OK;
+}
+
+EL_API int el_upload(el_ctx* ctx, int field, const void* host, size_t bytes) {
+    CHECK_CTX(ctx);
+    if (field < 0 || field >= EL_FIELD_COUNT || !host) return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "bad field");
+    if (bytes != ctx->field_bytes[field])
+        return set_error(ctx, EL_ERR_INVALID_ARGUMENT,
+                         "field size mismatch: expected " + std::to_string(ctx->field_bytes[field]) + " bytes");
+    EL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->field[field], host, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    EL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return EL_OK;
+}
+
+EL_API int el_download(el_ctx* ctx, int field, void* host, size_t bytes) {
+    CHECK_CTX(ctx);
+    if (field < 0 || field >= EL_FIELD_COUNT || !host) return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "bad field");
+    if (bytes != ctx->field_bytes[field])
+        return set_error(ctx, EL_ERR_INVALID_ARGUMENT,
+                         "field size mismatch: expected " + std::to_string(ctx->field_bytes[field]) + " bytes");
+    EL_CUDA_TRY(ctx, cudaMemcpyAsync(host, ctx->field[field], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    EL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return EL_OK;
+}
+
+EL_API int el_field_device_ptr(el_ctx* ctx, int field, void** dptr, size_t* bytes) {
+    if (!ctx || field < 0 || field >= EL_FIELD_COUNT || !dptr) return EL_ERR_INVALID_ARGUMENT;
+    *dptr = ctx->field[field];
+    if (bytes) *bytes = ctx->field_bytes[field];
+    return EL_OK;
+}
+
+static int finish(el_ctx* ctx, int launched, const char* what) {
+    ctx->launches += launched;
+    return check_launch(ctx, what);
+}
+
+// ---- scene set-up -----------------------------------------------------------------------
+
+EL_API int el_emit_clear(el_ctx* ctx, int target) {
+    CHECK_CTX(ctx);
+    if (target != 0 && target != 1) return EL_ERR_INVALID_ARGUMENT;
+    return finish(ctx, launch_emit(ctx, target, 0, nullptr, 0), "emit");
+}
+
+EL_API int el_emit_sphere(el_ctx* ctx, int target, double cx, double cy, double cz, double r) {
+    CHECK_CTX(ctx);
+    if (target != 0 && target != 1) return EL_ERR_INVALID_ARGUMENT;
+    const double a[4] = {cx, cy, cz, r};
+    return finish(ctx, launch_emit(ctx, target, 1, a, 4), "emit");
+}
+
+EL_API int el_emit_pool(el_ctx* ctx, int target, double height) {
+    CHECK_CTX(ctx);
+    if (target != 0 && target != 1) return EL_ERR_INVALID_ARGUMENT;
+    return finish(ctx, launch_emit(ctx, target, 2, &height, 1), "emit");
+}
+
+EL_API int el_emit_box(el_ctx* ctx, int target, const double lo[3], const double hi[3]) {
+    CHECK_CTX(ctx);
+    if ((target != 0 && target != 1) || !lo || !hi) return EL_ERR_INVALID_ARGUMENT;
+    const double a[6] = {lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]};
+    return finish(ctx, launch_emit(ctx, target, 3, a, 6), "emit");
+}
+
+EL_API int el_emit_room(el_ctx* ctx, int target) {
+    CHECK_CTX(ctx);
+    if (target != 0 && target != 1) return EL_ERR_INVALID_ARGUMENT;
+    return finish(ctx, launch_emit(ctx, target, 4, nullptr, 0), "emit");
+}
+
+// ---- boundary ----------------------------------------------------------------------------
+
+EL_API int el_compute_weights(el_ctx* ctx) {
+    CHECK_CTX(ctx);
+    int n = launch_weights(ctx->dtype, ctx->ni, ctx->nj, ctx->nk, ctx->field[EL_FIELD_SOLID_NODAL],
+                           ctx->field[EL_FIELD_WEIGHT_U], ctx->field[EL_FIELD_WEIGHT_V], ctx->field[EL_FIELD_WEIGHT_W],
+                           ctx->stream);
+    return finish(ctx, n, "compute_weights");
+}
+
+EL_API int el_calc_cell_centered_solid_phi(el_ctx* ctx) {
+    CHECK_CTX(ctx);
+    // computes the cell-centred solid phi; the level-set valid mask is refreshed too (it is a
+    // pure function of it, simulator.cpp:160-167)
+    return finish(ctx, launch_cell_solid(ctx), "cell_centered_solid_phi");
+}
+
+EL_API int el_find_valid_level_set(el_ctx* ctx) {
+    CHECK_CTX(ctx);
+    return finish(ctx, launch_cell_solid(ctx), "find_valid_level_set");
+}
+
+// ---- hot path -----------------------------------------------------------------------------
+
+static bool valid_scheme(int trace, int sample) {
+    return (trace == EL_TRACE_RK2 || trace == EL_TRACE_RK3) &&
+           (sample == EL_SAMPLE_TRILINEAR || sample == EL_SAMPLE_WENO6);
+}
+
+// phi <- phi(trace(x, -dt)) through the current velocity (simulator.cpp:84-87)
+static double nbytes(el_ctx* ctx, int field) { return (double)ctx->field_bytes[field]; }
+
+static int advect_level_set_impl(el_ctx* ctx, const Scalars* dts, double dt, int trace, int sample) {
+    // reads phi, u, v, w; writes phi
+    ProfScope prof(ctx, EL_KC_ADVECT_PHI, 2 * nbytes(ctx, EL_FIELD_PHI) + nbytes(ctx, EL_FIELD_U) +
+                                              nbytes(ctx, EL_FIELD_V) + nbytes(ctx, EL_FIELD_W));
+    int n = advect_any(ctx->dtype, ctx->ni, ctx->nj, ctx->nk, ctx->dx, 0, ctx->tmp[0], ctx->field[EL_FIELD_PHI],
+                       ctx->field[EL_FIELD_U], ctx->field[EL_FIELD_V], ctx->field[EL_FIELD_W], dts, dt, trace,
+                       sample, ctx->stream);
+    std::swap(ctx->tmp[0], ctx->field[EL_FIELD_PHI]);
+    return n;
+}
+
+// u, v, w <- each component advected through the old velocity (simulator.cpp:79-82)
+static int advect_velocity_impl(el_ctx* ctx, const Scalars* dts, double dt, int trace, int sample) {
+    int n = 0;
+    const double vel_bytes = nbytes(ctx, EL_FIELD_U) + nbytes(ctx, EL_FIELD_V) + nbytes(ctx, EL_FIELD_W);
+    for (int comp = 0; comp < 3; ++comp) {
+        // reads u, v, w (the advected component among them); writes the component
+        ProfScope prof(ctx, EL_KC_ADVECT_VEL, vel_bytes + nbytes(ctx, EL_FIELD_U + comp));
+        n += advect_any(ctx->dtype, ctx->ni, ctx->nj, ctx->nk, ctx->dx, comp + 1, ctx->tmp[1 + comp],
+                        ctx->field[EL_FIELD_U + comp], ctx->field[EL_FIELD_U], ctx->field[EL_FIELD_V],
+                        ctx->field[EL_FIELD_W], dts, dt, trace, sample, ctx->stream);
+    }
+    for (int comp = 0; comp < 3; ++comp) std::swap(ctx->tmp[1 + comp], ctx->field[EL_FIELD_U + comp]);
+    return n;
+}
+
+EL_API int el_advect_level_set(el_ctx* ctx, double dt, int trace, int sample) {
+    CHECK_CTX(ctx);
+    if (!valid_scheme(trace, sample)) return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "bad advection scheme");
+    return finish(ctx, advect_level_set_impl(ctx, nullptr, dt, trace, sample), "advect_level_set");
+}
+
+EL_API int el_advect_velocity(el_ctx* ctx, double dt, int trace, int sample) {
+    CHECK_CTX(ctx);
+    if (!valid_scheme(trace, sample)) return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "bad advection scheme");
+    return finish(ctx, advect_velocity_impl(ctx, nullptr, dt, trace, sample), "advect_velocity");
+}
+
+EL_API int el_add_gravity(el_ctx* ctx, double dt, double gravity) {
+    CHECK_CTX(ctx);
+    return finish(ctx, launch_gravity(ctx, gravity, nullptr, dt), "add_gravity");
+}
+
+EL_API int el_extrapolate_level_set(el_ctx* ctx, int layers) {
+    CHECK_CTX(ctx);
+    if (layers < 0) return EL_ERR_INVALID_ARGUMENT;
+    return finish(ctx,
+                  launch_extrapolate(ctx, EL_FIELD_PHI, (uint8_t*)ctx->field[EL_FIELD_VALID_PHI], layers, false),
+                  "extrapolate_level_set");
+}
+
+EL_API int el_extrapolate_velocity(el_ctx* ctx, int layers) {
+    CHECK_CTX(ctx);
+    if (layers < 0) return EL_ERR_INVALID_ARGUMENT;
+    int n = 0;
+    for (int comp = 0; comp < 3; ++comp)
+        n += launch_extrapolate(ctx, EL_FIELD_U + comp, (uint8_t*)ctx->field[EL_FIELD_VALID_U + comp], layers, true);
+    return finish(ctx, n, "extrapolate_velocity");
+}
+
+EL_API int el_find_valid_velocity(el_ctx* ctx) {
+    CHECK_CTX(ctx);
+    return finish(ctx, launch_masks(ctx, false, 0.0, nullptr, 0.0, false), "find_valid_velocity");
+}
+
+EL_API int el_set_invalid_velocity_zero(el_ctx* ctx) {
+    CHECK_CTX(ctx);
+    return finish(ctx, launch_zero_invalid(ctx), "set_invalid_velocity_zero");
+}
+
+static int extrapolate_prof(el_ctx* ctx, int field, uint8_t* valid, int layers, bool write_back) {
+    // per layer: the stamp mask and the field, each read once (invalid cells also write)
+    const double per = (double)ctx->field_bytes[field] + ctx->field_bytes[field] / ctx->esz;
+    ProfScope prof(ctx, EL_KC_EXTRAPOLATE, per * layers);
+    return launch_extrapolate(ctx, field, valid, layers, write_back);
+}
+
+static int masks_prof(el_ctx* ctx, bool gravity, double g, const Scalars* s, double dtv, bool zero) {
+    // per face: the component read and written, its weight read, its mask written; phi read
+    double b = nbytes(ctx, EL_FIELD_PHI);
+    for (int c = 0; c < 3; ++c) b += 3 * nbytes(ctx, EL_FIELD_U + c) + nbytes(ctx, EL_FIELD_VALID_U + c);
+    ProfScope prof(ctx, EL_KC_MASKS, b);
+    return launch_masks(ctx, gravity, g, s, dtv, zero);
+}
+
+static int build_prof(el_ctx* ctx, bool inner32) {
+    // flags: 3 weights + phi read, flags written; build: 3 velocities + 3 weights + phi + flags
+    // read, diag (f64), 3 couplings, rhs (f64) written (+ the FP32 diagonal)
+    const double N = (double)ctx->ni * ctx->nj * ctx->nk;
+    double faces = 0;
+    for (int c = 0; c < 3; ++c) faces += nbytes(ctx, EL_FIELD_U + c);
+    double b = faces + nbytes(ctx, EL_FIELD_PHI) + N;
+    b += 2 * faces + nbytes(ctx, EL_FIELD_PHI) + N + 16 * N + 3 * N * ctx->esz + (inner32 ? 4 * N : 0);
+    ProfScope prof(ctx, EL_KC_BUILD, b);
+    return launch_flags_build(ctx, inner32);
+}
+
+static int solve_pressure_impl(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) {
+    int rc = ensure_solver(ctx, prm.solver);
+    if (rc != EL_OK) return rc;
+    const bool inner32 = prm.solver == EL_SOLVER_MIXED;
+    ctx->launches += build_prof(ctx, inner32);
+    rc = check_launch(ctx, "build_matrix");
+    if (rc != EL_OK) return rc;
+    EL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->hscal, ctx->dscal, sizeof(Scalars), cudaMemcpyDeviceToHost, ctx->stream));
+    EL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    st->fluid_cells = ctx->hscal->count;
+    if (ctx->hscal->count == 0) {
+        st->status = EL_ERR_NO_FLUID;
+        return set_error(ctx, EL_ERR_NO_FLUID, "No fluid");
+    }
+    rc = solve_system(ctx, prm, st);
+    if (rc != EL_OK) return rc;
+    ctx->launches += launch_scatter_pressure(ctx);
+    ctx->launches += launch_update_velocity(ctx, ctx->dscal, 0.0);
+    return check_launch(ctx, "update_velocity_using_pressure");
+}
+
+static bool valid_params(const el_solve_params* p) {
+    return p && (p->solver >= EL_SOLVER_JACOBI_FP64 && p->solver <= EL_SOLVER_MIXED) && p->tol > 0 &&
+           p->max_iter > 0 && p->check_every > 0;
+}
+
+EL_API int el_solve_pressure(el_ctx* ctx, double dt, const el_solve_params* params, el_solve_stats* stats) {
+    CHECK_CTX(ctx);
+    if (!valid_params(params) || !(dt > 0)) return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "bad solve parameters");
+    el_solve_stats local{};
+    el_solve_stats* st = stats ? stats : &local;
+    *st = el_solve_stats{};
+    ctx->launches += launch_set_dt(ctx, dt);
+    int rc = solve_pressure_impl(ctx, *params, st);
+    if (rc != EL_OK) return rc;
+    return st->status == EL_OK ? EL_OK : set_error(ctx, st->status, "pressure solve did not converge");
+}
+
+EL_API int el_calc_time_step(el_ctx* ctx, double cfl, double* dt_out) {
+    CHECK_CTX(ctx);
+    if (!dt_out) return EL_ERR_INVALID_ARGUMENT;
+    unsigned long long* scratch = (unsigned long long*)(ctx->dscal + 3);
+    ctx->launches += launch_time_step(ctx, cfl, scratch);
+    int rc = check_launch(ctx, "calc_time_step");
+    if (rc != EL_OK) return rc;
+    EL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->hscal, ctx->dscal, sizeof(Scalars), cudaMemcpyDeviceToHost, ctx->stream));
+    EL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    *dt_out = ctx->hscal->dt;
+    return EL_OK;
+}
+
+EL_API int el_step(el_ctx* ctx, double dt, const el_step_params* p, el_step_stats* stats) {
+    CHECK_CTX(ctx);
+    if (!p || !valid_params(&p->solve) || !valid_scheme(p->trace_phi, p->sample_phi) ||
+        !valid_scheme(p->trace_vel, p->sample_vel) || p->extrapolation_layers < 0 || !(dt > 0))
+        return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "bad step parameters");
+    el_step_stats local{};
+    el_step_stats* st = stats ? stats : &local;
+    *st = el_step_stats{};
+    st->dt = dt;
+    int rc = ensure_solver(ctx, p->solve.solver);
+    if (rc != EL_OK) return rc;
+    int n = launch_set_dt(ctx, dt);
+    const Scalars* dts = ctx->dscal;
+    // update_second_order (apps/eulerian_liquid_3d.cpp:106-120), reinitialize() excluded
+    for (int comp = 0; comp < 3; ++comp)
+        n += extrapolate_prof(ctx, EL_FIELD_U + comp, (uint8_t*)ctx->field[EL_FIELD_VALID_U + comp],
+                              p->extrapolation_layers, true);
+    n += extrapolate_prof(ctx, EL_FIELD_PHI, (uint8_t*)ctx->field[EL_FIELD_VALID_PHI], p->extrapolation_layers,
+                          false);
+    n += advect_level_set_impl(ctx, dts, dt, p->trace_phi, p->sample_phi);
+    n += advect_velocity_impl(ctx, dts, dt, p->trace_vel, p->sample_vel);
+    n += masks_prof(ctx, true, p->gravity, dts, dt, true);
+    ctx->launches += n;
+    rc = check_launch(ctx, "step");
+    if (rc != EL_OK) return rc;
+    rc = solve_pressure_impl(ctx, p->solve, &st->solve);
+    if (rc != EL_OK) return rc;
+    return st->solve.status == EL_OK ? EL_OK : set_error(ctx, st->solve.status, "pressure solve did not converge");
+}
+
+// ---- projection pieces --------------------------------------------------------------------
+
+EL_API int el_assign_indices(el_ctx* ctx, int* mat_size) {
+    CHECK_CTX(ctx);
+    int rc = ensure_projection(ctx);
+    if (rc != EL_OK) return rc;
+    ctx->launches += launch_flags_build(ctx, false, false);
+    const long long n = (long long)ctx->ni * ctx->nj * ctx->nk;
+    const int nchunks = (int)((n + 2047) / 2048);
+    int* scratch = (int*)ctx_alloc(ctx, (size_t)(nchunks + 1) * sizeof(int));
+    if (!scratch) return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "assign_indices scratch");
+    ctx->launches += launch_assign_indices(ctx, scratch, scratch + nchunks);
+    rc = check_launch(ctx, "assign_indices");
+    if (rc != EL_OK) return rc;
+    int total = 0;
+    EL_CUDA_TRY(ctx, cudaMemcpyAsync(&total, scratch + nchunks, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    EL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    // the scratch is returned at once rather than kept for the context's lifetime
+    ctx->allocations.pop_back();
+    cudaFree(scratch);
+    if (mat_size) *mat_size = total;
+    if (total == 0) return set_error(ctx, EL_ERR_NO_FLUID, "No fluid");
+    return EL_OK;
+}
+
+EL_API int el_build_matrix(el_ctx* ctx, double dt) {
+    CHECK_CTX(ctx);
+    if (!(dt > 0)) return EL_ERR_INVALID_ARGUMENT;
+    int rc = ensure_projection(ctx);
+    if (rc != EL_OK) return rc;
+    ctx->launches += launch_set_dt(ctx, dt);
+    ctx->launches += launch_flags_build(ctx, false);
+    return check_launch(ctx, "build_matrix");
+}
+
+EL_API int el_download_matrix(el_ctx* ctx, double* diag, double* offx, double* offy, double* offz, double* rhs) {
+    CHECK_CTX(ctx);
+    if (!ctx->flags) return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "no matrix built yet");
+    const size_t n = (size_t)ctx->ni * ctx->nj * ctx->nk;
+    if (diag) EL_CUDA_TRY(ctx, cudaMemcpyAsync(diag, ctx->diag64, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if (rhs) EL_CUDA_TRY(ctx, cudaMemcpyAsync(rhs, ctx->rhs64, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    double* outs[3] = {offx, offy, offz};
+    std::vector<float> tmp;
+    for (int a = 0; a < 3; ++a) {
+        if (!outs[a]) continue;
+        if (ctx->dtype == EL_F64) {
+            EL_CUDA_TRY(ctx, cudaMemcpyAsync(outs[a], ctx->off[a], n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        } else {
+            tmp.resize(n);
+            EL_CUDA_TRY(ctx, cudaMemcpyAsync(tmp.data(), ctx->off[a], n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+            EL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+            for (size_t q = 0; q < n; ++q) outs[a][q] = tmp[q];
+        }
+    }
+    EL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return EL_OK;
+}
+
+EL_API int el_update_velocity_using_pressure(el_ctx* ctx, double dt) {
+    CHECK_CTX(ctx);
+    if (!(dt > 0)) return EL_ERR_INVALID_ARGUMENT;
+    return finish(ctx, launch_update_velocity(ctx, nullptr, dt), "update_velocity_using_pressure");
+}
+
+// ---- stateless operators ----------------------------------------------------------------------
+
+static bool valid_grid(const el_grid* g, int dtype) {
+    return g && g->ni > 0 && g->nj > 0 && g->nk > 0 && g->dx > 0 && (dtype == EL_F32 || dtype == EL_F64) &&
+           (long long)(g->ni + 1) * (g->nj + 1) * (g->nk + 1) < 0x7fffffffLL;
+}
+
+EL_API int el_advect_collocated_grid(const el_grid* g, int dtype, void* out, const void* in, const void* vu,
+                                     const void* vv, const void* vw, double dt, int trace, int sample,
+                                     void* stream) {
+    if (!valid_grid(g, dtype) || !out || !in || !vu || !vv || !vw || out == in || !valid_scheme(trace, sample))
+        return EL_ERR_INVALID_ARGUMENT;
+    advect_any(dtype, g->ni, g->nj, g->nk, g->dx, 0, out, in, vu, vv, vw, nullptr, dt, trace, sample,
+               (cudaStream_t)stream);
+    return cudaGetLastError() == cudaSuccess ? EL_OK : EL_ERR_CUDA;
+}
+
+EL_API int el_advect_staggered_grid(const el_grid* g, int dtype, void* ou, void* ov, void* ow, const void* iu,
+                                    const void* iv, const void* iw, const void* vu, const void* vv, const void* vw,
+                                    double dt, int trace, int sample, void* stream) {
+    if (!valid_grid(g, dtype) || !ou || !ov || !ow || !iu || !iv || !iw || !vu || !vv || !vw ||
+        !valid_scheme(trace, sample))
+        return EL_ERR_INVALID_ARGUMENT;
+    const void* outs[3] = {ou, ov, ow};
+    const void* ins[3] = {vu, vv, vw};
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+            if (outs[a] == ins[b] || outs[a] == (a == 0 ? iu : a == 1 ? iv : iw)) return EL_ERR_INVALID_ARGUMENT;
+    const void* src[3] = {iu, iv, iw};
+    void* dst[3] = {ou, ov, ow};
+    for (int c = 0; c < 3; ++c)
+        advect_any(dtype, g->ni, g->nj, g->nk, g->dx, c + 1, dst[c], src[c], vu, vv, vw, nullptr, dt, trace, sample,
+                   (cudaStream_t)stream);
+    return cudaGetLastError() == cudaSuccess ? EL_OK : EL_ERR_CUDA;
+}
+
+EL_API int el_compute_staggered_grid_weight(const el_grid* g, int dtype, void* wu, void* wv, void* ww,
+                                            const void* solid, void* stream) {
+    if (!valid_grid(g, dtype) || !wu || !wv || !ww || !solid) return EL_ERR_INVALID_ARGUMENT;
+    launch_weights(dtype, g->ni, g->nj, g->nk, solid, wu, wv, ww, (cudaStream_t)stream);
+    return cudaGetLastError() == cudaSuccess ? EL_OK : EL_ERR_CUDA;
+}

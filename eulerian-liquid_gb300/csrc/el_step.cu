@@ -1,0 +1,330 @@
+// el_step.cu -- the step pieces around advection and projection, on the device.
+//
+// Reference: src/project/3d/fluid/extrapolation.cpp:5-51 (extrapolate),
+// src/project/3d/eulerian_liquid/simulator.cpp:90-178 (add_gravity, find_valid_velocity,
+// set_invalid_velocity_zero), src/project/3d/fluid/time_stepping.cpp:5-7 (calc_time_step),
+// src/project/3d/fluid/levelset_emitter.cpp:10-79 (emitters).
+#include "el_internal.cuh"
+
+namespace el {
+
+__device__ __forceinline__ float mul_rn2(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn2(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn2(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn2(double a, double b) { return __dadd_rn(a, b); }
+
+// ---------------------------------------------------------------------------------------
+// Extrapolation.  Jacobi layers as extrapolate() does them, computed in place: a cell's
+// value changes only in the layer it becomes valid, and it reads only neighbours that were
+// valid before that layer began, whose values no longer change.  Validity is kept as a
+// stamp: 0 = valid from the start, l+1 = became valid in layer l, 255 = still invalid;
+// "valid before layer l" is stamp <= l.
+
+__global__ void stamps_from_valid_kernel(long long n, const uint8_t* __restrict__ valid, uint8_t* __restrict__ stamp) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        stamp[c] = valid[c] ? 0 : 255;
+}
+
+__global__ void valid_from_stamps_kernel(long long n, const uint8_t* __restrict__ stamp, uint8_t* __restrict__ valid) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        valid[c] = stamp[c] != 255 ? 1 : 0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) extrapolate_layer_kernel(int n0, int n1, int n2, T* __restrict__ g,
+                                                                uint8_t* __restrict__ stamp, int layer) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= n0 || j >= n1) return;
+    const long long c = lin3(i, j, k, n0, n1);
+    if (stamp[c] <= layer) return;  // valid before this layer
+    T sum = T(0);
+    int count = 0;
+    for (int dk = -1; dk <= 1; ++dk) {
+        const int z = k + dk;
+        if (z < 0 || z >= n2) continue;
+        for (int dj = -1; dj <= 1; ++dj) {
+            const int y = j + dj;
+            if (y < 0 || y >= n1) continue;
+            for (int di = -1; di <= 1; ++di) {
+                const int x = i + di;
+                if (x < 0 || x >= n0) continue;
+                const long long q = lin3(x, y, z, n0, n1);
+                if (stamp[q] <= layer) {
+                    sum = add_rn2(sum, g[q]);
+                    ++count;
+                }
+            }
+        }
+    }
+    if (count > 0) {
+        g[c] = sum / (T)count;
+        stamp[c] = (uint8_t)(layer + 1);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// add_gravity + find_valid_velocity + set_invalid_velocity_zero, fused per face component
+// (simulator.cpp:90-93, 125-158, 169-178).  The phi test applies on faces with index in
+// [1, n) along the normal and [1, n-1) along the tangential axes, as the reference's loops.
+template <typename T>
+__global__ void masks_kernel(int ni, int nj, int nk, int comp, T* __restrict__ f, const T* __restrict__ wt,
+                             const T* __restrict__ phi, uint8_t* __restrict__ valid, int apply_gravity,
+                             T gravity, const Scalars* s, double dt_value, int zero_invalid) {
+    const int f0 = ni + (comp == 0), f1 = nj + (comp == 1), f2 = nk + (comp == 2);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= f0 || j >= f1 || k >= f2) return;
+    const long long fi = lin3(i, j, k, f0, f1);
+    T val = f[fi];
+    if (apply_gravity) {
+        const T dt = (T)(s ? s->dt : dt_value);
+        val = val - mul_rn2(gravity, dt);
+    }
+    bool ok = wt[fi] != T(0);
+    const int ei = comp == 0 ? ni : ni - 1, ej = comp == 1 ? nj : nj - 1, ek = comp == 2 ? nk : nk - 1;
+    if (ok && i >= 1 && j >= 1 && k >= 1 && i < ei && j < ej && k < ek) {
+        const long long b = lin3(i, j, k, ni, nj);
+        const long long a = comp == 0 ? b - 1 : (comp == 1 ? b - ni : b - (long long)ni * nj);
+        if (phi[a] >= T(0) && phi[b] >= T(0)) ok = false;
+    }
+    valid[fi] = ok ? 1 : 0;
+    if (zero_invalid && !ok) val = T(0);
+    if (apply_gravity || (zero_invalid && !ok)) f[fi] = val;
+}
+
+template <typename T>
+__global__ void gravity_kernel(long long n, T* __restrict__ v, T gravity, const Scalars* s, double dt_value) {
+    const T dt = (T)(s ? s->dt : dt_value);
+    const T dv = mul_rn2(gravity, dt);
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        v[c] = v[c] - dv;
+}
+
+template <typename T>
+__global__ void zero_invalid_kernel(long long n, T* __restrict__ f, const uint8_t* __restrict__ valid) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        if (!valid[c]) f[c] = T(0);
+}
+
+// max |u| over the MAC grid (staggered_grid.h:230-248): |x| as unsigned bits orders like x.
+__device__ __forceinline__ void atomic_max_abs(unsigned long long* m, double v) {
+    atomicMax(m, (unsigned long long)__double_as_longlong(fabs(v)));
+}
+
+template <typename T>
+__global__ void maxabs_kernel(long long n, const T* __restrict__ a, unsigned long long* out) {
+    double m = 0.0;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        m = fmax(m, fabs((double)a[c]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomic_max_abs(out, m);
+}
+
+// dt = cfl * dx / max(max|u|, 1e-4) in the field type (time_stepping.cpp:5-7)
+template <typename T>
+__global__ void time_step_kernel(const unsigned long long* m, T cfl, T dx, Scalars* s) {
+    const T mx = (T)__longlong_as_double((long long)*m);
+    const T den = mx > T(1e-4) ? mx : T(1e-4);
+    const T dt = mul_rn2(cfl, dx) / den;
+    s->maxabs = (double)mx;
+    s->dt = (double)dt;
+}
+
+__global__ void set_dt_kernel(Scalars* s, double dt) { s->dt = dt; }
+
+// ---------------------------------------------------------------------------------------
+// emitters (levelset_emitter.cpp:10-79): min(field, f(x)) at the grid's sample positions.
+enum { EMIT_CLEAR = 0, EMIT_SPHERE = 1, EMIT_POOL = 2, EMIT_BOX = 3, EMIT_ROOM = 4 };
+
+struct EmitArgs {
+    int kind;
+    double a[8];
+};
+
+template <typename T>
+__global__ void emit_kernel(int n0, int n1, int n2, T* __restrict__ g, T ox, T dx, EmitArgs e) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= n0 || j >= n1) return;
+    const long long c = lin3(i, j, k, n0, n1);
+    if (e.kind == EMIT_CLEAR) {
+        g[c] = (T)3.402823466e+38;  // FLT_MAX, as LevelSetEmitterList::apply
+        return;
+    }
+    // GridBase::pos (grid.h:355-367): (idx + 0.5) * dx + origin
+    const T px = add_rn2(mul_rn2(i + T(0.5), dx), ox);
+    const T py = add_rn2(mul_rn2(j + T(0.5), dx), ox);
+    const T pz = add_rn2(mul_rn2(k + T(0.5), dx), ox);
+    T val;
+    if (e.kind == EMIT_SPHERE) {
+        const T qx = px - (T)e.a[0], qy = py - (T)e.a[1], qz = pz - (T)e.a[2];
+        const T ss = add_rn2(add_rn2(mul_rn2(qx, qx), mul_rn2(qy, qy)), mul_rn2(qz, qz));
+        val = sqrt(ss) - (T)e.a[3];
+    } else if (e.kind == EMIT_POOL) {
+        val = py - (T)e.a[0];
+    } else if (e.kind == EMIT_BOX) {
+        const T p[3] = {px, py, pz};
+        T outside2 = T(0), inside = -(T)3.402823466e+38;
+        for (int ax = 0; ax < 3; ++ax) {
+            const T lo = (T)e.a[ax], hi = (T)e.a[3 + ax];
+            const T q = fmax(lo - p[ax], p[ax] - hi);
+            if (q > T(0)) outside2 = add_rn2(outside2, mul_rn2(q, q));
+            inside = fmax(inside, q);
+        }
+        val = outside2 > T(0) ? sqrt(outside2) : inside;
+    } else {  // room: nodal wall layers (levelset_emitter.cpp:18-32)
+        if (i == 0 || i == n0 - 1 || j == 0 || j == n1 - 1 || k == 0 || k == n2 - 1)
+            val = (T)-1.0;
+        else if (i == 1 || i == n0 - 2 || j == 1 || j == n1 - 2 || k == 1 || k == n2 - 2)
+            val = (T)-0.01;
+        else
+            val = (T)1.0;
+    }
+    const T old = g[c];
+    g[c] = val < old ? val : old;
+}
+
+// ---------------------------------------------------------------------------------------
+// launchers
+
+static dim3 pgrid(int n0, int n1, int n2, dim3 b) { return dim3((n0 + b.x - 1) / b.x, (n1 + b.y - 1) / b.y, n2); }
+
+static int g1(el_ctx* ctx, long long n) {
+    return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, (long long)ctx->num_sms * 8));
+}
+
+static void field_dims(el_ctx* ctx, int field, int& n0, int& n1, int& n2) {
+    n0 = ctx->ni;
+    n1 = ctx->nj;
+    n2 = ctx->nk;
+    if (field == EL_FIELD_U || field == EL_FIELD_WEIGHT_U || field == EL_FIELD_VALID_U) n0++;
+    if (field == EL_FIELD_V || field == EL_FIELD_WEIGHT_V || field == EL_FIELD_VALID_V) n1++;
+    if (field == EL_FIELD_W || field == EL_FIELD_WEIGHT_W || field == EL_FIELD_VALID_W) n2++;
+    if (field == EL_FIELD_SOLID_NODAL) {
+        n0++;
+        n1++;
+        n2++;
+    }
+}
+
+// extrapolate `field` over `layers` Jacobi layers using the mask `valid`; when write_back the
+// mask is updated like extrapolate() (velocity), else left alone like extrapolate_const().
+int launch_extrapolate(el_ctx* ctx, int field, uint8_t* valid, int layers, bool write_back) {
+    int n0, n1, n2;
+    field_dims(ctx, field, n0, n1, n2);
+    const long long n = (long long)n0 * n1 * n2;
+    uint8_t* stamp = ctx->valid_tmp;
+    stamps_from_valid_kernel<<<g1(ctx, n), 256, 0, ctx->stream>>>(n, valid, stamp);
+    dim3 block(32, 4, 1);
+    dim3 grid = pgrid(n0, n1, n2, block);
+    const int L = std::min(layers, 254);
+    for (int l = 0; l < L; ++l) {
+        if (ctx->dtype == EL_F64)
+            extrapolate_layer_kernel<double><<<grid, block, 0, ctx->stream>>>(n0, n1, n2, (double*)ctx->field[field],
+                                                                              stamp, l);
+        else
+            extrapolate_layer_kernel<float><<<grid, block, 0, ctx->stream>>>(n0, n1, n2, (float*)ctx->field[field],
+                                                                             stamp, l);
+    }
+    int launched = 1 + L;
+    if (write_back) {
+        valid_from_stamps_kernel<<<g1(ctx, n), 256, 0, ctx->stream>>>(n, stamp, valid);
+        ++launched;
+    }
+    return launched;
+}
+
+template <typename T>
+static int launch_masks_t(el_ctx* ctx, bool gravity, double g, const Scalars* s, double dtv, bool zero) {
+    dim3 block(32, 4, 1);
+    for (int comp = 0; comp < 3; ++comp) {
+        int n0, n1, n2;
+        field_dims(ctx, EL_FIELD_U + comp, n0, n1, n2);
+        masks_kernel<T><<<pgrid(n0, n1, n2, block), block, 0, ctx->stream>>>(
+            ctx->ni, ctx->nj, ctx->nk, comp, (T*)ctx->field[EL_FIELD_U + comp],
+            (const T*)ctx->field[EL_FIELD_WEIGHT_U + comp], (const T*)ctx->field[EL_FIELD_PHI],
+            (uint8_t*)ctx->field[EL_FIELD_VALID_U + comp], (gravity && comp == 1) ? 1 : 0, (T)g, s, dtv,
+            zero ? 1 : 0);
+    }
+    return 3;
+}
+
+int launch_masks(el_ctx* ctx, bool gravity, double g, const Scalars* s, double dtv, bool zero) {
+    return ctx->dtype == EL_F64 ? launch_masks_t<double>(ctx, gravity, g, s, dtv, zero)
+                                : launch_masks_t<float>(ctx, gravity, g, s, dtv, zero);
+}
+
+int launch_gravity(el_ctx* ctx, double g, const Scalars* s, double dtv) {
+    const long long n = (long long)ctx->ni * (ctx->nj + 1) * ctx->nk;
+    if (ctx->dtype == EL_F64)
+        gravity_kernel<double><<<g1(ctx, n), 256, 0, ctx->stream>>>(n, (double*)ctx->field[EL_FIELD_V], g, s, dtv);
+    else
+        gravity_kernel<float><<<g1(ctx, n), 256, 0, ctx->stream>>>(n, (float*)ctx->field[EL_FIELD_V], (float)g, s, dtv);
+    return 1;
+}
+
+int launch_zero_invalid(el_ctx* ctx) {
+    for (int comp = 0; comp < 3; ++comp) {
+        int n0, n1, n2;
+        field_dims(ctx, EL_FIELD_U + comp, n0, n1, n2);
+        const long long n = (long long)n0 * n1 * n2;
+        const uint8_t* valid = (const uint8_t*)ctx->field[EL_FIELD_VALID_U + comp];
+        if (ctx->dtype == EL_F64)
+            zero_invalid_kernel<double><<<g1(ctx, n), 256, 0, ctx->stream>>>(n, (double*)ctx->field[EL_FIELD_U + comp], valid);
+        else
+            zero_invalid_kernel<float><<<g1(ctx, n), 256, 0, ctx->stream>>>(n, (float*)ctx->field[EL_FIELD_U + comp], valid);
+    }
+    return 3;
+}
+
+// Computes dt into ctx->dscal[0].dt on the device.
+int launch_time_step(el_ctx* ctx, double cfl, unsigned long long* scratch_max) {
+    cudaMemsetAsync(scratch_max, 0, sizeof(unsigned long long), ctx->stream);
+    for (int comp = 0; comp < 3; ++comp) {
+        int n0, n1, n2;
+        field_dims(ctx, EL_FIELD_U + comp, n0, n1, n2);
+        const long long n = (long long)n0 * n1 * n2;
+        if (ctx->dtype == EL_F64)
+            maxabs_kernel<double><<<g1(ctx, n), 256, 0, ctx->stream>>>(n, (const double*)ctx->field[EL_FIELD_U + comp], scratch_max);
+        else
+            maxabs_kernel<float><<<g1(ctx, n), 256, 0, ctx->stream>>>(n, (const float*)ctx->field[EL_FIELD_U + comp], scratch_max);
+    }
+    if (ctx->dtype == EL_F64)
+        time_step_kernel<double><<<1, 1, 0, ctx->stream>>>(scratch_max, cfl, ctx->dx, ctx->dscal);
+    else
+        time_step_kernel<float><<<1, 1, 0, ctx->stream>>>(scratch_max, (float)cfl, (float)ctx->dx, ctx->dscal);
+    return 4;
+}
+
+int launch_set_dt(el_ctx* ctx, double dt) {
+    set_dt_kernel<<<1, 1, 0, ctx->stream>>>(ctx->dscal, dt);
+    return 1;
+}
+
+int launch_emit(el_ctx* ctx, int target, int kind, const double* a, int na) {
+    const int field = target == 0 ? EL_FIELD_PHI : EL_FIELD_SOLID_NODAL;
+    int n0, n1, n2;
+    field_dims(ctx, field, n0, n1, n2);
+    EmitArgs e;
+    e.kind = kind;
+    for (int q = 0; q < 8; ++q) e.a[q] = q < na ? a[q] : 0.0;
+    dim3 block(32, 4, 1);
+    dim3 grid = pgrid(n0, n1, n2, block);
+    if (ctx->dtype == EL_F64) {
+        const double dx = ctx->dx;
+        const double ox = target == 0 ? 0.0 : -(dx * 0.5);
+        emit_kernel<double><<<grid, block, 0, ctx->stream>>>(n0, n1, n2, (double*)ctx->field[field], ox, dx, e);
+    } else {
+        const float dx = (float)ctx->dx;
+        const float ox = target == 0 ? 0.0f : -(dx * 0.5f);
+        emit_kernel<float><<<grid, block, 0, ctx->stream>>>(n0, n1, n2, (float*)ctx->field[field], ox, dx, e);
+    }
+    return 1;
+}
+
+}  // namespace el

@@ -1,0 +1,234 @@
+/*
+ * eulerian_liquid_gb300.h -- C ABI of the GB300 (sm_103a) implementation of the
+ * daichi-nama/eulerian-liquid per-step grid hot path: semi-Lagrangian (trilinear / WENO6,
+ * RK2 / RK3) advection of the MAC velocity and the level set, and the ghost-fluid PCG
+ * pressure projection, plus the step pieces on either side of them.
+ *
+ * Conventions
+ *   - Every function returns an int status (EL_OK = 0); no exception crosses the ABI.
+ *     el_ctx_last_error() gives a one-line message for the last failure on a context.
+ *   - Arrays are i-fastest, flat index i + n0*(j + n1*k), exactly the reference's layout
+ *     (include/nama/common/array.h:281-286), so a host Grid3f / StaggeredGrid3f component
+ *     uploads with one contiguous copy.
+ *       phi, pressure, cell solid phi, indices : ni x nj x nk
+ *       u, weight_u, valid_u                    : (ni+1) x nj x nk
+ *       v, weight_v, valid_v                    : ni x (nj+1) x nk
+ *       w, weight_w, valid_w                    : ni x nj x (nk+1)
+ *       nodal solid phi                         : (ni+1) x (nj+1) x (nk+1)
+ *     Grid origins: cells at (0,0,0), faces shifted by -dx/2 along their normal, nodes by
+ *     -dx/2 on every axis (include/nama/common/staggered_grid.h:100-112,
+ *     src/project/3d/eulerian_liquid/simulator.cpp:52-70).
+ *   - Field type is chosen per context: EL_F32 (the reference's Grid3f) or EL_F64.  The
+ *     matrix diagonal, right-hand side and solution are always double, as in
+ *     src/project/3d/fluid/projection.cpp:30-33.
+ *   - One CUDA stream per context (its own, or one given with el_ctx_set_stream).  Calls
+ *     on one context are not re-entrant, like the reference's Simulator.
+ */
+#ifndef EULERIAN_LIQUID_GB300_H
+#define EULERIAN_LIQUID_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------- */
+#define EL_OK 0
+#define EL_ERR_INVALID_ARGUMENT 1
+#define EL_ERR_NO_FLUID 2      /* projection.cpp:24-26 throws std::runtime_error("No fluid") */
+#define EL_ERR_NOT_CONVERGED 3 /* simulator.cpp:107-109 never checks solver.info(); we report */
+#define EL_ERR_NAN 4           /* a non-finite residual or field was detected */
+#define EL_ERR_CUDA 5
+#define EL_ERR_OUT_OF_MEMORY 6
+#define EL_ERR_TIMEOUT 7 /* a bounded device wait gave up */
+
+/* ---- field types and ids ------------------------------------------------------------ */
+#define EL_F32 0
+#define EL_F64 1
+
+enum el_field {
+    EL_FIELD_PHI = 0,         /* Simulator::m_level_set            (simulator.h:68)     */
+    EL_FIELD_U = 1,           /* Simulator::m_velocity.u()         (simulator.h:64)     */
+    EL_FIELD_V = 2,
+    EL_FIELD_W = 3,
+    EL_FIELD_SOLID_NODAL = 4, /* Simulator::m_nodal_solid_phi      (simulator.h:73)     */
+    EL_FIELD_WEIGHT_U = 5,    /* Simulator::m_velocity_weight.u()  (simulator.h:66)     */
+    EL_FIELD_WEIGHT_V = 6,
+    EL_FIELD_WEIGHT_W = 7,
+    EL_FIELD_PRESSURE = 8,    /* Simulator::m_pressure             (simulator.h:71)     */
+    EL_FIELD_SOLID_CELL = 9,  /* m_cell_centered_solid_level_set   (simulator.h:74)     */
+    EL_FIELD_VALID_U = 10,    /* m_velocity_valid.u(), uint8       (simulator.h:65)     */
+    EL_FIELD_VALID_V = 11,
+    EL_FIELD_VALID_W = 12,
+    EL_FIELD_VALID_PHI = 13,  /* m_level_set_valid, uint8          (simulator.h:69)     */
+    EL_FIELD_INDICES = 14,    /* m_indices, int32 (INT_MAX = not a fluid cell) (simulator.h:70) */
+    EL_FIELD_COUNT = 15
+};
+
+/* ---- advection schemes -------------------------------------------------------------- */
+#define EL_TRACE_RK2 0        /* math::trace_rk2, midpoint rule (include/nama/math/ode.h:30-35) */
+#define EL_TRACE_RK3 1        /* Ralston RK3 (new; the reference has RK1/RK2 only)          */
+#define EL_SAMPLE_TRILINEAR 0 /* math::lerp(x, grid) (include/nama/math/interpolation.h:35-72) */
+#define EL_SAMPLE_WENO6 1     /* math::weno6_interp(x, grid) (interpolation.h:139-184)      */
+
+/* ---- pressure solver ---------------------------------------------------------------- */
+#define EL_SOLVER_JACOBI_FP64 0 /* plain FP64 PCG, Jacobi preconditioner                     */
+#define EL_SOLVER_MG_FP64 1     /* FP64 PCG, multigrid V-cycle preconditioner                */
+#define EL_SOLVER_MIXED 2       /* FP32 multigrid PCG inside FP64 iterative refinement       */
+
+typedef struct el_solve_params {
+    int solver;         /* EL_SOLVER_*                                                   */
+    double tol;         /* relative residual |b - A p| / |b| to reach (reference: 1e-4)  */
+    int max_iter;       /* PCG iteration cap, inner iterations summed for EL_SOLVER_MIXED */
+    int check_every;    /* host convergence poll period in iterations (>= 1)             */
+    int max_outer;      /* EL_SOLVER_MIXED: refinement sweeps cap                        */
+    double inner_floor; /* EL_SOLVER_MIXED: smallest inner relative tolerance (FP32)     */
+} el_solve_params;
+
+typedef struct el_solve_stats {
+    int status;          /* EL_OK, EL_ERR_NOT_CONVERGED, EL_ERR_NO_FLUID, EL_ERR_NAN        */
+    int iterations;      /* PCG iterations (inner iterations summed for EL_SOLVER_MIXED)   */
+    int outer_iterations;/* refinement sweeps (EL_SOLVER_MIXED), else 1                    */
+    int fluid_cells;     /* matrix size: what assign_indices returns (projection.cpp:14-28)  */
+    double relres;       /* final relative residual the solver stopped on                  */
+} el_solve_stats;
+
+typedef struct el_step_params {
+    int trace_phi, sample_phi;   /* level-set advection scheme                              */
+    int trace_vel, sample_vel;   /* velocity advection scheme                               */
+    double gravity;              /* m/s^2 subtracted from v (reference: 9.80665)            */
+    int extrapolation_layers;    /* reference: 10 (simulator.cpp:115-123)                   */
+    el_solve_params solve;
+} el_step_params;
+
+typedef struct el_step_stats {
+    double dt;
+    el_solve_stats solve;
+} el_step_stats;
+
+typedef struct el_ctx el_ctx;
+
+/* ---- context ------------------------------------------------------------------------ */
+/* Simulator::create_grid (src/project/3d/eulerian_liquid/simulator.cpp:52-70): allocate a
+ * device-resident scene of ni x nj x nk cells of size dx.  All fields start at zero except
+ * the valid masks (1), as in create_grid.  device = CUDA ordinal. */
+int el_ctx_create(int ni, int nj, int nk, double dx, int dtype, int device, el_ctx** out);
+int el_ctx_destroy(el_ctx* ctx);
+const char* el_ctx_last_error(const el_ctx* ctx);
+const char* el_status_string(int status);
+/* Use the caller's stream (a cudaStream_t) for all work on this context; NULL = own stream. */
+int el_ctx_set_stream(el_ctx* ctx, void* cuda_stream);
+void* el_ctx_get_stream(el_ctx* ctx);
+int el_ctx_sync(el_ctx* ctx);
+/* Number of kernels this library launched on the context since creation. */
+int64_t el_ctx_kernel_launches(const el_ctx* ctx);
+
+/* ---- per-kernel-class timing ---------------------------------------------------------
+ * While profiling is on, every launch of a class in `class_mask` (bit = 1 << EL_KC_*) is
+ * bracketed by CUDA events on the context's stream; el_ctx_profile_end synchronises and
+ * returns, per class, the launches, their summed device time and their summed algorithmic
+ * bytes (each array a kernel must read or write counted once per launch). */
+enum el_kernel_class {
+    EL_KC_ADVECT_PHI = 0,   /* level-set advection                                   */
+    EL_KC_ADVECT_VEL = 1,   /* velocity advection (one launch per face component)    */
+    EL_KC_EXTRAPOLATE = 2,  /* extrapolation layers                                  */
+    EL_KC_MASKS = 3,        /* gravity + valid masks + zeroing                       */
+    EL_KC_BUILD = 4,        /* cell flags + ghost-fluid coefficients                 */
+    EL_KC_DIR_SPMV = 5,     /* PCG: p = z + beta p fused with A p and p.Ap           */
+    EL_KC_UPDATE = 6,       /* PCG: x, r update fused with the residual norms        */
+    EL_KC_SMOOTH = 7,       /* multigrid smoothing on the finest level               */
+    EL_KC_RESTRICT = 8,     /* multigrid residual + restriction from the finest level */
+    EL_KC_MG_COARSE = 9,    /* all multigrid work below the finest level             */
+    EL_KC_RESIDUAL = 10,    /* FP64 refinement residual r = b - A x                  */
+    EL_KC_OTHER = 11,
+    EL_KC_COUNT = 12
+};
+
+typedef struct el_profile_entry {
+    int64_t launches;
+    double ms;
+    double bytes;
+} el_profile_entry;
+
+int el_ctx_profile_begin(el_ctx* ctx, uint32_t class_mask);
+/* out must hold EL_KC_COUNT entries */
+int el_ctx_profile_end(el_ctx* ctx, el_profile_entry* out);
+
+/* Host <-> device copies of a whole field (bytes must equal the field's size). */
+int el_upload(el_ctx* ctx, int field, const void* host, size_t bytes);
+int el_download(el_ctx* ctx, int field, void* host, size_t bytes);
+/* Device pointer of a field, for zero-copy use by a caller that owns device memory. */
+int el_field_device_ptr(el_ctx* ctx, int field, void** dptr, size_t* bytes);
+
+/* ---- scene set-up (src/project/3d/fluid/levelset_emitter.cpp:10-79) -------------------
+ * target 0 = liquid level set (cell centres), 1 = nodal solid level set.  Each emitter
+ * writes min(field, f(x)); el_emit_clear fills with FLT_MAX like LevelSetEmitterList::apply. */
+int el_emit_clear(el_ctx* ctx, int target);
+int el_emit_sphere(el_ctx* ctx, int target, double cx, double cy, double cz, double r);
+int el_emit_pool(el_ctx* ctx, int target, double height);
+int el_emit_box(el_ctx* ctx, int target, const double lo[3], const double hi[3]);
+int el_emit_room(el_ctx* ctx, int target);
+
+/* ---- boundary (init time) ---------------------------------------------------------- */
+int el_compute_weights(el_ctx* ctx);            /* fluid::compute_staggered_grid_weight, boundary.cpp:6-34 */
+int el_calc_cell_centered_solid_phi(el_ctx* ctx);/* simulator.cpp:191-200 */
+int el_find_valid_level_set(el_ctx* ctx);       /* simulator.cpp:160-167 */
+
+/* ---- hot path: Simulator step methods (include/nama/project/3d/eulerian_liquid/simulator.h:32-53) */
+int el_advect_level_set(el_ctx* ctx, double dt, int trace, int sample); /* simulator.cpp:84-87 */
+int el_advect_velocity(el_ctx* ctx, double dt, int trace, int sample);  /* simulator.cpp:79-82 */
+int el_add_gravity(el_ctx* ctx, double dt, double gravity);             /* simulator.cpp:90-93 */
+int el_extrapolate_level_set(el_ctx* ctx, int layers);                  /* simulator.cpp:115-117 */
+int el_extrapolate_velocity(el_ctx* ctx, int layers);                   /* simulator.cpp:119-123 */
+int el_find_valid_velocity(el_ctx* ctx);                                /* simulator.cpp:125-158 */
+int el_set_invalid_velocity_zero(el_ctx* ctx);                          /* simulator.cpp:169-178 */
+int el_solve_pressure(el_ctx* ctx, double dt, const el_solve_params* params,
+                      el_solve_stats* stats);                           /* simulator.cpp:96-112 */
+/* fluid::calc_time_step (src/project/3d/fluid/time_stepping.cpp:5-7): cfl*dx/max(max|u|,1e-4) */
+int el_calc_time_step(el_ctx* ctx, double cfl, double* dt_out);
+/* update_second_order (apps/eulerian_liquid_3d.cpp:106-120) without reinitialize(), which
+ * stays the reference's own CPU code: extrapolate velocity and level set, advect level set,
+ * advect velocity, gravity, valid masks, zero invalid faces, solve pressure. */
+int el_step(el_ctx* ctx, double dt, const el_step_params* params, el_step_stats* stats);
+
+/* ---- projection pieces (include/nama/project/3d/fluid/projection.h:10-22) ------------- */
+/* assign_indices (projection.cpp:14-28): k-j-i numbering into EL_FIELD_INDICES. */
+int el_assign_indices(el_ctx* ctx, int* mat_size);
+/* build_matrix (projection.cpp:30-83) into the context's grid-shaped coefficients. */
+int el_build_matrix(el_ctx* ctx, double dt);
+/* Copy the grid-shaped matrix out as doubles (ni*nj*nk each): diagonal, the couplings of
+ * each cell with its +x / +y / +z neighbour, and the right-hand side.  Any may be NULL. */
+int el_download_matrix(el_ctx* ctx, double* diag, double* offx, double* offy, double* offz,
+                       double* rhs);
+/* build_grid_from_vector + update_velocity_using_pressure (projection.cpp:85-134) using the
+ * EL_FIELD_PRESSURE grid as it stands (after a solve, or after el_upload). */
+int el_update_velocity_using_pressure(el_ctx* ctx, double dt);
+
+/* ---- stateless operators on caller-owned device memory ------------------------------
+ * The reference's free functions (include/nama/project/3d/fluid/advection.h:8-11,
+ * boundary.h:8) over raw device pointers; no allocation, work enqueued on `stream`. */
+typedef struct el_grid {
+    int ni, nj, nk;
+    double dx;
+} el_grid;
+
+/* advect_collocated_grid (advection.cpp:9-16): out = in(trace(x, -dt, vel)) at cell centres */
+int el_advect_collocated_grid(const el_grid* g, int dtype, void* out, const void* in,
+                              const void* vel_u, const void* vel_v, const void* vel_w,
+                              double dt, int trace, int sample, void* stream);
+/* advect_staggered_grid (advection.cpp:18-27): each face component of `in` through `vel` */
+int el_advect_staggered_grid(const el_grid* g, int dtype, void* out_u, void* out_v, void* out_w,
+                             const void* in_u, const void* in_v, const void* in_w,
+                             const void* vel_u, const void* vel_v, const void* vel_w,
+                             double dt, int trace, int sample, void* stream);
+/* compute_staggered_grid_weight (boundary.cpp:6-34) */
+int el_compute_staggered_grid_weight(const el_grid* g, int dtype, void* weight_u, void* weight_v,
+                                     void* weight_w, const void* nodal_solid, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EULERIAN_LIQUID_GB300_H */
