@@ -1,0 +1,417 @@
+"""Benchmark: steps/s of the per-step grid hot path on one GB300 (or N replicas).
+
+Workload (one "step" = one pass of the hot path): a 256^3 unit-cube MAC grid, FP32 fields, the
+spheres-over-pool scene (pool y < 0.3, three seeded spheres r in [0.08, 0.2], room walls and a
+seeded solid box holding 5-10 % of the cells); each step extrapolates velocity and level set,
+advects the level set (WENO6 sampling, RK2 backtrace) and the velocity (trilinear, RK3),
+adds gravity (9.8), rebuilds the valid masks and solves the ghost-fluid pressure to relative
+residual 1e-6, then updates the velocity -- update_second_order of the reference without
+reinitialisation.  dt = min(CFL 1.0 step, 1/60 s).
+
+value      steps/s with the mixed solver (FP32 multigrid PCG inside FP64 refinement), inputs
+           resident in HBM, CUDA events on the library's stream.
+plain_fp64 the same workload with plain FP64 PCG (Jacobi); mg_fp64: FP64 multigrid PCG.
+e2e        steps/s through the C ABI with host buffers: every step uploads phi, u, v, w from
+           pinned host memory and downloads phi, u, v, w and the pressure.
+roofline   the dominant kernel class, algorithmic bytes / device time over the timed region.
+cpu_baseline  the CPU oracle (OpenMP restatement with MIC(0)-PCG) on one step of the workload.
+
+--impl reference times the reference's CPU path for the same workload: the oracle port (the
+reference itself cannot be built without Eigen).  Under torchrun rank 0 alone runs it.
+"""
+
+import argparse
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+METRIC = "steps/s at 256^3, mixed vs plain FP64 GPU PCG, same GB300, rel. resid 1e-6"
+KC_NAMES = ["advect_phi", "advect_vel", "extrapolate", "masks", "build", "dir_spmv", "update", "mg_smooth_fine",
+            "mg_restrict_fine", "mg_coarse", "residual_fp64", "other"]
+
+
+def load_package():
+    name = "eulerian_liquid_gb300"
+    if name in sys.modules:
+        return sys.modules[name]
+    pkg_dir = os.path.join(ROOT, "eulerian-liquid_gb300")
+    spec = importlib.util.spec_from_file_location(name, os.path.join(pkg_dir, "__init__.py"),
+                                                  submodule_search_locations=[pkg_dir])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def parse_args(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--tol", type=float, default=1e-6)
+    ap.add_argument("--plain-steps", type=int, default=None, help="timed steps of the plain FP64 arm")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--error-steps", type=int, default=2)
+    return ap.parse_args(argv)
+
+
+# ---- distributed plumbing (replicas: no data-path collective) -----------------------------
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            backend = "nccl" if _cuda_available() else "gloo"
+            td.init_process_group(backend=backend)
+            self.pg = td
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, value):
+        if not self.pg:
+            return value
+        import torch
+        dev = "cuda" if self.pg.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def _cuda_available():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def aggregate(values_per_rank, steps, world):
+    """Whole-job steps/s from each rank's elapsed ms: all ranks' steps over the slowest rank."""
+    slowest = max(values_per_rank)
+    return steps * world / (slowest / 1000.0), slowest / steps
+
+
+# ---- clocks during the timed region --------------------------------------------------------
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "100"], stdout=open(self.path, "w"),
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = [r.split(", ") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for r in rows if len(r) >= 9 for q in range(4) if r[5 + q].strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---- our arm -------------------------------------------------------------------------------
+
+def workload(el, n, seed):
+    return el.scenes.spheres_pool(n, seed)
+
+
+def step_params(el, solver, tol):
+    return el.step_params(trace_phi=el.TRACE_RK2, sample_phi=el.SAMPLE_WENO6, trace_vel=el.TRACE_RK3,
+                          sample_vel=el.SAMPLE_TRILINEAR, gravity=9.8, extrapolation_layers=10, solver=solver,
+                          tol=tol, max_iter=20000, check_every=4 if solver == el.SOLVER_MIXED else 16)
+
+
+def next_dt(sim, cfl=1.0, frame=1.0 / 60.0):
+    return min(sim.calc_time_step(cfl), frame)
+
+
+def make_sim(el, torch, n, seed):
+    sim = el.Simulator(n, n, n, dtype=el.EL_F32, device=torch.cuda.current_device())
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
+    sim.init_scene(workload(el, n, seed))
+    return sim, stream
+
+
+def timed_steps(el, torch, sim, stream, params, steps, dist, profile_mask=0, sampler=None):
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    stats = []
+    dist.barrier()
+    torch.cuda.synchronize()
+    if profile_mask:
+        sim._check(sim.lib.el_ctx_profile_begin(sim.h, profile_mask), "profile_begin")
+    launches0 = sim.kernel_launches()
+    if sampler:
+        sampler.start()
+    ev0.record(stream)
+    for _ in range(steps):
+        dt = next_dt(sim)
+        stats.append(sim.step(dt, params))
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop() if sampler else None
+    dist.barrier()
+    launches = sim.kernel_launches() - launches0
+    prof = None
+    if profile_mask:
+        prof = read_profile(el, sim)
+    return ev0.elapsed_time(ev1), stats, launches, prof, clocks
+
+
+def read_profile(el, sim):
+    import ctypes as C
+
+    class Entry(C.Structure):
+        _fields_ = [("launches", C.c_int64), ("ms", C.c_double), ("bytes", C.c_double)]
+
+    out = (Entry * 12)()
+    sim.lib.el_ctx_profile_end.argtypes = [C.c_void_p, C.c_void_p]
+    sim._check(sim.lib.el_ctx_profile_end(sim.h, C.cast(out, C.c_void_p)), "profile_end")
+    return {KC_NAMES[c]: {"launches": int(out[c].launches), "ms": out[c].ms, "bytes": out[c].bytes}
+            for c in range(12) if out[c].launches}
+
+
+def pressure_error(el, sim, params_mixed, n_steps):
+    """Mixed-solver pressure vs a FP64 multigrid PCG solve to 1e-12 from the same step input."""
+    import numpy as np
+    ref_params = step_params(el, el.SOLVER_MG_FP64, 1e-12)
+    fields = ["phi", "u", "v", "w", "valid_u", "valid_v", "valid_w"]
+    errs = []
+    for _ in range(n_steps):
+        saved = {f: sim.download(f) for f in fields}
+        dt = next_dt(sim)
+        sim.step(dt, ref_params)
+        p_ref = sim.download("pressure").astype(np.float64)
+        for f in fields:
+            sim.upload(f, saved[f])
+        sim.step(dt, params_mixed)
+        p = sim.download("pressure").astype(np.float64)
+        errs.append(float(np.linalg.norm(p - p_ref) / max(np.linalg.norm(p_ref), 1e-300)))
+    return errs
+
+
+def e2e_steps(el, torch, sim, stream, params, steps):
+    """Steps through the C ABI with host buffers: inputs up, results down, every step."""
+    host = {}
+    for f in ("phi", "u", "v", "w", "pressure"):
+        t = torch.empty(sim.shape(f), dtype=torch.float32, pin_memory=True)
+        host[f] = t.numpy()
+        host[f][...] = sim.download(f)
+    h2d = sum(host[f].nbytes for f in ("phi", "u", "v", "w"))
+    d2h = sum(host[f].nbytes for f in ("phi", "u", "v", "w", "pressure"))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for f in ("phi", "u", "v", "w"):
+            sim.upload(f, host[f])
+        dt = next_dt(sim)
+        sim.step(dt, params)
+        for f in ("phi", "u", "v", "w", "pressure"):
+            sim.download(f, out=host[f])
+    torch.cuda.synchronize()
+    elapsed = time.perf_counter() - t0
+    return steps / elapsed, h2d, d2h
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def run_ours(args, dist):
+    import torch
+
+    el = load_package()
+    el.load()
+    torch.cuda.set_device(dist.local_rank)
+    n, K, W = args.n, args.steps, max(3, args.warmup)
+    params = step_params(el, el.SOLVER_MIXED, args.tol)
+
+    sim, stream = make_sim(el, torch, n, args.seed)
+    for _ in range(W):
+        sim.step(next_dt(sim), params)
+    # class breakdown on two untimed steps, to pick the dominant kernel class
+    _, _, _, breakdown, _ = timed_steps(el, torch, sim, stream, params, 2, dist, profile_mask=(1 << 12) - 1)
+    dominant = max(breakdown, key=lambda k: breakdown[k]["ms"])
+    sampler = ClockSampler(dist.local_rank) if dist.rank == 0 else None
+    elapsed, stats, launches, prof, clocks = timed_steps(el, torch, sim, stream, params, K, dist,
+                                                         profile_mask=1 << KC_NAMES.index(dominant),
+                                                         sampler=sampler)
+    elapsed = dist.max(elapsed)
+    value, ms_per_step = aggregate([elapsed], K, dist.world)
+    iters = [s["iterations"] for s in stats]
+    relres = max(s["relres"] for s in stats)
+    ok = all(s["status"] == 0 for s in stats)
+
+    err = pressure_error(el, sim, params, args.error_steps) if args.error_steps else []
+    e2e = None
+    if not args.no_e2e:
+        e2e_value, h2d, d2h = e2e_steps(el, torch, sim, stream, params, max(3, K // 2))
+        slowest_step_s = dist.max(1.0 / e2e_value)
+        e2e = {"value": dist.world / slowest_step_s, "unit": "steps/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h}
+    sim.close()
+
+    plain = mgd = None
+    if not args.no_plain:
+        Kp = args.plain_steps or max(3, K // 4)
+        for solver, key in ((el.SOLVER_JACOBI_FP64, "plain"), (el.SOLVER_MG_FP64, "mg")):
+            p = step_params(el, solver, args.tol)
+            s2, st2 = make_sim(el, torch, n, args.seed)
+            for _ in range(W):
+                s2.step(next_dt(s2), p)
+            el_ms, stats2, _, _, _ = timed_steps(el, torch, s2, st2, p, Kp, dist)
+            el_ms = dist.max(el_ms)
+            v2, ms2 = aggregate([el_ms], Kp, dist.world)
+            rec = {"value": v2, "ms_per_step": ms2, "steps": Kp,
+                   "pcg_iterations_mean": statistics.mean(s["iterations"] for s in stats2),
+                   "relres_max": max(s["relres"] for s in stats2)}
+            if key == "plain":
+                plain = rec
+            else:
+                mgd = rec
+            s2.close()
+
+    hbm, peak_kind = peaks()
+    d = prof[dominant]
+    achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9
+    roofline = {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": None,
+                "launches": d["launches"], "avg_launch_us": d["ms"] * 1e3 / max(1, d["launches"]),
+                "bytes_per_launch": d["bytes"] / max(1, d["launches"])}
+    out = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": dist.world, "steps": K, "warmup": W,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 fields; pressure solve f32 inner / f64 refinement", "data": "synthetic",
+        "config": {"workload": f"spheres_pool {n}^3 seed {args.seed}: pool y<0.3 + 3 seeded spheres r in "
+                               f"[0.08,0.2], room walls, seeded solid box 5-10% of cells; phi WENO6/RK2, "
+                               f"velocity trilinear/RK3, g 9.8, CFL 1.0, mixed PCG to rel. resid {args.tol}",
+                   "n": n, "seed": args.seed, "parallelism": f"replicas x{dist.world}",
+                   "l2": "inputs larger than L2 (fields + solver vectors > 2 GB), no flush"},
+        "mixed": {"pcg_iterations_mean": statistics.mean(iters), "relres_max": relres, "all_converged": ok,
+                  "pressure_rel_err_vs_fp64_1e-12": err},
+        "plain_fp64": plain, "mg_fp64": mgd,
+        "mixed_over_plain": (value / plain["value"]) if plain else None,
+        "roofline": roofline, "kernel_breakdown_2_steps": breakdown, "gpu_launches": launches,
+        "clocks": clocks, "e2e": e2e,
+    }
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(n, args.seed, args.tol, steps=1)
+    return out
+
+
+# ---- the reference's CPU path (the oracle port) ------------------------------------------
+
+def cpu_baseline(n, seed, tol, steps):
+    import numpy as np
+
+    sys.path.insert(0, ROOT)
+    import oracle as O
+    from oracle import step as S
+
+    spec = _scenes_module().spheres_pool(n, seed)
+    phi, solid = O.rasterise(spec, np.float32)
+    wts = O.compute_weights(solid)
+    st = S.initial_state(phi, wts, O.cell_solid_phi(solid), O.float_dx(n, np.float32))
+    cores = os.cpu_count()
+    t0 = time.perf_counter()
+    its = []
+    for _ in range(steps):
+        dt = min(O.calc_time_step(st["u"], st["v"], st["w"], st["dx"], 1.0), 1.0 / 60.0)
+        st, _ = S.step(st, dt, 0, 1, 1, 0, 9.8, tol=tol, maxit=20000)
+        its.append(st["pcg_iterations"])
+    elapsed = time.perf_counter() - t0
+    return {"value": steps / elapsed, "unit": "steps/s", "cores": cores, "kind": "port",
+            "sample": f"{steps} full step(s) of the {n}^3 workload from the initial scene on the CPU oracle "
+                      f"(OpenMP, FP32 fields, MIC(0)-PCG FP64 to {tol}; {its} iterations), {elapsed:.1f} s"}
+
+
+def _scenes_module():
+    spec = importlib.util.spec_from_file_location("el_scenes", os.path.join(ROOT, "eulerian-liquid_gb300", "scenes.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def run_reference(args, dist):
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+    steps = max(1, min(args.steps, 2))
+    base = cpu_baseline(args.n, args.seed, args.tol, steps)
+    return {"metric": METRIC, "value": base["value"], "unit": "steps/s", "n_gpus": dist.world, "steps": steps,
+            "warmup": 0, "ms_per_step": 1e3 / base["value"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 fields; pressure f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"spheres_pool {args.n}^3 seed {args.seed} (same as our arm)",
+                       "n": args.n, "seed": args.seed, "parallelism": "host cores"},
+            "cpu_baseline": {"kind": base["kind"], "cores": base["cores"], "sample": base["sample"],
+                             "value": base["value"], "unit": "steps/s"},
+            "e2e": {"value": base["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            if dist.rank == 0:
+                print(json.dumps(run_reference(args, dist)), flush=True)
+            return 0
+        out = run_ours(args, dist)
+        if dist.rank == 0:
+            print(json.dumps(out), flush=True)
+        return 0
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

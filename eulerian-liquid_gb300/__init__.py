@@ -233,8 +233,11 @@ class Simulator:
             raise ValueError(f"{field}: shape {a.shape} != {self.shape(field)}")
         self._check(self.lib.el_upload(self.h, FIELDS[field], a.ctypes.data, a.nbytes), f"upload {field}")
 
-    def download(self, field):
-        a = np.empty(self.shape(field), dtype=self.field_dtype(field))
+    def download(self, field, out=None):
+        """Copy a field to the host (into `out`, e.g. a pinned buffer, when given)."""
+        a = out if out is not None else np.empty(self.shape(field), dtype=self.field_dtype(field))
+        if a.shape != self.shape(field) or a.dtype != self.field_dtype(field) or not a.flags.c_contiguous:
+            raise ValueError(f"{field}: output buffer must be a C-contiguous {self.field_dtype(field)} {self.shape(field)}")
         self._check(self.lib.el_download(self.h, FIELDS[field], a.ctypes.data, a.nbytes), f"download {field}")
         return a
 

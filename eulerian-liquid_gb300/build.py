@@ -2,9 +2,12 @@
 
 Every CUDA translation unit under ``csrc/`` is compiled for sm_103a only
 (``-gencode arch=compute_103a,code=sm_103a``), in parallel, then linked into one shared
-library whose exported symbols are exactly the C ABI of
-``include/eulerian_liquid_gb300.h``.  The C++ host shim (``host/``) is compiled into the same
-library.  Usage: ``python eulerian-liquid_gb300/build.py [--force]``.
+library whose exported symbols are exactly the C ABI of ``include/eulerian_liquid_gb300.h``.
+
+The C++ host interface in ``host/`` (the reference's fluid:: functions and Simulator methods
+over that ABI) is compiled on the caller's side: ``build_cpp_program`` compiles it together with
+a C++ program and links the library, as a C++ user of the reference would.
+Usage: ``python eulerian-liquid_gb300/build.py [--force]``.
 """
 
 import concurrent.futures as cf
@@ -37,18 +40,12 @@ def nvcc():
 
 def sources():
     cu = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
-    cpp = []
-    if os.path.isdir(HOST):
-        cpp = sorted(os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".cpp"))
-    return cu, cpp
+    return cu, []
 
 
 def headers():
     hs = [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
     hs += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    if os.path.isdir(HOST):
-        for dp, _, fs in os.walk(HOST):
-            hs += [os.path.join(dp, f) for f in fs if f.endswith((".h", ".hpp"))]
     return hs
 
 
@@ -89,6 +86,28 @@ def build(force=False, verbose=False):
     if verbose:
         print(LIB)
     return LIB
+
+
+def build_cpp_program(main_src, out_name, force=False):
+    """Compile a C++ program with the host interface (host/shim.cpp) against the library."""
+    lib = build()
+    out = os.path.join(OUT_DIR, out_name)
+    srcs = [main_src, os.path.join(HOST, "shim.cpp"), os.path.join(HOST, "nama_gb300.h")]
+    if not force and os.path.exists(out) and all(os.path.getmtime(f) <= os.path.getmtime(out) for f in srcs + [lib]):
+        return out
+    cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+    libdirs = [d for d in (os.path.join(cuda, "lib64"), os.path.join(cuda, "lib")) if os.path.isdir(d)]
+    cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-I", HOST, "-I",
+           os.path.join(cuda, "include"), main_src, os.path.join(HOST, "shim.cpp"), "-o", out + ".tmp", "-L", OUT_DIR,
+           "-leulerian_liquid_gb300", "-Wl,-rpath," + OUT_DIR]
+    for d in libdirs:
+        cmd += ["-L", d, "-Wl,-rpath," + d]
+    cmd += ["-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(out + ".tmp", out)
+    return out
 
 
 if __name__ == "__main__":

@@ -41,29 +41,10 @@ def scene_fields(orc, spec, dtype):
 
 def oracle_step(orc, state, dt, trace_phi, sample_phi, trace_vel, sample_vel, gravity, layers=10,
                 precond=None, tol=1e-13):
-    """update_second_order (apps/eulerian_liquid_3d.cpp:106-120) minus reinitialize(), on the oracle."""
-    s = dict(state)
-    dtype = s["phi"].dtype
-    dx = s["dx"]
-    for c, f in enumerate(("u", "v", "w")):
-        s[f], s["valid_" + f] = orc.extrapolate(s[f], s["valid_" + f], layers)
-    s["phi"], _ = orc.extrapolate(s["phi"], s["valid_phi"], layers)
-    phi_new = orc.advect_collocated(s["phi"], s["u"], s["v"], s["w"], dx, dt, trace_phi, sample_phi)
-    u, v, w = orc.advect_staggered(s["u"], s["v"], s["w"], dx, dt, trace_vel, sample_vel)
-    t = dtype.type
-    v = (v - t(t(gravity) * t(dt))).astype(dtype)
-    wu, wv, ww = s["weights"]
-    vu, vv, vw = orc.find_valid_velocity(phi_new, wu, wv, ww)
-    u = np.where(vu == 0, t(0), u).astype(dtype)
-    v = np.where(vv == 0, t(0), v).astype(dtype)
-    w = np.where(vw == 0, t(0), w).astype(dtype)
-    D, X, Y, Z, B = orc.build_matrix(phi_new, u, v, w, wu, wv, ww, dx, dt)
-    x, st, it, rr = orc.pcg(D, X, Y, Z, B, precond=orc.PRE_MIC0 if precond is None else precond, tol=tol,
-                            maxit=20000)
-    p = np.where(D > 0, x, 0.0).astype(dtype)
-    u, v, w = orc.update_velocity(u, v, w, p, phi_new, dx, dt)
-    s.update(phi=phi_new, u=u, v=v, w=w, valid_u=vu, valid_v=vv, valid_w=vw, pressure=p)
-    return s, (D, X, Y, Z, B)
+    """One step on the oracle (oracle/step.py)."""
+    from oracle import step as ostep
+    return ostep.step(state, dt, trace_phi, sample_phi, trace_vel, sample_vel, gravity, layers,
+                      orc.PRE_MIC0 if precond is None else precond, tol)
 
 
 def residual_rel(orc, mats, p):
