@@ -160,12 +160,15 @@ EL_API int el_ctx_create(int ni, int nj, int nk, double dx, int dtype, int devic
     for (int f = EL_FIELD_VALID_U; f <= EL_FIELD_VALID_PHI; ++f)
         biggest_face = std::max(biggest_face, ctx->field_bytes[f]);
     ctx->valid_tmp = (uint8_t*)ctx_alloc(ctx, biggest_face);
+    // tiles of 32 x 8 x 8 cells over the largest face grid, two maps
+    const size_t tiles = (size_t)((ni + 1 + 31) / 32) * ((nj + 1 + 7) / 8) * ((nk + 1 + 7) / 8);
+    ctx->ex_tiles = (uint8_t*)ctx_alloc(ctx, 2 * tiles);
     ctx->dscal = (Scalars*)ctx_alloc(ctx, 4 * sizeof(Scalars));
     Geom g = stencil_geom(ni, nj, nk, ctx->num_sms);
     ctx->max_partials = std::max(g.blocks(), ctx->num_sms * 8) * 2 + 64;
     ctx->partials = (double*)ctx_alloc(ctx, ctx->max_partials * sizeof(double));
     ctx->counter = (unsigned*)ctx_alloc(ctx, 64);
-    ok = ok && ctx->valid_tmp && ctx->dscal && ctx->partials && ctx->counter;
+    ok = ok && ctx->valid_tmp && ctx->ex_tiles && ctx->dscal && ctx->partials && ctx->counter;
     if (ok && cudaMallocHost(&ctx->hscal, 4 * sizeof(Scalars)) != cudaSuccess) ok = false;
     if (ok) {
         // create_grid (simulator.cpp:58-69): valid masks start at 1
@@ -187,6 +190,8 @@ EL_API int el_ctx_destroy(el_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (void* p : ctx->allocations) cudaFree(p);
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
+    for (auto& g : ctx->iter_graph)
+        if (g) cudaGraphExecDestroy(g);
     if (ctx->hscal) cudaFreeHost(ctx->hscal);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -436,7 +441,7 @@ static int build_prof(el_ctx* ctx, bool inner32) {
     double faces = 0;
     for (int c = 0; c < 3; ++c) faces += nbytes(ctx, EL_FIELD_U + c);
     double b = faces + nbytes(ctx, EL_FIELD_PHI) + N;
-    b += 2 * faces + nbytes(ctx, EL_FIELD_PHI) + N + 16 * N + 3 * N * ctx->esz + (inner32 ? 4 * N : 0);
+    b += 2 * faces + nbytes(ctx, EL_FIELD_PHI) + N + 16 * N + 3 * N * ctx->esz;
     ProfScope prof(ctx, EL_KC_BUILD, b);
     return launch_flags_build(ctx, inner32);
 }

@@ -47,15 +47,33 @@ struct Scalars {
     int count;       // fluid cells / changed cells, depending on the kernel
 };
 
-// One level of the multigrid hierarchy; level 0 aliases the fine inner matrix.
+// Active row segments of one grid level: a segment is 32 consecutive cells of one (j, k) row;
+// `desc` lists, in increasing order, the segments that hold at least one active cell
+// (diagonal > 0).  Solver kernels run one warp per listed segment.
+struct SegList {
+    int nsr = 0;            // segments per row = ceil(n0 / 32)
+    long long total = 0;    // nsr * n1 * n2
+    int4* desc = nullptr;   // active segments, ordered: {first cell index, i0, j, k}
+    int* count = nullptr;   // number of active segments (device)
+    uint8_t* flags = nullptr;
+    int* chunk = nullptr;   // scan scratch
+};
+
+// Coefficient record of one cell: diagonal and the couplings with the +x, +y, +z neighbours.
+struct Rec64 {
+    double d, x, y, z;
+};
+
+// One level of the multigrid hierarchy.  `rec` points at records of the level's type: level 0
+// half4 (mixed) or Rec64 (FP64 multigrid); coarse levels float4 or Rec64.
 template <typename V>
 struct MGLevel {
     int n0 = 0, n1 = 0, n2 = 0;
-    V* diag = nullptr;
-    V* off[3] = {nullptr, nullptr, nullptr};
+    void* rec = nullptr;
     V* b = nullptr;
     V* x = nullptr;
     V* t = nullptr;
+    SegList seg;
 };
 
 struct DeviceBuffer {
@@ -82,6 +100,7 @@ struct el_ctx {
     // advection / extrapolation ping-pong buffers (same shapes as phi, u, v, w)
     void* tmp[4] = {};
     uint8_t* valid_tmp = nullptr;  // largest face mask
+    uint8_t* ex_tiles = nullptr;   // extrapolation tile activity (two maps)
 
     // projection
     uint8_t* flags = nullptr;
@@ -91,11 +110,14 @@ struct el_ctx {
     // FP64 Krylov vectors
     double *x64 = nullptr, *r64 = nullptr, *z64 = nullptr, *p64 = nullptr, *ap64 = nullptr;
     double* p64b = nullptr;  // second direction buffer (the fused K1 writes p out of place)
-    // FP32 inner system (mixed solver)
-    float* diag32 = nullptr;
-    float* off32[3] = {};
+    // FP32 inner system (mixed solver): the PCG operator as float4 records and the level-0
+    // multigrid operator as half4 records
+    float4* A32 = nullptr;
+    ushort4* A16 = nullptr;
     float *x32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *ap32 = nullptr;
     float* p32b = nullptr;
+    el::Rec64* A64rec = nullptr;  // level-0 records of the FP64 multigrid
+    el::SegList seg0;             // active segments of the finest level
     std::vector<el::MGLevel<float>> mg32;
     std::vector<el::MGLevel<double>> mg64;
 
@@ -107,6 +129,12 @@ struct el_ctx {
 
     std::vector<void*> allocations;
     std::string last_error;
+
+    // captured CUDA graphs of PCG iteration batches, one per solver (index EL_SOLVER_*)
+    cudaGraphExec_t iter_graph[3] = {nullptr, nullptr, nullptr};
+    int iter_graph_len[3] = {0, 0, 0};
+    int iter_graph_kernels[3] = {0, 0, 0};
+    bool use_graphs = true;
 
     // per-kernel-class timing (el_ctx_profile_begin / _end)
     uint32_t prof_mask = 0;
@@ -319,39 +347,66 @@ __device__ __forceinline__ T sample_trilinear(const GridView<T>& g, T x, T y, T 
 }
 
 // Six-point WENO interpolation on nodes -2..3 at x = f in [0,1) (interpolation.h:74-111):
-// three cubic candidates in Newton form on nodes {-2..1}, {-1..2}, {0..3}; linear weights
-// C = (2-x)(3-x)/20, (3-x)(x+2)/10, (x+2)(x+1)/20; the published smoothness indicators
-// (quadratic forms / 180); alpha_s = C_s / (1e-6 + IS_s)^2; result sum(alpha p)/sum(alpha).
-// Evaluated entirely in T (the reference's float instantiation forms a few products in
-// double; the FP32 path differs from it at the 1e-7 relative level).
+// three cubic candidates on nodes {-2..1}, {-1..2}, {0..3}; linear weights
+// C = (2-x)(3-x)/20, (3-x)(x+2)/10, (x+2)(x+1)/20; smoothness indicators IS_s (the published
+// quadratic forms / 180); alpha_s = C_s / (1e-6 + IS_s)^2; result sum(alpha p) / sum(alpha).
+//
+// Evaluation here: everything that depends only on x (the candidates' Lagrange weights and the
+// linear weights) is formed once per axis and shared by all passes along that axis (36 along x,
+// 6 along y, 1 along z per sample), and each IS is written as the equivalent quadratic form in
+// the first differences d_m = v_m - v_{m-1} (the forms are translation invariant):
+//   180 IS0 = 244 d1^2 - 1171 d1 d2 + 683 d1 d3 + 1561 d2^2 - 1951 d2 d3 + 814 d3^2
+//   180 IS1 = 244 d2^2 -  781 d2 d3 + 293 d2 d4 +  961 d3^2 -  781 d3 d4 + 244 d4^2
+//   180 IS2 = 814 d3^2 - 1951 d3 d4 + 683 d3 d5 + 1561 d4^2 - 1171 d4 d5 + 244 d5^2
+// which avoids the cancellation of the value form (terms ~ v^2 cancelling to ~ d^2) in float.
 template <typename T>
-__device__ __forceinline__ T weno6_1d(T v0, T v1, T v2, T v3, T v4, T v5, T x) {
+struct WenoAxis {
+    T L[3][4];  // candidate s = sum_m L[s][m] v[s+m]
+    T C[3];     // linear weights
+};
+
+template <typename T>
+__device__ __forceinline__ WenoAxis<T> weno_axis(T x) {
+    WenoAxis<T> w;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+        // Newton form on nodes s-2, s-1, s, s+1: v_s + d e0 + d2 e0 e1 / 2 + d3 e0 e1 e2 / 6
+        const T e0 = x + T(2 - s), e1 = x + T(1 - s), e2 = x - T(s);
+        const T n1 = e0, n2 = e0 * e1 * T(0.5), n3 = e0 * e1 * e2 * T(1.0 / 6.0);
+        w.L[s][0] = T(1) - n1 + n2 - n3;
+        w.L[s][1] = n1 - T(2) * n2 + T(3) * n3;
+        w.L[s][2] = n2 - T(3) * n3;
+        w.L[s][3] = n3;
+    }
+    w.C[0] = (T(2) - x) * (T(3) - x) * T(1.0 / 20.0);
+    w.C[1] = (T(3) - x) * (x + T(2)) * T(1.0 / 10.0);
+    w.C[2] = (x + T(2)) * (x + T(1)) * T(1.0 / 20.0);
+    return w;
+}
+
+template <typename T>
+__device__ __forceinline__ T weno6_eval(const WenoAxis<T>& w, T v0, T v1, T v2, T v3, T v4, T v5) {
     const T eps = T(1e-6);
-    const T xm2 = x + T(2), xm1 = x + T(1), xp1 = x - T(1), xp2 = x - T(2), xp3 = x - T(3);
-    // candidate on nodes -2,-1,0,1
-    const T d1a = v1 - v0, d2a = v2 - T(2) * v1 + v0, d3a = v3 - T(3) * v2 + T(3) * v1 - v0;
-    const T pa = v0 + d1a * xm2 + T(0.5) * d2a * xm2 * xm1 + d3a * T(1.0 / 6.0) * xm2 * xm1 * x;
-    // candidate on nodes -1,0,1,2
-    const T d1b = v2 - v1, d2b = v3 - T(2) * v2 + v1, d3b = v4 - T(3) * v3 + T(3) * v2 - v1;
-    const T pb = v1 + d1b * xm1 + T(0.5) * d2b * xm1 * x + d3b * T(1.0 / 6.0) * xm1 * x * xp1;
-    // candidate on nodes 0,1,2,3
-    const T d1c = v3 - v2, d2c = v4 - T(2) * v3 + v2, d3c = v5 - T(3) * v4 + T(3) * v3 - v2;
-    const T pc = v2 + d1c * x + T(0.5) * d2c * x * xp1 + d3c * T(1.0 / 6.0) * x * xp1 * xp2;
-    const T ca = -xp2 * -xp3 * T(1.0 / 20.0);
-    const T cb = -xp3 * xm2 * T(1.0 / 10.0);
-    const T cc = xm2 * xm1 * T(1.0 / 20.0);
-    const T ia = (T(814) * v3 * v3 + T(4326) * v2 * v2 + T(2976) * v1 * v1 + T(244) * v0 * v0
-                  - T(3579) * v2 * v3 - T(6927) * v2 * v1 + T(1854) * v2 * v0 + T(2634) * v3 * v1
-                  - T(683) * v3 * v0 - T(1659) * v1 * v0) * T(1.0 / 180.0);
-    const T ib = (T(1986) * v3 * v3 + T(1986) * v2 * v2 + T(244) * v1 * v1 + T(244) * v4 * v4
-                  + T(1074) * v2 * v4 - T(3777) * v2 * v3 - T(1269) * v2 * v1 + T(1074) * v3 * v1
-                  - T(1269) * v4 * v3 - T(293) * v4 * v1) * T(1.0 / 180.0);
-    const T ic = (T(814) * v2 * v2 + T(4326) * v3 * v3 + T(2976) * v4 * v4 + T(244) * v5 * v5
-                  - T(683) * v2 * v5 + T(2634) * v2 * v4 - T(3579) * v2 * v3 - T(6927) * v3 * v4
-                  + T(1854) * v3 * v5 - T(1659) * v4 * v5) * T(1.0 / 180.0);
+    const T d1 = v1 - v0, d2 = v2 - v1, d3 = v3 - v2, d4 = v4 - v3, d5 = v5 - v4;
+    const T pa = w.L[0][0] * v0 + w.L[0][1] * v1 + w.L[0][2] * v2 + w.L[0][3] * v3;
+    const T pb = w.L[1][0] * v1 + w.L[1][1] * v2 + w.L[1][2] * v3 + w.L[1][3] * v4;
+    const T pc = w.L[2][0] * v2 + w.L[2][1] * v3 + w.L[2][2] * v4 + w.L[2][3] * v5;
+    const T k = T(1.0 / 180.0);
+    const T ia = (d1 * (T(244) * d1 - T(1171) * d2 + T(683) * d3) + d2 * (T(1561) * d2 - T(1951) * d3) +
+                  T(814) * d3 * d3) * k;
+    const T ib = (d2 * (T(244) * d2 - T(781) * d3 + T(293) * d4) + d3 * (T(961) * d3 - T(781) * d4) +
+                  T(244) * d4 * d4) * k;
+    const T ic = (d3 * (T(814) * d3 - T(1951) * d4 + T(683) * d5) + d4 * (T(1561) * d4 - T(1171) * d5) +
+                  T(244) * d5 * d5) * k;
     const T sa = eps + ia, sb = eps + ib, sc = eps + ic;
-    const T aa = ca / (sa * sa), ab = cb / (sb * sb), ac = cc / (sc * sc);
-    return (aa * pa + ab * pb + ac * pc) / (aa + ab + ac);
+    if constexpr (sizeof(T) == 8) {
+        const T aa = w.C[0] / (sa * sa), ab = w.C[1] / (sb * sb), ac = w.C[2] / (sc * sc);
+        return (aa * pa + ab * pb + ac * pc) / (aa + ab + ac);
+    } else {
+        // FP32: fast divisions (within 2 ulp)
+        const T aa = __fdividef(w.C[0], sa * sa), ab = __fdividef(w.C[1], sb * sb), ac = __fdividef(w.C[2], sc * sc);
+        return __fdividef(aa * pa + ab * pb + ac * pc, aa + ab + ac);
+    }
 }
 
 // weno6_interp(x, grid) in 3-D: 6^3 clamped gather at offsets -2..3; x-passes, then y, then z
@@ -363,27 +418,37 @@ __device__ __forceinline__ T sample_weno6(const GridView<T>& g, T x, T y, T z, T
     index_fraction(x, g.ox, dx, inv_dx, i, fx);
     index_fraction(y, g.oy, dx, inv_dx, j, fy);
     index_fraction(z, g.oz, dx, inv_dx, k, fz);
-    int ii[6];
-    long long jr[6], kr[6];
+    int ii[6], jr[6];
 #pragma unroll
     for (int d = 0; d < 6; ++d) {
         ii[d] = clampi(i + d - 2, 0, g.n0 - 1);
-        jr[d] = (long long)g.n0 * clampi(j + d - 2, 0, g.n1 - 1);
-        kr[d] = (long long)g.n0 * g.n1 * clampi(k + d - 2, 0, g.n2 - 1);
+        jr[d] = g.n0 * clampi(j + d - 2, 0, g.n1 - 1);
     }
+    const long long plane = (long long)g.n0 * g.n1;
+    const WenoAxis<T> wx = weno_axis(fx);
     T zl[6];
+    // the z loop stays rolled: its body (six 6-point x-passes and a y-pass) already holds
+    // plenty of independent loads, and unrolling it overflows the instruction cache
 #pragma unroll 1
     for (int dk = 0; dk < 6; ++dk) {
+        const T* base = g.d + plane * clampi(k + dk - 2, 0, g.n2 - 1);
         T yl[6];
 #pragma unroll
         for (int dj = 0; dj < 6; ++dj) {
-            const T* row = g.d + kr[dk] + jr[dj];
-            yl[dj] = weno6_1d(__ldg(row + ii[0]), __ldg(row + ii[1]), __ldg(row + ii[2]),
-                              __ldg(row + ii[3]), __ldg(row + ii[4]), __ldg(row + ii[5]), fx);
+            const T* row = base + jr[dj];
+            yl[dj] = weno6_eval(wx, __ldg(row + ii[0]), __ldg(row + ii[1]), __ldg(row + ii[2]), __ldg(row + ii[3]),
+                                __ldg(row + ii[4]), __ldg(row + ii[5]));
         }
-        zl[dk] = weno6_1d(yl[0], yl[1], yl[2], yl[3], yl[4], yl[5], fy);
+        const T zv = weno6_eval(weno_axis(fy), yl[0], yl[1], yl[2], yl[3], yl[4], yl[5]);
+        // registers, not a dynamically indexed array
+        zl[0] = dk == 0 ? zv : zl[0];
+        zl[1] = dk == 1 ? zv : zl[1];
+        zl[2] = dk == 2 ? zv : zl[2];
+        zl[3] = dk == 3 ? zv : zl[3];
+        zl[4] = dk == 4 ? zv : zl[4];
+        zl[5] = dk == 5 ? zv : zl[5];
     }
-    return weno6_1d(zl[0], zl[1], zl[2], zl[3], zl[4], zl[5], fz);
+    return weno6_eval(weno_axis(fz), zl[0], zl[1], zl[2], zl[3], zl[4], zl[5]);
 }
 
 // fraction_inside(phi_left, phi_right) (include/nama/math/level_set.h:68-80)

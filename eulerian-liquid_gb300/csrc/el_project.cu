@@ -163,8 +163,6 @@ struct CoeffOut {
     double* diag64;
     T* off[3];
     double* rhs64;
-    float* diag32;   // optional inner copies
-    float* off32[3]; // optional (only when T is double)
 };
 
 // build_matrix (projection.cpp:30-83), grid-shaped, plus |b|^2.
@@ -214,11 +212,6 @@ __global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restric
             o.rhs64[c] = b;
 #pragma unroll
             for (int a = 0; a < 3; ++a) o.off[a][c] = (T)offv[a];
-            if (o.diag32) o.diag32[c] = (float)d;
-            if (o.off32[0]) {
-#pragma unroll
-                for (int a = 0; a < 3; ++a) o.off32[a][c] = (float)offv[a];
-            }
             bb[0] += b * b;
         }
     }
@@ -385,8 +378,7 @@ static int launch_flags_build_t(el_ctx* ctx, bool inner32, bool build) {
     o.diag64 = ctx->diag64;
     o.rhs64 = ctx->rhs64;
     for (int a = 0; a < 3; ++a) o.off[a] = (T*)ctx->off[a];
-    o.diag32 = inner32 ? ctx->diag32 : nullptr;
-    for (int a = 0; a < 3; ++a) o.off32[a] = (inner32 && sizeof(T) == 8) ? ctx->off32[a] : nullptr;
+    (void)inner32;
     build_kernel<T><<<g.grid, g.block, 0, ctx->stream>>>(vel, wt, phi, ctx->flags, o, (T)ctx->dx, ctx->dscal,
                                                          ctx->partials, ctx->counter);
     return 2;

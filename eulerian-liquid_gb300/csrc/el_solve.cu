@@ -7,22 +7,34 @@
 //   EL_SOLVER_JACOBI_FP64  plain FP64 PCG, Jacobi preconditioner (the correctness baseline)
 //   EL_SOLVER_MG_FP64      FP64 PCG with a multigrid V-cycle preconditioner
 //   EL_SOLVER_MIXED        FP64 iterative refinement: r = b - A x in FP64, the correction
-//                          solved by FP32 multigrid PCG on the FP32 copy of the matrix,
-//                          x += |r| * e accumulated in FP64
+//                          solved by FP32 multigrid PCG on the FP32 operator, x += |r| e in FP64
+//
+// Work distribution: every level keeps an ordered list of its active row segments (32 cells
+// of one (j, k) row holding at least one cell with a positive diagonal).  Kernels run one
+// warp per listed segment with a fixed grid, so cells that are air or solid cost nothing,
+// all loads of a cell are issued before any is used, and the partial sums of the dot
+// products are formed in a fixed order (deterministic).  Vector entries outside the active
+// segments are never written; they stay finite and always meet a zero coupling.
+//
+// Operators are stored as per-cell records {diagonal, coupling with +x, +y, +z}: float4 for
+// the FP32 PCG operator, Rec64 for the FP64 multigrid, and half4 for the level-0 operator the
+// FP32 multigrid smooths with (diagonal rounded up, couplings rounded towards zero, so the
+// record operator stays diagonally dominant, hence SPD).
 //
 // Multigrid: coarse operators by aggregation of 2x2x2 blocks scaled by 1/2
-// (A_c = 1/2 P^T A P with piecewise-constant P, which reproduces the rediscretised Laplacian
-// for constant coefficients and carries the ghost-fluid Dirichlet terms down by summation),
+// (A_c = 1/2 P^T A P, piecewise-constant P; it reproduces the rediscretised Laplacian for
+// constant coefficients and carries the ghost-fluid Dirichlet terms down by summation),
 // restriction R = P^T, damped Jacobi (omega = 0.8) with two sweeps before and two after, and
-// 30 Jacobi sweeps on the coarsest level (at most 8 cells per axis) in one block's shared
-// memory.  Same smoother before and after and R = P^T make the V-cycle a symmetric
-// operator, as PCG needs.
+// 30 sweeps on the coarsest level (at most 8 cells per axis) in one block's shared memory.
+// Same smoother on both legs and R = P^T make the V-cycle symmetric, as PCG needs.
 //
 // Per PCG iteration:  K1  p = z + beta p ; Ap = A p ; alpha = rz / p.Ap
 //                     K2  x += alpha p ; r -= alpha Ap ; rr = r.r (; rz = r.D^-1 r for Jacobi)
 //                     V   z = M^-1 r ; rz = r.z ; beta            (multigrid solvers)
 // Scalars live in device memory; once converged the remaining launched kernels return at
 // entry, so the host polls only every `check_every` iterations.
+#include <cuda_fp16.h>
+
 #include "el_internal.cuh"
 
 namespace el {
@@ -31,65 +43,387 @@ constexpr double kOmega = 0.8;
 constexpr int kCoarsestSweeps = 30;
 constexpr int kCoarsestMaxDim = 8;
 constexpr int kCoarsestMaxCells = 512;
-
-template <typename DT, typename OT>
-struct Stencil {
-    int n0, n1, n2;
-    const DT* __restrict__ diag;
-    const OT* __restrict__ ox;
-    const OT* __restrict__ oy;
-    const OT* __restrict__ oz;
-};
-
-// (A y)(c) for y given by a functor of the neighbour's linear index and coordinates;
-// neighbours outside the grid are skipped (their couplings are zero anyway).
-template <typename V, typename DT, typename OT, typename F>
-__device__ __forceinline__ V apply_row(const Stencil<DT, OT>& A, int i, int j, int k, long long c, V yc,
-                                       F&& y) {
-    const long long s1 = A.n0, s2 = (long long)A.n0 * A.n1;
-    V s = (V)A.diag[c] * yc;
-    if (i > 0) s += (V)A.ox[c - 1] * y(c - 1, i - 1, j, k);
-    if (i < A.n0 - 1) s += (V)A.ox[c] * y(c + 1, i + 1, j, k);
-    if (j > 0) s += (V)A.oy[c - s1] * y(c - s1, i, j - 1, k);
-    if (j < A.n1 - 1) s += (V)A.oy[c] * y(c + s1, i, j + 1, k);
-    if (k > 0) s += (V)A.oz[c - s2] * y(c - s2, i, j, k - 1);
-    if (k < A.n2 - 1) s += (V)A.oz[c] * y(c + s2, i, j, k + 1);
-    return s;
-}
+constexpr int kSegThreads = 256;
 
 __device__ __forceinline__ bool finite_d(double v) { return isfinite(v); }
 
 // ---------------------------------------------------------------------------------------
-// K1: new search direction fused with the SpMV and p.Ap.  JAC: z = r / diag on the fly.
-template <typename V, typename DT, typename OT, bool JAC>
-__global__ void __launch_bounds__(256) dir_spmv_kernel(Stencil<DT, OT> A, const V* __restrict__ zr,
-                                                       const V* __restrict__ p_in, V* __restrict__ p_out,
-                                                       V* __restrict__ ap, Scalars* s, int first,
-                                                       double* partials, unsigned* counter) {
+// coefficient records
+
+template <typename V>
+struct Co {
+    V d, x, y, z;
+};
+
+__device__ __forceinline__ Co<float> ldrec(const float4* r, long long c) {
+    const float4 v = __ldg(r + c);
+    return {v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ Co<float> ldrec(const ushort4* r, long long c) {
+    const ushort4 v = __ldg(r + c);
+    return {__half2float(__ushort_as_half(v.x)), __half2float(__ushort_as_half(v.y)),
+            __half2float(__ushort_as_half(v.z)), __half2float(__ushort_as_half(v.w))};
+}
+__device__ __forceinline__ Co<double> ldrec(const Rec64* r, long long c) {
+    const double2* p = reinterpret_cast<const double2*>(r + c);
+    const double2 a = __ldg(p), b = __ldg(p + 1);
+    return {a.x, a.y, b.x, b.y};
+}
+
+// The FP64 operator of the context: diag64 plus three coupling arrays of the field type.
+template <typename OT>
+struct SplitOp {
+    const double* __restrict__ d;
+    const OT* __restrict__ x;
+    const OT* __restrict__ y;
+    const OT* __restrict__ z;
+};
+
+// ---------------------------------------------------------------------------------------
+// segment geometry
+
+struct LGeom {
+    int n0, n1, n2, nsr;
+    int s1, s2;  // strides of j and k (every grid holds fewer than 2^31 cells)
+};
+
+inline LGeom make_geom(int n0, int n1, int n2) {
+    return LGeom{n0, n1, n2, (n0 + 31) / 32, n0, n0 * n1};
+}
+
+__device__ __forceinline__ void seg_cell(int id, const LGeom& g, int lane, int& i, int& j, int& k) {
+    const int row = id / g.nsr;
+    i = (id - row * g.nsr) * 32 + lane;
+    j = row % g.n1;
+    k = row / g.n1;
+}
+
+struct SegArg {
+    const int4* __restrict__ desc;  // {first cell index, i0, j, k}
+    const int* __restrict__ count;
+};
+
+// Walks the active segments, one warp per segment; defines lane, i, j, k, c (cell index, int:
+// every grid holds fewer than 2^31 cells) and live (i < n0).  Lanes past the row end stay in
+// the loop (live = false) so that warp shuffles see all 32 lanes.
+#define SEG_LOOP_ALL_BEGIN(seg, g)                                                \
+    const int lane = threadIdx.x & 31;                                            \
+    const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;         \
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;                             \
+    const int nseg = *(seg).count;                                                \
+    for (int qs = warp_global; qs < nseg; qs += nwarps) {                         \
+        const int4 sd = (seg).desc[qs];                                           \
+        const int i = sd.y + lane, j = sd.z, k = sd.w;                            \
+        const int c = sd.x + lane;                                                \
+        const bool live = i < (g).n0;
+
+#define SEG_LOOP_BEGIN(seg, g) \
+    SEG_LOOP_ALL_BEGIN(seg, g) \
+    if (!live) continue;
+
+#define SEG_LOOP_END }
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// ---------------------------------------------------------------------------------------
+// segment lists: per-segment activity flag, then an ordered compaction
+
+constexpr int kSegChunk = 1024;
+
+template <typename R>
+__global__ void seg_flags_rec_kernel(LGeom g, const R* __restrict__ rec, long long total, uint8_t* __restrict__ flags) {
+    const int lane = threadIdx.x & 31;
+    const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long id = w0; id < total; id += nw) {
+        int i, j, k;
+        seg_cell((int)id, g, lane, i, j, k);
+        bool act = false;
+        if (i < g.n0) act = ldrec(rec, i + g.s1 * j + g.s2 * k).d > 0;
+        const unsigned m = __ballot_sync(0xffffffffu, act);
+        if (lane == 0) flags[id] = m ? 1 : 0;
+    }
+}
+
+__global__ void seg_flags_diag_kernel(LGeom g, const double* __restrict__ diag, long long total,
+                                      uint8_t* __restrict__ flags) {
+    const int lane = threadIdx.x & 31;
+    const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long id = w0; id < total; id += nw) {
+        int i, j, k;
+        seg_cell((int)id, g, lane, i, j, k);
+        bool act = false;
+        if (i < g.n0) act = diag[i + g.s1 * j + g.s2 * k] > 0;
+        const unsigned m = __ballot_sync(0xffffffffu, act);
+        if (lane == 0) flags[id] = m ? 1 : 0;
+    }
+}
+
+__global__ void seg_count_kernel(const uint8_t* __restrict__ flags, long long total, int* __restrict__ chunk) {
+    __shared__ int sh[8];
+    const long long base = (long long)blockIdx.x * kSegChunk;
+    int cnt = 0;
+    for (int q = threadIdx.x; q < kSegChunk; q += blockDim.x) {
+        const long long id = base + q;
+        if (id < total && flags[id]) ++cnt;
+    }
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+        chunk[blockIdx.x] = t;
+    }
+}
+
+__global__ void seg_scan_kernel(int* __restrict__ chunk, int nchunks, int* __restrict__ total_out) {
+    __shared__ int span[1024];
+    const int per = (nchunks + blockDim.x - 1) / blockDim.x;
+    const int lo = threadIdx.x * per, hi = min(nchunks, lo + per);
+    int s = 0;
+    for (int q = lo; q < hi; ++q) s += chunk[q];
+    span[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int t = 0; t < (int)blockDim.x; ++t) {
+            const int v = span[t];
+            span[t] = run;
+            run += v;
+        }
+        *total_out = run;
+    }
+    __syncthreads();
+    int run = span[threadIdx.x];
+    for (int q = lo; q < hi; ++q) {
+        const int v = chunk[q];
+        chunk[q] = run;
+        run += v;
+    }
+}
+
+__global__ void seg_write_kernel(LGeom g, const uint8_t* __restrict__ flags, long long total,
+                                 const int* __restrict__ chunk, int4* __restrict__ desc) {
+    const long long base = (long long)blockIdx.x * kSegChunk;
+    const int lane = threadIdx.x;
+    int run = chunk[blockIdx.x];
+    for (int q = 0; q < kSegChunk; q += 32) {
+        const long long id = base + q + lane;
+        const bool f = id < total && flags[id];
+        const unsigned m = __ballot_sync(0xffffffffu, f);
+        if (f) {
+            int i0, j, k;
+            seg_cell((int)id, g, 0, i0, j, k);
+            desc[run + __popc(m & ((1u << lane) - 1u))] = make_int4((int)(i0 + g.s1 * j + g.s2 * k), i0, j, k);
+        }
+        run += __popc(m);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// operator packing (once per solve)
+
+// float4 PCG records and half4 multigrid records of the FP32 inner system.
+template <typename OT>
+__global__ void pack32_kernel(long long n, const double* __restrict__ d, const OT* __restrict__ ox,
+                              const OT* __restrict__ oy, const OT* __restrict__ oz, float4* __restrict__ a32,
+                              ushort4* __restrict__ a16) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        const float4 r = make_float4((float)d[c], (float)ox[c], (float)oy[c], (float)oz[c]);
+        a32[c] = r;
+        // diagonal rounded up, (non-positive) couplings rounded towards zero: the half record
+        // operator keeps diag >= sum |couplings| row by row
+        a16[c] = make_ushort4(__half_as_ushort(__float2half_ru(r.x)), __half_as_ushort(__float2half_rz(r.y)),
+                              __half_as_ushort(__float2half_rz(r.z)), __half_as_ushort(__float2half_rz(r.w)));
+    }
+}
+
+template <typename OT>
+__global__ void pack64_kernel(long long n, const double* __restrict__ d, const OT* __restrict__ ox,
+                              const OT* __restrict__ oy, const OT* __restrict__ oz, Rec64* __restrict__ a) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        a[c] = Rec64{d[c], (double)ox[c], (double)oy[c], (double)oz[c]};
+}
+
+// Coarse records A_c = 1/2 P^T A P over 2x2x2 blocks.
+template <typename RF, typename RC>
+__global__ void coarsen_kernel(LGeom F, const RF* __restrict__ fr, LGeom C, RC* __restrict__ cr) {
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    const int K = blockIdx.z;
+    if (I >= C.n0 || J >= C.n1) return;
+    double d = 0, sx = 0, sy = 0, sz = 0, inner = 0;
+    for (int kk = 0; kk < 2; ++kk)
+        for (int jj = 0; jj < 2; ++jj)
+            for (int ii = 0; ii < 2; ++ii) {
+                const int i = 2 * I + ii, j = 2 * J + jj, k = 2 * K + kk;
+                if (i >= F.n0 || j >= F.n1 || k >= F.n2) continue;
+                const auto r = ldrec(fr, i + F.s1 * j + F.s2 * k);
+                d += r.d;
+                if (ii == 0) inner += r.x; else sx += r.x;
+                if (jj == 0) inner += r.y; else sy += r.y;
+                if (kk == 0) inner += r.z; else sz += r.z;
+            }
+    double dc = 0.5 * (d + 2.0 * inner);
+    // an aggregate coupled to nothing outside it (an enclosed Neumann pocket) has a zero row
+    // sum; its diagonal is raised to half the children's, which keeps the operator SPD
+    if (d > 0 && !(dc > 1e-6 * d)) dc = 0.5 * d;
+    const long long q = I + C.s1 * J + C.s2 * K;
+    if constexpr (sizeof(RC) == sizeof(float4))
+        cr[q] = make_float4((float)dc, (float)(0.5 * sx), (float)(0.5 * sy), (float)(0.5 * sz));
+    else
+        cr[q] = Rec64{dc, 0.5 * sx, 0.5 * sy, 0.5 * sz};
+}
+
+// ---------------------------------------------------------------------------------------
+// The 7-point stencil around each lane's cell.  recf(q) loads a cell's record (diagonal and
+// +x/+y/+z couplings), rawf(q, qi, qj, qk) loads the vector data of a cell and valf(raw, rec)
+// turns it into the value the stencil applies to.  Every load of the stencil (including the
+// cells just outside the segment, fetched by lanes 0 and 31) is issued before any value is
+// formed, so a lane waits for memory once; the i-neighbours of the other lanes come by shuffle.
+// ALL: every neighbour's record is needed (for its diagonal); else only those carrying a
+// coupling (-x, -y, -z) are loaded.  Must be called by all 32 lanes.
+template <typename V>
+struct St7 {
+    V v0, vxm, vxp, vym, vyp, vzm, vzp;  // values at the centre and the six neighbours
+    V d, cxm, cxp, cym, cyp, czm, czp;   // diagonal and couplings
+};
+
+template <typename V, bool ALL, typename RF, typename LF, typename VF>
+__device__ __forceinline__ St7<V> gather7(const LGeom& g, int c, int i, int j, int k, bool live, int lane, RF&& recf,
+                                          LF&& rawf, VF&& valf) {
+    const Co<V> z4{V(0), V(0), V(0), V(0)};
+    const bool iym = live && j > 0, iyp = live && j < g.n1 - 1;
+    const bool izm = live && k > 0, izp = live && k < g.n2 - 1;
+    const bool ixm = lane == 0 && live && i > 0;
+    const bool ixp = lane == 31 && live && i + 1 < g.n0;
+    // loads
+    const Co<V> r0 = live ? recf(c) : z4;
+    const Co<V> rym = iym ? recf(c - g.s1) : z4;
+    const Co<V> ryp = (ALL && iyp) ? recf(c + g.s1) : z4;
+    const Co<V> rzm = izm ? recf(c - g.s2) : z4;
+    const Co<V> rzp = (ALL && izp) ? recf(c + g.s2) : z4;
+    const Co<V> rxm = ixm ? recf(c - 1) : z4;
+    const Co<V> rxp = (ALL && ixp) ? recf(c + 1) : z4;
+    using Raw = decltype(rawf(0, 0, 0, 0));
+    const Raw a0 = live ? rawf(c, i, j, k) : Raw{};
+    const Raw aym = iym ? rawf(c - g.s1, i, j - 1, k) : Raw{};
+    const Raw ayp = iyp ? rawf(c + g.s1, i, j + 1, k) : Raw{};
+    const Raw azm = izm ? rawf(c - g.s2, i, j, k - 1) : Raw{};
+    const Raw azp = izp ? rawf(c + g.s2, i, j, k + 1) : Raw{};
+    const Raw axm = ixm ? rawf(c - 1, i - 1, j, k) : Raw{};
+    const Raw axp = ixp ? rawf(c + 1, i + 1, j, k) : Raw{};
+    // values and couplings
+    St7<V> st;
+    st.d = r0.d;
+    st.cxp = r0.x;
+    st.cyp = r0.y;
+    st.czp = r0.z;
+    st.cym = rym.y;
+    st.czm = rzm.z;
+    st.v0 = live ? valf(a0, r0) : V(0);
+    st.vym = iym ? valf(aym, rym) : V(0);
+    st.vyp = iyp ? valf(ayp, ryp) : V(0);
+    st.vzm = izm ? valf(azm, rzm) : V(0);
+    st.vzp = izp ? valf(azp, rzp) : V(0);
+    const V sxm = __shfl_up_sync(kFull, st.v0, 1);
+    const V sxp = __shfl_down_sync(kFull, st.v0, 1);
+    const V scm = __shfl_up_sync(kFull, r0.x, 1);
+    st.vxm = lane == 0 ? (ixm ? valf(axm, rxm) : V(0)) : sxm;
+    st.cxm = lane == 0 ? rxm.x : scm;
+    st.vxp = (live && i + 1 < g.n0) ? (lane == 31 ? valf(axp, rxp) : sxp) : V(0);
+    return st;
+}
+
+template <typename V>
+__device__ __forceinline__ V apply7(const St7<V>& st) {
+    return st.d * st.v0 + st.cxm * st.vxm + st.cxp * st.vxp + st.cym * st.vym + st.cyp * st.vyp + st.czm * st.vzm +
+           st.czp * st.vzp;
+}
+
+template <typename V, typename R>
+struct RecLoad {
+    const R* __restrict__ a;
+    __device__ __forceinline__ Co<V> operator()(int q) const {
+        const auto r = ldrec(a, q);
+        return Co<V>{(V)r.d, (V)r.x, (V)r.y, (V)r.z};
+    }
+};
+
+template <typename OT>
+struct SplitLoad {
+    SplitOp<OT> a;
+    __device__ __forceinline__ Co<double> operator()(int q) const {
+        return Co<double>{a.d[q], (double)a.x[q], (double)a.y[q], (double)a.z[q]};
+    }
+};
+
+// K1: new direction fused with A p and p.Ap over the active segments.
+// Record operator (FP32 inner / FP64 multigrid).
+template <typename V, typename R>
+__global__ void __launch_bounds__(kSegThreads) dir_spmv_rec_kernel(LGeom g, SegArg seg, const R* __restrict__ A,
+                                                                   const V* __restrict__ z, const V* __restrict__ p_in,
+                                                                   V* __restrict__ p_out, V* __restrict__ ap,
+                                                                   Scalars* s, int first, double* partials,
+                                                                   unsigned* counter) {
     if (s->done) return;
     const V beta = first ? V(0) : (V)s->beta;
-    auto pn = [&](long long q, int, int, int) -> V {
-        const DT d = A.diag[q];
-        if (d == DT(0)) return V(0);
-        const V z = JAC ? zr[q] / (V)d : zr[q];
-        return first ? z : z + beta * p_in[q];
-    };
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
     double acc[1] = {0.0};
-    if (i < A.n0 && j < A.n1) {
-        for (int k = blockIdx.z; k < A.n2; k += gridDim.z) {
-            const long long c = lin3(i, j, k, A.n0, A.n1);
-            V pc = V(0), apc = V(0);
-            if (A.diag[c] != DT(0)) {
-                pc = pn(c, i, j, k);
-                apc = apply_row<V>(A, i, j, k, c, pc, pn);
-            }
-            p_out[c] = pc;
-            ap[c] = apc;
-            acc[0] += (double)pc * (double)apc;
+    const RecLoad<V, R> recf{A};
+    auto rawf = [&](int q, int, int, int) -> V { return first ? z[q] : z[q] + beta * p_in[q]; };
+    auto valf = [](V raw, const Co<V>&) -> V { return raw; };
+    SEG_LOOP_ALL_BEGIN(seg, g)
+    const St7<V> st = gather7<V, false>(g, c, i, j, k, live, lane, recf, rawf, valf);
+    if (live) {
+        V pc = V(0), apc = V(0);
+        if (st.d > V(0)) {
+            pc = st.v0;
+            apc = apply7(st);
+        }
+        p_out[c] = pc;
+        ap[c] = apc;
+        acc[0] += (double)pc * (double)apc;
+    }
+    SEG_LOOP_END
+    double tot[1];
+    if (grid_sum<1>(acc, partials, counter, tot)) {
+        const double alpha = s->rz / tot[0];
+        s->alpha = alpha;
+        if (!finite_d(alpha)) {
+            s->bad = 1;
+            s->done = 1;
         }
     }
+}
+
+// Split FP64 operator with the Jacobi preconditioner applied on the fly (plain FP64 PCG).
+template <typename OT>
+__global__ void __launch_bounds__(kSegThreads) dir_spmv_jacobi_kernel(LGeom g, SegArg seg, SplitOp<OT> A,
+                                                                      const double* __restrict__ r,
+                                                                      const double* __restrict__ p_in,
+                                                                      double* __restrict__ p_out,
+                                                                      double* __restrict__ ap, Scalars* s, int first,
+                                                                      double* partials, unsigned* counter) {
+    if (s->done) return;
+    const double beta = first ? 0.0 : s->beta;
+    double acc[1] = {0.0};
+    const SplitLoad<OT> recf{A};
+    // raw = (r, p) packed as a pair of doubles
+    auto rawf = [&](int q, int, int, int) -> double2 { return make_double2(r[q], first ? 0.0 : p_in[q]); };
+    auto valf = [&](double2 raw, const Co<double>& rec) -> double {
+        return rec.d > 0.0 ? raw.x / rec.d + beta * raw.y : 0.0;
+    };
+    SEG_LOOP_ALL_BEGIN(seg, g)
+    const St7<double> st = gather7<double, true>(g, c, i, j, k, live, lane, recf, rawf, valf);
+    if (live) {
+        const double apc = st.d > 0.0 ? apply7(st) : 0.0;
+        p_out[c] = st.v0;
+        ap[c] = apc;
+        acc[0] += st.v0 * apc;
+    }
+    SEG_LOOP_END
     double tot[1];
     if (grid_sum<1>(acc, partials, counter, tot)) {
         const double alpha = s->rz / tot[0];
@@ -102,25 +436,25 @@ __global__ void __launch_bounds__(256) dir_spmv_kernel(Stencil<DT, OT> A, const 
 }
 
 // K2: x += alpha p ; r -= alpha Ap ; |r|^2 (and r.D^-1 r for Jacobi, giving beta).
-template <typename V, typename DT, bool JAC>
-__global__ void __launch_bounds__(256) update_kernel(long long n, const DT* __restrict__ diag,
-                                                     V* __restrict__ x, V* __restrict__ r,
-                                                     const V* __restrict__ p, const V* __restrict__ ap,
-                                                     Scalars* s, double* partials, unsigned* counter) {
+template <typename V, bool JAC>
+__global__ void __launch_bounds__(kSegThreads) update_kernel(LGeom g, SegArg seg, const double* __restrict__ diag,
+                                                             V* __restrict__ x, V* __restrict__ r,
+                                                             const V* __restrict__ p, const V* __restrict__ ap,
+                                                             Scalars* s, double* partials, unsigned* counter) {
     if (s->done) return;
     const V alpha = (V)s->alpha;
     double acc[2] = {0.0, 0.0};
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-         c += (long long)gridDim.x * blockDim.x) {
-        const V rc = r[c] - alpha * ap[c];
-        x[c] = x[c] + alpha * p[c];
-        r[c] = rc;
-        acc[0] += (double)rc * (double)rc;
-        if (JAC) {
-            const DT d = diag[c];
-            if (d != DT(0)) acc[1] += (double)rc * (double)(rc / (V)d);
-        }
+    SEG_LOOP_BEGIN(seg, g)
+    const V pc = p[c], apc = ap[c], xc = x[c], rc0 = r[c];
+    const V rc = rc0 - alpha * apc;
+    x[c] = xc + alpha * pc;
+    r[c] = rc;
+    acc[0] += (double)rc * (double)rc;
+    if (JAC) {
+        const double d = diag[c];
+        if (d > 0.0) acc[1] += (double)rc * ((double)rc / d);
     }
+    SEG_LOOP_END
     double tot[2];
     if (grid_sum<2>(acc, partials, counter, tot)) {
         s->rr = tot[0];
@@ -139,27 +473,24 @@ __global__ void __launch_bounds__(256) update_kernel(long long n, const DT* __re
 }
 
 // Jacobi start: rz = r . D^-1 r
-template <typename V, typename DT>
-__global__ void jacobi_rz_kernel(long long n, const DT* __restrict__ diag, const V* __restrict__ r, Scalars* s,
-                                 double* partials, unsigned* counter) {
+__global__ void jacobi_rz_kernel(LGeom g, SegArg seg, const double* __restrict__ diag, const double* __restrict__ r,
+                                 Scalars* s, double* partials, unsigned* counter) {
     double acc[1] = {0.0};
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-         c += (long long)gridDim.x * blockDim.x) {
-        const DT d = diag[c];
-        if (d != DT(0)) acc[0] += (double)r[c] * (double)(r[c] / (V)d);
-    }
+    SEG_LOOP_BEGIN(seg, g)
+    const double d = diag[c];
+    if (d > 0.0) acc[0] += r[c] * (r[c] / d);
+    SEG_LOOP_END
     double tot[1];
     if (grid_sum<1>(acc, partials, counter, tot)) s->rz = tot[0];
 }
 
-// solve start (outer / plain): x = 0, r = b, thresholds.
-__global__ void solve_init_kernel(long long n, const double* __restrict__ b, double* __restrict__ x,
+// solve start (outer / plain): x = 0, r = b on the active segments, thresholds.
+__global__ void solve_init_kernel(LGeom g, SegArg seg, const double* __restrict__ b, double* __restrict__ x,
                                   double* __restrict__ r, Scalars* s, double tol) {
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-         c += (long long)gridDim.x * blockDim.x) {
-        x[c] = 0.0;
-        r[c] = b[c];
-    }
+    SEG_LOOP_BEGIN(seg, g)
+    x[c] = 0.0;
+    r[c] = b[c];
+    SEG_LOOP_END
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         const double bb = s->bb;
         s->thresh = tol * tol * bb;
@@ -172,19 +503,18 @@ __global__ void solve_init_kernel(long long n, const double* __restrict__ b, dou
 }
 
 // mixed solver: inner system r32 = r64 / |r64|, x32 = 0, inner thresholds.
-__global__ void inner_init_kernel(long long n, const double* __restrict__ r64, float* __restrict__ r32,
+__global__ void inner_init_kernel(LGeom g, SegArg seg, const double* __restrict__ r64, float* __restrict__ r32,
                                   float* __restrict__ x32, const Scalars* so, Scalars* si, double tau,
                                   double* partials, unsigned* counter) {
     const double norm = sqrt(so->rr);
     const double inv = norm > 0.0 ? 1.0 / norm : 0.0;
     double acc[1] = {0.0};
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-         c += (long long)gridDim.x * blockDim.x) {
-        const float v = (float)(r64[c] * inv);
-        r32[c] = v;
-        x32[c] = 0.0f;
-        acc[0] += (double)v * (double)v;
-    }
+    SEG_LOOP_BEGIN(seg, g)
+    const float v = (float)(r64[c] * inv);
+    r32[c] = v;
+    x32[c] = 0.0f;
+    acc[0] += (double)v * (double)v;
+    SEG_LOOP_END
     double tot[1];
     if (grid_sum<1>(acc, partials, counter, tot)) {
         si->bb = tot[0];
@@ -199,32 +529,32 @@ __global__ void inner_init_kernel(long long n, const double* __restrict__ r64, f
 }
 
 // mixed solver: x64 += |r| * x32
-__global__ void accumulate_kernel(long long n, double* __restrict__ x64, const float* __restrict__ x32,
+__global__ void accumulate_kernel(LGeom g, SegArg seg, double* __restrict__ x64, const float* __restrict__ x32,
                                   const Scalars* si) {
     const double norm = si->norm;
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-         c += (long long)gridDim.x * blockDim.x)
-        x64[c] += norm * (double)x32[c];
+    SEG_LOOP_BEGIN(seg, g)
+    x64[c] += norm * (double)x32[c];
+    SEG_LOOP_END
 }
 
 // FP64 residual r = b - A x and |r|^2 (outer refinement step).
 template <typename OT>
-__global__ void __launch_bounds__(256) residual_kernel(Stencil<double, OT> A, const double* __restrict__ b,
-                                                       const double* __restrict__ x, double* __restrict__ r,
-                                                       Scalars* s, double* partials, unsigned* counter) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+__global__ void __launch_bounds__(kSegThreads) residual_kernel(LGeom g, SegArg seg, SplitOp<OT> A,
+                                                               const double* __restrict__ b,
+                                                               const double* __restrict__ x, double* __restrict__ r,
+                                                               Scalars* s, double* partials, unsigned* counter) {
     double acc[1] = {0.0};
-    auto xv = [&](long long q, int, int, int) -> double { return x[q]; };
-    if (i < A.n0 && j < A.n1) {
-        for (int k = blockIdx.z; k < A.n2; k += gridDim.z) {
-            const long long c = lin3(i, j, k, A.n0, A.n1);
-            double rc = 0.0;
-            if (A.diag[c] != 0.0) rc = b[c] - apply_row<double>(A, i, j, k, c, x[c], xv);
-            r[c] = rc;
-            acc[0] += rc * rc;
-        }
+    const SplitLoad<OT> recf{A};
+    auto rawf = [&](int q, int, int, int) -> double { return x[q]; };
+    auto valf = [](double raw, const Co<double>&) -> double { return raw; };
+    SEG_LOOP_ALL_BEGIN(seg, g)
+    const St7<double> st = gather7<double, false>(g, c, i, j, k, live, lane, recf, rawf, valf);
+    if (live) {
+        const double rc = st.d > 0.0 ? b[c] - apply7(st) : 0.0;
+        r[c] = rc;
+        acc[0] += rc * rc;
     }
+    SEG_LOOP_END
     double tot[1];
     if (grid_sum<1>(acc, partials, counter, tot)) {
         s->rr = tot[0];
@@ -237,99 +567,47 @@ __global__ void __launch_bounds__(256) residual_kernel(Stencil<double, OT> A, co
     }
 }
 
-template <typename S, typename D>
-__global__ void convert_kernel(long long n, const S* __restrict__ a, D* __restrict__ b) {
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-         c += (long long)gridDim.x * blockDim.x)
-        b[c] = (D)a[c];
-}
 
 // ---------------------------------------------------------------------------------------
-// multigrid kernels
-
-template <typename V>
-struct Level {
-    int n0, n1, n2;
-    const V* __restrict__ diag;
-    const V* __restrict__ ox;
-    const V* __restrict__ oy;
-    const V* __restrict__ oz;
-};
-
-template <typename V>
-__device__ __forceinline__ Stencil<V, V> as_stencil(const Level<V>& L) {
-    return Stencil<V, V>{L.n0, L.n1, L.n2, L.diag, L.ox, L.oy, L.oz};
-}
-
-// Coarse operator A_c = 1/2 P^T A P over 2x2x2 blocks.
-template <typename V>
-__global__ void coarsen_kernel(Level<V> F, int m0, int m1, int m2, V* __restrict__ cd, V* __restrict__ cx,
-                               V* __restrict__ cy, V* __restrict__ cz) {
-    const int I = blockIdx.x * blockDim.x + threadIdx.x;
-    const int J = blockIdx.y * blockDim.y + threadIdx.y;
-    const int K = blockIdx.z;
-    if (I >= m0 || J >= m1) return;
-    V d = 0, sx = 0, sy = 0, sz = 0, inner = 0;
-    for (int kk = 0; kk < 2; ++kk)
-        for (int jj = 0; jj < 2; ++jj)
-            for (int ii = 0; ii < 2; ++ii) {
-                const int i = 2 * I + ii, j = 2 * J + jj, k = 2 * K + kk;
-                if (i >= F.n0 || j >= F.n1 || k >= F.n2) continue;
-                const long long c = lin3(i, j, k, F.n0, F.n1);
-                d += F.diag[c];
-                if (ii == 0) inner += F.ox[c]; else sx += F.ox[c];
-                if (jj == 0) inner += F.oy[c]; else sy += F.oy[c];
-                if (kk == 0) inner += F.oz[c]; else sz += F.oz[c];
-            }
-    V dc = V(0.5) * (d + V(2) * inner);
-    const long long q = lin3(I, J, K, m0, m1);
-    // an aggregate with no coupling to anything outside it (an enclosed Neumann pocket) has
-    // a zero row sum; it is left out of the coarse problem
-    const bool active = dc > V(1e-30) * (d > V(0) ? d : V(1));
-    cd[q] = active ? dc : V(0);
-    cx[q] = active ? V(0.5) * sx : V(0);
-    cy[q] = active ? V(0.5) * sy : V(0);
-    cz[q] = active ? V(0.5) * sz : V(0);
-}
-
-// Smoothing sweeps.  MODE 0: two sweeps from x = 0 (the first, omega b / D, formed on the
-// fly).  MODE 1: one sweep from x_in + P e (e = coarse correction, formed on the fly).
-// MODE 2: one sweep from x_in.  DOT (level 0, last sweep): rz = b . x_out and beta.
+// multigrid smoothing over the active segments of one level
+//
+// MODE 0: two sweeps from x = 0 (the first, omega b / D, formed on the fly)
+// MODE 1: one sweep from x_in + P e (e = coarse correction, formed on the fly)
+// MODE 2: one sweep from x_in.   DOT (finest level, last sweep): rz = b . x_out and beta.
 enum { SM_ZERO2 = 0, SM_PROLONG = 1, SM_PLAIN = 2 };
 enum { DOT_NONE = 0, DOT_INIT = 1, DOT_BETA = 2 };
 
-template <typename V, int MODE, int DOT>
-__global__ void __launch_bounds__(256) smooth_kernel(Level<V> L, const V* __restrict__ b, const V* __restrict__ x_in,
-                                                     const V* __restrict__ e, int m0, int m1,
-                                                     V* __restrict__ x_out, Scalars* s, double* partials,
-                                                     unsigned* counter) {
+template <typename V, typename R, int MODE, int DOT>
+__global__ void __launch_bounds__(kSegThreads) smooth_kernel(LGeom g, SegArg seg, const R* __restrict__ A,
+                                                             const V* __restrict__ b, const V* __restrict__ x_in,
+                                                             LGeom gc, const V* __restrict__ e,
+                                                             V* __restrict__ x_out, Scalars* s, double* partials,
+                                                             unsigned* counter) {
     if (s->done) return;
     const V omega = V(kOmega);
-    const Stencil<V, V> A = as_stencil(L);
-    auto xv = [&](long long q, int qi, int qj, int qk) -> V {
-        const V d = L.diag[q];
-        if (d == V(0)) return V(0);
-        if (MODE == SM_ZERO2) return omega * b[q] / d;
-        if (MODE == SM_PROLONG) return x_in[q] + e[lin3(qi >> 1, qj >> 1, qk >> 1, m0, m1)];
-        return x_in[q];
-    };
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
     double acc[1] = {0.0};
-    if (i < L.n0 && j < L.n1) {
-        for (int k = blockIdx.z; k < L.n2; k += gridDim.z) {
-            const long long c = lin3(i, j, k, L.n0, L.n1);
-            const V d = L.diag[c];
-            V xo = V(0);
-            if (d != V(0)) {
-                const V xc = xv(c, i, j, k);
-                const V ax = apply_row<V>(A, i, j, k, c, xc, xv);
-                xo = xc + omega * (b[c] - ax) / d;
-            }
-            x_out[c] = xo;
-            if (DOT != DOT_NONE) acc[0] += (double)b[c] * (double)xo;
-        }
+    const RecLoad<V, R> recf{A};
+    // value of the current iterate at a cell, zero on inactive cells
+    auto rawf = [&](int q, int qi, int qj, int qk) -> V {
+        if (MODE == SM_ZERO2) return b[q];
+        V v = x_in[q];
+        if (MODE == SM_PROLONG) v += e[(qi >> 1) + gc.s1 * (qj >> 1) + gc.s2 * (qk >> 1)];
+        return v;
+    };
+    auto valf = [&](V raw, const Co<V>& rec) -> V {
+        if (!(rec.d > V(0))) return V(0);
+        return MODE == SM_ZERO2 ? omega * raw / rec.d : raw;
+    };
+    SEG_LOOP_ALL_BEGIN(seg, g)
+    const St7<V> st = gather7<V, true>(g, c, i, j, k, live, lane, recf, rawf, valf);
+    if (live) {
+        const V bc = b[c];
+        V xo = V(0);
+        if (st.d > V(0)) xo = st.v0 + omega * (bc - apply7(st)) / st.d;
+        x_out[c] = xo;
+        if (DOT != DOT_NONE) acc[0] += (double)bc * (double)xo;
     }
+    SEG_LOOP_END
     if (DOT != DOT_NONE) {
         double tot[1];
         if (grid_sum<1>(acc, partials, counter, tot)) {
@@ -343,74 +621,88 @@ __global__ void __launch_bounds__(256) smooth_kernel(Level<V> L, const V* __rest
     }
 }
 
-// Residual of the fine level summed onto the coarse right-hand side (R = P^T).  Blocks are
-// 32 x 8 fine cells in (i, j) and march over coarse planes K (fine planes 2K, 2K+1).
-template <typename V>
-__global__ void __launch_bounds__(256) restrict_kernel(Level<V> L, const V* __restrict__ b, const V* __restrict__ x,
-                                                       int m0, int m1, int m2, V* __restrict__ bc, const Scalars* s) {
+// Residual of the fine level summed onto the coarse right-hand side (R = P^T), one warp per
+// active coarse segment: the warp walks the 64 x 2 x 2 fine cells under it one fine row
+// segment at a time (one fine cell per lane, coalesced), the i-pairs are summed by shuffle.
+template <typename V, typename R>
+__global__ void __launch_bounds__(kSegThreads) restrict_kernel(LGeom g, const R* __restrict__ A, const V* __restrict__ b,
+                                                               const V* __restrict__ x, LGeom gc, SegArg cseg,
+                                                               V* __restrict__ bc, const Scalars* s) {
     if (s->done) return;
-    __shared__ V sh[kBY][kBX];
-    const Stencil<V, V> A = as_stencil(L);
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int i = blockIdx.x * kBX + tx;
-    const int j = blockIdx.y * kBY + ty;
-    auto xv = [&](long long q, int, int, int) -> V { return x[q]; };
-    for (int K = blockIdx.z; K < m2; K += gridDim.z) {
-        V rsum = V(0);
-        if (i < L.n0 && j < L.n1) {
-            for (int kk = 0; kk < 2; ++kk) {
-                const int k = 2 * K + kk;
-                if (k >= L.n2) break;
-                const long long c = lin3(i, j, k, L.n0, L.n1);
-                if (L.diag[c] != V(0)) rsum += b[c] - apply_row<V>(A, i, j, k, c, x[c], xv);
-            }
+    const RecLoad<V, R> recf{A};
+    auto rawf = [&](int q, int, int, int) -> V { return x[q]; };
+    auto valf = [](V raw, const Co<V>&) -> V { return raw; };
+    const int lane = threadIdx.x & 31;
+    const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int nseg = *cseg.count;
+    for (int qs = warp_global; qs < nseg; qs += nwarps) {
+        const int4 sd = cseg.desc[qs];
+        const int I0 = sd.y, J = sd.z, K = sd.w;
+        V sum[2] = {V(0), V(0)};  // fine i in [2*I0, 2*I0+32) and [2*I0+32, 2*I0+64)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int i = 2 * I0 + 32 * h + lane;
+#pragma unroll
+            for (int kk = 0; kk < 2; ++kk)
+#pragma unroll
+                for (int jj = 0; jj < 2; ++jj) {
+                    const int j = 2 * J + jj, k = 2 * K + kk;
+                    // warp-uniform: the row exists for all lanes or for none
+                    if (j >= g.n1 || k >= g.n2) continue;
+                    const bool live = i < g.n0;
+                    const int c = i + g.s1 * j + g.s2 * k;
+                    const St7<V> st = gather7<V, false>(g, c, i, j, k, live, lane, recf, rawf, valf);
+                    if (live && st.d > V(0)) sum[h] += b[c] - apply7(st);
+                }
         }
-        rsum += __shfl_down_sync(0xffffffffu, rsum, 1);
-        sh[ty][tx] = rsum;
-        __syncthreads();
-        if ((tx & 1) == 0 && (ty & 1) == 0) {
-            const int I = i >> 1, J = j >> 1;
-            if (I < m0 && J < m1) bc[lin3(I, J, K, m0, m1)] = sh[ty][tx] + sh[ty + 1][tx];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const V pair = sum[h] + __shfl_down_sync(kFull, sum[h], 1);
+            const int I = I0 + 16 * h + (lane >> 1);
+            if ((lane & 1) == 0 && I < gc.n0) bc[I + gc.s1 * J + gc.s2 * K] = pair;
         }
-        __syncthreads();
     }
 }
 
+
 // Coarsest level: omega-Jacobi sweeps from zero in one block's shared memory.
-template <typename V>
-__global__ void __launch_bounds__(kCoarsestMaxCells) coarsest_kernel(Level<V> L, const V* __restrict__ b,
-                                                                     V* __restrict__ x, int sweeps, const Scalars* s) {
+template <typename V, typename R>
+__global__ void __launch_bounds__(kCoarsestMaxCells) coarsest_kernel(LGeom g, const R* __restrict__ A,
+                                                                     const V* __restrict__ b, V* __restrict__ x,
+                                                                     int sweeps, const Scalars* s) {
     if (s->done) return;
     __shared__ V sd[kCoarsestMaxCells], sx[kCoarsestMaxCells], sy[kCoarsestMaxCells], sz[kCoarsestMaxCells];
     __shared__ V sb[kCoarsestMaxCells], xa[kCoarsestMaxCells], xb[kCoarsestMaxCells];
-    const int n = L.n0 * L.n1 * L.n2;
+    const int n = g.n0 * g.n1 * g.n2;
     const int c = threadIdx.x;
     const V omega = V(kOmega);
     if (c < n) {
-        sd[c] = L.diag[c];
-        sx[c] = L.ox[c];
-        sy[c] = L.oy[c];
-        sz[c] = L.oz[c];
+        const auto r = ldrec(A, c);
+        sd[c] = (V)r.d;
+        sx[c] = (V)r.x;
+        sy[c] = (V)r.y;
+        sz[c] = (V)r.z;
         sb[c] = b[c];
-        xa[c] = sd[c] != V(0) ? omega * sb[c] / sd[c] : V(0);
+        xa[c] = sd[c] > V(0) ? omega * sb[c] / sd[c] : V(0);
     }
     __syncthreads();
-    const int i = c % L.n0, j = (c / L.n0) % L.n1, k = c / (L.n0 * L.n1);
-    const int s1 = L.n0, s2 = L.n0 * L.n1;
+    const int i = c % g.n0, j = (c / g.n0) % g.n1, k = c / (g.n0 * g.n1);
+    const int s1 = g.n0, s2 = g.n0 * g.n1;
     V* cur = xa;
     V* nxt = xb;
     for (int it = 1; it < sweeps; ++it) {
         if (c < n) {
             V xo = V(0);
             const V d = sd[c];
-            if (d != V(0)) {
+            if (d > V(0)) {
                 V a = d * cur[c];
                 if (i > 0) a += sx[c - 1] * cur[c - 1];
-                if (i < L.n0 - 1) a += sx[c] * cur[c + 1];
+                if (i < g.n0 - 1) a += sx[c] * cur[c + 1];
                 if (j > 0) a += sy[c - s1] * cur[c - s1];
-                if (j < L.n1 - 1) a += sy[c] * cur[c + s1];
+                if (j < g.n1 - 1) a += sy[c] * cur[c + s1];
                 if (k > 0) a += sz[c - s2] * cur[c - s2];
-                if (k < L.n2 - 1) a += sz[c] * cur[c + s2];
+                if (k < g.n2 - 1) a += sz[c] * cur[c + s2];
                 xo = cur[c] + omega * (sb[c] - a) / d;
             }
             nxt[c] = xo;
@@ -426,18 +718,48 @@ __global__ void __launch_bounds__(kCoarsestMaxCells) coarsest_kernel(Level<V> L,
 // ---------------------------------------------------------------------------------------
 // host side
 
+static int seg_blocks(el_ctx* ctx, long long total_segments) {
+    const long long warps = (long long)ctx->num_sms * 6 * (kSegThreads / 32);
+    const long long need = std::max<long long>(1, std::min<long long>(total_segments, warps));
+    return (int)((need * 32 + kSegThreads - 1) / kSegThreads);
+}
+
+static SegArg seg_arg(const SegList& l) { return SegArg{l.desc, l.count}; }
+
+static int alloc_seglist(el_ctx* ctx, SegList& l, int n0, int n1, int n2) {
+    l.nsr = (n0 + 31) / 32;
+    l.total = (long long)l.nsr * n1 * n2;
+    const long long nchunks = (l.total + kSegChunk - 1) / kSegChunk;
+    l.desc = (int4*)ctx_alloc(ctx, l.total * sizeof(int4));
+    l.flags = (uint8_t*)ctx_alloc(ctx, l.total);
+    l.chunk = (int*)ctx_alloc(ctx, (nchunks + 1) * sizeof(int));
+    l.count = l.chunk + nchunks;
+    return (l.desc && l.flags && l.chunk) ? EL_OK : set_error(ctx, EL_ERR_OUT_OF_MEMORY, "segment lists");
+}
+
+// compaction of the flags into the ordered id list
+static int enqueue_compact(el_ctx* ctx, SegList& l, const LGeom& g) {
+    const int nchunks = (int)((l.total + kSegChunk - 1) / kSegChunk);
+    seg_count_kernel<<<nchunks, 256, 0, ctx->stream>>>(l.flags, l.total, l.chunk);
+    seg_scan_kernel<<<1, 1024, 0, ctx->stream>>>(l.chunk, nchunks, l.count);
+    seg_write_kernel<<<nchunks, 32, 0, ctx->stream>>>(g, l.flags, l.total, l.chunk, l.desc);
+    return 3;
+}
+
+template <typename R>
+static int enqueue_seglist_rec(el_ctx* ctx, SegList& l, const LGeom& g, const R* rec) {
+    ProfScope prof(ctx, EL_KC_OTHER, (double)g.n0 * g.n1 * g.n2 * sizeof(R));
+    seg_flags_rec_kernel<R><<<seg_blocks(ctx, l.total), kSegThreads, 0, ctx->stream>>>(g, rec, l.total, l.flags);
+    return 1 + enqueue_compact(ctx, l, g);
+}
+
 static int grid1d(el_ctx* ctx, long long n) {
     return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, (long long)ctx->num_sms * 8));
 }
 
+// Hierarchy below the finest level (allocated once per context and solver precision).
 template <typename V>
-static Level<V> level_view(const MGLevel<V>& L) {
-    return Level<V>{L.n0, L.n1, L.n2, L.diag, L.off[0], L.off[1], L.off[2]};
-}
-
-// Allocate the hierarchy below the given level-0 dimensions (level 0 arrays set by caller).
-template <typename V>
-static void build_hierarchy(el_ctx* ctx, std::vector<MGLevel<V>>& mg) {
+static int build_hierarchy(el_ctx* ctx, std::vector<MGLevel<V>>& mg, size_t coarse_rec_bytes) {
     mg.clear();
     MGLevel<V> L0;
     L0.n0 = ctx->ni;
@@ -445,6 +767,7 @@ static void build_hierarchy(el_ctx* ctx, std::vector<MGLevel<V>>& mg) {
     L0.n2 = ctx->nk;
     const long long n = (long long)ctx->ni * ctx->nj * ctx->nk;
     L0.t = (V*)ctx_alloc(ctx, n * sizeof(V));
+    if (!L0.t) return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "multigrid");
     mg.push_back(L0);
     while (std::max(mg.back().n0, std::max(mg.back().n1, mg.back().n2)) > kCoarsestMaxDim) {
         MGLevel<V> C;
@@ -452,124 +775,121 @@ static void build_hierarchy(el_ctx* ctx, std::vector<MGLevel<V>>& mg) {
         C.n1 = (mg.back().n1 + 1) / 2;
         C.n2 = (mg.back().n2 + 1) / 2;
         const long long m = (long long)C.n0 * C.n1 * C.n2;
-        C.diag = (V*)ctx_alloc(ctx, m * sizeof(V));
-        for (int a = 0; a < 3; ++a) C.off[a] = (V*)ctx_alloc(ctx, m * sizeof(V));
+        C.rec = ctx_alloc(ctx, m * coarse_rec_bytes);
         C.b = (V*)ctx_alloc(ctx, m * sizeof(V));
         C.x = (V*)ctx_alloc(ctx, m * sizeof(V));
         C.t = (V*)ctx_alloc(ctx, m * sizeof(V));
+        if (!C.rec || !C.b || !C.x || !C.t) return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "multigrid");
+        int rc = alloc_seglist(ctx, C.seg, C.n0, C.n1, C.n2);
+        if (rc != EL_OK) return rc;
         mg.push_back(C);
     }
+    return EL_OK;
 }
 
-template <typename V>
+// Coarse records and segment lists of every level below the finest.
+template <typename V, typename R0, typename RC>
 static int enqueue_coarsen(el_ctx* ctx, std::vector<MGLevel<V>>& mg) {
     int launched = 0;
     for (size_t l = 0; l + 1 < mg.size(); ++l) {
         const MGLevel<V>& F = mg[l];
         MGLevel<V>& C = mg[l + 1];
-        ProfScope prof(ctx, EL_KC_MG_COARSE,
-                       (double)F.n0 * F.n1 * F.n2 * 4 * sizeof(V) + (double)C.n0 * C.n1 * C.n2 * 4 * sizeof(V));
+        const LGeom gf = make_geom(F.n0, F.n1, F.n2), gc = make_geom(C.n0, C.n1, C.n2);
         dim3 block(32, 4, 1);
         dim3 grid((C.n0 + 31) / 32, (C.n1 + 3) / 4, C.n2);
-        coarsen_kernel<V><<<grid, block, 0, ctx->stream>>>(level_view(F), C.n0, C.n1, C.n2, C.diag, C.off[0],
-                                                           C.off[1], C.off[2]);
-        ++launched;
+        {
+            ProfScope prof(ctx, EL_KC_MG_COARSE, (double)F.n0 * F.n1 * F.n2 * (l == 0 ? sizeof(R0) : sizeof(RC)) +
+                                                     (double)C.n0 * C.n1 * C.n2 * sizeof(RC));
+            if (l == 0)
+                coarsen_kernel<R0, RC><<<grid, block, 0, ctx->stream>>>(gf, (const R0*)F.rec, gc, (RC*)C.rec);
+            else
+                coarsen_kernel<RC, RC><<<grid, block, 0, ctx->stream>>>(gf, (const RC*)F.rec, gc, (RC*)C.rec);
+        }
+        launched += 1 + enqueue_seglist_rec<RC>(ctx, C.seg, gc, (const RC*)C.rec);
     }
     return launched;
 }
 
-// z = M^-1 r with r = mg[0].b and z = mg[0].x; dot = DOT_INIT or DOT_BETA
-template <typename V>
-static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, Scalars* s, int dot) {
+template <typename V, typename R, int MODE, int DOT>
+static void launch_smooth(el_ctx* ctx, const MGLevel<V>& F, const SegList& seg, const V* x_in, const MGLevel<V>* C,
+                          V* x_out, Scalars* s) {
+    const LGeom g = make_geom(F.n0, F.n1, F.n2);
+    const LGeom gc = C ? make_geom(C->n0, C->n1, C->n2) : g;
+    smooth_kernel<V, R, MODE, DOT><<<seg_blocks(ctx, seg.total), kSegThreads, 0, ctx->stream>>>(
+        g, seg_arg(seg), (const R*)F.rec, F.b, x_in, gc, C ? C->x : nullptr, x_out, s, ctx->partials, ctx->counter);
+}
+
+// z = M^-1 r with r = mg[0].b and z = mg[0].x; dot = DOT_INIT or DOT_BETA.  R0 / RC are the
+// record types of the finest / coarse levels.
+template <typename V, typename R0, typename RC>
+static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegList& seg0, Scalars* s, int dot) {
     int launched = 0;
     const int L = (int)mg.size();
-    if (L == 1) {
-        // grid too small to coarsen: the whole problem is solved by the coarsest sweeps, then
-        // one plain sweep computes the dot product
-        MGLevel<V>& C = mg[0];
-        coarsest_kernel<V><<<1, kCoarsestMaxCells, 0, ctx->stream>>>(level_view(C), C.b, C.t, kCoarsestSweeps, s);
-        Geom g = stencil_geom(C.n0, C.n1, C.n2, ctx->num_sms);
-        if (dot == DOT_INIT)
-            smooth_kernel<V, SM_PLAIN, DOT_INIT><<<g.grid, g.block, 0, ctx->stream>>>(
-                level_view(C), C.b, C.t, nullptr, 0, 0, C.x, s, ctx->partials, ctx->counter);
-        else
-            smooth_kernel<V, SM_PLAIN, DOT_BETA><<<g.grid, g.block, 0, ctx->stream>>>(
-                level_view(C), C.b, C.t, nullptr, 0, 0, C.x, s, ctx->partials, ctx->counter);
-        return 2;
-    }
+    auto segof = [&](int l) -> const SegList& { return l == 0 ? seg0 : mg[l].seg; };
     auto cells = [](const MGLevel<V>& X) { return (double)X.n0 * X.n1 * X.n2; };
     const double vs = sizeof(V);
+    if (L == 1) {
+        // too small to coarsen: the coarsest sweeps solve it, one more sweep gives the dot
+        MGLevel<V>& C = mg[0];
+        coarsest_kernel<V, R0><<<1, kCoarsestMaxCells, 0, ctx->stream>>>(make_geom(C.n0, C.n1, C.n2), (const R0*)C.rec,
+                                                                         C.b, C.t, kCoarsestSweeps, s);
+        if (dot == DOT_INIT)
+            launch_smooth<V, R0, SM_PLAIN, DOT_INIT>(ctx, C, seg0, C.t, nullptr, C.x, s);
+        else
+            launch_smooth<V, R0, SM_PLAIN, DOT_BETA>(ctx, C, seg0, C.t, nullptr, C.x, s);
+        return 2;
+    }
     for (int l = 0; l < L - 1; ++l) {
         MGLevel<V>& F = mg[l];
         MGLevel<V>& C = mg[l + 1];
-        Geom g = stencil_geom(F.n0, F.n1, F.n2, ctx->num_sms);
+        const double rb = l == 0 ? sizeof(R0) : sizeof(RC);
         {
-            // reads b, diag, 3 couplings; writes x
-            ProfScope prof(ctx, l == 0 ? EL_KC_SMOOTH : EL_KC_MG_COARSE, cells(F) * vs * 6);
-            smooth_kernel<V, SM_ZERO2, DOT_NONE><<<g.grid, g.block, 0, ctx->stream>>>(
-                level_view(F), F.b, nullptr, nullptr, 0, 0, F.x, s, ctx->partials, ctx->counter);
+            // reads b and records; writes x
+            ProfScope prof(ctx, l == 0 ? EL_KC_SMOOTH : EL_KC_MG_COARSE, cells(F) * (2 * vs + rb));
+            if (l == 0)
+                launch_smooth<V, R0, SM_ZERO2, DOT_NONE>(ctx, F, segof(l), nullptr, nullptr, F.x, s);
+            else
+                launch_smooth<V, RC, SM_ZERO2, DOT_NONE>(ctx, F, segof(l), nullptr, nullptr, F.x, s);
         }
-        Geom gr = stencil_geom(F.n0, F.n1, C.n2, ctx->num_sms);
         {
-            // reads b, x, diag, 3 couplings; writes the coarse b
-            ProfScope prof(ctx, l == 0 ? EL_KC_RESTRICT : EL_KC_MG_COARSE, cells(F) * vs * 6 + cells(C) * vs);
-            restrict_kernel<V><<<gr.grid, gr.block, 0, ctx->stream>>>(level_view(F), F.b, F.x, C.n0, C.n1, C.n2,
-                                                                      C.b, s);
+            // reads b, x and records; writes the coarse b
+            ProfScope prof(ctx, l == 0 ? EL_KC_RESTRICT : EL_KC_MG_COARSE, cells(F) * (2 * vs + rb) + cells(C) * vs);
+            const LGeom gf = make_geom(F.n0, F.n1, F.n2), gc = make_geom(C.n0, C.n1, C.n2);
+            if (l == 0)
+                restrict_kernel<V, R0><<<seg_blocks(ctx, C.seg.total), kSegThreads, 0, ctx->stream>>>(
+                    gf, (const R0*)F.rec, F.b, F.x, gc, seg_arg(C.seg), C.b, s);
+            else
+                restrict_kernel<V, RC><<<seg_blocks(ctx, C.seg.total), kSegThreads, 0, ctx->stream>>>(
+                    gf, (const RC*)F.rec, F.b, F.x, gc, seg_arg(C.seg), C.b, s);
         }
         launched += 2;
     }
     {
         MGLevel<V>& C = mg[L - 1];
-        ProfScope prof(ctx, EL_KC_MG_COARSE, cells(C) * vs * 6);
-        coarsest_kernel<V><<<1, kCoarsestMaxCells, 0, ctx->stream>>>(level_view(C), C.b, C.x, kCoarsestSweeps, s);
+        ProfScope prof(ctx, EL_KC_MG_COARSE, cells(C) * (3 * vs + sizeof(RC)));
+        coarsest_kernel<V, RC><<<1, kCoarsestMaxCells, 0, ctx->stream>>>(make_geom(C.n0, C.n1, C.n2), (const RC*)C.rec,
+                                                                         C.b, C.x, kCoarsestSweeps, s);
         ++launched;
     }
     for (int l = L - 2; l >= 0; --l) {
         MGLevel<V>& F = mg[l];
         MGLevel<V>& C = mg[l + 1];
-        Geom g = stencil_geom(F.n0, F.n1, F.n2, ctx->num_sms);
-        // prolongation sweep reads b, x, diag, 3 couplings and the coarse x, writes t; the last
-        // sweep reads b, t, diag, 3 couplings and writes x
-        ProfScope prof(ctx, l == 0 ? EL_KC_SMOOTH : EL_KC_MG_COARSE, cells(F) * vs * 14 + cells(C) * vs);
-        smooth_kernel<V, SM_PROLONG, DOT_NONE><<<g.grid, g.block, 0, ctx->stream>>>(
-            level_view(F), F.b, F.x, C.x, C.n0, C.n1, F.t, s, ctx->partials, ctx->counter);
-        if (l > 0)
-            smooth_kernel<V, SM_PLAIN, DOT_NONE><<<g.grid, g.block, 0, ctx->stream>>>(
-                level_view(F), F.b, F.t, nullptr, 0, 0, F.x, s, ctx->partials, ctx->counter);
-        else if (dot == DOT_INIT)
-            smooth_kernel<V, SM_PLAIN, DOT_INIT><<<g.grid, g.block, 0, ctx->stream>>>(
-                level_view(F), F.b, F.t, nullptr, 0, 0, F.x, s, ctx->partials, ctx->counter);
-        else
-            smooth_kernel<V, SM_PLAIN, DOT_BETA><<<g.grid, g.block, 0, ctx->stream>>>(
-                level_view(F), F.b, F.t, nullptr, 0, 0, F.x, s, ctx->partials, ctx->counter);
+        const double rb = l == 0 ? sizeof(R0) : sizeof(RC);
+        // prolongation sweep: b, x, records, coarse x read, t written; last sweep: b, t,
+        // records read, x written
+        ProfScope prof(ctx, l == 0 ? EL_KC_SMOOTH : EL_KC_MG_COARSE, cells(F) * (6 * vs + 2 * rb) + cells(C) * vs);
+        if (l == 0) {
+            launch_smooth<V, R0, SM_PROLONG, DOT_NONE>(ctx, F, segof(l), F.x, &C, F.t, s);
+            if (dot == DOT_INIT)
+                launch_smooth<V, R0, SM_PLAIN, DOT_INIT>(ctx, F, segof(l), F.t, nullptr, F.x, s);
+            else
+                launch_smooth<V, R0, SM_PLAIN, DOT_BETA>(ctx, F, segof(l), F.t, nullptr, F.x, s);
+        } else {
+            launch_smooth<V, RC, SM_PROLONG, DOT_NONE>(ctx, F, segof(l), F.x, &C, F.t, s);
+            launch_smooth<V, RC, SM_PLAIN, DOT_NONE>(ctx, F, segof(l), F.t, nullptr, F.x, s);
+        }
         launched += 2;
     }
-    return launched;
-}
-
-// One PCG iteration: K1, K2 and, for the multigrid solvers, the V-cycle.
-template <typename V, typename DT, typename OT, bool JAC>
-static int enqueue_iteration(el_ctx* ctx, const Stencil<DT, OT>& A, V* x, V* r, V* z, V*& p, V*& p_alt, V* ap,
-                             Scalars* s, int first, std::vector<MGLevel<V>>* mg) {
-    Geom g = stencil_geom(A.n0, A.n1, A.n2, ctx->num_sms);
-    const long long n = (long long)A.n0 * A.n1 * A.n2;
-    const double nv = (double)n * sizeof(V);
-    {
-        // reads z (or r), p (not on the first iteration), diag, 3 couplings; writes p, Ap
-        ProfScope prof(ctx, EL_KC_DIR_SPMV,
-                       nv * (first ? 3 : 4) + (double)n * (sizeof(DT) + 3 * sizeof(OT)));
-        dir_spmv_kernel<V, DT, OT, JAC><<<g.grid, g.block, 0, ctx->stream>>>(A, JAC ? r : z, p, p_alt, ap, s, first,
-                                                                            ctx->partials, ctx->counter);
-    }
-    std::swap(p, p_alt);
-    {
-        // reads x, r, p, Ap (and diag for Jacobi); writes x, r
-        ProfScope prof(ctx, EL_KC_UPDATE, nv * 6 + (JAC ? (double)n * sizeof(DT) : 0.0));
-        update_kernel<V, DT, JAC><<<grid1d(ctx, n), 256, 0, ctx->stream>>>(n, A.diag, x, r, p, ap, s, ctx->partials,
-                                                                          ctx->counter);
-    }
-    int launched = 2;
-    if (!JAC) launched += enqueue_vcycle<V>(ctx, *mg, s, DOT_BETA);
     return launched;
 }
 
@@ -580,22 +900,100 @@ static int poll(el_ctx* ctx, Scalars* host_copy, int which) {
     return EL_OK;
 }
 
-// Run PCG iterations until converged or `budget` iterations were launched; returns status.
-template <typename V, typename DT, typename OT, bool JAC>
-static int run_pcg(el_ctx* ctx, const Stencil<DT, OT>& A, V* x, V* r, V* z, V* p, V* p_alt, V* ap, int which,
-                   std::vector<MGLevel<V>>* mg, int budget, int check_every, Scalars* out) {
-    Scalars* s = ctx->dscal + which;
+// One PCG iteration of a multigrid-preconditioned solve (record operator A).
+template <typename V, typename RA, typename R0, typename RC>
+static int enqueue_mg_iteration(el_ctx* ctx, const RA* A, V* x, V* r, V* z, V*& p, V*& p_alt, V* ap, Scalars* s,
+                                int first, std::vector<MGLevel<V>>& mg) {
+    const LGeom g = make_geom(ctx->ni, ctx->nj, ctx->nk);
+    const SegList& seg = ctx->seg0;
+    const double N = (double)ctx->ni * ctx->nj * ctx->nk, vs = sizeof(V);
+    {
+        // reads z, p (not on the first iteration), records; writes p, Ap
+        ProfScope prof(ctx, EL_KC_DIR_SPMV, N * (vs * (first ? 3 : 4) + sizeof(RA)));
+        dir_spmv_rec_kernel<V, RA><<<seg_blocks(ctx, seg.total), kSegThreads, 0, ctx->stream>>>(
+            g, seg_arg(seg), A, z, p, p_alt, ap, s, first, ctx->partials, ctx->counter);
+    }
+    std::swap(p, p_alt);
+    {
+        // reads x, r, p, Ap; writes x, r
+        ProfScope prof(ctx, EL_KC_UPDATE, N * vs * 6);
+        update_kernel<V, false><<<seg_blocks(ctx, seg.total), kSegThreads, 0, ctx->stream>>>(
+            g, seg_arg(seg), nullptr, x, r, p, ap, s, ctx->partials, ctx->counter);
+    }
+    return 2 + enqueue_vcycle<V, R0, RC>(ctx, mg, seg, s, DOT_BETA);
+}
+
+template <typename OT>
+static int enqueue_jacobi_iteration(el_ctx* ctx, const SplitOp<OT>& A, double*& p, double*& p_alt, Scalars* s,
+                                    int first) {
+    const LGeom g = make_geom(ctx->ni, ctx->nj, ctx->nk);
+    const SegList& seg = ctx->seg0;
+    const double N = (double)ctx->ni * ctx->nj * ctx->nk;
+    {
+        // reads r, p (not on the first iteration), diag, 3 couplings; writes p, Ap
+        ProfScope prof(ctx, EL_KC_DIR_SPMV, N * (8.0 * (first ? 4 : 5) + 3 * sizeof(OT)));
+        dir_spmv_jacobi_kernel<OT><<<seg_blocks(ctx, seg.total), kSegThreads, 0, ctx->stream>>>(
+            g, seg_arg(seg), A, ctx->r64, p, p_alt, ctx->ap64, s, first, ctx->partials, ctx->counter);
+    }
+    std::swap(p, p_alt);
+    {
+        // reads x, r, p, Ap, diag; writes x, r
+        ProfScope prof(ctx, EL_KC_UPDATE, N * 8.0 * 7);
+        update_kernel<double, true><<<seg_blocks(ctx, seg.total), kSegThreads, 0, ctx->stream>>>(
+            g, seg_arg(seg), A.d, ctx->x64, ctx->r64, p, ctx->ap64, s, ctx->partials, ctx->counter);
+    }
+    return 2;
+}
+
+// Launch PCG iterations (check_every per poll) until converged or `budget` are launched.
+//
+// The first iteration is launched directly; the following ones in batches of `check_every`
+// (rounded up to even, so the two direction buffers are back in place after a batch).  A batch
+// is captured once per context and solver as a CUDA graph and replayed afterwards: all its
+// pointers and launch shapes are fixed per context, and the kernels read everything that
+// changes (scalars, segment lists) from device memory.  While kernel classes are being
+// profiled the batches are launched directly instead.
+template <typename F>
+static int run_iterations(el_ctx* ctx, int solver, int which, int budget, int check_every, Scalars* out,
+                          F&& enqueue) {
     int launched_iters = 0;
-    bool first = true;
     int st = poll(ctx, out, which);
     if (st != EL_OK) return st;
+    if (out->done || budget <= 0) return EL_OK;
+    ctx->launches += enqueue(1);
+    launched_iters = 1;
+    const int batch = std::max(2, (check_every + 1) / 2 * 2);
+    const bool graphs = ctx->use_graphs && ctx->prof_mask == 0;
+    if (graphs && ctx->iter_graph[solver] && ctx->iter_graph_len[solver] != batch) {
+        cudaGraphExecDestroy(ctx->iter_graph[solver]);
+        ctx->iter_graph[solver] = nullptr;
+    }
+    st = poll(ctx, out, which);
+    if (st != EL_OK) return st;
     while (!out->done && launched_iters < budget) {
-        const int batch = std::min(check_every, budget - launched_iters);
-        for (int q = 0; q < batch; ++q) {
-            ctx->launches += enqueue_iteration<V, DT, OT, JAC>(ctx, A, x, r, z, p, p_alt, ap, s, first ? 1 : 0, mg);
-            first = false;
+        // a full batch may run past the budget by up to batch - 1 iterations only when the
+        // budget is not a multiple of it; the iteration count reported is the device's
+        if (graphs && budget - launched_iters >= batch) {
+            if (!ctx->iter_graph[solver]) {
+                cudaGraph_t graph = nullptr;
+                EL_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+                int n = 0;
+                for (int q = 0; q < batch; ++q) n += enqueue(0);
+                EL_CUDA_TRY(ctx, cudaStreamEndCapture(ctx->stream, &graph));
+                const cudaError_t e = cudaGraphInstantiate(&ctx->iter_graph[solver], graph, 0);
+                cudaGraphDestroy(graph);
+                if (e != cudaSuccess) return set_error(ctx, EL_ERR_CUDA, std::string("graph: ") + cudaGetErrorString(e));
+                ctx->iter_graph_len[solver] = batch;
+                ctx->iter_graph_kernels[solver] = n;
+            }
+            EL_CUDA_TRY(ctx, cudaGraphLaunch(ctx->iter_graph[solver], ctx->stream));
+            ctx->launches += ctx->iter_graph_kernels[solver];
+            launched_iters += batch;
+        } else {
+            const int b = std::min(batch, budget - launched_iters);
+            for (int q = 0; q < b; ++q) ctx->launches += enqueue(0);
+            launched_iters += b;
         }
-        launched_iters += batch;
         st = check_launch(ctx, "pcg iteration");
         if (st != EL_OK) return st;
         st = poll(ctx, out, which);
@@ -605,76 +1003,110 @@ static int run_pcg(el_ctx* ctx, const Stencil<DT, OT>& A, V* x, V* r, V* z, V* p
 }
 
 template <typename T>
-static Stencil<double, T> fine_stencil64(el_ctx* ctx) {
-    return Stencil<double, T>{ctx->ni, ctx->nj, ctx->nk, ctx->diag64, (const T*)ctx->off[0], (const T*)ctx->off[1],
-                              (const T*)ctx->off[2]};
+static SplitOp<T> split_op(el_ctx* ctx) {
+    return SplitOp<T>{ctx->diag64, (const T*)ctx->off[0], (const T*)ctx->off[1], (const T*)ctx->off[2]};
+}
+
+static void reset_vectors(el_ctx* ctx) {
+    const size_t n = (size_t)ctx->ni * ctx->nj * ctx->nk;
+    for (double* v : {ctx->x64, ctx->r64, ctx->z64, ctx->p64, ctx->p64b, ctx->ap64})
+        if (v) cudaMemsetAsync(v, 0, n * 8, ctx->stream);
+    for (float* v : {ctx->x32, ctx->r32, ctx->z32, ctx->p32, ctx->p32b, ctx->ap32})
+        if (v) cudaMemsetAsync(v, 0, n * 4, ctx->stream);
+    for (auto& L : ctx->mg32) {
+        const size_t m = (size_t)L.n0 * L.n1 * L.n2 * 4;
+        for (float* v : {L.t, L.rec ? L.b : nullptr, L.rec ? L.x : nullptr})
+            if (v) cudaMemsetAsync(v, 0, m, ctx->stream);
+    }
+    for (auto& L : ctx->mg64) {
+        const size_t m = (size_t)L.n0 * L.n1 * L.n2 * 8;
+        for (double* v : {L.t, L.rec ? L.b : nullptr, L.rec ? L.x : nullptr})
+            if (v) cudaMemsetAsync(v, 0, m, ctx->stream);
+    }
 }
 
 // Solve A x64 = rhs64 (matrix already built, s0.bb set).  Fills stats.
 template <typename T>
 static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) {
     const long long n = (long long)ctx->ni * ctx->nj * ctx->nk;
+    const LGeom g = make_geom(ctx->ni, ctx->nj, ctx->nk);
     const int check = std::max(1, prm.check_every);
     Scalars* s0 = ctx->dscal;
     Scalars* h = ctx->hscal;
-    solve_init_kernel<<<grid1d(ctx, n), 256, 0, ctx->stream>>>(n, ctx->rhs64, ctx->x64, ctx->r64, s0, prm.tol);
+    const SplitOp<T> A64 = split_op<T>(ctx);
+    // active segments of the finest level
+    {
+        ProfScope prof(ctx, EL_KC_OTHER, (double)n * 8);
+        seg_flags_diag_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
+            g, ctx->diag64, ctx->seg0.total, ctx->seg0.flags);
+    }
+    ctx->launches += 1 + enqueue_compact(ctx, ctx->seg0, g);
+    {
+        ProfScope prof(ctx, EL_KC_OTHER, (double)n * 24);
+        solve_init_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
+            g, seg_arg(ctx->seg0), ctx->rhs64, ctx->x64, ctx->r64, s0, prm.tol);
+    }
     ctx->launches += 1;
     int rc = EL_OK;
-    const Stencil<double, T> A64 = fine_stencil64<T>(ctx);
     st->outer_iterations = 1;
     if (prm.solver == EL_SOLVER_JACOBI_FP64) {
-        jacobi_rz_kernel<double, double><<<grid1d(ctx, n), 256, 0, ctx->stream>>>(n, ctx->diag64, ctx->r64, s0,
-                                                                                 ctx->partials, ctx->counter);
+        jacobi_rz_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
+            g, seg_arg(ctx->seg0), ctx->diag64, ctx->r64, s0, ctx->partials, ctx->counter);
         ctx->launches += 1;
-        rc = run_pcg<double, double, T, true>(ctx, A64, ctx->x64, ctx->r64, nullptr, ctx->p64, ctx->z64, ctx->ap64, 0,
-                                              nullptr, prm.max_iter, check, h);
+        double* p = ctx->p64;
+        double* p_alt = ctx->p64b;
+        rc = run_iterations(ctx, EL_SOLVER_JACOBI_FP64, 0, prm.max_iter, check, h,
+                            [&](int first) { return enqueue_jacobi_iteration<T>(ctx, A64, p, p_alt, s0, first); });
         st->iterations = h->iter;
         st->relres = h->bb > 0 ? sqrt(h->rr / h->bb) : 0.0;
     } else if (prm.solver == EL_SOLVER_MG_FP64) {
         auto& mg = ctx->mg64;
-        // level 0 views: coefficients in double (copies when the field type is float)
-        mg[0].diag = ctx->diag64;
+        mg[0].rec = ctx->A64rec;
         mg[0].b = ctx->r64;
         mg[0].x = ctx->z64;
-        if (sizeof(T) == 4) {
-            for (int a = 0; a < 3; ++a) {
-                convert_kernel<float, double><<<grid1d(ctx, n), 256, 0, ctx->stream>>>(n, (const float*)ctx->off[a],
-                                                                                       mg[0].off[a]);
-            }
-            ctx->launches += 3;
-        } else {
-            for (int a = 0; a < 3; ++a) mg[0].off[a] = (double*)ctx->off[a];
-        }
-        ctx->launches += enqueue_coarsen<double>(ctx, mg);
-        ctx->launches += enqueue_vcycle<double>(ctx, mg, s0, DOT_INIT);
-        rc = run_pcg<double, double, T, false>(ctx, A64, ctx->x64, ctx->r64, ctx->z64, ctx->p64, ctx->p64b,
-                                               ctx->ap64, 0, &mg, prm.max_iter, check, h);
+        pack64_kernel<T><<<grid1d(ctx, n), 256, 0, ctx->stream>>>(n, ctx->diag64, A64.x, A64.y, A64.z, ctx->A64rec);
+        ctx->launches += 1 + enqueue_coarsen<double, Rec64, Rec64>(ctx, mg);
+        ctx->launches += enqueue_vcycle<double, Rec64, Rec64>(ctx, mg, ctx->seg0, s0, DOT_INIT);
+        double* p = ctx->p64;
+        double* p_alt = ctx->p64b;
+        rc = run_iterations(ctx, EL_SOLVER_MG_FP64, 0, prm.max_iter, check, h, [&](int first) {
+            return enqueue_mg_iteration<double, Rec64, Rec64, Rec64>(ctx, ctx->A64rec, ctx->x64, ctx->r64, ctx->z64, p,
+                                                                    p_alt, ctx->ap64, s0, first, mg);
+        });
         st->iterations = h->iter;
         st->relres = h->bb > 0 ? sqrt(h->rr / h->bb) : 0.0;
     } else {
         // mixed: FP64 refinement around FP32 multigrid PCG
         auto& mg = ctx->mg32;
-        mg[0].diag = ctx->diag32;
-        for (int a = 0; a < 3; ++a) mg[0].off[a] = ctx->off32[a];
+        mg[0].rec = ctx->A16;
         mg[0].b = ctx->r32;
         mg[0].x = ctx->z32;
-        ctx->launches += enqueue_coarsen<float>(ctx, mg);
-        const Stencil<float, float> A32{ctx->ni, ctx->nj, ctx->nk, ctx->diag32, ctx->off32[0], ctx->off32[1],
-                                        ctx->off32[2]};
+        {
+            ProfScope prof(ctx, EL_KC_OTHER, (double)n * (8 + 3 * sizeof(T) + 24));
+            pack32_kernel<T><<<grid1d(ctx, n), 256, 0, ctx->stream>>>(n, ctx->diag64, A64.x, A64.y, A64.z, ctx->A32,
+                                                                      ctx->A16);
+        }
+        ctx->launches += 1 + enqueue_coarsen<float, ushort4, float4>(ctx, mg);
         Scalars* s1 = ctx->dscal + 1;
         Scalars hi;
         rc = poll(ctx, h, 0);
         int inner_total = 0, outer = 0;
-        Geom g = stencil_geom(ctx->ni, ctx->nj, ctx->nk, ctx->num_sms);
+        float* p = ctx->p32;
+        float* p_alt = ctx->p32b;
         while (rc == EL_OK && !h->done && outer < std::max(1, prm.max_outer) && inner_total < prm.max_iter) {
             const double want = prm.tol * sqrt(h->bb / h->rr);
             const double tau = std::min(0.5, std::max(prm.inner_floor, 0.5 * want));
-            inner_init_kernel<<<grid1d(ctx, n), 256, 0, ctx->stream>>>(n, ctx->r64, ctx->r32, ctx->x32, s0, s1, tau,
-                                                                       ctx->partials, ctx->counter);
+            {
+                ProfScope prof(ctx, EL_KC_OTHER, (double)n * 16);
+                inner_init_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
+                    g, seg_arg(ctx->seg0), ctx->r64, ctx->r32, ctx->x32, s0, s1, tau, ctx->partials, ctx->counter);
+            }
             ctx->launches += 1;
-            ctx->launches += enqueue_vcycle<float>(ctx, mg, s1, DOT_INIT);
-            rc = run_pcg<float, float, float, false>(ctx, A32, ctx->x32, ctx->r32, ctx->z32, ctx->p32, ctx->p32b,
-                                                     ctx->ap32, 1, &mg, prm.max_iter - inner_total, check, &hi);
+            ctx->launches += enqueue_vcycle<float, ushort4, float4>(ctx, mg, ctx->seg0, s1, DOT_INIT);
+            rc = run_iterations(ctx, EL_SOLVER_MIXED, 1, prm.max_iter - inner_total, check, &hi, [&](int first) {
+                return enqueue_mg_iteration<float, float4, ushort4, float4>(ctx, ctx->A32, ctx->x32, ctx->r32, ctx->z32,
+                                                                            p, p_alt, ctx->ap32, s1, first, mg);
+            });
             if (rc != EL_OK) break;
             inner_total += hi.iter;
             if (hi.bad) {
@@ -683,13 +1115,14 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
             }
             {
                 ProfScope prof(ctx, EL_KC_OTHER, (double)n * 20);
-                accumulate_kernel<<<grid1d(ctx, n), 256, 0, ctx->stream>>>(n, ctx->x64, ctx->x32, s1);
+                accumulate_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
+                    g, seg_arg(ctx->seg0), ctx->x64, ctx->x32, s1);
             }
             {
                 // reads x, b, diag (f64), 3 couplings; writes r (f64)
                 ProfScope prof(ctx, EL_KC_RESIDUAL, (double)n * (32 + 3 * sizeof(T)));
-                residual_kernel<T><<<g.grid, g.block, 0, ctx->stream>>>(A64, ctx->rhs64, ctx->x64, ctx->r64, s0,
-                                                                        ctx->partials, ctx->counter);
+                residual_kernel<T><<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
+                    g, seg_arg(ctx->seg0), A64, ctx->rhs64, ctx->x64, ctx->r64, s0, ctx->partials, ctx->counter);
             }
             ctx->launches += 2;
             ++outer;
@@ -700,7 +1133,12 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
         st->relres = h->bb > 0 ? sqrt(h->rr / h->bb) : 0.0;
     }
     if (rc != EL_OK) return rc;
-    if (h->bad) return set_error(ctx, EL_ERR_NAN, "non-finite value in the pressure solve");
+    if (h->bad) {
+        // entries outside the active segments are never rewritten and must stay finite (they
+        // meet zero couplings), so a failed solve leaves every solver vector cleared
+        reset_vectors(ctx);
+        return set_error(ctx, EL_ERR_NAN, "non-finite value in the pressure solve");
+    }
     st->status = h->done ? EL_OK : EL_ERR_NOT_CONVERGED;
     return EL_OK;
 }
@@ -716,28 +1154,32 @@ int setup_solver_storage(el_ctx* ctx, int solver) {
         ctx->r64 = (double*)ctx_alloc(ctx, n * 8);
         ctx->z64 = (double*)ctx_alloc(ctx, n * 8);
         ctx->p64 = (double*)ctx_alloc(ctx, n * 8);
+        ctx->p64b = (double*)ctx_alloc(ctx, n * 8);
         ctx->ap64 = (double*)ctx_alloc(ctx, n * 8);
-        if (!ctx->x64 || !ctx->r64 || !ctx->z64 || !ctx->p64 || !ctx->ap64)
+        if (!ctx->x64 || !ctx->r64 || !ctx->z64 || !ctx->p64 || !ctx->p64b || !ctx->ap64)
             return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "solver vectors");
+        int rc = alloc_seglist(ctx, ctx->seg0, ctx->ni, ctx->nj, ctx->nk);
+        if (rc != EL_OK) return rc;
     }
     if (solver == EL_SOLVER_MG_FP64 && ctx->mg64.empty()) {
-        build_hierarchy<double>(ctx, ctx->mg64);
-        if (ctx->dtype == EL_F32)
-            for (int a = 0; a < 3; ++a) ctx->mg64[0].off[a] = (double*)ctx_alloc(ctx, n * 8);
-        ctx->p64b = (double*)ctx_alloc(ctx, n * 8);
+        ctx->A64rec = (Rec64*)ctx_alloc(ctx, n * sizeof(Rec64));
+        if (!ctx->A64rec) return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "multigrid records");
+        int rc = build_hierarchy<double>(ctx, ctx->mg64, sizeof(Rec64));
+        if (rc != EL_OK) return rc;
     }
     if (solver == EL_SOLVER_MIXED && !ctx->x32) {
         ctx->x32 = (float*)ctx_alloc(ctx, n * 4);
         ctx->r32 = (float*)ctx_alloc(ctx, n * 4);
         ctx->z32 = (float*)ctx_alloc(ctx, n * 4);
         ctx->p32 = (float*)ctx_alloc(ctx, n * 4);
-        ctx->ap32 = (float*)ctx_alloc(ctx, n * 4);
         ctx->p32b = (float*)ctx_alloc(ctx, n * 4);
-        ctx->diag32 = (float*)ctx_alloc(ctx, n * 4);
-        for (int a = 0; a < 3; ++a)
-            ctx->off32[a] = ctx->dtype == EL_F32 ? (float*)ctx->off[a] : (float*)ctx_alloc(ctx, n * 4);
-        build_hierarchy<float>(ctx, ctx->mg32);
-        if (!ctx->x32 || !ctx->diag32) return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "mixed solver vectors");
+        ctx->ap32 = (float*)ctx_alloc(ctx, n * 4);
+        ctx->A32 = (float4*)ctx_alloc(ctx, n * sizeof(float4));
+        ctx->A16 = (ushort4*)ctx_alloc(ctx, n * sizeof(ushort4));
+        if (!ctx->x32 || !ctx->r32 || !ctx->z32 || !ctx->p32 || !ctx->p32b || !ctx->ap32 || !ctx->A32 || !ctx->A16)
+            return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "mixed solver vectors");
+        int rc = build_hierarchy<float>(ctx, ctx->mg32, sizeof(float4));
+        if (rc != EL_OK) return rc;
     }
     return EL_OK;
 }

@@ -30,37 +30,86 @@ __global__ void valid_from_stamps_kernel(long long n, const uint8_t* __restrict_
         valid[c] = stamp[c] != 255 ? 1 : 0;
 }
 
+// One layer over the active tiles.  Tiles are 32 x 8 x 8 cells (i, j, k); a persistent grid
+// walks them, skipping those not flagged in act_in.  A cell can only become valid in layer
+// l+1 next to a cell that became valid in layer l (otherwise it would have become valid in
+// layer l already), so layer l+1 only visits tiles whose 3x3x3 tile neighbourhood changed in
+// layer l; layer 0 visits every tile.  Inside a tile the block marches its 8 planes with the
+// stamps of planes k-1, k, k+1 (plus a one-cell halo) in a shared-memory ring, so the 3x3x3
+// validity test runs on shared memory; only cells with a valid neighbour read field values,
+// and the sum walks the neighbours in z, y, x order like the reference loop.  Stamps of cells
+// updated in this layer become layer + 1, which reads as "not yet valid" whether a block sees
+// the old or the new byte.
+constexpr int kExBX = 32, kExBY = 8, kExBZ = 8;
+
+struct TileGrid {
+    int tx, ty, tz;  // tiles per axis
+};
+
 template <typename T>
-__global__ void __launch_bounds__(128) extrapolate_layer_kernel(int n0, int n1, int n2, T* __restrict__ g,
-                                                                uint8_t* __restrict__ stamp, int layer) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
-    if (i >= n0 || j >= n1) return;
-    const long long c = lin3(i, j, k, n0, n1);
-    if (stamp[c] <= layer) return;  // valid before this layer
-    T sum = T(0);
-    int count = 0;
-    for (int dk = -1; dk <= 1; ++dk) {
-        const int z = k + dk;
-        if (z < 0 || z >= n2) continue;
-        for (int dj = -1; dj <= 1; ++dj) {
-            const int y = j + dj;
-            if (y < 0 || y >= n1) continue;
-            for (int di = -1; di <= 1; ++di) {
-                const int x = i + di;
-                if (x < 0 || x >= n0) continue;
-                const long long q = lin3(x, y, z, n0, n1);
-                if (stamp[q] <= layer) {
-                    sum = add_rn2(sum, g[q]);
-                    ++count;
+__global__ void __launch_bounds__(kExBX * kExBY) extrapolate_layer_kernel(int n0, int n1, int n2, T* __restrict__ g,
+                                                                          uint8_t* __restrict__ stamp, int layer,
+                                                                          TileGrid tg, const uint8_t* __restrict__ act_in,
+                                                                          uint8_t* __restrict__ act_out) {
+    __shared__ uint8_t ring[3][kExBY + 2][kExBX + 2];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = tx + kExBX * ty;
+    const int ntiles = tg.tx * tg.ty * tg.tz;
+    constexpr int kHalo = (kExBX + 2) * (kExBY + 2);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        if (act_in && !act_in[t]) continue;  // block-uniform
+        const int bx = t % tg.tx, by = (t / tg.tx) % tg.ty, bz = t / (tg.tx * tg.ty);
+        const int i0 = bx * kExBX, j0 = by * kExBY, k0 = bz * kExBZ, k1 = min(n2, k0 + kExBZ);
+        const int i = i0 + tx, j = j0 + ty;
+        // plane z of the tile + halo into a ring slot; out-of-grid cells read as invalid (255)
+        auto load_plane = [&](int slot, int z) {
+            bool any = false;
+            for (int q = tid; q < kHalo; q += kExBX * kExBY) {
+                const int hx = q % (kExBX + 2), hy = q / (kExBX + 2);
+                const int x = i0 + hx - 1, y = j0 + hy - 1;
+                uint8_t v = 255;
+                if (z >= 0 && z < n2 && x >= 0 && x < n0 && y >= 0 && y < n1) v = stamp[lin3(x, y, z, n0, n1)];
+                ring[slot][hy][hx] = v;
+                any = any || v <= layer;
+            }
+            return any;
+        };
+        int has_valid[3];
+        has_valid[0] = __syncthreads_or(load_plane(0, k0 - 1));
+        has_valid[1] = __syncthreads_or(load_plane(1, k0));
+        bool changed = false;
+        for (int k = k0; k < k1; ++k) {
+            const int sm = (k - k0) % 3, sc = (k - k0 + 1) % 3, sp = (k - k0 + 2) % 3;
+            has_valid[sp] = __syncthreads_or(load_plane(sp, k + 1));
+            if ((has_valid[0] | has_valid[1] | has_valid[2]) && i < n0 && j < n1 && ring[sc][ty + 1][tx + 1] > layer) {
+                const int slots[3] = {sm, sc, sp};
+                T sum = T(0);
+                int count = 0;
+#pragma unroll
+                for (int dk = 0; dk < 3; ++dk)
+#pragma unroll
+                    for (int dj = 0; dj < 3; ++dj)
+#pragma unroll
+                        for (int di = 0; di < 3; ++di)
+                            if (ring[slots[dk]][ty + dj][tx + di] <= layer) {
+                                sum = add_rn2(sum, g[lin3(i + di - 1, j + dj - 1, k + dk - 1, n0, n1)]);
+                                ++count;
+                            }
+                if (count > 0) {
+                    const long long c = lin3(i, j, k, n0, n1);
+                    g[c] = sum / (T)count;
+                    stamp[c] = (uint8_t)(layer + 1);
+                    changed = true;
                 }
             }
+            __syncthreads();
         }
-    }
-    if (count > 0) {
-        g[c] = sum / (T)count;
-        stamp[c] = (uint8_t)(layer + 1);
+        // flag this tile's 3x3x3 tile neighbourhood for the next layer
+        if (__syncthreads_or(changed) && act_out && tid < 27) {
+            const int ox = bx + tid % 3 - 1, oy = by + (tid / 3) % 3 - 1, oz = bz + tid / 9 - 1;
+            if (ox >= 0 && ox < tg.tx && oy >= 0 && oy < tg.ty && oz >= 0 && oz < tg.tz)
+                act_out[ox + tg.tx * (oy + tg.ty * oz)] = 1;
+        }
     }
 }
 
@@ -220,18 +269,26 @@ int launch_extrapolate(el_ctx* ctx, int field, uint8_t* valid, int layers, bool 
     const long long n = (long long)n0 * n1 * n2;
     uint8_t* stamp = ctx->valid_tmp;
     stamps_from_valid_kernel<<<g1(ctx, n), 256, 0, ctx->stream>>>(n, valid, stamp);
-    dim3 block(32, 4, 1);
-    dim3 grid = pgrid(n0, n1, n2, block);
-    const int L = std::min(layers, 254);
+    dim3 block(kExBX, kExBY, 1);
+    const TileGrid tg{(n0 + kExBX - 1) / kExBX, (n1 + kExBY - 1) / kExBY, (n2 + kExBZ - 1) / kExBZ};
+    const int ntiles = tg.tx * tg.ty * tg.tz;
+    const int grid = std::max(1, std::min(ntiles, ctx->num_sms * 6));
+    // two activity maps (the layer's input and output) live in the context's tile buffer
+    uint8_t* act[2] = {ctx->ex_tiles, ctx->ex_tiles + ntiles};
+    const int L = std::min(layers, 254);  // stamps are bytes: 255 marks "still invalid"
+    int launched = 1;
     for (int l = 0; l < L; ++l) {
+        uint8_t* in = l == 0 ? nullptr : act[l & 1];
+        uint8_t* out = act[(l + 1) & 1];
+        cudaMemsetAsync(out, 0, ntiles, ctx->stream);
         if (ctx->dtype == EL_F64)
             extrapolate_layer_kernel<double><<<grid, block, 0, ctx->stream>>>(n0, n1, n2, (double*)ctx->field[field],
-                                                                              stamp, l);
+                                                                              stamp, l, tg, in, out);
         else
             extrapolate_layer_kernel<float><<<grid, block, 0, ctx->stream>>>(n0, n1, n2, (float*)ctx->field[field],
-                                                                             stamp, l);
+                                                                             stamp, l, tg, in, out);
+        ++launched;
     }
-    int launched = 1 + L;
     if (write_back) {
         valid_from_stamps_kernel<<<g1(ctx, n), 256, 0, ctx->stream>>>(n, stamp, valid);
         ++launched;
