@@ -29,6 +29,7 @@ EL_ERR_NAN = 4
 EL_ERR_CUDA = 5
 EL_ERR_OUT_OF_MEMORY = 6
 EL_ERR_TIMEOUT = 7
+EL_ERR_TOO_LARGE = 8
 
 EL_F32, EL_F64 = 0, 1
 TRACE_RK2, TRACE_RK3 = 0, 1

@@ -3,6 +3,7 @@
 // functions.  No exception crosses this boundary; every call returns a status code.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <new>
 
 #include "el_internal.cuh"
@@ -116,6 +117,7 @@ EL_API const char* el_status_string(int status) {
         case EL_ERR_CUDA: return "CUDA error";
         case EL_ERR_OUT_OF_MEMORY: return "out of device memory";
         case EL_ERR_TIMEOUT: return "device wait timed out";
+        case EL_ERR_TOO_LARGE: return "grid exceeds the no-allocation scratch limit (EL_NOALLOC_MAX_CELLS)";
         default: return "unknown status";
     }
 }
@@ -632,4 +634,130 @@ EL_API int el_compute_staggered_grid_weight(const el_grid* g, int dtype, void* w
     if (!valid_grid(g, dtype) || !wu || !wv || !ww || !solid) return EL_ERR_INVALID_ARGUMENT;
     launch_weights(dtype, g->ni, g->nj, g->nk, solid, wu, wv, ww, (cudaStream_t)stream);
     return cudaGetLastError() == cudaSuccess ? EL_OK : EL_ERR_CUDA;
+}
+
+// ---- pressure solve that allocates no device memory ----------------------------------------
+//
+// For callers that cannot call cudaMalloc (device memory reserved by another allocator, or
+// loops that cannot afford an allocation's device synchronisation).  Everything the plain FP64
+// Jacobi solve needs beyond the caller's fields is carved out of one file-scope device array
+// sized for EL_NOALLOC_MAX_CELLS cells; a context that owns nothing points the existing kernels
+// at the caller's arrays and at that scratch.
+
+namespace {
+
+constexpr long long kNoAllocCells = EL_NOALLOC_MAX_CELLS;
+constexpr size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
+constexpr long long kNoAllocPartials = 8192;  // doubles
+constexpr size_t kNoAllocBytes =
+    round256(kNoAllocCells)                                 // cell flags
+    + round256(8 * kNoAllocCells)                           // diagonal (f64)
+    + 3 * round256(4 * kNoAllocCells)                       // couplings (f32)
+    + round256(8 * kNoAllocCells)                           // right-hand side (f64)
+    + 5 * round256(8 * kNoAllocCells)                       // x, r, p, p', Ap (f64)
+    + round256(16 * kNoAllocCells)                          // segment descriptors (<= one per cell)
+    + round256(kNoAllocCells)                               // segment flags
+    + round256(4 * (kNoAllocCells / 1024 + 2))              // scan chunks and the segment count
+    + round256(8 * kNoAllocPartials)                        // reduction partials
+    + round256(64)                                          // reduction ticket
+    + round256(4 * sizeof(el::Scalars));                    // device scalars
+constexpr int kNoAllocMaxDevices = 64;
+
+std::mutex g_noalloc_mutex;
+void* g_noalloc_address[kNoAllocMaxDevices] = {};
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+EL_API int el_solve_pressure_noalloc(const el_grid* g, const float* phi, float* u, float* v, float* w,
+                                     const float* weight_u, const float* weight_v, const float* weight_w,
+                                     float* pressure, double dt, double tol, int max_iter, el_solve_stats* stats,
+                                     void* stream) {
+    if (!g || !phi || !u || !v || !w || !weight_u || !weight_v || !weight_w || !pressure || !(dt > 0) ||
+        !(tol > 0) || max_iter < 1 || g->ni < 1 || g->nj < 1 || g->nk < 1 || !(g->dx > 0))
+        return EL_ERR_INVALID_ARGUMENT;
+    const long long n = (long long)g->ni * g->nj * g->nk;
+    if (n > kNoAllocCells) return EL_ERR_TOO_LARGE;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return EL_ERR_CUDA;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return EL_ERR_CUDA;
+    const Geom geom = stencil_geom(g->ni, g->nj, g->nk, sms);
+    const long long partials_needed = (long long)std::max(geom.blocks(), sms * 8) * 2 + 64;
+    if (partials_needed > kNoAllocPartials) return EL_ERR_TOO_LARGE;
+
+    // once per device, with that device current: the scratch array's device address
+    unsigned char* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_address[dev]) {
+            void* addr = nullptr;
+            if (cudaGetSymbolAddress(&addr, g_noalloc_scratch) != cudaSuccess || !addr) return EL_ERR_CUDA;
+            g_noalloc_address[dev] = addr;
+        }
+        base = static_cast<unsigned char*>(g_noalloc_address[dev]);
+    }
+
+    el_ctx ctx;  // a view: the caller's fields and the scratch, nothing owned
+    ctx.device = dev;
+    ctx.ni = g->ni;
+    ctx.nj = g->nj;
+    ctx.nk = g->nk;
+    ctx.dx = g->dx;
+    ctx.dtype = EL_F32;
+    ctx.esz = 4;
+    ctx.num_sms = sms;
+    ctx.stream = static_cast<cudaStream_t>(stream);
+    ctx.own_stream = false;
+    ctx.use_graphs = false;  // instantiating a graph would allocate
+    ctx.field[EL_FIELD_PHI] = const_cast<float*>(phi);
+    ctx.field[EL_FIELD_U] = u;
+    ctx.field[EL_FIELD_V] = v;
+    ctx.field[EL_FIELD_W] = w;
+    ctx.field[EL_FIELD_WEIGHT_U] = const_cast<float*>(weight_u);
+    ctx.field[EL_FIELD_WEIGHT_V] = const_cast<float*>(weight_v);
+    ctx.field[EL_FIELD_WEIGHT_W] = const_cast<float*>(weight_w);
+    ctx.field[EL_FIELD_PRESSURE] = pressure;
+    size_t off = 0;
+    auto carve = [&](size_t bytes) {
+        unsigned char* p = base + off;
+        off += round256(bytes);
+        return p;
+    };
+    ctx.flags = carve(kNoAllocCells);
+    ctx.diag64 = (double*)carve(8 * kNoAllocCells);
+    for (int a = 0; a < 3; ++a) ctx.off[a] = carve(4 * kNoAllocCells);
+    ctx.rhs64 = (double*)carve(8 * kNoAllocCells);
+    ctx.x64 = (double*)carve(8 * kNoAllocCells);
+    ctx.r64 = (double*)carve(8 * kNoAllocCells);
+    ctx.p64 = (double*)carve(8 * kNoAllocCells);
+    ctx.p64b = (double*)carve(8 * kNoAllocCells);
+    ctx.ap64 = (double*)carve(8 * kNoAllocCells);
+    ctx.z64 = ctx.p64b;  // not read by the Jacobi solve
+    SegList& seg = ctx.seg0;
+    seg.nsr = (g->ni + 31) / 32;
+    seg.total = (long long)seg.nsr * g->nj * g->nk;  // <= n
+    seg.desc = (int4*)carve(16 * kNoAllocCells);
+    seg.flags = (uint8_t*)carve(kNoAllocCells);
+    seg.chunk = (int*)carve(4 * (kNoAllocCells / 1024 + 2));
+    seg.count = seg.chunk + (seg.total + 1023) / 1024;
+    ctx.partials = (double*)carve(8 * kNoAllocPartials);
+    ctx.max_partials = (int)kNoAllocPartials;
+    ctx.counter = (unsigned*)carve(64);
+    ctx.dscal = (Scalars*)carve(4 * sizeof(Scalars));
+    Scalars host_scalars[4] = {};
+    ctx.hscal = host_scalars;  // pageable host copy of the device scalars
+
+    // the array keeps the previous call's contents: the reduction ticket and the scalars start
+    // at zero; everything else is written before it is read
+    EL_CUDA_TRY(&ctx, cudaMemsetAsync(ctx.counter, 0, 64, ctx.stream));
+    EL_CUDA_TRY(&ctx, cudaMemsetAsync(ctx.dscal, 0, 4 * sizeof(Scalars), ctx.stream));
+    el_solve_stats local{};
+    el_solve_stats* st = stats ? stats : &local;
+    *st = el_solve_stats{};
+    const el_solve_params prm{EL_SOLVER_JACOBI_FP64, tol, max_iter, 8, 1, 1e-4};
+    ctx.launches += launch_set_dt(&ctx, dt);
+    const int rc = solve_pressure_impl(&ctx, prm, st);
+    if (rc != EL_OK) return rc;
+    return st->status;
 }

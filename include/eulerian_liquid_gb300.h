@@ -227,6 +227,34 @@ int el_advect_staggered_grid(const el_grid* g, int dtype, void* out_u, void* out
 int el_compute_staggered_grid_weight(const el_grid* g, int dtype, void* weight_u, void* weight_v,
                                      void* weight_w, const void* nodal_solid, void* stream);
 
+/* ---- pressure solve that allocates no device memory ------------------------------------
+ * No counterpart in the reference.  Some callers of the pressure solve cannot call cudaMalloc:
+ * applications whose device memory is reserved up front by another allocator (a renderer's
+ * or framework's memory pool), where a further cudaMalloc fails or is not permitted, and
+ * latency-critical loops that cannot afford an allocation, which may synchronise the whole
+ * device.  el_solve_pressure_noalloc does what el_solve_pressure does with
+ * EL_SOLVER_JACOBI_FP64 (plain FP64 PCG, Jacobi preconditioner), on caller-owned device arrays,
+ * and allocates nothing: its scratch (cell flags, the grid-shaped matrix, the PCG vectors,
+ * segment lists, reduction partials and scalars) is one fixed array of about 23 MB in the
+ * library's device memory, which every GPU that loads the library holds until the process exits.
+ *   - at most EL_NOALLOC_MAX_CELLS cells (64^3); larger grids return EL_ERR_TOO_LARGE before any
+ *     device work;
+ *   - FP32 fields in the layouts of el_upload: phi and the face weights are read, u, v, w are
+ *     updated in place (update_velocity_using_pressure), pressure is written (0 outside the
+ *     fluid); tol / max_iter as in el_solve_params;
+ *   - the work goes on `stream` (a cudaStream_t, NULL = the default stream); the call returns
+ *     after the solve, because it reads the convergence scalars back on the host;
+ *   - the first call on a device looks up the scratch array's device address, once per device,
+ *     with that device current; make that first call before any stream capture;
+ *   - all calls share the one array, which keeps the last call's contents: calls that overlap
+ *     on the GPU (from several threads or streams) race, and the caller must serialise them. */
+#define EL_ERR_TOO_LARGE 8
+#define EL_NOALLOC_MAX_CELLS 262144
+int el_solve_pressure_noalloc(const el_grid* g, const float* phi, float* u, float* v, float* w,
+                              const float* weight_u, const float* weight_v, const float* weight_w,
+                              float* pressure, double dt, double tol, int max_iter,
+                              el_solve_stats* stats, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
