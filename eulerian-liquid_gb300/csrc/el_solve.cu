@@ -625,7 +625,7 @@ __global__ void __launch_bounds__(kSegThreads) smooth_kernel(LGeom g, SegArg seg
 // active coarse segment: the warp walks the 64 x 2 x 2 fine cells under it one fine row
 // segment at a time (one fine cell per lane, coalesced), the i-pairs are summed by shuffle.
 template <typename V, typename R>
-__global__ void __launch_bounds__(kSegThreads) restrict_kernel(LGeom g, const R* __restrict__ A, const V* __restrict__ b,
+__global__ void __launch_bounds__(kSegThreads, 4) restrict_kernel(LGeom g, const R* __restrict__ A, const V* __restrict__ b,
                                                                const V* __restrict__ x, LGeom gc, SegArg cseg,
                                                                V* __restrict__ bc, const Scalars* s) {
     if (s->done) return;

@@ -20,11 +20,6 @@ __device__ __forceinline__ double add_rn2(double a, double b) { return __dadd_rn
 // stamp: 0 = valid from the start, l+1 = became valid in layer l, 255 = still invalid;
 // "valid before layer l" is stamp <= l.
 
-__global__ void stamps_from_valid_kernel(long long n, const uint8_t* __restrict__ valid, uint8_t* __restrict__ stamp) {
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
-        stamp[c] = valid[c] ? 0 : 255;
-}
-
 __global__ void valid_from_stamps_kernel(long long n, const uint8_t* __restrict__ stamp, uint8_t* __restrict__ valid) {
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
         valid[c] = stamp[c] != 255 ? 1 : 0;
@@ -34,55 +29,87 @@ __global__ void valid_from_stamps_kernel(long long n, const uint8_t* __restrict_
 // walks them, skipping those not flagged in act_in.  A cell can only become valid in layer
 // l+1 next to a cell that became valid in layer l (otherwise it would have become valid in
 // layer l already), so layer l+1 only visits tiles whose 3x3x3 tile neighbourhood changed in
-// layer l; layer 0 visits every tile.  Inside a tile the block marches its 8 planes with the
-// stamps of planes k-1, k, k+1 (plus a one-cell halo) in a shared-memory ring, so the 3x3x3
-// validity test runs on shared memory; only cells with a valid neighbour read field values,
-// and the sum walks the neighbours in z, y, x order like the reference loop.  Stamps of cells
-// updated in this layer become layer + 1, which reads as "not yet valid" whether a block sees
-// the old or the new byte.
+// layer l; layer 0 visits the tiles that hold an invalid cell and have a valid cell in their
+// tile neighbourhood.  A visited tile loads the stamps of its cells plus a one-cell halo
+// (10 x 10 x 34 bytes) into shared memory behind one barrier, so the 3x3x3 validity test runs
+// on shared memory; only cells with a valid neighbour read field values, and the sum walks the
+// neighbours in z, y, x order like the reference loop.  Stamps of cells updated in this layer
+// become layer + 1, which reads as "not yet valid" whether a block sees the old or new byte.
 constexpr int kExBX = 32, kExBY = 8, kExBZ = 8;
 
 struct TileGrid {
     int tx, ty, tz;  // tiles per axis
 };
 
+// stamps from the valid mask, and per tile: any valid cell (bit 0), any invalid cell (bit 1)
+__global__ void __launch_bounds__(kExBX * kExBY) stamps_init_kernel(int n0, int n1, int n2,
+                                                                    const uint8_t* __restrict__ valid,
+                                                                    uint8_t* __restrict__ stamp, TileGrid tg,
+                                                                    uint8_t* __restrict__ tile_bits) {
+    const int t = blockIdx.x;
+    const int bx = t % tg.tx, by = (t / tg.tx) % tg.ty, bz = t / (tg.tx * tg.ty);
+    const int i = bx * kExBX + threadIdx.x, j = by * kExBY + threadIdx.y;
+    bool any_valid = false, any_invalid = false;
+    if (i < n0 && j < n1) {
+        for (int k = bz * kExBZ; k < min(n2, bz * kExBZ + kExBZ); ++k) {
+            const long long c = lin3(i, j, k, n0, n1);
+            const bool v = valid[c] != 0;
+            stamp[c] = v ? 0 : 255;
+            any_valid = any_valid || v;
+            any_invalid = any_invalid || !v;
+        }
+    }
+    const int bv = __syncthreads_or(any_valid), bi = __syncthreads_or(any_invalid);
+    if (threadIdx.x == 0 && threadIdx.y == 0) tile_bits[t] = (uint8_t)((bv ? 1 : 0) | (bi ? 2 : 0));
+}
+
+// layer-0 activity: tiles with an invalid cell and a valid cell in their tile neighbourhood
+__global__ void tiles_layer0_kernel(TileGrid tg, const uint8_t* __restrict__ tile_bits, uint8_t* __restrict__ act) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ntiles = tg.tx * tg.ty * tg.tz;
+    if (t >= ntiles) return;
+    const int bx = t % tg.tx, by = (t / tg.tx) % tg.ty, bz = t / (tg.tx * tg.ty);
+    bool near_valid = false;
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int x = bx + dx, y = by + dy, z = bz + dz;
+                if (x < 0 || y < 0 || z < 0 || x >= tg.tx || y >= tg.ty || z >= tg.tz) continue;
+                near_valid = near_valid || (tile_bits[x + tg.tx * (y + tg.ty * z)] & 1);
+            }
+    act[t] = ((tile_bits[t] & 2) && near_valid) ? 1 : 0;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kExBX * kExBY) extrapolate_layer_kernel(int n0, int n1, int n2, T* __restrict__ g,
                                                                           uint8_t* __restrict__ stamp, int layer,
                                                                           TileGrid tg, const uint8_t* __restrict__ act_in,
                                                                           uint8_t* __restrict__ act_out) {
-    __shared__ uint8_t ring[3][kExBY + 2][kExBX + 2];
+    __shared__ uint8_t box[kExBZ + 2][kExBY + 2][kExBX + 2];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = tx + kExBX * ty;
     const int ntiles = tg.tx * tg.ty * tg.tz;
-    constexpr int kHalo = (kExBX + 2) * (kExBY + 2);
+    constexpr int kBox = (kExBZ + 2) * (kExBY + 2) * (kExBX + 2);
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        if (act_in && !act_in[t]) continue;  // block-uniform
+        if (!act_in[t]) continue;  // block-uniform
         const int bx = t % tg.tx, by = (t / tg.tx) % tg.ty, bz = t / (tg.tx * tg.ty);
-        const int i0 = bx * kExBX, j0 = by * kExBY, k0 = bz * kExBZ, k1 = min(n2, k0 + kExBZ);
+        const int i0 = bx * kExBX, j0 = by * kExBY, k0 = bz * kExBZ;
         const int i = i0 + tx, j = j0 + ty;
-        // plane z of the tile + halo into a ring slot; out-of-grid cells read as invalid (255)
-        auto load_plane = [&](int slot, int z) {
-            bool any = false;
-            for (int q = tid; q < kHalo; q += kExBX * kExBY) {
-                const int hx = q % (kExBX + 2), hy = q / (kExBX + 2);
-                const int x = i0 + hx - 1, y = j0 + hy - 1;
-                uint8_t v = 255;
-                if (z >= 0 && z < n2 && x >= 0 && x < n0 && y >= 0 && y < n1) v = stamp[lin3(x, y, z, n0, n1)];
-                ring[slot][hy][hx] = v;
-                any = any || v <= layer;
-            }
-            return any;
-        };
-        int has_valid[3];
-        has_valid[0] = __syncthreads_or(load_plane(0, k0 - 1));
-        has_valid[1] = __syncthreads_or(load_plane(1, k0));
+        // stamps of the tile and its one-cell halo; out-of-grid cells read as invalid (255)
+        for (int q = tid; q < kBox; q += kExBX * kExBY) {
+            const int hx = q % (kExBX + 2), hy = (q / (kExBX + 2)) % (kExBY + 2), hz = q / ((kExBX + 2) * (kExBY + 2));
+            const int x = i0 + hx - 1, y = j0 + hy - 1, z = k0 + hz - 1;
+            uint8_t v = 255;
+            if (x >= 0 && x < n0 && y >= 0 && y < n1 && z >= 0 && z < n2) v = stamp[lin3(x, y, z, n0, n1)];
+            box[hz][hy][hx] = v;
+        }
+        __syncthreads();
         bool changed = false;
-        for (int k = k0; k < k1; ++k) {
-            const int sm = (k - k0) % 3, sc = (k - k0 + 1) % 3, sp = (k - k0 + 2) % 3;
-            has_valid[sp] = __syncthreads_or(load_plane(sp, k + 1));
-            if ((has_valid[0] | has_valid[1] | has_valid[2]) && i < n0 && j < n1 && ring[sc][ty + 1][tx + 1] > layer) {
-                const int slots[3] = {sm, sc, sp};
+        if (i < n0 && j < n1) {
+            for (int kk = 0; kk < kExBZ; ++kk) {
+                const int k = k0 + kk;
+                if (k >= n2) break;
+                if (box[kk + 1][ty + 1][tx + 1] <= layer) continue;
                 T sum = T(0);
                 int count = 0;
 #pragma unroll
@@ -91,7 +118,7 @@ __global__ void __launch_bounds__(kExBX * kExBY) extrapolate_layer_kernel(int n0
                     for (int dj = 0; dj < 3; ++dj)
 #pragma unroll
                         for (int di = 0; di < 3; ++di)
-                            if (ring[slots[dk]][ty + dj][tx + di] <= layer) {
+                            if (box[kk + dk][ty + dj][tx + di] <= layer) {
                                 sum = add_rn2(sum, g[lin3(i + di - 1, j + dj - 1, k + dk - 1, n0, n1)]);
                                 ++count;
                             }
@@ -102,10 +129,10 @@ __global__ void __launch_bounds__(kExBX * kExBY) extrapolate_layer_kernel(int n0
                     changed = true;
                 }
             }
-            __syncthreads();
         }
-        // flag this tile's 3x3x3 tile neighbourhood for the next layer
-        if (__syncthreads_or(changed) && act_out && tid < 27) {
+        // flag this tile's 3x3x3 tile neighbourhood for the next layer (the barrier also keeps
+        // the box intact until every thread is done with it)
+        if (__syncthreads_or(changed) && tid < 27) {
             const int ox = bx + tid % 3 - 1, oy = by + (tid / 3) % 3 - 1, oz = bz + tid / 9 - 1;
             if (ox >= 0 && ox < tg.tx && oy >= 0 && oy < tg.ty && oz >= 0 && oz < tg.tz)
                 act_out[ox + tg.tx * (oy + tg.ty * oz)] = 1;
@@ -268,17 +295,19 @@ int launch_extrapolate(el_ctx* ctx, int field, uint8_t* valid, int layers, bool 
     field_dims(ctx, field, n0, n1, n2);
     const long long n = (long long)n0 * n1 * n2;
     uint8_t* stamp = ctx->valid_tmp;
-    stamps_from_valid_kernel<<<g1(ctx, n), 256, 0, ctx->stream>>>(n, valid, stamp);
     dim3 block(kExBX, kExBY, 1);
     const TileGrid tg{(n0 + kExBX - 1) / kExBX, (n1 + kExBY - 1) / kExBY, (n2 + kExBZ - 1) / kExBZ};
     const int ntiles = tg.tx * tg.ty * tg.tz;
+    // three tile maps in the context's tile buffer: per-tile bits, and the layer's input and output
+    uint8_t* bits = ctx->ex_tiles;
+    uint8_t* act[2] = {ctx->ex_tiles + ntiles, ctx->ex_tiles + 2 * ntiles};
+    stamps_init_kernel<<<ntiles, block, 0, ctx->stream>>>(n0, n1, n2, valid, stamp, tg, bits);
+    tiles_layer0_kernel<<<(ntiles + 255) / 256, 256, 0, ctx->stream>>>(tg, bits, act[0]);
+    int launched = 2;
     const int grid = std::max(1, std::min(ntiles, ctx->num_sms * 6));
-    // two activity maps (the layer's input and output) live in the context's tile buffer
-    uint8_t* act[2] = {ctx->ex_tiles, ctx->ex_tiles + ntiles};
     const int L = std::min(layers, 254);  // stamps are bytes: 255 marks "still invalid"
-    int launched = 1;
     for (int l = 0; l < L; ++l) {
-        uint8_t* in = l == 0 ? nullptr : act[l & 1];
+        uint8_t* in = act[l & 1];
         uint8_t* out = act[(l + 1) & 1];
         cudaMemsetAsync(out, 0, ntiles, ctx->stream);
         if (ctx->dtype == EL_F64)
