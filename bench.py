@@ -52,9 +52,12 @@ def load_package():
 def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (pool256: 20, batch32: 100)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="pool256", choices=["pool256", "batch32"],
+                    help="pool256: one 256^3 scene (the headline); batch32: 32 scenes in one graph per step")
+    ap.add_argument("--scenes", type=int, default=32, help="batch32: number of scenes")
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--tol", type=float, default=1e-6)
@@ -63,7 +66,10 @@ def parse_args(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--error-steps", type=int, default=2)
-    return ap.parse_args(argv)
+    args = ap.parse_args(argv)
+    if args.steps is None:
+        args.steps = 100 if args.workload == "batch32" else 20
+    return args
 
 
 # ---- distributed plumbing (replicas: no data-path collective) -----------------------------
@@ -349,6 +355,158 @@ def run_ours(args, dist):
     return out
 
 
+# ---- batched scenes ---------------------------------------------------------------------------
+
+BATCH_METRIC = "aggregate cell-updates/s, batched scenes (one CUDA graph launch per step)"
+
+
+def batch_specs(el, args):
+    return el.scenes.batch_scenes(args.scenes, args.seed)
+
+
+def batch_workload_name(args):
+    return (f"batch of {args.scenes} scenes, seed {args.seed}: sizes U{{48..160}} per axis, fill 0.2-0.6, "
+            f"dam break or sphere drop, room walls; FP32 fields, mixed PCG (FP64 refinement) to rel. resid "
+            f"{args.tol}; phi WENO6/RK2, velocity trilinear/RK3, g 9.8, CFL 1.0 sub-steps of 1/60 s frames")
+
+
+def step_bytes(el, sim, params):
+    """Algorithmic bytes of one step of a scene, summed over the kernel classes (one profiled step)."""
+    sim._check(sim.lib.el_ctx_profile_begin(sim.h, (1 << 12) - 1), "profile_begin")
+    sim.step(next_dt(sim), params)
+    prof = read_profile(el, sim)
+    return sum(v["bytes"] for v in prof.values())
+
+
+def run_batch(args, dist):
+    import numpy as np
+    import torch
+
+    el = load_package()
+    el.load()
+    torch.cuda.set_device(dist.local_rank)
+    K, W = args.steps, max(3, args.warmup)
+    params = step_params(el, el.SOLVER_MIXED, args.tol)
+    specs = batch_specs(el, args)
+    dev = torch.cuda.current_device()
+    sims = []
+    for spec in specs:
+        sim = el.Simulator(*spec["shape"], dtype=el.EL_F32, device=dev)
+        sim.init_scene(spec)
+        sims.append(sim)
+    cells = sum(s.ni * s.nj * s.nk for s in sims)
+    # algorithmic bytes of a step of every scene, from one profiled step of a copy of each
+    total_bytes = 0.0
+    for spec in specs:
+        with el.Simulator(*spec["shape"], dtype=el.EL_F32, device=dev) as c:
+            c.init_scene(spec)
+            total_bytes += step_bytes(el, c, params)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    batch = el.Batch(sims, params=params, cfl=1.0, dt_frame=1.0 / 60.0)
+    capture_s = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(batch.stream)
+    batch.step(W)
+    batch.sync()
+    batch.reset_stats()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(dist.local_rank) if dist.rank == 0 else None
+    dist.barrier()
+    torch.cuda.synchronize()
+    if sampler:
+        sampler.start()
+    ev0.record(stream)
+    batch.step(K)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop() if sampler else None
+    dist.barrier()
+    elapsed = dist.max(ev0.elapsed_time(ev1))
+    stats = batch.stats()
+    launches = sum(s["kernels"] for s in stats)
+    ms_per_step = elapsed / K
+    value = cells * K * dist.world / (elapsed / 1e3)
+
+    e2e = None
+    if not args.no_e2e:
+        Ke = max(3, min(K, 10))
+        host = []
+        for sim in sims:
+            h = {}
+            for f in ("phi", "u", "v", "w", "pressure"):
+                h[f] = torch.empty(sim.shape(f), dtype=torch.float32, pin_memory=True).numpy()
+                sim.download(f, out=h[f])
+            host.append(h)
+        h2d = sum(h[f].nbytes for h in host for f in ("phi", "u", "v", "w"))
+        d2h = sum(h[f].nbytes for h in host for f in ("phi", "u", "v", "w", "pressure"))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(Ke):
+            for sim, h in zip(sims, host):
+                for f in ("phi", "u", "v", "w"):
+                    sim.upload(f, h[f])
+            batch.step(1)
+            for sim, h in zip(sims, host):
+                for f in ("phi", "u", "v", "w", "pressure"):
+                    sim.download(f, out=h[f])
+        torch.cuda.synchronize()
+        e2e_s = dist.max((time.perf_counter() - t0) / Ke)
+        e2e = {"value": cells * dist.world / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "steps": Ke}
+    batch.close()
+    for s in sims:
+        s.close()
+
+    hbm, peak_kind = peaks()
+    achieved = total_bytes / (ms_per_step / 1e3) / 1e9
+    roofline = {"kernel": "whole step, all scenes (every kernel class)", "bound": "hbm", "achieved": achieved,
+                "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": None,
+                "bytes_per_launch": total_bytes}
+    iters = [s["iterations"] / max(1, s["steps"]) for s in stats]
+    out = {
+        "metric": BATCH_METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": dist.world, "steps": K,
+        "warmup": W, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 fields; pressure solve f32 inner / f64 refinement", "data": "synthetic",
+        "config": {"workload": batch_workload_name(args), "scenes": args.scenes, "seed": args.seed,
+                   "cells": cells, "sizes": [list(s["shape"]) for s in specs],
+                   "parallelism": f"replicas x{dist.world}",
+                   "l2": f"inputs larger than L2 ({cells} cells, > 1 GB of fields), no flush"},
+        "batch": {"graph_capture_s": capture_s, "pcg_iterations_per_step_mean": statistics.mean(iters),
+                  "unconverged_steps": sum(s["unconverged_steps"] for s in stats),
+                  "no_fluid_steps": sum(s["no_fluid_steps"] for s in stats),
+                  "bad_steps": sum(s["bad_steps"] for s in stats),
+                  "max_relres": max(s["max_relres"] for s in stats),
+                  "simulated_time_s": [round(s["time"], 6) for s in stats]},
+        "roofline": roofline, "gpu_launches": launches, "graph_launches": K, "clocks": clocks, "e2e": e2e,
+    }
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_batch(specs, args.tol)
+    return out
+
+
+def cpu_baseline_batch(specs, tol, which=0):
+    """One step of one scene of the batch on the CPU oracle, as cell-updates/s."""
+    import numpy as np
+
+    sys.path.insert(0, ROOT)
+    import oracle as O
+    from oracle import step as S
+
+    spec = specs[which]
+    ni, nj, nk = spec["shape"]
+    phi, solid = O.rasterise(spec, np.float32)
+    wts = O.compute_weights(solid)
+    st = S.initial_state(phi, wts, O.cell_solid_phi(solid), O.float_dx(ni, np.float32))
+    t0 = time.perf_counter()
+    dt = min(O.calc_time_step(st["u"], st["v"], st["w"], st["dx"], 1.0), 1.0 / 60.0)
+    st, _ = S.step(st, dt, 0, 1, 1, 0, 9.8, tol=tol, maxit=20000)
+    elapsed = time.perf_counter() - t0
+    return {"value": ni * nj * nk / elapsed, "unit": "cell-updates/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"1 step of scene {which} ({ni}x{nj}x{nk}) of the batch on the CPU oracle (OpenMP, FP32 "
+                      f"fields, MIC(0)-PCG FP64 to {tol}; {st['pcg_iterations']} iterations), {elapsed:.2f} s"}
+
+
 # ---- the reference's CPU path (the oracle port) ------------------------------------------
 
 def cpu_baseline(n, seed, tol, steps):
@@ -382,9 +540,37 @@ def _scenes_module():
     return mod
 
 
+def run_reference_batch(args, dist):
+    scenes = _scenes_module()
+    specs = scenes.batch_scenes(args.scenes, args.seed)
+    # a bounded sample: one step of each of the first scenes until about 10 s of CPU work
+    t0 = time.perf_counter()
+    cells = 0
+    samples = []
+    for q in range(len(specs)):
+        b = cpu_baseline_batch(specs, args.tol, q)
+        cells += specs[q]["shape"][0] * specs[q]["shape"][1] * specs[q]["shape"][2]
+        samples.append(q)
+        if time.perf_counter() - t0 > 10.0:
+            break
+    elapsed = time.perf_counter() - t0
+    value = cells / elapsed
+    return {"metric": BATCH_METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": dist.world, "steps": 1,
+            "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 fields; pressure f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": batch_workload_name(args) + " (same as our arm)", "scenes": args.scenes,
+                       "seed": args.seed, "parallelism": "host cores"},
+            "cpu_baseline": {"kind": "port", "cores": b["cores"], "value": value, "unit": "cell-updates/s",
+                             "sample": f"1 step each of scenes {samples} on the CPU oracle (OpenMP), "
+                                       f"{cells} cell-updates in {elapsed:.1f} s"},
+            "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def run_reference(args, dist):
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
     os.environ.setdefault("OMP_PROC_BIND", "close")
+    if args.workload == "batch32":
+        return run_reference_batch(args, dist)
     steps = max(1, min(args.steps, 2))
     base = cpu_baseline(args.n, args.seed, args.tol, steps)
     return {"metric": METRIC, "value": base["value"], "unit": "steps/s", "n_gpus": dist.world, "steps": steps,
@@ -405,7 +591,7 @@ def main(argv=None):
             if dist.rank == 0:
                 print(json.dumps(run_reference(args, dist)), flush=True)
             return 0
-        out = run_ours(args, dist)
+        out = run_batch(args, dist) if args.workload == "batch32" else run_ours(args, dist)
         if dist.rank == 0:
             print(json.dumps(out), flush=True)
         return 0

@@ -84,6 +84,16 @@ class Grid(C.Structure):
     _fields_ = [("ni", C.c_int), ("nj", C.c_int), ("nk", C.c_int), ("dx", C.c_double)]
 
 
+class BatchStats(C.Structure):
+    _fields_ = [("steps", C.c_int64), ("frames", C.c_int64), ("iterations", C.c_int64),
+                ("outer_iterations", C.c_int64), ("kernels", C.c_int64), ("unconverged_steps", C.c_int64),
+                ("no_fluid_steps", C.c_int64), ("bad_steps", C.c_int64), ("time", C.c_double),
+                ("last_dt", C.c_double), ("max_relres", C.c_double), ("frame_time", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _lib = None
 
 
@@ -148,6 +158,19 @@ def _declare(L):
     L.el_advect_collocated_grid.argtypes = [C.POINTER(Grid), i, vp, vp, vp, vp, vp, d, i, i, vp]
     L.el_advect_staggered_grid.argtypes = [C.POINTER(Grid), i, vp, vp, vp, vp, vp, vp, vp, vp, vp, d, i, i, vp]
     L.el_compute_staggered_grid_weight.argtypes = [C.POINTER(Grid), i, vp, vp, vp, vp, vp]
+    bp = C.c_void_p
+    L.el_batch_create.argtypes = [C.POINTER(C.c_void_p), i, C.POINTER(StepParams), d, d, C.POINTER(C.c_void_p)]
+    L.el_batch_destroy.argtypes = [bp]
+    L.el_batch_last_error.argtypes = [bp]
+    L.el_batch_last_error.restype = C.c_char_p
+    L.el_batch_step.argtypes = [bp, i]
+    L.el_batch_sync.argtypes = [bp]
+    L.el_batch_stats_get.argtypes = [bp, C.POINTER(BatchStats)]
+    L.el_batch_stats_reset.argtypes = [bp]
+    L.el_batch_get_stream.argtypes = [bp]
+    L.el_batch_get_stream.restype = vp
+    L.el_batch_graph_kernels.argtypes = [bp]
+    L.el_batch_graph_kernels.restype = C.c_int64
 
 
 def status_string(status):
@@ -358,6 +381,68 @@ class Simulator:
 
     def update_velocity_using_pressure(self, dt):
         self._check(self.lib.el_update_velocity_using_pressure(self.h, dt), "update_velocity_using_pressure")
+
+
+class Batch:
+    """Scenes advanced together, one CUDA graph launch per sub-step (el_batch_*).
+
+    Each sub-step is Simulator::update's CFL sub-step (simulator.cpp:23-42) of every scene with
+    its own dt, decided on the device.  `scenes` are Simulator objects; they must outlive the
+    batch and must not be stepped on their own between batch steps."""
+
+    def __init__(self, scenes, params=None, cfl=1.0, dt_frame=1.0 / 60.0, **kw):
+        self.lib = load()
+        self.scenes = list(scenes)
+        prm = params if params is not None else step_params(**kw)
+        arr = (C.c_void_p * len(self.scenes))(*[s.h.value for s in self.scenes])
+        h = C.c_void_p()
+        st = self.lib.el_batch_create(arr, len(self.scenes), C.byref(prm), cfl, dt_frame, C.byref(h))
+        if st != EL_OK:
+            msg = self.lib.el_ctx_last_error(self.scenes[0].h).decode() if self.scenes else ""
+            raise ELError(st, f"el_batch_create: {status_string(st)}: {msg}")
+        self.h = h
+
+    def _check(self, st, what):
+        if st != EL_OK:
+            raise ELError(st, f"{what}: {status_string(st)}: {self.lib.el_batch_last_error(self.h).decode()}")
+
+    def step(self, steps=1):
+        self._check(self.lib.el_batch_step(self.h, steps), "el_batch_step")
+
+    def sync(self):
+        self._check(self.lib.el_batch_sync(self.h), "el_batch_sync")
+
+    def stats(self):
+        out = (BatchStats * len(self.scenes))()
+        self._check(self.lib.el_batch_stats_get(self.h, out), "el_batch_stats_get")
+        return [o.as_dict() for o in out]
+
+    def reset_stats(self):
+        self._check(self.lib.el_batch_stats_reset(self.h), "el_batch_stats_reset")
+
+    @property
+    def stream(self):
+        return self.lib.el_batch_get_stream(self.h)
+
+    def graph_kernels(self):
+        return self.lib.el_batch_graph_kernels(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.el_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 # ---- stateless operators on caller-owned device memory ------------------------------------

@@ -29,6 +29,10 @@ int launch_set_dt(el_ctx* ctx, double dt);
 int launch_emit(el_ctx* ctx, int target, int kind, const double* a, int na);
 int solve_system(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st);
 int setup_solver_storage(el_ctx* ctx, int solver);
+int launch_substep(el_ctx* ctx, double cfl, double dt_frame, const BatchRecord* rec, unsigned long long* scratch_max);
+int enqueue_solve_device(el_ctx* ctx, const el_solve_params& prm, int kernels[3]);
+int enqueue_step_device(el_ctx* ctx, const el_step_params& p, double cfl, double dt_frame, const BatchRecord* rec,
+                        int kernels[3]);
 
 int set_error(el_ctx* ctx, int code, const std::string& msg) {
     if (ctx) ctx->last_error = msg;
@@ -194,6 +198,8 @@ EL_API int el_ctx_destroy(el_ctx* ctx) {
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     for (auto& g : ctx->iter_graph)
         if (g) cudaGraphExecDestroy(g);
+    for (auto& bs : ctx->body_stream)
+        if (bs) cudaStreamDestroy(bs);
     if (ctx->hscal) cudaFreeHost(ctx->hscal);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -527,6 +533,32 @@ EL_API int el_step(el_ctx* ctx, double dt, const el_step_params* p, el_step_stat
     rc = solve_pressure_impl(ctx, p->solve, &st->solve);
     if (rc != EL_OK) return rc;
     return st->solve.status == EL_OK ? EL_OK : set_error(ctx, st->solve.status, "pressure solve did not converge");
+}
+
+// One sub-step of a scene with nothing decided on the host, for capture into a batch graph:
+// device dt (cut at the frame end), el_step's work, the solve with both loops on the device.
+// kernels[0]: kernels outside the solver loops; [1] per refinement sweep; [2] per PCG pass.
+int el::enqueue_step_device(el_ctx* ctx, const el_step_params& p, double cfl, double dt_frame,
+                            const BatchRecord* rec, int kernels[3]) {
+    int n = launch_substep(ctx, cfl, dt_frame, rec, (unsigned long long*)(ctx->dscal + 3));
+    const Scalars* dts = ctx->dscal;
+    for (int comp = 0; comp < 3; ++comp)
+        n += launch_extrapolate(ctx, EL_FIELD_U + comp, (uint8_t*)ctx->field[EL_FIELD_VALID_U + comp],
+                                p.extrapolation_layers, true);
+    n += launch_extrapolate(ctx, EL_FIELD_PHI, (uint8_t*)ctx->field[EL_FIELD_VALID_PHI], p.extrapolation_layers,
+                            false);
+    n += advect_level_set_impl(ctx, dts, 0.0, p.trace_phi, p.sample_phi);
+    n += advect_velocity_impl(ctx, dts, 0.0, p.trace_vel, p.sample_vel);
+    n += launch_masks(ctx, true, p.gravity, dts, 0.0, true);
+    n += launch_flags_build(ctx, true);
+    int rc = check_launch(ctx, "captured step");
+    if (rc != EL_OK) return rc;
+    rc = enqueue_solve_device(ctx, p.solve, kernels);
+    if (rc != EL_OK) return rc;
+    n += launch_scatter_pressure(ctx);
+    n += launch_update_velocity(ctx, ctx->dscal, 0.0);
+    kernels[0] += n;
+    return check_launch(ctx, "captured step");
 }
 
 // ---- projection pieces --------------------------------------------------------------------

@@ -45,6 +45,15 @@ struct Scalars {
     int done;        // 1 once converged (later iteration kernels return at once)
     int bad;         // non-finite value met
     int count;       // fluid cells / changed cells, depending on the kernel
+    int outer;       // mixed solver: refinement sweeps done
+    int inner_total; // mixed solver: inner iterations summed over the sweeps
+    int inner_passes;// device-driven mixed solver: passes of its PCG loop
+};
+
+// Per-scene running totals of a batch (el_batch_stats on the device).
+struct BatchRecord {
+    long long steps, frames, iterations, outer, passes, unconverged, no_fluid, bad;
+    double time, last_dt, max_relres, frame_t;
 };
 
 // Active row segments of one grid level: a segment is 32 consecutive cells of one (j, k) row;
@@ -132,6 +141,7 @@ struct el_ctx {
 
     // captured CUDA graphs of PCG iteration batches, one per solver (index EL_SOLVER_*)
     cudaGraphExec_t iter_graph[3] = {nullptr, nullptr, nullptr};
+    cudaStream_t body_stream[2] = {nullptr, nullptr};  // capture of conditional-node bodies
     int iter_graph_len[3] = {0, 0, 0};
     int iter_graph_kernels[3] = {0, 0, 0};
     bool use_graphs = true;

@@ -499,13 +499,20 @@ __global__ void solve_init_kernel(LGeom g, SegArg seg, const double* __restrict_
         s->bad = finite_d(bb) ? 0 : 1;
         s->done = (bb == 0.0 || bb < s->thresh || s->bad) ? 1 : 0;
         s->beta = 0.0;
+        s->outer = 0;
+        s->inner_total = 0;
+        s->inner_passes = 0;
     }
 }
 
-// mixed solver: inner system r32 = r64 / |r64|, x32 = 0, inner thresholds.
+// mixed solver: inner system r32 = r64 / |r64|, x32 = 0, inner thresholds.  The inner relative
+// tolerance is what the outer one still needs, halved, kept within [floor, 1/2] (FP32 cannot go
+// much below 1e-4 reliably): tau = clamp(0.5 tol |b| / |r|, floor, 0.5).
 __global__ void inner_init_kernel(LGeom g, SegArg seg, const double* __restrict__ r64, float* __restrict__ r32,
-                                  float* __restrict__ x32, const Scalars* so, Scalars* si, double tau,
-                                  double* partials, unsigned* counter) {
+                                  float* __restrict__ x32, const Scalars* so, Scalars* si, double tol,
+                                  double tau_floor, double* partials, unsigned* counter) {
+    const double want = so->rr > 0.0 ? 0.5 * tol * sqrt(so->bb / so->rr) : 0.5;
+    const double tau = fmin(0.5, fmax(tau_floor, want));
     const double norm = sqrt(so->rr);
     const double inv = norm > 0.0 ? 1.0 / norm : 0.0;
     double acc[1] = {0.0};
@@ -1094,12 +1101,11 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
         float* p = ctx->p32;
         float* p_alt = ctx->p32b;
         while (rc == EL_OK && !h->done && outer < std::max(1, prm.max_outer) && inner_total < prm.max_iter) {
-            const double want = prm.tol * sqrt(h->bb / h->rr);
-            const double tau = std::min(0.5, std::max(prm.inner_floor, 0.5 * want));
             {
                 ProfScope prof(ctx, EL_KC_OTHER, (double)n * 16);
                 inner_init_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
-                    g, seg_arg(ctx->seg0), ctx->r64, ctx->r32, ctx->x32, s0, s1, tau, ctx->partials, ctx->counter);
+                    g, seg_arg(ctx->seg0), ctx->r64, ctx->r32, ctx->x32, s0, s1, prm.tol, prm.inner_floor,
+                    ctx->partials, ctx->counter);
             }
             ctx->launches += 1;
             ctx->launches += enqueue_vcycle<float, ushort4, float4>(ctx, mg, ctx->seg0, s1, DOT_INIT);
@@ -1141,6 +1147,160 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
     }
     st->status = h->done ? EL_OK : EL_ERR_NOT_CONVERGED;
     return EL_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Capture-safe mixed solve: the same kernels, with the refinement sweeps and the PCG iterations
+// driven on the device by conditional WHILE nodes of a CUDA graph (no host polling), for
+// steps that are captured whole.  Must be enqueued on a stream that is being captured.
+
+// Condition of the PCG loop: not converged and the inner iteration budget not spent.
+__global__ void inner_cond_kernel(cudaGraphConditionalHandle h, Scalars* so, const Scalars* si, int max_iter,
+                                  int count_pass) {
+    if (count_pass) so->inner_passes += 1;
+    cudaGraphSetConditional(h, (!si->done && si->iter + so->inner_total < max_iter) ? 1u : 0u);
+}
+
+// Condition of the refinement loop.  count_sweep: called after a sweep (adds its iterations);
+// otherwise it sets the condition for the first sweep.
+__global__ void outer_cond_kernel(cudaGraphConditionalHandle h, Scalars* so, const Scalars* si, int max_outer,
+                                  int max_iter, int count_sweep) {
+    if (count_sweep) {
+        so->outer += 1;
+        so->inner_total += si->iter;
+        if (si->bad) so->bad = 1;
+    }
+    const bool go = !so->done && !so->bad && so->outer < max_outer && so->inner_total < max_iter;
+    cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+// A conditional handle on the graph being captured on ctx->stream.
+static int new_handle(el_ctx* ctx, cudaGraphConditionalHandle* handle) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t graph = nullptr;
+    EL_CUDA_TRY(ctx, cudaStreamGetCaptureInfo(ctx->stream, &cs, nullptr, &graph, nullptr, nullptr, nullptr));
+    if (cs != cudaStreamCaptureStatusActive) return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "stream is not capturing");
+    EL_CUDA_TRY(ctx, cudaGraphConditionalHandleCreate(handle, graph, 0, cudaGraphCondAssignDefault));
+    return EL_OK;
+}
+
+// Adds a WHILE node on `handle` after the work captured so far on ctx->stream and redirects
+// ctx->stream to the capture of its body (ended by end_while).  The condition must have been
+// set by a kernel captured before this call.
+static int begin_while(el_ctx* ctx, int depth, cudaGraphConditionalHandle handle, cudaStream_t* parent) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t graph = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* edges = nullptr;
+    size_t ndeps = 0;
+    EL_CUDA_TRY(ctx, cudaStreamGetCaptureInfo(ctx->stream, &cs, nullptr, &graph, &deps, &edges, &ndeps));
+    if (cs != cudaStreamCaptureStatusActive) return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "stream is not capturing");
+    cudaGraphNodeParams prm = {};
+    prm.type = cudaGraphNodeTypeConditional;
+    prm.conditional.handle = handle;
+    prm.conditional.type = cudaGraphCondTypeWhile;
+    prm.conditional.size = 1;
+    cudaGraphNode_t node;
+    EL_CUDA_TRY(ctx, cudaGraphAddNode(&node, graph, deps, edges, ndeps, &prm));
+    EL_CUDA_TRY(ctx, cudaStreamUpdateCaptureDependencies(ctx->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    if (!ctx->body_stream[depth]) return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "loop streams not prepared");
+    EL_CUDA_TRY(ctx, cudaStreamBeginCaptureToGraph(ctx->body_stream[depth], prm.conditional.phGraph_out[0], nullptr,
+                                                   nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    *parent = ctx->stream;
+    ctx->stream = ctx->body_stream[depth];
+    return EL_OK;
+}
+
+static int end_while(el_ctx* ctx, cudaStream_t parent) {
+    cudaGraph_t body = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(ctx->stream, &body);
+    ctx->stream = parent;
+    if (e != cudaSuccess) return set_error(ctx, EL_ERR_CUDA, std::string("loop body: ") + cudaGetErrorString(e));
+    return EL_OK;
+}
+
+// The mixed solve with both loops on the device: no host polling, so it can sit inside a
+// captured step.  The PCG loop runs iterations in pairs (the two direction buffers are back in
+// place after each pass), so it may run one iteration past the budget.
+template <typename T>
+static int enqueue_solve_device_t(el_ctx* ctx, const el_solve_params& prm, int kernels[3]) {
+    const long long n = (long long)ctx->ni * ctx->nj * ctx->nk;
+    const LGeom g = make_geom(ctx->ni, ctx->nj, ctx->nk);
+    Scalars* s0 = ctx->dscal;
+    Scalars* s1 = ctx->dscal + 1;
+    const SplitOp<T> A64 = split_op<T>(ctx);
+    const int max_outer = std::max(1, prm.max_outer);
+    auto& mg = ctx->mg32;
+    mg[0].rec = ctx->A16;
+    mg[0].b = ctx->r32;
+    mg[0].x = ctx->z32;
+    int nk = 0;
+    seg_flags_diag_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
+        g, ctx->diag64, ctx->seg0.total, ctx->seg0.flags);
+    nk += 1 + enqueue_compact(ctx, ctx->seg0, g);
+    solve_init_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
+        g, seg_arg(ctx->seg0), ctx->rhs64, ctx->x64, ctx->r64, s0, prm.tol);
+    pack32_kernel<T><<<grid1d(ctx, n), 256, 0, ctx->stream>>>(n, ctx->diag64, A64.x, A64.y, A64.z, ctx->A32, ctx->A16);
+    nk += 2 + enqueue_coarsen<float, ushort4, float4>(ctx, mg);
+    float* p = ctx->p32;
+    float* p_alt = ctx->p32b;
+    cudaGraphConditionalHandle h_outer, h_inner;
+    cudaStream_t parent_outer, parent_inner;
+    int rc = new_handle(ctx, &h_outer);
+    if (rc != EL_OK) return rc;
+    outer_cond_kernel<<<1, 1, 0, ctx->stream>>>(h_outer, s0, s1, max_outer, prm.max_iter, 0);
+    rc = begin_while(ctx, 0, h_outer, &parent_outer);
+    if (rc != EL_OK) return rc;
+    // one refinement sweep: inner system, its PCG loop, correction and FP64 residual
+    inner_init_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
+        g, seg_arg(ctx->seg0), ctx->r64, ctx->r32, ctx->x32, s0, s1, prm.tol, prm.inner_floor, ctx->partials,
+        ctx->counter);
+    int body = 1 + enqueue_vcycle<float, ushort4, float4>(ctx, mg, ctx->seg0, s1, DOT_INIT);
+    body += enqueue_mg_iteration<float, float4, ushort4, float4>(ctx, ctx->A32, ctx->x32, ctx->r32, ctx->z32, p,
+                                                                p_alt, ctx->ap32, s1, 1, mg);
+    rc = new_handle(ctx, &h_inner);
+    if (rc == EL_OK) {
+        inner_cond_kernel<<<1, 1, 0, ctx->stream>>>(h_inner, s0, s1, prm.max_iter, 0);
+        rc = begin_while(ctx, 1, h_inner, &parent_inner);
+    }
+    if (rc != EL_OK) {
+        end_while(ctx, parent_outer);
+        return rc;
+    }
+    int inner = 0;
+    for (int q = 0; q < 2; ++q)
+        inner += enqueue_mg_iteration<float, float4, ushort4, float4>(ctx, ctx->A32, ctx->x32, ctx->r32, ctx->z32, p,
+                                                                     p_alt, ctx->ap32, s1, 0, mg);
+    inner_cond_kernel<<<1, 1, 0, ctx->stream>>>(h_inner, s0, s1, prm.max_iter, 1);
+    rc = end_while(ctx, parent_inner);
+    accumulate_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
+        g, seg_arg(ctx->seg0), ctx->x64, ctx->x32, s1);
+    residual_kernel<T><<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
+        g, seg_arg(ctx->seg0), A64, ctx->rhs64, ctx->x64, ctx->r64, s0, ctx->partials, ctx->counter);
+    outer_cond_kernel<<<1, 1, 0, ctx->stream>>>(h_outer, s0, s1, max_outer, prm.max_iter, 1);
+    const int rc2 = end_while(ctx, parent_outer);
+    if (rc != EL_OK) return rc;
+    if (rc2 != EL_OK) return rc2;
+    // kernels outside the loops, per refinement sweep, per pass of the PCG loop
+    kernels[0] = nk + 1;
+    kernels[1] = body + 1 + 2 + 1;
+    kernels[2] = inner + 1;
+    return check_launch(ctx, "captured solve");
+}
+
+// Streams on which the loop bodies are captured (created outside any capture).
+int prepare_device_solve(el_ctx* ctx) {
+    for (auto& bs : ctx->body_stream)
+        if (!bs) EL_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
+    return EL_OK;
+}
+
+// Enqueues (for stream capture) the mixed solve of the built system; results land in the
+// device scalars (s0: converged flag, |r|^2, |b|^2, sweeps, inner iterations).
+int enqueue_solve_device(el_ctx* ctx, const el_solve_params& prm, int kernels[3]) {
+    if (prm.solver != EL_SOLVER_MIXED) return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "captured steps use the mixed solver");
+    return ctx->dtype == EL_F64 ? enqueue_solve_device_t<double>(ctx, prm, kernels)
+                                : enqueue_solve_device_t<float>(ctx, prm, kernels);
 }
 
 int solve_system(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) {

@@ -212,6 +212,23 @@ __global__ void time_step_kernel(const unsigned long long* m, T cfl, T dx, Scala
 
 __global__ void set_dt_kernel(Scalars* s, double dt) { s->dt = dt; }
 
+// One sub-step of Simulator::update with use_cfl (simulator.cpp:28-36): dt_sub = calc_time_step
+// in the field type, cut so that the frame ends exactly: if (t + dt_sub > dt_frame) dt_sub =
+// dt_frame - t, with t the time already taken in this frame (kept by the batch record).
+template <typename T>
+__global__ void substep_kernel(const unsigned long long* m, T cfl, T dx, T dt_frame, const BatchRecord* r,
+                               Scalars* s) {
+    const T mx = (T)__longlong_as_double((long long)*m);
+    const T den = mx > T(1e-4) ? mx : T(1e-4);
+    T dt = mul_rn2(cfl, dx) / den;
+    if (dt_frame > T(0)) {
+        const T t = (T)r->frame_t;
+        if (t + dt > dt_frame) dt = dt_frame - t;
+    }
+    s->maxabs = (double)mx;
+    s->dt = (double)dt;
+}
+
 // ---------------------------------------------------------------------------------------
 // emitters (levelset_emitter.cpp:10-79): min(field, f(x)) at the grid's sample positions.
 enum { EMIT_CLEAR = 0, EMIT_SPHERE = 1, EMIT_POOL = 2, EMIT_BOX = 3, EMIT_ROOM = 4 };
@@ -384,6 +401,26 @@ int launch_time_step(el_ctx* ctx, double cfl, unsigned long long* scratch_max) {
         time_step_kernel<double><<<1, 1, 0, ctx->stream>>>(scratch_max, cfl, ctx->dx, ctx->dscal);
     else
         time_step_kernel<float><<<1, 1, 0, ctx->stream>>>(scratch_max, (float)cfl, (float)ctx->dx, ctx->dscal);
+    return 4;
+}
+
+// dt of a batch sub-step into ctx->dscal[0].dt on the device (no host involvement).
+int launch_substep(el_ctx* ctx, double cfl, double dt_frame, const BatchRecord* rec, unsigned long long* scratch_max) {
+    cudaMemsetAsync(scratch_max, 0, sizeof(unsigned long long), ctx->stream);
+    for (int comp = 0; comp < 3; ++comp) {
+        int n0, n1, n2;
+        field_dims(ctx, EL_FIELD_U + comp, n0, n1, n2);
+        const long long n = (long long)n0 * n1 * n2;
+        if (ctx->dtype == EL_F64)
+            maxabs_kernel<double><<<g1(ctx, n), 256, 0, ctx->stream>>>(n, (const double*)ctx->field[EL_FIELD_U + comp], scratch_max);
+        else
+            maxabs_kernel<float><<<g1(ctx, n), 256, 0, ctx->stream>>>(n, (const float*)ctx->field[EL_FIELD_U + comp], scratch_max);
+    }
+    if (ctx->dtype == EL_F64)
+        substep_kernel<double><<<1, 1, 0, ctx->stream>>>(scratch_max, cfl, ctx->dx, dt_frame, rec, ctx->dscal);
+    else
+        substep_kernel<float><<<1, 1, 0, ctx->stream>>>(scratch_max, (float)cfl, (float)ctx->dx, (float)dt_frame, rec,
+                                                        ctx->dscal);
     return 4;
 }
 

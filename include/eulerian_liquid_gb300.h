@@ -227,6 +227,52 @@ int el_advect_staggered_grid(const el_grid* g, int dtype, void* out_u, void* out
 int el_compute_staggered_grid_weight(const el_grid* g, int dtype, void* weight_u, void* weight_v,
                                      void* weight_w, const void* nodal_solid, void* stream);
 
+/* ---- batched scenes: many contexts advanced by one graph launch per step ----------------
+ * No counterpart in the reference, which runs one Simulator per process.  A batch applies the
+ * reference's Simulator::update(update_second_order, dt_frame, use_cfl=true) loop
+ * (simulator.cpp:23-42, apps/eulerian_liquid_3d.cpp:106-120, reinitialize() excluded) to every
+ * scene at once: each batch step is one sub-step of every scene, with the scene's own
+ *   dt_sub = calc_time_step(cfl) (time_stepping.cpp:5-7), cut to end the frame exactly,
+ * computed on the device, then el_step's work with EL_SOLVER_MIXED, whose refinement and PCG
+ * loops run on the device (conditional graph nodes).  All scenes' steps form ONE CUDA graph
+ * (a branch per scene, run concurrently), launched once per batch step.
+ *   - scenes must be distinct contexts on one device, profiling off, solver EL_SOLVER_MIXED;
+ *   - the graph holds the contexts' device buffers: destroy the batch before its contexts, and
+ *     do not step a scene outside the batch between batch steps (el_batch_step checks);
+ *   - uploads and downloads through the contexts are ordered with the batch's launches. */
+typedef struct el_batch el_batch;
+
+typedef struct el_batch_stats {
+    int64_t steps;             /* sub-steps taken */
+    int64_t frames;            /* frames completed (sub-steps summing to dt_frame) */
+    int64_t iterations;        /* inner PCG iterations, summed */
+    int64_t outer_iterations;  /* refinement sweeps, summed */
+    int64_t kernels;           /* kernels the scene's branch ran */
+    int64_t unconverged_steps; /* solves that stopped at max_iter / max_outer */
+    int64_t no_fluid_steps;    /* projections with no fluid cell ("No fluid") */
+    int64_t bad_steps;         /* non-finite residuals */
+    double time;               /* simulated time */
+    double last_dt;
+    double max_relres;         /* largest final |r|/|b| over the steps */
+    double frame_time;         /* time into the current frame */
+} el_batch_stats;
+
+int el_batch_create(el_ctx* const* scenes, int count, const el_step_params* params, double cfl,
+                    double dt_frame, el_batch** out);
+int el_batch_destroy(el_batch* batch);
+const char* el_batch_last_error(const el_batch* batch);
+/* Enqueue `steps` sub-steps (one graph launch each) on the batch's stream; returns without
+ * waiting. */
+int el_batch_step(el_batch* batch, int steps);
+int el_batch_sync(el_batch* batch);
+/* Waits for the batch, then copies `count` per-scene statistics (since creation or the last
+ * reset) to `out`. */
+int el_batch_stats_get(el_batch* batch, el_batch_stats* out);
+int el_batch_stats_reset(el_batch* batch);
+void* el_batch_get_stream(el_batch* batch);
+/* Kernel nodes in the graph outside the solver loops, all scenes. */
+int64_t el_batch_graph_kernels(const el_batch* batch);
+
 /* ---- pressure solve that allocates no device memory ------------------------------------
  * No counterpart in the reference.  Some callers of the pressure solve cannot call cudaMalloc:
  * applications whose device memory is reserved up front by another allocator (a renderer's

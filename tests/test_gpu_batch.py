@@ -1,0 +1,134 @@
+"""Batched scenes (el_batch_*): every scene's CFL sub-step in one CUDA graph launch, with dt and
+the solver loops decided on the device.
+
+The batch must reproduce, scene by scene, the host-driven path that Simulator::update
+(simulator.cpp:23-42) describes: dt_sub = calc_time_step(cfl), cut at the frame end in float,
+then one el_step with the mixed solver.  The same kernels run in the same order with the same
+deterministic device reductions, so the fields are expected to agree exactly; the test allows
+1e-6 relative."""
+
+import numpy as np
+import pytest
+
+import conftest
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("phi", "u", "v", "w", "pressure")
+MATCH = 1e-6
+
+
+def _scene_set(el, specs):
+    sims = []
+    for spec in specs:
+        ni, nj, nk = spec["shape"]
+        sim = el.Simulator(ni, nj, nk, dtype=el.EL_F32)
+        sim.init_scene(spec)
+        sims.append(sim)
+    return sims
+
+
+def _specs(count, seed, lo, hi):
+    return conftest.load_package().scenes.batch_scenes(count, seed, lo=lo, hi=hi)
+
+
+def _params(el, sample_phi=None):
+    return el.step_params(sample_phi=el.SAMPLE_WENO6 if sample_phi is None else sample_phi,
+                          trace_vel=el.TRACE_RK3, gravity=9.8, solver=el.SOLVER_MIXED, tol=1e-6,
+                          max_iter=400, check_every=4, max_outer=8)
+
+
+def _host_substeps(el, sim, params, cfl, dt_frame, steps, frame_t=0.0):
+    """Simulator::update's sub-stepping driven from the host through el_calc_time_step/el_step."""
+    f32 = np.float32
+    out = []
+    for _ in range(steps):
+        dt = f32(sim.calc_time_step(cfl))
+        t = f32(frame_t)
+        if dt_frame > 0 and t + dt > f32(dt_frame):
+            dt = f32(dt_frame) - t
+        st = sim.step(float(dt), params)
+        out.append(st)
+        t = f32(frame_t) + dt
+        frame_t = 0.0 if (dt_frame > 0 and not t < f32(dt_frame)) else float(t)
+    return out, frame_t
+
+
+@pytest.mark.parametrize("cfl,dt_frame", [(1.0, 1.0 / 60.0), (3.0, 0.004)])
+def test_batch_matches_host_driven_steps(el, cfl, dt_frame):
+    specs = _specs(3, 7, 20, 44)
+    params = _params(el)
+    batch_sims = _scene_set(el, specs)
+    host_sims = _scene_set(el, specs)
+    batch = el.Batch(batch_sims, params=params, cfl=cfl, dt_frame=dt_frame)
+    # an odd number of launches, then one more: both graphs and both buffer assignments
+    batch.step(3)
+    batch.step(1)
+    stats = batch.stats()
+    for q, (bs, hs) in enumerate(zip(batch_sims, host_sims)):
+        host, frame_t = _host_substeps(el, hs, params, cfl, dt_frame, 4)
+        for f in FIELDS:
+            a, b = bs.download(f), hs.download(f)
+            assert np.all(np.isfinite(a)), (q, f)
+            assert rel_err(a, b) <= MATCH, (q, f, rel_err(a, b))
+        st = stats[q]
+        assert st["steps"] == 4 and st["bad_steps"] == 0 and st["no_fluid_steps"] == 0
+        assert st["unconverged_steps"] == 0
+        assert st["iterations"] == sum(h["iterations"] for h in host)
+        assert st["outer_iterations"] == sum(h["outer_iterations"] for h in host)
+        assert st["time"] == pytest.approx(sum(h["dt"] for h in host), rel=1e-12)
+        assert st["frame_time"] == pytest.approx(frame_t, rel=1e-6, abs=1e-12)
+        assert st["max_relres"] < 1e-6
+        assert st["kernels"] > 0
+    batch.close()
+    for s in batch_sims + host_sims:
+        s.close()
+
+
+def test_batch_frames_and_reset(el):
+    specs = _specs(2, 3, 24, 32)
+    sims = _scene_set(el, specs)
+    dt_frame = 0.003
+    batch = el.Batch(sims, params=_params(el, el.SAMPLE_TRILINEAR), cfl=4.0, dt_frame=dt_frame)
+    batch.step(6)
+    st = batch.stats()
+    for s in st:
+        # every completed frame is dt_frame long; the clock holds the rest
+        assert s["steps"] == 6
+        assert s["time"] == pytest.approx(s["frames"] * dt_frame + s["frame_time"], rel=1e-5)
+        assert s["last_dt"] <= dt_frame * (1 + 1e-6)
+    batch.reset_stats()
+    st2 = batch.stats()
+    assert all(s["steps"] == 0 and s["iterations"] == 0 for s in st2)
+    assert [s["frame_time"] for s in st2] == [s["frame_time"] for s in st]
+    batch.step(2)
+    assert all(s["steps"] == 2 for s in batch.stats())
+    batch.close()
+    for s in sims:
+        s.close()
+
+
+def test_batch_refuses_scene_stepped_outside(el):
+    specs = _specs(2, 5, 20, 24)
+    sims = _scene_set(el, specs)
+    params = _params(el, el.SAMPLE_TRILINEAR)
+    batch = el.Batch(sims, params=params, cfl=1.0)
+    batch.step(1)
+    sims[1].step(0.001, params)  # swaps that scene's buffers behind the batch's back
+    with pytest.raises(el.ELError) as e:
+        batch.step(1)
+    assert e.value.status == el.EL_ERR_INVALID_ARGUMENT
+    batch.close()
+    for s in sims:
+        s.close()
+
+
+def test_batch_rejects_bad_arguments(el):
+    sims = _scene_set(el, _specs(1, 1, 20, 20))
+    with pytest.raises(el.ELError):
+        el.Batch(sims + sims, params=_params(el))  # the same context twice
+    with pytest.raises(el.ELError):
+        el.Batch(sims, params=el.step_params(solver=el.SOLVER_JACOBI_FP64))
+    for s in sims:
+        s.close()
