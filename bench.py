@@ -58,6 +58,7 @@ def parse_args(argv=None):
     ap.add_argument("--workload", default="pool256", choices=["pool256", "batch32"],
                     help="pool256: one 256^3 scene (the headline); batch32: 32 scenes in one graph per step")
     ap.add_argument("--scenes", type=int, default=32, help="batch32: number of scenes")
+    ap.add_argument("--no-tune", action="store_true", help="batch32: default launch shapes, no autotuning")
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--tol", type=float, default=1e-6)
@@ -401,6 +402,11 @@ def run_batch(args, dist):
         with el.Simulator(*spec["shape"], dtype=el.EL_F32, device=dev) as c:
             c.init_scene(spec)
             total_bytes += step_bytes(el, c, params)
+    tuned = None
+    if not args.no_tune:
+        t0 = time.perf_counter()
+        tuned = el.autotune.tune_batch(el, sims, params, 1.0, 1.0 / 60.0, device_name=torch.cuda.get_device_name())
+        tuned["seconds"] = time.perf_counter() - t0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     batch = el.Batch(sims, params=params, cfl=1.0, dt_frame=1.0 / 60.0)
@@ -472,7 +478,7 @@ def run_batch(args, dist):
                    "cells": cells, "sizes": [list(s["shape"]) for s in specs],
                    "parallelism": f"replicas x{dist.world}",
                    "l2": f"inputs larger than L2 ({cells} cells, > 1 GB of fields), no flush"},
-        "batch": {"graph_capture_s": capture_s, "pcg_iterations_per_step_mean": statistics.mean(iters),
+        "batch": {"graph_capture_s": capture_s, "tuning": tuned, "pcg_iterations_per_step_mean": statistics.mean(iters),
                   "unconverged_steps": sum(s["unconverged_steps"] for s in stats),
                   "no_fluid_steps": sum(s["no_fluid_steps"] for s in stats),
                   "bad_steps": sum(s["bad_steps"] for s in stats),

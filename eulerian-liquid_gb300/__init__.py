@@ -17,6 +17,7 @@ import os
 import numpy as np
 
 from . import build as _build_mod
+from . import autotune  # noqa: F401  (re-exported)
 from . import scenes  # noqa: F401  (re-exported)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -84,6 +85,14 @@ class Grid(C.Structure):
     _fields_ = [("ni", C.c_int), ("nj", C.c_int), ("nk", C.c_int), ("dx", C.c_double)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("seg_blocks_per_sm", C.c_int), ("stencil_blocks_per_sm", C.c_int),
+                ("extrapolate_blocks_per_sm", C.c_int), ("advect_rows", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class BatchStats(C.Structure):
     _fields_ = [("steps", C.c_int64), ("frames", C.c_int64), ("iterations", C.c_int64),
                 ("outer_iterations", C.c_int64), ("kernels", C.c_int64), ("unconverged_steps", C.c_int64),
@@ -132,6 +141,8 @@ def _declare(L):
     L.el_ctx_sync.argtypes = [ctxp]
     L.el_ctx_kernel_launches.argtypes = [ctxp]
     L.el_ctx_kernel_launches.restype = C.c_int64
+    L.el_ctx_set_tuning.argtypes = [ctxp, C.POINTER(Tuning)]
+    L.el_ctx_get_tuning.argtypes = [ctxp, C.POINTER(Tuning)]
     L.el_upload.argtypes = [ctxp, i, vp, sz]
     L.el_download.argtypes = [ctxp, i, vp, sz]
     L.el_field_device_ptr.argtypes = [ctxp, i, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)]
@@ -233,6 +244,16 @@ class Simulator:
         if st == EL_ERR_NO_FLUID:
             raise NoFluid(st, "No fluid")
         raise ELError(st, f"{what}: {status_string(st)}: {msg}")
+
+    # -- launch shapes ----------------------------------------------------------------------
+    def get_tuning(self):
+        t = Tuning()
+        self._check(self.lib.el_ctx_get_tuning(self.h, C.byref(t)), "get_tuning")
+        return t.as_dict()
+
+    def set_tuning(self, **kw):
+        t = Tuning(**{**self.get_tuning(), **kw})
+        self._check(self.lib.el_ctx_set_tuning(self.h, C.byref(t)), "set_tuning")
 
     # -- fields ---------------------------------------------------------------------------
     def shape(self, field):

@@ -58,7 +58,7 @@ __device__ __forceinline__ void backtrace(const Mac<T>& m, T& x, T& y, T& z, T h
 // out(x) = src(trace(x, -dt)) for every sample of src's grid (cell centres or one face
 // component); positions are GridBase::pos = (idx + 0.5) * dx + origin (grid.h:355-367).
 template <typename T, int TRACE, int SAMPLE>
-__global__ void __launch_bounds__(128) advect_kernel(GridView<T> src, T* __restrict__ out, Mac<T> mac,
+__global__ void __launch_bounds__(256) advect_kernel(GridView<T> src, T* __restrict__ out, Mac<T> mac,
                                                      DtArg dt, T dx, T inv_dx) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -89,25 +89,25 @@ GridView<T> make_view(const void* d, int ni, int nj, int nk, T dx, int comp) {
 }
 
 template <typename T, int TRACE, int SAMPLE>
-static void launch_one(const GridView<T>& src, void* out, const Mac<T>& mac, DtArg dt, T dx,
+static void launch_one(const GridView<T>& src, void* out, const Mac<T>& mac, DtArg dt, T dx, int rows,
                        cudaStream_t s) {
-    dim3 block(32, 4, 1);
-    dim3 grid((src.n0 + 31) / 32, (src.n1 + 3) / 4, src.n2);
+    dim3 block(32, rows, 1);
+    dim3 grid((src.n0 + 31) / 32, (src.n1 + rows - 1) / rows, src.n2);
     advect_kernel<T, TRACE, SAMPLE><<<grid, block, 0, s>>>(src, static_cast<T*>(out), mac, dt, dx,
                                                            T(1) / dx);
 }
 
 template <typename T>
 static void launch_dispatch(const GridView<T>& src, void* out, const Mac<T>& mac, DtArg dt, T dx,
-                            int trace, int sample, cudaStream_t s) {
+                            int trace, int sample, int rows, cudaStream_t s) {
     if (trace == EL_TRACE_RK2 && sample == EL_SAMPLE_TRILINEAR)
-        launch_one<T, EL_TRACE_RK2, EL_SAMPLE_TRILINEAR>(src, out, mac, dt, dx, s);
+        launch_one<T, EL_TRACE_RK2, EL_SAMPLE_TRILINEAR>(src, out, mac, dt, dx, rows, s);
     else if (trace == EL_TRACE_RK2 && sample == EL_SAMPLE_WENO6)
-        launch_one<T, EL_TRACE_RK2, EL_SAMPLE_WENO6>(src, out, mac, dt, dx, s);
+        launch_one<T, EL_TRACE_RK2, EL_SAMPLE_WENO6>(src, out, mac, dt, dx, rows, s);
     else if (trace == EL_TRACE_RK3 && sample == EL_SAMPLE_TRILINEAR)
-        launch_one<T, EL_TRACE_RK3, EL_SAMPLE_TRILINEAR>(src, out, mac, dt, dx, s);
+        launch_one<T, EL_TRACE_RK3, EL_SAMPLE_TRILINEAR>(src, out, mac, dt, dx, rows, s);
     else
-        launch_one<T, EL_TRACE_RK3, EL_SAMPLE_WENO6>(src, out, mac, dt, dx, s);
+        launch_one<T, EL_TRACE_RK3, EL_SAMPLE_WENO6>(src, out, mac, dt, dx, rows, s);
 }
 
 // Launch the advection of `which` (0 = cell-centred grid `in`, 1..3 = face component) into out.
@@ -115,22 +115,23 @@ static void launch_dispatch(const GridView<T>& src, void* out, const Mac<T>& mac
 template <typename T>
 static int advect_launch(int ni, int nj, int nk, double dx_d, int comp, void* out, const void* in,
                          const void* vu, const void* vv, const void* vw, DtArg dt, int trace,
-                         int sample, cudaStream_t s) {
+                         int sample, int rows, cudaStream_t s) {
     const T dx = (T)dx_d;
     Mac<T> mac{make_view<T>(vu, ni, nj, nk, dx, 1), make_view<T>(vv, ni, nj, nk, dx, 2),
                make_view<T>(vw, ni, nj, nk, dx, 3)};
     GridView<T> src = make_view<T>(in, ni, nj, nk, dx, comp);
-    launch_dispatch<T>(src, out, mac, dt, dx, trace, sample, s);
+    launch_dispatch<T>(src, out, mac, dt, dx, trace, sample, rows, s);
     return 1;
 }
 
 int advect_any(int dtype, int ni, int nj, int nk, double dx, int comp, void* out, const void* in,
                const void* vu, const void* vv, const void* vw, const Scalars* dts, double dtv,
-               int trace, int sample, cudaStream_t s) {
+               int trace, int sample, cudaStream_t s, int rows) {
     DtArg dt{dts, dtv};
+    rows = (rows == 1 || rows == 2 || rows == 8) ? rows : 4;
     if (dtype == EL_F64)
-        return advect_launch<double>(ni, nj, nk, dx, comp, out, in, vu, vv, vw, dt, trace, sample, s);
-    return advect_launch<float>(ni, nj, nk, dx, comp, out, in, vu, vv, vw, dt, trace, sample, s);
+        return advect_launch<double>(ni, nj, nk, dx, comp, out, in, vu, vv, vw, dt, trace, sample, rows, s);
+    return advect_launch<float>(ni, nj, nk, dx, comp, out, in, vu, vv, vw, dt, trace, sample, rows, s);
 }
 
 }  // namespace el

@@ -12,7 +12,7 @@ namespace el {
 // launchers defined in the kernel translation units
 int advect_any(int dtype, int ni, int nj, int nk, double dx, int comp, void* out, const void* in, const void* vu,
                const void* vv, const void* vw, const Scalars* dts, double dtv, int trace, int sample,
-               cudaStream_t s);
+               cudaStream_t s, int rows = 4);
 int launch_weights(int dtype, int ni, int nj, int nk, const void* solid, void* wu, void* wv, void* ww,
                    cudaStream_t s);
 int launch_cell_solid(el_ctx* ctx);
@@ -230,6 +230,36 @@ EL_API int el_ctx_sync(el_ctx* ctx) {
 
 EL_API int64_t el_ctx_kernel_launches(const el_ctx* ctx) { return ctx ? ctx->launches : -1; }
 
+EL_API int el_ctx_set_tuning(el_ctx* ctx, const el_tuning* t) {
+    CHECK_CTX(ctx);
+    if (!t || t->seg_blocks_per_sm < 1 || t->seg_blocks_per_sm > 8 || t->stencil_blocks_per_sm < 1 ||
+        t->stencil_blocks_per_sm > 8 || t->extrapolate_blocks_per_sm < 1 || t->extrapolate_blocks_per_sm > 16 ||
+        (t->advect_rows != 1 && t->advect_rows != 2 && t->advect_rows != 4 && t->advect_rows != 8))
+        return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "tuning out of range");
+    // the reduction partials are sized for 8 blocks per SM (el_ctx_create)
+    ctx->seg_per_sm = t->seg_blocks_per_sm;
+    ctx->stencil_per_sm = t->stencil_blocks_per_sm;
+    ctx->extrap_per_sm = t->extrapolate_blocks_per_sm;
+    ctx->advect_rows = t->advect_rows;
+    // cached PCG iteration graphs hold the old launch shapes
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& g : ctx->iter_graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    return EL_OK;
+}
+
+EL_API int el_ctx_get_tuning(const el_ctx* ctx, el_tuning* t) {
+    if (!ctx || !t) return EL_ERR_INVALID_ARGUMENT;
+    t->seg_blocks_per_sm = ctx->seg_per_sm;
+    t->stencil_blocks_per_sm = ctx->stencil_per_sm;
+    t->extrapolate_blocks_per_sm = ctx->extrap_per_sm;
+    t->advect_rows = ctx->advect_rows;
+    return EL_OK;
+}
+
 EL_API int el_ctx_profile_begin(el_ctx* ctx, uint32_t class_mask) {
     CHECK_CTX(ctx);
     EL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -363,7 +393,7 @@ static int advect_level_set_impl(el_ctx* ctx, const Scalars* dts, double dt, int
                                               nbytes(ctx, EL_FIELD_V) + nbytes(ctx, EL_FIELD_W));
     int n = advect_any(ctx->dtype, ctx->ni, ctx->nj, ctx->nk, ctx->dx, 0, ctx->tmp[0], ctx->field[EL_FIELD_PHI],
                        ctx->field[EL_FIELD_U], ctx->field[EL_FIELD_V], ctx->field[EL_FIELD_W], dts, dt, trace,
-                       sample, ctx->stream);
+                       sample, ctx->stream, ctx->advect_rows);
     std::swap(ctx->tmp[0], ctx->field[EL_FIELD_PHI]);
     return n;
 }
@@ -377,7 +407,7 @@ static int advect_velocity_impl(el_ctx* ctx, const Scalars* dts, double dt, int 
         ProfScope prof(ctx, EL_KC_ADVECT_VEL, vel_bytes + nbytes(ctx, EL_FIELD_U + comp));
         n += advect_any(ctx->dtype, ctx->ni, ctx->nj, ctx->nk, ctx->dx, comp + 1, ctx->tmp[1 + comp],
                         ctx->field[EL_FIELD_U + comp], ctx->field[EL_FIELD_U], ctx->field[EL_FIELD_V],
-                        ctx->field[EL_FIELD_W], dts, dt, trace, sample, ctx->stream);
+                        ctx->field[EL_FIELD_W], dts, dt, trace, sample, ctx->stream, ctx->advect_rows);
     }
     for (int comp = 0; comp < 3; ++comp) std::swap(ctx->tmp[1 + comp], ctx->field[EL_FIELD_U + comp]);
     return n;

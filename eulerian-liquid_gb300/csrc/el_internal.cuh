@@ -99,6 +99,10 @@ struct el_ctx {
     int dtype = EL_F32;
     size_t esz = 4;
     int num_sms = 152;
+    // launch-shape tuning (el_ctx_set_tuning): resident blocks per SM of the segment kernels,
+    // of the grid-wide stencil / element-wise kernels and of the extrapolation, and the rows of
+    // the advection tile (32 x rows cells per block)
+    int seg_per_sm = 6, stencil_per_sm = 8, extrap_per_sm = 6, advect_rows = 4;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int64_t launches = 0;
@@ -213,12 +217,12 @@ struct Geom {
     int blocks() const { return grid.x * grid.y * grid.z; }
 };
 
-inline Geom stencil_geom(int n0, int n1, int n2, int num_sms) {
+inline Geom stencil_geom(int n0, int n1, int n2, int num_sms, int per_sm = 8) {
     Geom g;
     g.block = dim3(kBX, kBY, 1);
     const int gx = (n0 + kBX - 1) / kBX, gy = (n1 + kBY - 1) / kBY;
-    // aim for ~8 resident blocks of 256 threads per SM, at least one plane per block
-    const long long want = (long long)num_sms * 8;
+    // aim for `per_sm` resident blocks of 256 threads per SM, at least one plane per block
+    const long long want = (long long)num_sms * per_sm;
     int kz = (int)std::max<long long>(1, ((long long)gx * gy * n2 + want - 1) / want);
     kz = std::min(kz, n2);
     const int gz = (n2 + kz - 1) / kz;

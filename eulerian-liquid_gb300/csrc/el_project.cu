@@ -359,7 +359,7 @@ int launch_cell_solid(el_ctx* ctx) {
 }
 
 static Geom plane_geom(el_ctx* ctx) {
-    Geom g = stencil_geom(ctx->ni, ctx->nj, ctx->nk, ctx->num_sms);
+    Geom g = stencil_geom(ctx->ni, ctx->nj, ctx->nk, ctx->num_sms, ctx->stencil_per_sm);
     return g;
 }
 

@@ -726,7 +726,7 @@ __global__ void __launch_bounds__(kCoarsestMaxCells) coarsest_kernel(LGeom g, co
 // host side
 
 static int seg_blocks(el_ctx* ctx, long long total_segments) {
-    const long long warps = (long long)ctx->num_sms * 6 * (kSegThreads / 32);
+    const long long warps = (long long)ctx->num_sms * ctx->seg_per_sm * (kSegThreads / 32);
     const long long need = std::max<long long>(1, std::min<long long>(total_segments, warps));
     return (int)((need * 32 + kSegThreads - 1) / kSegThreads);
 }
@@ -761,7 +761,7 @@ static int enqueue_seglist_rec(el_ctx* ctx, SegList& l, const LGeom& g, const R*
 }
 
 static int grid1d(el_ctx* ctx, long long n) {
-    return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, (long long)ctx->num_sms * 8));
+    return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, (long long)ctx->num_sms * ctx->stencil_per_sm));
 }
 
 // Hierarchy below the finest level (allocated once per context and solver precision).

@@ -288,7 +288,7 @@ __global__ void emit_kernel(int n0, int n1, int n2, T* __restrict__ g, T ox, T d
 static dim3 pgrid(int n0, int n1, int n2, dim3 b) { return dim3((n0 + b.x - 1) / b.x, (n1 + b.y - 1) / b.y, n2); }
 
 static int g1(el_ctx* ctx, long long n) {
-    return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, (long long)ctx->num_sms * 8));
+    return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, (long long)ctx->num_sms * ctx->stencil_per_sm));
 }
 
 static void field_dims(el_ctx* ctx, int field, int& n0, int& n1, int& n2) {
@@ -321,7 +321,7 @@ int launch_extrapolate(el_ctx* ctx, int field, uint8_t* valid, int layers, bool 
     stamps_init_kernel<<<ntiles, block, 0, ctx->stream>>>(n0, n1, n2, valid, stamp, tg, bits);
     tiles_layer0_kernel<<<(ntiles + 255) / 256, 256, 0, ctx->stream>>>(tg, bits, act[0]);
     int launched = 2;
-    const int grid = std::max(1, std::min(ntiles, ctx->num_sms * 6));
+    const int grid = std::max(1, std::min(ntiles, ctx->num_sms * ctx->extrap_per_sm));
     const int L = std::min(layers, 254);  // stamps are bytes: 255 marks "still invalid"
     for (int l = 0; l < L; ++l) {
         uint8_t* in = act[l & 1];

@@ -125,6 +125,18 @@ int el_ctx_sync(el_ctx* ctx);
 /* Number of kernels this library launched on the context since creation. */
 int64_t el_ctx_kernel_launches(const el_ctx* ctx);
 
+/* Launch shapes of the context's kernels (no counterpart in the reference).  Results do not
+ * depend on them beyond the summation order of the device reductions.  A batch takes the
+ * shapes its scenes have when it is created. */
+typedef struct el_tuning {
+    int seg_blocks_per_sm;       /* solver kernels over active row segments, 1..8 (default 6)   */
+    int stencil_blocks_per_sm;   /* matrix build, masks, element-wise kernels, 1..8 (default 8) */
+    int extrapolate_blocks_per_sm; /* extrapolation tiles in flight per SM, 1..16 (default 6)   */
+    int advect_rows;             /* advection tile of 32 x rows cells: 1, 2, 4 or 8 (default 4)  */
+} el_tuning;
+int el_ctx_set_tuning(el_ctx* ctx, const el_tuning* t);
+int el_ctx_get_tuning(const el_ctx* ctx, el_tuning* t);
+
 /* ---- per-kernel-class timing ---------------------------------------------------------
  * While profiling is on, every launch of a class in `class_mask` (bit = 1 << EL_KC_*) is
  * bracketed by CUDA events on the context's stream; el_ctx_profile_end synchronises and

@@ -132,3 +132,44 @@ def test_batch_rejects_bad_arguments(el):
         el.Batch(sims, params=el.step_params(solver=el.SOLVER_JACOBI_FP64))
     for s in sims:
         s.close()
+
+
+def test_autotune_picks_and_caches(el, tmp_path, monkeypatch):
+    cache = tmp_path / "tuning.json"
+    monkeypatch.setenv("EL_GB300_TUNING_CACHE", str(cache))
+    specs = _specs(3, 9, 20, 36)
+    sims = _scene_set(el, specs)
+    params = _params(el, el.SAMPLE_TRILINEAR)
+    before = [s.download("phi") for s in sims]
+    cands = [(6, 8, 6, 4), (2, 4, 3, 2)]
+    r = el.autotune.tune_batch(el, sims, params, device_name="test", steps=2, candidates=cands)
+    assert not r["cached"] and len(r["trials"]) == 2 and cache.exists()
+    # the scenes are back where they started and carry the chosen shapes
+    for s, b in zip(sims, before):
+        assert np.array_equal(s.download("phi"), b)
+        assert s.get_tuning() == r["tuning"]
+    # a second call hits the cache and applies the same shapes
+    for s in sims:
+        s.set_tuning(seg_blocks_per_sm=5)
+    r2 = el.autotune.tune_batch(el, sims, params, device_name="test", steps=2, candidates=cands)
+    assert r2["cached"] and r2["tuning"] == r["tuning"]
+    assert all(s.get_tuning() == r["tuning"] for s in sims)
+    # any tuning gives the same step to round-off of the reductions' order
+    b = el.Batch(sims, params=params)
+    b.step(2)
+    st = b.stats()
+    assert all(x["unconverged_steps"] == 0 and x["bad_steps"] == 0 for x in st)
+    b.close()
+    for s in sims:
+        s.close()
+
+
+def test_tuning_rejects_out_of_range(el):
+    sim = el.Simulator(16, 16, 16)
+    with pytest.raises(el.ELError):
+        sim.set_tuning(seg_blocks_per_sm=9)
+    with pytest.raises(el.ELError):
+        sim.set_tuning(advect_rows=3)
+    sim.set_tuning(seg_blocks_per_sm=2, advect_rows=8)
+    assert sim.get_tuning()["seg_blocks_per_sm"] == 2 and sim.get_tuning()["advect_rows"] == 8
+    sim.close()
