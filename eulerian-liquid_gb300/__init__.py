@@ -60,7 +60,7 @@ class NoFluid(ELError):
 
 class SolveParams(C.Structure):
     _fields_ = [("solver", C.c_int), ("tol", C.c_double), ("max_iter", C.c_int), ("check_every", C.c_int),
-                ("max_outer", C.c_int), ("inner_floor", C.c_double)]
+                ("max_outer", C.c_int), ("inner_floor", C.c_double), ("initial_guess", C.c_int)]
 
 
 class SolveStats(C.Structure):
@@ -188,8 +188,9 @@ def status_string(status):
     return load().el_status_string(status).decode()
 
 
-def solve_params(solver=SOLVER_MIXED, tol=1e-6, max_iter=2000, check_every=4, max_outer=8, inner_floor=1e-4):
-    return SolveParams(solver, tol, max_iter, check_every, max_outer, inner_floor)
+def solve_params(solver=SOLVER_MIXED, tol=1e-6, max_iter=2000, check_every=4, max_outer=8, inner_floor=1e-4,
+                 initial_guess=0):
+    return SolveParams(solver, tol, max_iter, check_every, max_outer, inner_floor, initial_guess)
 
 
 def step_params(trace_phi=TRACE_RK2, sample_phi=SAMPLE_TRILINEAR, trace_vel=TRACE_RK2,
@@ -400,6 +401,13 @@ class Simulator:
         self._check(self.lib.el_download_matrix(self.h, *[o.ctypes.data for o in outs]), "download_matrix")
         return tuple(outs)  # diag, offx, offy, offz, rhs
 
+    def matrix(self):
+        """The system the last build made (no rebuild): diag, offx, offy, offz, rhs as doubles."""
+        shape = (self.nk, self.nj, self.ni)
+        outs = [np.empty(shape, np.float64) for _ in range(5)]
+        self._check(self.lib.el_download_matrix(self.h, *[o.ctypes.data for o in outs]), "download_matrix")
+        return tuple(outs)
+
     def update_velocity_using_pressure(self, dt):
         self._check(self.lib.el_update_velocity_using_pressure(self.h, dt), "update_velocity_using_pressure")
 
@@ -490,3 +498,6 @@ def compute_staggered_grid_weight(ni, nj, nk, dx, dtype, w_ptrs, solid_ptr, stre
     st = load().el_compute_staggered_grid_weight(C.byref(g), dtype, *w_ptrs, solid_ptr, stream)
     if st != EL_OK:
         raise ELError(st, "el_compute_staggered_grid_weight")
+
+
+from . import warmstart  # noqa: E402,F401  (re-exported; needs the names above)

@@ -505,6 +505,56 @@ __global__ void solve_init_kernel(LGeom g, SegArg seg, const double* __restrict_
     }
 }
 
+// ---- warm start: x0 = alpha g with g the pressure grid as it stands --------------------
+// x = g on fluid cells (0 elsewhere); the residual kernel then gives r0 = b - A g.
+template <typename T>
+__global__ void guess_load_kernel(LGeom g, SegArg seg, const T* __restrict__ guess, const double* __restrict__ diag,
+                                  double* __restrict__ x) {
+    SEG_LOOP_BEGIN(seg, g)
+    x[c] = diag[c] > 0.0 ? (double)guess[c] : 0.0;
+    SEG_LOOP_END
+}
+
+// alpha = (g.b) / (g.A g) with A g = b - r0: the scaling of g that minimises |x - x*|_A, so the
+// scaled guess is never further from the solution in that norm than zero is.
+__global__ void guess_alpha_kernel(LGeom g, SegArg seg, const double* __restrict__ x, const double* __restrict__ b,
+                                   const double* __restrict__ r, Scalars* s, double* partials, unsigned* counter) {
+    double acc[2] = {0.0, 0.0};
+    SEG_LOOP_BEGIN(seg, g)
+    const double xc = x[c];
+    acc[0] += xc * b[c];
+    acc[1] += xc * (b[c] - r[c]);
+    SEG_LOOP_END
+    double tot[2];
+    if (grid_sum<2>(acc, partials, counter, tot)) {
+        const double a = (tot[1] > 0.0 && finite_d(tot[0]) && finite_d(tot[1])) ? tot[0] / tot[1] : 0.0;
+        s->aux = a;
+    }
+}
+
+// x = alpha g, r = b - alpha A g = (1 - alpha) b + alpha r0, |r|^2 and the stopping test.
+__global__ void guess_scale_kernel(LGeom g, SegArg seg, double* __restrict__ x, const double* __restrict__ b,
+                                   double* __restrict__ r, Scalars* s, double* partials, unsigned* counter) {
+    const double a = s->aux;
+    double acc[1] = {0.0};
+    SEG_LOOP_BEGIN(seg, g)
+    x[c] = a * x[c];
+    const double rc = (1.0 - a) * b[c] + a * r[c];
+    r[c] = rc;
+    acc[0] += rc * rc;
+    SEG_LOOP_END
+    double tot[1];
+    if (grid_sum<1>(acc, partials, counter, tot)) {
+        s->rr = tot[0];
+        if (!finite_d(tot[0])) {
+            s->bad = 1;
+            s->done = 1;
+        } else {
+            s->done = (s->bb == 0.0 || tot[0] < s->thresh) ? 1 : 0;
+        }
+    }
+}
+
 // mixed solver: inner system r32 = r64 / |r64|, x32 = 0, inner thresholds.  The inner relative
 // tolerance is what the outer one still needs, halved, kept within [floor, 1/2] (FP32 cannot go
 // much below 1e-4 reliably): tau = clamp(0.5 tol |b| / |r|, floor, 0.5).
@@ -1054,6 +1104,20 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
             g, seg_arg(ctx->seg0), ctx->rhs64, ctx->x64, ctx->r64, s0, prm.tol);
     }
     ctx->launches += 1;
+    if (prm.initial_guess) {
+        ProfScope prof(ctx, EL_KC_OTHER, (double)n * 56);
+        const int nb = seg_blocks(ctx, ctx->seg0.total);
+        guess_load_kernel<T><<<nb, kSegThreads, 0, ctx->stream>>>(g, seg_arg(ctx->seg0),
+                                                                  (const T*)ctx->field[EL_FIELD_PRESSURE], ctx->diag64,
+                                                                  ctx->x64);
+        residual_kernel<T><<<nb, kSegThreads, 0, ctx->stream>>>(g, seg_arg(ctx->seg0), A64, ctx->rhs64, ctx->x64,
+                                                                ctx->r64, s0, ctx->partials, ctx->counter);
+        guess_alpha_kernel<<<nb, kSegThreads, 0, ctx->stream>>>(g, seg_arg(ctx->seg0), ctx->x64, ctx->rhs64, ctx->r64,
+                                                                s0, ctx->partials, ctx->counter);
+        guess_scale_kernel<<<nb, kSegThreads, 0, ctx->stream>>>(g, seg_arg(ctx->seg0), ctx->x64, ctx->rhs64, ctx->r64,
+                                                                s0, ctx->partials, ctx->counter);
+        ctx->launches += 4;
+    }
     int rc = EL_OK;
     st->outer_iterations = 1;
     if (prm.solver == EL_SOLVER_JACOBI_FP64) {

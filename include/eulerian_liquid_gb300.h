@@ -85,6 +85,10 @@ typedef struct el_solve_params {
     int check_every;    /* host convergence poll period in iterations (>= 1)             */
     int max_outer;      /* EL_SOLVER_MIXED: refinement sweeps cap                        */
     double inner_floor; /* EL_SOLVER_MIXED: smallest inner relative tolerance (FP32)     */
+    int initial_guess;  /* 1: start from the EL_FIELD_PRESSURE grid as it stands (a warm
+                           start, Eigen's solveWithGuess) instead of zero; the guess is first
+                           scaled by the factor that minimises its energy-norm error,
+                           (g.b)/(g.Ag), so it never starts worse than zero does        */
 } el_solve_params;
 
 typedef struct el_solve_stats {
@@ -284,6 +288,97 @@ int el_batch_stats_reset(el_batch* batch);
 void* el_batch_get_stream(el_batch* batch);
 /* Kernel nodes in the graph outside the solver loops, all scenes. */
 int64_t el_batch_graph_kernels(const el_batch* batch);
+
+/* ---- learned warm start --------------------------------------------------------------
+ * No counterpart in the reference (its pressure solve always starts from zero).  A small 3D
+ * convolutional encoder-decoder maps (level set, divergence, solid mask) to a pressure guess
+ * that el_solve_pressure refines with initial_guess = 1.  Its kernels are below; the network,
+ * the data recorder and the training loop that drive them are eulerian-liquid_gb300/warmstart.py.
+ *
+ * Scene side (contexts; grid sizes divisible by 8).  el_warmstart_features writes the network
+ * input for the context's current system: 16 bf16 channels per cell, channels-last
+ * ((k*nj + j)*ni + i)*16 + c: clamp(phi / 3dx, -1, 1), the right-hand side b / rms(b) on fluid
+ * cells, the solid mask (cell-centred solid phi < 0), zeros.  With build = 1 it first builds the
+ * system for time step dt (as el_build_matrix); with build = 0 it uses the one the last solve
+ * built (recording after el_step).  target (nullable) receives the pressure in the same scaling,
+ * p * a / rms(b) with a = mean(diagonal) / 6, couplings (nullable) the scaled operator A / a in
+ * Laplacian form as 4 bf16 per cell: the diagonal's excess over the fluid faces (the
+ * ghost-fluid terms) and the face weights -A(c, c+e) with the +x, +y, +z neighbours (zeros off
+ * the fluid), and fluid (nullable) 1 on fluid cells: a training tuple.  el_warmstart_set_guess
+ * writes pred * rms(b) / a into EL_FIELD_PRESSURE (0 off the fluid), the scaling of the last
+ * el_warmstart_features call.  scales (nullable, synchronises) receives {rms(b), a, the energy
+ * of the scaled solution target . (A / a) target}. */
+int el_warmstart_features(el_ctx* ctx, int build, double dt, void* features, void* couplings,
+                          float* target, uint8_t* fluid, double* scales);
+int el_warmstart_set_guess(el_ctx* ctx, const float* pred);
+
+/* Network side: stateless kernels on caller-owned device memory, work enqueued on `stream`.
+ * Activations are bf16 channels-last (x fastest, then y, z; channels innermost), one sample.
+ * A 3x3x3 convolution (zero padding, stride 1) reads the concatenation of in_a (ca channels,
+ * optionally at half resolution and upsampled by nearest neighbour on the fly) and in_b (cb
+ * channels); cin = ca + cb; channel counts multiples of 16 (ca, cb multiples of 8).  Supported
+ * (cin, cout): (16,16) (16,32) (32,32) (32,64) (64,64) (128,64) (96,32) (48,16) and, for the
+ * backward-data pass, (32,16) (64,32) (64,128) (32,96) (16,48).  BF16 tensor-core products with
+ * FP32 accumulation. */
+typedef struct el_nn_conv_args {
+    int nx, ny, nz;          /* output grid = fine input grid                                    */
+    int cin, cout;
+    const void* in_a;        /* bf16 [.., ca]                                                    */
+    int ca, upsample_a;      /* upsample_a: in_a is (nx/2, ny/2, nz/2)                            */
+    const void* in_b;        /* bf16 [.., cb]; NULL reads cb channels of zeros                    */
+    int cb;
+    const void* mask;        /* NULL, or bf16 [.., cin]: input zeroed where mask <= 0 (ReLU')     */
+    const void* weights;     /* packed by el_nn_pack_weights (forward or backward-data packing);
+                                unused by el_nn_conv3_backward_weight                             */
+    const float* bias;       /* [cout] or NULL                                                   */
+    int relu;
+    void* out_a;             /* bf16 [.., out_a_channels]: output channels [0, out_a_channels)    */
+    int out_a_channels;
+    void* out_b;             /* bf16 [.., cout - out_a_channels]: the rest (may be NULL if none)  */
+} el_nn_conv_args;
+
+/* y = act(conv(x, W) + bias).  The backward-data pass is the same call with the gradient of the
+ * layer's output as in_a (ca = that layer's cout), mask = the layer's forward output (ReLU'),
+ * the backward packing of W, no bias, no relu, and out_a / out_b the gradients of the layer's
+ * two inputs (the upsampled part at fine resolution; see el_nn_gather8). */
+int el_nn_conv3_forward(const el_nn_conv_args* args, void* stream);
+/* dW[cout][27][cin] += sum_v gm[v][co] x[v + tap][ci] and db += sum_v gm, gm = grad_out * (y > 0)
+ * with y = args->out_a (the layer's forward output); args describes the forward call.  FP32,
+ * summed in a fixed order (deterministic). */
+size_t el_nn_conv3_backward_weight_workspace(int nx, int ny, int nz, int cin, int cout);
+int el_nn_conv3_backward_weight(const el_nn_conv_args* args, const void* grad_out, float* dw, float* db,
+                                void* workspace, size_t workspace_bytes, void* stream);
+/* FP32 master weights [cout][27][cin] -> bf16 forward packing (and, if packed_bwd is not NULL,
+ * the backward-data packing of the transposed, tap-mirrored kernel); each 27*cin*cout*2 bytes. */
+size_t el_nn_packed_weight_bytes(int cin, int cout);
+int el_nn_pack_weights(int cin, int cout, const float* w, void* packed_fwd, void* packed_bwd, void* stream);
+/* 2x2x2 average pooling; its backward is el_nn_spread(scale 1/8, accumulate 1) */
+int el_nn_pool(int nx, int ny, int nz, int c, const void* in, void* out, void* stream);
+/* fine[v] = (accumulate ? fine[v] : 0) + scale * coarse[v / 2] ; (nx, ny, nz) = fine grid */
+int el_nn_spread(int nx, int ny, int nz, int c, const void* coarse, void* fine, float scale, int accumulate,
+                 void* stream);
+/* coarse[V] = sum of its 8 fine children: the backward of nearest upsampling */
+int el_nn_gather8(int nx, int ny, int nz, int c, const void* fine, void* coarse, void* stream);
+/* head: pred[v] = w . d[v] + b over 16 channels (FP32 out) */
+int el_nn_head_forward(int64_t n, const void* d, const float* w, const float* b, float* pred, void* stream);
+/* masked MSE loss and the head's backward: on cells with mask != 0, e = pred - target;
+ * loss[0] += sum e^2 inv_n, grad_d = 2 e inv_n w (bf16, 0 off the mask), dw[16] += dL/dw,
+ * db[0] += dL/db.  The workspace (el_nn_head_workspace bytes) must be zeroed once. */
+size_t el_nn_head_workspace(int64_t n);
+int el_nn_head_loss_backward(int64_t n, const void* d, const float* pred, const float* target, const uint8_t* mask,
+                             const float* w, double inv_n, void* grad_d, double* loss, float* dw, float* db,
+                             void* workspace, size_t workspace_bytes, void* stream);
+/* energy-norm loss (the norm conjugate gradients minimises) and the head's backward, on the
+ * (nx, ny, nz) grid: e = pred - target on cells with fluid != 0, loss[0] += e . A^ e inv_n with
+ * A^ the scaled operator from el_warmstart_features' couplings, grad_d = 2 (A^ e) inv_n w;
+ * dw, db, workspace as el_nn_head_loss_backward. */
+int el_nn_head_energy_loss_backward(int nx, int ny, int nz, const void* d, const float* pred, const float* target,
+                                    const void* couplings, const uint8_t* fluid, const float* w, double inv_n,
+                                    void* grad_d, double* loss, float* dw, float* db, void* workspace,
+                                    size_t workspace_bytes, void* stream);
+/* Adam (bias-corrected, step >= 1) on FP32 parameters; zeroes g afterwards. */
+int el_nn_adam(int64_t n, float* w, float* g, float* m, float* v, float lr, float beta1, float beta2, float eps,
+               int step, void* stream);
 
 /* ---- pressure solve that allocates no device memory ------------------------------------
  * No counterpart in the reference.  Some callers of the pressure solve cannot call cudaMalloc:
