@@ -55,8 +55,15 @@ def parse_args(argv=None):
     ap.add_argument("--steps", type=int, default=None, help="timed steps (pool256: 20, batch32: 100)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="pool256", choices=["pool256", "batch32"],
-                    help="pool256: one 256^3 scene (the headline); batch32: 32 scenes in one graph per step")
+    ap.add_argument("--workload", default="pool256", choices=["pool256", "batch32", "warmstart128"],
+                    help="pool256: one 256^3 scene (the headline); batch32: 32 scenes in one graph per step; "
+                         "warmstart128: record, train and evaluate the learned warm start at 128^3")
+    ap.add_argument("--ws-n", type=int, default=128, help="warmstart128: grid size")
+    ap.add_argument("--ws-samples", type=int, default=4000, help="warmstart128: recorded solves (capped by memory)")
+    ap.add_argument("--ws-steps-per-scene", type=int, default=20)
+    ap.add_argument("--ws-epochs", type=int, default=2)
+    ap.add_argument("--ws-batch", type=int, default=8)
+    ap.add_argument("--ws-eval-scenes", type=int, default=6)
     ap.add_argument("--scenes", type=int, default=32, help="batch32: number of scenes")
     ap.add_argument("--no-tune", action="store_true", help="batch32: default launch shapes, no autotuning")
     ap.add_argument("--n", type=int, default=256)
@@ -513,6 +520,150 @@ def cpu_baseline_batch(specs, tol, which=0):
                       f"fields, MIC(0)-PCG FP64 to {tol}; {st['pcg_iterations']} iterations), {elapsed:.2f} s"}
 
 
+# ---- learned warm start ------------------------------------------------------------------------
+
+WS_METRIC = "pressure-solve speed-up from the learned warm start at 128^3 (zero-guess time / learned time, to 1e-6)"
+
+
+def conv_flops(n):
+    """FLOPs of one forward pass of the network's 3x3x3 convolutions on an n^3 grid."""
+    el = load_package()
+    f = 0
+    for name, _, _, _, cin, cout, level in el.warmstart.CONVS:
+        f += 2 * 27 * cin * cout * (n >> level) ** 3
+    return f
+
+
+def run_warmstart(args, dist):
+    import numpy as np
+    import torch
+
+    el = load_package()
+    el.load()
+    torch.cuda.set_device(dist.local_rank)
+    W = el.warmstart
+    n = args.ws_n
+    params = step_params(el, el.SOLVER_MIXED, args.tol)
+    # memory: 4 + 4 bf16 channels, FP32 target, mask per cell and tuple
+    per = n ** 3 * (8 + 8 + 4 + 1)
+    free, _ = torch.cuda.mem_get_info()
+    samples = int(min(args.ws_samples, 0.6 * free // per))
+    spp = args.ws_steps_per_scene
+    specs = [el.scenes.spheres_pool(n, 1000 + s) for s in range((samples + spp - 1) // spp)]
+    t0 = time.perf_counter()
+    ds = W.record(el, torch, specs, spp, (n, n, n), params, capacity=samples)
+    record_s = time.perf_counter() - t0
+    net = W.WarmStartNet(torch, seed=args.seed, lr=1e-3)
+    # training: one timed step first (CUDA events around forward + backward + Adam of one batch)
+    x = net.input_buffer(n, n, n)
+    x.zero_()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    stream = torch.cuda.current_stream()
+    for warm in range(2):
+        x[..., :4].copy_(ds.x[0])
+        net.forward(n, n, n)
+        net.backward(n, n, n, ds.t[0], ds.f[0], 1.0 / ds.energy[0], couplings=ds.c[0])
+    net.grads.zero_()
+    net.take_loss(n, n, n)
+    torch.cuda.synchronize()
+    reps = 5
+    ev[0].record(stream)
+    for _ in range(reps):
+        net.forward(n, n, n)
+    ev[1].record(stream)
+    for _ in range(reps):
+        net.backward(n, n, n, ds.t[0], ds.f[0], 1.0 / ds.energy[0], couplings=ds.c[0])
+    ev[2].record(stream)
+    torch.cuda.synchronize()
+    fwd_ms = ev[0].elapsed_time(ev[1]) / reps
+    bwd_ms = ev[1].elapsed_time(ev[2]) / reps
+    net.grads.zero_()
+    net.take_loss(n, n, n)
+    F = conv_flops(n)
+    first = 2 * 27 * 16 * 16 * n ** 3  # the first layer has no backward-data pass
+    t0 = time.perf_counter()
+    tr = W.train(net, ds, epochs=args.ws_epochs, batch=args.ws_batch, log=max(1, len(ds) // args.ws_batch // 10))
+    train_s = time.perf_counter() - t0
+    # evaluation on held-out scenes: every step's projection solved from zero and from the guess
+    res = {s: {"zero_it": [], "warm_it": [], "zero_ms": [], "warm_ms": [], "infer_ms": []}
+           for s in ("mixed", "plain_fp64")}
+    solvers = {"mixed": el.SOLVER_MIXED, "plain_fp64": el.SOLVER_JACOBI_FP64}
+    fields = ("phi", "u", "v", "w", "valid_u", "valid_v", "valid_w")
+    for seed in range(args.ws_eval_scenes):
+        sim = el.Simulator(n, n, n, dtype=el.EL_F32)
+        sim.set_stream(stream.cuda_stream)
+        sim.init_scene(el.scenes.spheres_pool(n, 90000 + seed))
+        for k in range(4):
+            dt = min(sim.calc_time_step(1.0), 1 / 60)
+            saved = {f: sim.download(f) for f in fields}
+            for key, solver in solvers.items():
+                for guess in (0, 1):
+                    for f, a in saved.items():
+                        sim.upload(f, a)
+                    sim.extrapolate_velocity(10)
+                    sim.extrapolate_level_set(10)
+                    sim.advect_level_set(dt, el.TRACE_RK2, el.SAMPLE_WENO6)
+                    sim.advect_velocity(dt, el.TRACE_RK3, el.SAMPLE_TRILINEAR)
+                    sim.add_gravity(dt, 9.8)
+                    sim.find_valid_velocity()
+                    sim.set_invalid_velocity_zero()
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    if guess:
+                        W.predict_guess(net, sim, dt)
+                        torch.cuda.synchronize()
+                        res[key]["infer_ms"].append((time.perf_counter() - t0) * 1e3)
+                    st = sim.solve_pressure(dt, solver=solver, tol=args.tol, max_iter=20000,
+                                            check_every=4 if key == "mixed" else 16, initial_guess=guess)
+                    torch.cuda.synchronize()
+                    ms = (time.perf_counter() - t0) * 1e3
+                    res[key]["warm_it" if guess else "zero_it"].append(st["iterations"])
+                    res[key]["warm_ms" if guess else "zero_ms"].append(ms)
+            # advance the scene with the last (warm, plain) step
+        sim.close()
+    summary = {}
+    for key, r in res.items():
+        summary[key] = {"iterations_zero_guess": statistics.mean(r["zero_it"]),
+                        "iterations_learned_guess": statistics.mean(r["warm_it"]),
+                        "ms_zero_guess": statistics.mean(r["zero_ms"]),
+                        "ms_learned_guess_incl_inference": statistics.mean(r["warm_ms"]),
+                        "ms_inference": statistics.mean(r["infer_ms"]),
+                        "speedup": statistics.mean(r["zero_ms"]) / statistics.mean(r["warm_ms"])}
+    hbm, _ = peaks()
+    tflops_peak, peak_kind = bf16_peak()
+    achieved = F / (fwd_ms / 1e3) / 1e12
+    out = {
+        "metric": WS_METRIC, "value": summary["mixed"]["speedup"], "unit": "x", "n_gpus": dist.world,
+        "steps": len(res["mixed"]["zero_it"]), "warmup": 0, "ms_per_step": summary["mixed"]["ms_learned_guess_incl_inference"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 network (FP32 accumulation); f32 fields, pressure f32 inner / f64 refinement",
+        "data": "synthetic: recorded from seeded spheres_pool scenes",
+        "config": {"workload": f"learned warm start at {n}^3: {len(ds)} solves recorded from {len(specs)} "
+                               f"spheres_pool scenes (seeds 1000+, {spp} steps each), 4-level encoder-decoder "
+                               f"16/32/64/64 trained {args.ws_epochs} epochs (batch {args.ws_batch}, Adam, energy-norm "
+                               f"loss); evaluated on {args.ws_eval_scenes} held-out scenes x 4 steps, solves to "
+                               f"{args.tol}", "n": n, "samples": len(ds), "parallelism": "single GPU"},
+        "warmstart": {"solvers": summary, "record_s": record_s, "train_s": train_s, "train_steps": tr["steps"],
+                      "loss_history": tr["history"][-5:], "fwd_ms": fwd_ms, "bwd_ms": bwd_ms},
+        "roofline": {"kernel": "network forward (all 3x3x3 convolutions, mma.sync bf16)", "bound": "tensor",
+                     "achieved": achieved, "peak": tflops_peak, "unit": "TFLOP/s", "frac": achieved / tflops_peak,
+                     "peak_kind": peak_kind, "traffic": None, "flops_per_launch": F,
+                     "backward_tflops": (2 * F - first) / (bwd_ms / 1e3) / 1e12},
+        "gpu_launches": None,
+    }
+    return out
+
+
+def bf16_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        for k in ("bf16_tflops", "bf16_dense_tflops"):
+            if k in d:
+                return float(d[k]), "measured"
+    return 1900.0, "fallback"
+
+
 # ---- the reference's CPU path (the oracle port) ------------------------------------------
 
 def cpu_baseline(n, seed, tol, steps):
@@ -597,7 +748,12 @@ def main(argv=None):
             if dist.rank == 0:
                 print(json.dumps(run_reference(args, dist)), flush=True)
             return 0
-        out = run_batch(args, dist) if args.workload == "batch32" else run_ours(args, dist)
+        if args.workload == "batch32":
+            out = run_batch(args, dist)
+        elif args.workload == "warmstart128":
+            out = run_warmstart(args, dist)
+        else:
+            out = run_ours(args, dist)
         if dist.rank == 0:
             print(json.dumps(out), flush=True)
         return 0

@@ -272,6 +272,7 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double (*sh)[32]) {
 }
 
 // Returns true in thread 0 of the last block, with out[] holding the grid totals.
+// `partials` must hold (number of blocks) * NV doubles.
 template <int NV>
 __device__ bool grid_sum(double (&v)[NV], double* partials, unsigned* counter, double (&out)[NV]) {
     __shared__ double sh[NV][32];

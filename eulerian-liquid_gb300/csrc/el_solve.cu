@@ -538,8 +538,9 @@ __global__ void guess_scale_kernel(LGeom g, SegArg seg, double* __restrict__ x, 
     const double a = s->aux;
     double acc[1] = {0.0};
     SEG_LOOP_BEGIN(seg, g)
-    x[c] = a * x[c];
-    const double rc = (1.0 - a) * b[c] + a * r[c];
+    // a == 0 (a useless or non-finite guess): exactly the zero start, whatever g held
+    x[c] = a != 0.0 ? a * x[c] : 0.0;
+    const double rc = a != 0.0 ? (1.0 - a) * b[c] + a * r[c] : b[c];
     r[c] = rc;
     acc[0] += rc * rc;
     SEG_LOOP_END

@@ -110,6 +110,11 @@ int blocks_for(el_ctx* ctx, long long n) {
     return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, (long long)ctx->num_sms * 8));
 }
 
+// a grid reduction of nv values needs nblocks * nv partials: stay within the context's buffer
+int reduce_blocks(el_ctx* ctx, long long n, int nv) {
+    return std::max(1, std::min(blocks_for(ctx, n), (int)(ctx->max_partials / nv)));
+}
+
 }  // namespace
 
 #define EL_API extern "C" __attribute__((visibility("default")))
@@ -134,7 +139,7 @@ EL_API int el_warmstart_features(el_ctx* ctx, int build, double dt, void* featur
     __nv_bfloat16* coup = static_cast<__nv_bfloat16*>(couplings);
     if (ctx->dtype == EL_F64) {
         const double* p = (const double*)ctx->field[EL_FIELD_PRESSURE];
-        warm_sums_kernel<double><<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(n, ctx->diag64, ctx->rhs64, p, s2,
+        warm_sums_kernel<double><<<reduce_blocks(ctx, n, 4), 256, 0, ctx->stream>>>(n, ctx->diag64, ctx->rhs64, p, s2,
                                                                               ctx->partials, ctx->counter);
         warm_features_kernel<double><<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(
             n, ctx->ni, ctx->nj, (const double*)ctx->field[EL_FIELD_PHI], (const double*)ctx->field[EL_FIELD_SOLID_CELL], ctx->diag64,
@@ -142,7 +147,7 @@ EL_API int el_warmstart_features(el_ctx* ctx, int build, double dt, void* featur
             s2, feat, coup, target, fluid);
     } else {
         const float* p = (const float*)ctx->field[EL_FIELD_PRESSURE];
-        warm_sums_kernel<float><<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(n, ctx->diag64, ctx->rhs64, p, s2,
+        warm_sums_kernel<float><<<reduce_blocks(ctx, n, 4), 256, 0, ctx->stream>>>(n, ctx->diag64, ctx->rhs64, p, s2,
                                                                              ctx->partials, ctx->counter);
         warm_features_kernel<float><<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(
             n, ctx->ni, ctx->nj, (const float*)ctx->field[EL_FIELD_PHI], (const float*)ctx->field[EL_FIELD_SOLID_CELL], ctx->diag64,

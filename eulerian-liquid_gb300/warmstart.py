@@ -374,7 +374,7 @@ def record(el, torch, specs, steps_per_scene, shape, params, cfl=1.0, frame=1.0 
             if st["status"] != EL_OK:
                 continue
             i = ds.n
-            scales = (C.c_double * 3)()
+            scales = (C.c_double * 3)()  # (asking for them also waits for the scene's stream)
             _ok(L.el_warmstart_features(sim.h, 0, 0.0, _p(feat), _p(ds.c[i]), _p(ds.t[i]), _p(ds.f[i]), scales),
                 "features")
             if not scales[2] > 0:
@@ -427,8 +427,12 @@ def predict_guess(net, sim, dt):
     """Build the scene's system for dt, run the network, write the scaled guess into the
     pressure field (ready for solve_pressure(initial_guess=1))."""
     L = lib()
+    torch = net.torch
     x = net.input_buffer(sim.ni, sim.nj, sim.nk)
+    torch.cuda.current_stream().synchronize()  # the input buffer is free
     sim._check(L.el_warmstart_features(sim.h, 1, dt, _p(x), None, None, None, None), "warmstart_features")
+    sim._check(sim.lib.el_ctx_sync(sim.h), "sync")  # features written (the scene's stream)
     pred = net.forward(sim.ni, sim.nj, sim.nk)
+    torch.cuda.current_stream().synchronize()  # prediction written (the network's stream)
     sim._check(L.el_warmstart_set_guess(sim.h, _p(pred)), "warmstart_set_guess")
     return pred
