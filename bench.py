@@ -55,9 +55,10 @@ def parse_args(argv=None):
     ap.add_argument("--steps", type=int, default=None, help="timed steps (pool256: 20, batch32: 100)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="pool256", choices=["pool256", "batch32", "warmstart128"],
+    ap.add_argument("--workload", default="pool256", choices=["pool256", "batch32", "warmstart128", "dam64", "dam128"],
                     help="pool256: one 256^3 scene (the headline); batch32: 32 scenes in one graph per step; "
-                         "warmstart128: record, train and evaluate the learned warm start at 128^3")
+                         "warmstart128: record, train and evaluate the learned warm start at 128^3; "
+                         "dam64 / dam128: the FP64 dam-break workloads at 64^3 and 128^3 (GPU vs the CPU path)")
     ap.add_argument("--ws-n", type=int, default=128, help="warmstart128: grid size")
     ap.add_argument("--ws-samples", type=int, default=4000, help="warmstart128: recorded solves (capped by memory)")
     ap.add_argument("--ws-steps-per-scene", type=int, default=20)
@@ -76,7 +77,7 @@ def parse_args(argv=None):
     ap.add_argument("--error-steps", type=int, default=2)
     args = ap.parse_args(argv)
     if args.steps is None:
-        args.steps = 100 if args.workload == "batch32" else 20
+        args.steps = {"batch32": 100, "dam64": 100, "dam128": 200}.get(args.workload, 20)
     return args
 
 
@@ -276,11 +277,11 @@ def e2e_batch_steps(el, torch, sims, batch, steps):
     return steps / (time.perf_counter() - t0), h2d, d2h
 
 
-def e2e_steps(el, torch, sim, stream, params, steps):
+def e2e_steps(el, torch, sim, stream, params, steps, dtype=None):
     """Steps through the C ABI with host buffers: inputs up, results down, every step."""
     host = {}
     for f in ("phi", "u", "v", "w", "pressure"):
-        t = torch.empty(sim.shape(f), dtype=torch.float32, pin_memory=True)
+        t = torch.empty(sim.shape(f), dtype=dtype or torch.float32, pin_memory=True)
         host[f] = t.numpy()
         host[f][...] = sim.download(f)
     h2d = sum(host[f].nbytes for f in ("phi", "u", "v", "w"))
@@ -550,6 +551,149 @@ def cpu_baseline_batch(specs, tol, which=0):
                       f"fields, MIC(0)-PCG FP64 to {tol}; {st['pcg_iterations']} iterations), {elapsed:.2f} s"}
 
 
+# ---- FP64 dam-break workloads (64^3 trilinear RK2; 128^3 WENO6/RK3 with a seeded velocity) ----------
+
+DAM_METRIC = "steps/s, FP64 dam break, plain FP64 GPU PCG to 1e-6"
+
+
+def dam_setup(args):
+    n = 64 if args.workload == "dam64" else 128
+    weno = args.workload == "dam128"
+    return n, weno
+
+
+def dam_state(el, n, weno, seed):
+    """Initial fields: the dam break scene; at 128^3 a seeded velocity U(-1e-3, 1e-3) on every face."""
+    import numpy as np
+    spec = el.scenes.dam_break(n)
+    fields = {}
+    if weno:
+        rng = np.random.default_rng(seed)
+        for f, shape in (("u", (n, n, n + 1)), ("v", (n, n + 1, n)), ("w", (n + 1, n, n))):
+            fields[f] = rng.uniform(-1e-3, 1e-3, shape)
+    return spec, fields
+
+
+def dam_params(el, weno, tol):
+    if weno:
+        return el.step_params(trace_phi=el.TRACE_RK2, sample_phi=el.SAMPLE_WENO6, trace_vel=el.TRACE_RK3,
+                              sample_vel=el.SAMPLE_TRILINEAR, gravity=9.8, extrapolation_layers=10,
+                              solver=el.SOLVER_JACOBI_FP64, tol=tol, max_iter=20000, check_every=16)
+    return el.step_params(trace_phi=el.TRACE_RK2, sample_phi=el.SAMPLE_TRILINEAR, trace_vel=el.TRACE_RK2,
+                          sample_vel=el.SAMPLE_TRILINEAR, gravity=9.8, extrapolation_layers=10,
+                          solver=el.SOLVER_JACOBI_FP64, tol=tol, max_iter=20000, check_every=16)
+
+
+def dam_workload_name(n, weno, tol, seed):
+    if weno:
+        return (f"dam break {n}^3 FP64 (box x<0.4,y<0.5 + sphere c=(0.7,0.75,0.5) r=0.12, room walls), seeded "
+                f"velocity U(-1e-3,1e-3) (seed {seed}), phi WENO6/RK2, velocity trilinear/RK3, g 9.8, CFL 1.0, "
+                f"plain FP64 PCG to {tol}")
+    return (f"dam break {n}^3 FP64 (box x<0.4,y<0.5 + sphere c=(0.7,0.75,0.5) r=0.12, room walls), u=0, "
+            f"trilinear RK2, g 9.8, CFL 1.0, plain FP64 PCG to {tol}")
+
+
+def run_dam(args, dist):
+    import numpy as np
+    import torch
+
+    el = load_package()
+    el.load()
+    torch.cuda.set_device(dist.local_rank)
+    n, weno = dam_setup(args)
+    K, W = args.steps, max(3, args.warmup)
+    params = dam_params(el, weno, args.tol)
+    spec, fields = dam_state(el, n, weno, args.seed)
+    sim = el.Simulator(n, n, n, dtype=el.EL_F64, device=torch.cuda.current_device())
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
+    sim.init_scene(spec)
+    for f, a in fields.items():
+        sim.upload(f, a)
+    # parity of the advected fields against the FP64 oracle, on the state after the warm-up steps
+    for _ in range(W):
+        sim.step(next_dt(sim), params)
+    parity = advect_parity(el, sim, weno)
+    sampler = ClockSampler(dist.local_rank) if dist.rank == 0 else None
+    elapsed, stats, launches, _, clocks = timed_steps(el, torch, sim, stream, params, K, dist, sampler=sampler)
+    elapsed = dist.max(elapsed)
+    value, ms_per_step = aggregate([elapsed], K, dist.world)
+    e2e = None
+    if not args.no_e2e:
+        ev, h2d, d2h = e2e_steps(el, torch, sim, stream, params, max(3, min(K, 20)), dtype=torch.float64)
+        e2e = {"value": dist.world / dist.max(1.0 / ev), "unit": "steps/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h}
+    sim.close()
+    out = {
+        "metric": DAM_METRIC, "value": value, "unit": "steps/s", "n_gpus": dist.world, "steps": K, "warmup": W,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": dam_workload_name(n, weno, args.tol, args.seed), "n": n, "seed": args.seed,
+                   "parallelism": f"replicas x{dist.world}", "l2": "no flush: fields re-read every step"},
+        "pcg": {"iterations_mean": statistics.mean(s["iterations"] for s in stats),
+                "relres_max": max(s["relres"] for s in stats), "all_converged": all(s["status"] == 0 for s in stats)},
+        "advected_parity_vs_fp64_oracle": parity, "gpu_launches": launches, "clocks": clocks, "e2e": e2e,
+        "roofline": None,
+    }
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_dam(args, steps=3 if n == 128 else 10)
+    return out
+
+
+def advect_parity(el, sim, weno):
+    """Max relative error of the GPU's advected phi, u, v, w against the FP64 oracle's, from the
+    scene's current state and the next CFL time step."""
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    import oracle as O
+
+    st = {f: sim.download(f) for f in ("phi", "u", "v", "w")}
+    dt = next_dt(sim)
+    tp, sp = (O.TRACE_RK2, O.SAMPLE_WENO6) if weno else (O.TRACE_RK2, O.SAMPLE_TRILINEAR)
+    tv = O.TRACE_RK3 if weno else O.TRACE_RK2
+    ref_phi = O.advect_collocated(st["phi"], st["u"], st["v"], st["w"], sim.dx, dt, tp, sp)
+    ref_u, ref_v, ref_w = O.advect_staggered(st["u"], st["v"], st["w"], sim.dx, dt, tv, O.SAMPLE_TRILINEAR)
+    sim.advect_level_set(dt, tp, sp)
+    sim.advect_velocity(dt, tv, el.SAMPLE_TRILINEAR)
+    out = {}
+    for f, ref in (("phi", ref_phi), ("u", ref_u), ("v", ref_v), ("w", ref_w)):
+        got = sim.download(f)
+        den = max(float(np.max(np.abs(ref))), 1e-300)
+        out[f] = float(np.max(np.abs(got - ref))) / den
+    for f, a in st.items():  # put the state back
+        sim.upload(f, a)
+    return out
+
+
+def cpu_baseline_dam(args, steps):
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    import oracle as O
+    from oracle import step as S
+
+    el_scenes = _scenes_module()
+    n, weno = dam_setup(args)
+    spec = el_scenes.dam_break(n)
+    phi, solid = O.rasterise(spec, np.float64)
+    wts = O.compute_weights(solid)
+    st = S.initial_state(phi, wts, O.cell_solid_phi(solid), O.float_dx(n, np.float64))
+    if weno:
+        rng = np.random.default_rng(args.seed)
+        for f in ("u", "v", "w"):
+            st[f] = rng.uniform(-1e-3, 1e-3, st[f].shape)
+    tp, sp, tv = (0, 1, 1) if weno else (0, 0, 0)
+    t0 = time.perf_counter()
+    its = []
+    for _ in range(steps):
+        dt = min(O.calc_time_step(st["u"], st["v"], st["w"], st["dx"], 1.0), 1.0 / 60.0)
+        st, _ = S.step(st, dt, tp, sp, tv, 0, 9.8, tol=args.tol, maxit=20000)
+        its.append(st["pcg_iterations"])
+    elapsed = time.perf_counter() - t0
+    return {"value": steps / elapsed, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{steps} full steps of the {n}^3 FP64 dam break from the initial state on the CPU oracle "
+                      f"(OpenMP, MIC(0)-PCG FP64 to {args.tol}; iterations {its}), {elapsed:.1f} s"}
+
+
 # ---- learned warm start ------------------------------------------------------------------------
 
 WS_METRIC = "pressure-solve speed-up from the learned warm start at 128^3 (zero-guess time / learned time, to 1e-6)"
@@ -758,6 +902,17 @@ def run_reference(args, dist):
     os.environ.setdefault("OMP_PROC_BIND", "close")
     if args.workload == "batch32":
         return run_reference_batch(args, dist)
+    if args.workload in ("dam64", "dam128"):
+        n, weno = dam_setup(args)
+        base = cpu_baseline_dam(args, steps=max(1, min(args.steps, 3 if n == 128 else 10)))
+        return {"metric": DAM_METRIC, "value": base["value"], "unit": "steps/s", "n_gpus": dist.world,
+                "steps": None, "warmup": 0, "ms_per_step": 1e3 / base["value"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+                "config": {"workload": dam_workload_name(n, weno, args.tol, args.seed) + " (same as our arm)",
+                           "n": n, "seed": args.seed, "parallelism": "host cores"},
+                "cpu_baseline": {"kind": base["kind"], "cores": base["cores"], "sample": base["sample"],
+                                 "value": base["value"], "unit": "steps/s"},
+                "e2e": {"value": base["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     steps = max(1, min(args.steps, 2))
     base = cpu_baseline(args.n, args.seed, args.tol, steps)
     return {"metric": METRIC, "value": base["value"], "unit": "steps/s", "n_gpus": dist.world, "steps": steps,
@@ -782,6 +937,8 @@ def main(argv=None):
             out = run_batch(args, dist)
         elif args.workload == "warmstart128":
             out = run_warmstart(args, dist)
+        elif args.workload in ("dam64", "dam128"):
+            out = run_dam(args, dist)
         else:
             out = run_ours(args, dist)
         if dist.rank == 0:
