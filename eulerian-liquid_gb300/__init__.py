@@ -18,6 +18,7 @@ import numpy as np
 
 from . import build as _build_mod
 from . import autotune  # noqa: F401  (re-exported)
+from . import state  # noqa: F401  (re-exported)
 from . import scenes  # noqa: F401  (re-exported)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -141,6 +142,8 @@ def _declare(L):
     L.el_ctx_sync.argtypes = [ctxp]
     L.el_ctx_kernel_launches.argtypes = [ctxp]
     L.el_ctx_kernel_launches.restype = C.c_int64
+    L.el_state_save.argtypes = [ctxp, C.c_char_p, d]
+    L.el_state_load.argtypes = [ctxp, C.c_char_p, C.POINTER(C.c_double)]
     L.el_ctx_set_tuning.argtypes = [ctxp, C.POINTER(Tuning)]
     L.el_ctx_get_tuning.argtypes = [ctxp, C.POINTER(Tuning)]
     L.el_upload.argtypes = [ctxp, i, vp, sz]
@@ -245,6 +248,15 @@ class Simulator:
         if st == EL_ERR_NO_FLUID:
             raise NoFluid(st, "No fluid")
         raise ELError(st, f"{what}: {status_string(st)}: {msg}")
+
+    # -- state files (el_state_save / el_state_load) ------------------------------------------
+    def save_state(self, path, time=0.0):
+        self._check(self.lib.el_state_save(self.h, os.fsencode(path), time), "save_state")
+
+    def load_state(self, path):
+        t = C.c_double()
+        self._check(self.lib.el_state_load(self.h, os.fsencode(path), C.byref(t)), "load_state")
+        return t.value
 
     # -- launch shapes ----------------------------------------------------------------------
     def get_tuning(self):

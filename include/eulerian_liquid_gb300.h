@@ -243,6 +243,17 @@ int el_advect_staggered_grid(const el_grid* g, int dtype, void* out_u, void* out
 int el_compute_staggered_grid_weight(const el_grid* g, int dtype, void* weight_u, void* weight_v,
                                      void* weight_w, const void* nodal_solid, void* stream);
 
+/* ---- state dump / restore -----------------------------------------------------------
+ * No counterpart in the reference (its only dumps are OBJ meshes and 2D text slices).  Writes
+ * every field but EL_FIELD_INDICES (derived) to `path`, raw, behind a 64-byte header, so that a
+ * run restarts exactly: header {char magic[8] = "ELGBSTAT"; uint32 version = 1; uint32 dtype;
+ * int32 ni, nj, nk; uint32 nfields; double dx; double time; 16 zero bytes}, then per field
+ * {uint32 field; uint32 element bytes; uint64 byte count; bytes in the layout of el_upload};
+ * little-endian.  el_state_load checks magic, version, grid and field type against the context
+ * and reads the whole file before changing anything; `time` is the caller's. */
+int el_state_save(el_ctx* ctx, const char* path, double time);
+int el_state_load(el_ctx* ctx, const char* path, double* time);
+
 /* ---- batched scenes: many contexts advanced by one graph launch per step ----------------
  * No counterpart in the reference, which runs one Simulator per process.  A batch applies the
  * reference's Simulator::update(update_second_order, dt_frame, use_cfl=true) loop
