@@ -84,54 +84,76 @@ template <typename T>
 __global__ void __launch_bounds__(kExBX * kExBY) extrapolate_layer_kernel(int n0, int n1, int n2, T* __restrict__ g,
                                                                           uint8_t* __restrict__ stamp, int layer,
                                                                           TileGrid tg, const uint8_t* __restrict__ act_in,
-                                                                          uint8_t* __restrict__ act_out) {
-    __shared__ uint8_t box[kExBZ + 2][kExBY + 2][kExBX + 2];
+                                                                          uint8_t* __restrict__ act_out,
+                                                                          uint8_t* __restrict__ tile_bits) {
+    // validity before this layer of the tile and its one-cell halo, one 34-bit row mask per
+    // (y, z) row: bit hx <-> cell i0 - 1 + hx
+    constexpr int kRows = (kExBZ + 2) * (kExBY + 2);
+    __shared__ unsigned long long rows[kExBZ + 2][kExBY + 2];
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int tid = tx + kExBX * ty;
+    const int warp = ty, lane = tx;  // blocks are 32 x 8: one warp per y row of threads
     const int ntiles = tg.tx * tg.ty * tg.tz;
-    constexpr int kBox = (kExBZ + 2) * (kExBY + 2) * (kExBX + 2);
+    const unsigned full = 0xffffffffu;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        if (!act_in[t]) continue;  // block-uniform
+        // block-uniform: tiles not flagged for this layer, and tiles with no invalid cell left
+        if (!act_in[t] || !(tile_bits[t] & 2)) continue;
         const int bx = t % tg.tx, by = (t / tg.tx) % tg.ty, bz = t / (tg.tx * tg.ty);
         const int i0 = bx * kExBX, j0 = by * kExBY, k0 = bz * kExBZ;
         const int i = i0 + tx, j = j0 + ty;
-        // stamps of the tile and its one-cell halo; out-of-grid cells read as invalid (255)
-        for (int q = tid; q < kBox; q += kExBX * kExBY) {
-            const int hx = q % (kExBX + 2), hy = (q / (kExBX + 2)) % (kExBY + 2), hz = q / ((kExBX + 2) * (kExBY + 2));
-            const int x = i0 + hx - 1, y = j0 + hy - 1, z = k0 + hz - 1;
-            uint8_t v = 255;
-            if (x >= 0 && x < n0 && y >= 0 && y < n1 && z >= 0 && z < n2) v = stamp[lin3(x, y, z, n0, n1)];
-            box[hz][hy][hx] = v;
+        // each warp ballots whole rows: lanes read cells i0-1+lane, lanes 0 and 1 also the two
+        // beyond; out-of-grid cells count as invalid
+        for (int r = warp; r < kRows; r += kExBY) {
+            const int hz = r / (kExBY + 2), hy = r - hz * (kExBY + 2);
+            const int y = j0 + hy - 1, z = k0 + hz - 1;
+            const bool row_in = y >= 0 && y < n1 && z >= 0 && z < n2;
+            const long long base = row_in ? lin3(0, y, z, n0, n1) : 0;
+            const int xa = i0 - 1 + lane, xb = i0 + 31 + lane;
+            const bool va = row_in && xa >= 0 && xa < n0 && stamp[base + xa] <= layer;
+            const bool vb = row_in && lane < 2 && xb < n0 && stamp[base + xb] <= layer;
+            const unsigned lo = __ballot_sync(full, va), hi = __ballot_sync(full, vb);
+            if (lane == 0) rows[hz][hy] = (unsigned long long)lo | ((unsigned long long)(hi & 3u) << 32);
         }
         __syncthreads();
-        bool changed = false;
+        bool changed = false, left = false;
         if (i < n0 && j < n1) {
             for (int kk = 0; kk < kExBZ; ++kk) {
                 const int k = k0 + kk;
                 if (k >= n2) break;
-                if (box[kk + 1][ty + 1][tx + 1] <= layer) continue;
+                if ((rows[kk + 1][ty + 1] >> (tx + 1)) & 1ull) continue;  // valid already
+                unsigned long long near = 0;
+#pragma unroll
+                for (int dk = 0; dk < 3; ++dk)
+#pragma unroll
+                    for (int dj = 0; dj < 3; ++dj) near |= rows[kk + dk][ty + dj];
+                if (!((near >> tx) & 7ull)) {  // no valid neighbour yet
+                    left = true;
+                    continue;
+                }
                 T sum = T(0);
                 int count = 0;
 #pragma unroll
                 for (int dk = 0; dk < 3; ++dk)
 #pragma unroll
-                    for (int dj = 0; dj < 3; ++dj)
+                    for (int dj = 0; dj < 3; ++dj) {
+                        const unsigned long long m = rows[kk + dk][ty + dj] >> tx;
 #pragma unroll
                         for (int di = 0; di < 3; ++di)
-                            if (box[kk + dk][ty + dj][tx + di] <= layer) {
+                            if ((m >> di) & 1ull) {
                                 sum = add_rn2(sum, g[lin3(i + di - 1, j + dj - 1, k + dk - 1, n0, n1)]);
                                 ++count;
                             }
-                if (count > 0) {
-                    const long long c = lin3(i, j, k, n0, n1);
-                    g[c] = sum / (T)count;
-                    stamp[c] = (uint8_t)(layer + 1);
-                    changed = true;
-                }
+                    }
+                const long long c = lin3(i, j, k, n0, n1);
+                g[c] = sum / (T)count;
+                stamp[c] = (uint8_t)(layer + 1);
+                changed = true;
             }
         }
-        // flag this tile's 3x3x3 tile neighbourhood for the next layer (the barrier also keeps
-        // the box intact until every thread is done with it)
+        // a tile whose cells are all valid now is never visited again; flag this tile's 3x3x3
+        // tile neighbourhood for the next layer (the barriers also keep the row masks intact
+        // until every thread is done with them)
+        const int tid = tx + kExBX * ty;
+        if (!__syncthreads_or(left) && tid == 0) tile_bits[t] &= (uint8_t)~2u;
         if (__syncthreads_or(changed) && tid < 27) {
             const int ox = bx + tid % 3 - 1, oy = by + (tid / 3) % 3 - 1, oz = bz + tid / 9 - 1;
             if (ox >= 0 && ox < tg.tx && oy >= 0 && oy < tg.ty && oz >= 0 && oz < tg.tz)
@@ -329,10 +351,10 @@ int launch_extrapolate(el_ctx* ctx, int field, uint8_t* valid, int layers, bool 
         cudaMemsetAsync(out, 0, ntiles, ctx->stream);
         if (ctx->dtype == EL_F64)
             extrapolate_layer_kernel<double><<<grid, block, 0, ctx->stream>>>(n0, n1, n2, (double*)ctx->field[field],
-                                                                              stamp, l, tg, in, out);
+                                                                              stamp, l, tg, in, out, bits);
         else
             extrapolate_layer_kernel<float><<<grid, block, 0, ctx->stream>>>(n0, n1, n2, (float*)ctx->field[field],
-                                                                             stamp, l, tg, in, out);
+                                                                             stamp, l, tg, in, out, bits);
         ++launched;
     }
     if (write_back) {
