@@ -177,6 +177,227 @@ __global__ void __launch_bounds__(kThreads) conv3_kernel(int X, int Y, int Z, Co
 }
 
 // ---------------------------------------------------------------------------------------
+// The same convolution on the 5th-generation tensor cores (tcgen05), for layers whose 27 taps
+// of weights fit in shared memory next to the input brick.  A CTA of 4 warps owns an
+// 8 (x) x 16 (y) x 1 (z) brick: M = 128 voxels, one TMEM lane each; N = output channels in TMEM
+// columns (FP32).  Both operands sit in shared memory in the no-swizzle K-major layout, whose
+// unit is an 8-row x 16-byte core matrix:
+//   A: the input brick with its halo (10 x 18 x 3 voxels), channel-chunk major: chunk c
+//      (channels 8c..8c+7) of voxel v at (c * 540 + v) * 16 bytes.  Eight x-consecutive voxels
+//      are one core matrix, the next 8 rows (the next y) are 10 voxels further (SBO = 160 B),
+//      the next chunk along K is 540 voxels further (LBO = 8640 B); tap (dx, dy, dz) only moves
+//      the start address, so the 27 shifted operands need no copies.
+//   B: per tap, [channel chunk][output channel] x 16 bytes: SBO = 128 B, LBO = cout * 16 B.
+// One thread issues the 27 * cin / 16 MMAs (K = 16 each) into one accumulator and commits them to
+// an mbarrier; the 4 warps wait (bounded), read their 32 TMEM lanes (tcgen05.ld) and store.
+// The CTA is persistent over bricks: the weights are staged once.
+namespace tc {
+
+__device__ int g_error;  // set when a bounded wait gave up; read and cleared by el_nn_take_error
+
+constexpr int TX = 8, TY = 16, HX = TX + 2, HY = TY + 2, HZ = 3, HV = HX * HY * HZ;  // 540 halo voxels
+constexpr int kThreads = 128;
+
+template <int CIN, int COUT>
+struct Shape {
+    static constexpr int KC = CIN / 8;                 // 16-byte channel chunks
+    static constexpr int WB = 27 * KC * COUT * 16;     // weight bytes
+    static constexpr int HB = KC * HV * 16;            // input brick bytes
+    static constexpr int SMEM = WB + HB + 16;          // + mbarrier and TMEM address
+    static constexpr uint32_t NCOL = COUT <= 32 ? 32u : (COUT <= 64 ? 64u : 128u);
+    // BF16 x BF16 -> FP32, both K-major, M = 128, N = COUT
+    static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(COUT >> 3) << 17) |
+                                      ((uint32_t)(128 >> 4) << 24);
+};
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo & 0x3FFFFu) >> 4) << 16;
+    d |= (uint64_t)((sbo & 0x3FFFFu) >> 4) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version of the 5th-generation tensor cores; no swizzle
+    return d;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t phase) {
+    // polls without suspending; gives up (and reports) after about two seconds of SM clock
+    const long long start = clock64();
+    while (true) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(addr), "r"(phase)
+            : "memory");
+        if (done) return true;
+        if (clock64() - start > (1LL << 32)) return false;
+    }
+}
+
+template <int CIN>
+__device__ __forceinline__ void stage_brick(unsigned char* hsm, const ConvIn& in, int X, int Y, int Z, int x0, int y0,
+                                            int z0) {
+    constexpr int KC = CIN / 8;
+    for (int idx = threadIdx.x; idx < HV * KC; idx += kThreads) {
+        const int hv = idx / KC, cv = idx - hv * KC;
+        const int hx = hv % HX, t = hv / HX, hy = t % HY, hz = t / HY;
+        const int x = x0 + hx - 1, y = y0 + hy - 1, z = z0 + hz - 1;
+        uint4 val = make_uint4(0u, 0u, 0u, 0u);
+        if (x >= 0 && x < X && y >= 0 && y < Y && z >= 0 && z < Z) {
+            const int c = cv * 8;
+            const long long fine = ((long long)z * Y + y) * X + x;
+            if (c < in.ca) {
+                const long long va = in.up_a ? ((long long)(z >> 1) * in.ay + (y >> 1)) * in.ax + (x >> 1) : fine;
+                val = __ldg(reinterpret_cast<const uint4*>(in.a + va * in.ca + c));
+            } else if (in.b) {
+                val = __ldg(reinterpret_cast<const uint4*>(in.b + fine * in.cb + (c - in.ca)));
+            }
+            if (in.mask) val = apply_relu_mask(val, __ldg(reinterpret_cast<const uint4*>(in.mask + fine * CIN + c)));
+        }
+        *reinterpret_cast<uint4*>(hsm + ((size_t)cv * HV + hv) * 16) = val;
+    }
+}
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(kThreads) conv3_tc_kernel(int X, int Y, int Z, ConvIn in,
+                                                            const uint4* __restrict__ wtc,
+                                                            const float* __restrict__ bias, int relu,
+                                                            __nv_bfloat16* __restrict__ out_a, int oca,
+                                                            __nv_bfloat16* __restrict__ out_b) {
+    using S = Shape<CIN, COUT>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char* wsm = smem_raw;
+    unsigned char* hsm = smem_raw + S::WB;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw + S::WB + S::HB);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + S::WB + S::HB + 8);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int q = tid; q < S::WB / 16; q += kThreads) reinterpret_cast<uint4*>(wsm)[q] = __ldg(wtc + q);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tslot)),
+                     "r"(S::NCOL)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(mbar)), "r"(1) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tslot;
+    const uint32_t wbase = smem_u32(wsm), hbase = smem_u32(hsm), mbar_a = smem_u32(mbar);
+    const int bx = (X + TX - 1) / TX, by = (Y + TY - 1) / TY;
+    const long long nbricks = (long long)bx * by * Z;
+    uint32_t phase = 0;
+    for (long long br = blockIdx.x; br < nbricks; br += gridDim.x) {
+        const int x0 = (int)(br % bx) * TX;
+        const long long rest = br / bx;
+        const int y0 = (int)(rest % by) * TY, z0 = (int)(rest / by);
+        stage_brick<CIN>(hsm, in, X, Y, Z, x0, y0, z0);
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // visible to the tensor cores
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+#pragma unroll 1
+            for (int tap = 0; tap < 27; ++tap) {
+                const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+                const uint32_t a0 = hbase + (uint32_t)(((dz * HY + dy) * HX + dx) * 16);
+                const uint32_t b0 = wbase + (uint32_t)(tap * S::KC * COUT * 16);
+#pragma unroll
+                for (int s = 0; s < S::KC / 2; ++s) {
+                    const uint64_t da = smem_desc(a0 + (uint32_t)(2 * s * HV * 16), HV * 16, HX * 16);
+                    const uint64_t db = smem_desc(b0 + (uint32_t)(2 * s * COUT * 16), COUT * 16, 128);
+                    const uint32_t acc = (tap | s) ? 1u : 0u;
+                    asm volatile(
+                        "{\n\t.reg .pred p;\n\t"
+                        "setp.ne.b32 p, %4, 0;\n\t"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+                        "l"(da), "l"(db), "r"(S::IDESC), "r"(acc)
+                        : "memory");
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             mbar_a)
+                         : "memory");
+        }
+        const bool ok = mbar_wait(mbar_a, phase);
+        phase ^= 1u;
+        if (!__syncthreads_and(ok)) {
+            if (tid == 0) atomicExch(&g_error, 1);
+            break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        // row r = 32 warp + lane of the accumulator is voxel (x0 + r % 8, y0 + r / 8, z0)
+        const int r = warp * 32 + lane;
+        const int x = x0 + (r & 7), y = y0 + (r >> 3);
+        const bool live = x < X && y < Y;
+        const long long v = ((long long)z0 * Y + y) * X + x;
+#pragma unroll
+        for (int c0 = 0; c0 < COUT; c0 += 16) {
+            uint32_t q[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];\n"
+                : "=r"(q[0]), "=r"(q[1]), "=r"(q[2]), "=r"(q[3]), "=r"(q[4]), "=r"(q[5]), "=r"(q[6]), "=r"(q[7]),
+                  "=r"(q[8]), "=r"(q[9]), "=r"(q[10]), "=r"(q[11]), "=r"(q[12]), "=r"(q[13]), "=r"(q[14]),
+                  "=r"(q[15])
+                : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (live) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    uint4 o;
+                    __nv_bfloat162* op = reinterpret_cast<__nv_bfloat162*>(&o);
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const int co = c0 + h * 8 + 2 * e;
+                        float f0 = __uint_as_float(q[h * 8 + 2 * e]), f1 = __uint_as_float(q[h * 8 + 2 * e + 1]);
+                        if (bias) {
+                            f0 += bias[co];
+                            f1 += bias[co + 1];
+                        }
+                        if (relu) {
+                            f0 = fmaxf(f0, 0.f);
+                            f1 = fmaxf(f1, 0.f);
+                        }
+                        op[e] = __floats2bfloat162_rn(f0, f1);
+                    }
+                    const int cb = c0 + h * 8;
+                    if (cb < oca)
+                        *reinterpret_cast<uint4*>(out_a + v * oca + cb) = o;
+                    else
+                        *reinterpret_cast<uint4*>(out_b + v * (COUT - oca) + (cb - oca)) = o;
+                }
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();  // accumulator read and brick consumed before the next brick
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(S::NCOL) : "memory");
+}
+
+// FP32 master [co][27][ci] -> the B layout above: [tap][ci / 8][co][ci % 8]
+__global__ void pack_weights_tc_kernel(int cin, int cout, const float* __restrict__ w, __nv_bfloat16* __restrict__ tf,
+                                       __nv_bfloat16* __restrict__ tb) {
+    const long long n = 27LL * cin * cout;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int ci = (int)(e % cin);
+        const long long t2 = e / cin;
+        const int tap = (int)(t2 % 27), co = (int)(t2 / 27);
+        const __nv_bfloat16 v = __float2bfloat16_rn(w[e]);
+        tf[(((size_t)tap * (cin / 8) + ci / 8) * cout + co) * 8 + (ci % 8)] = v;
+        // backward data: the transposed, tap-mirrored kernel (cin' = cout, cout' = cin)
+        if (tb) tb[(((size_t)(26 - tap) * (cout / 8) + co / 8) * cin + ci) * 8 + (co % 8)] = v;
+    }
+}
+
+}  // namespace tc
+
+// ---------------------------------------------------------------------------------------
 // backward weight: dW[co][tap][ci] = sum_v gm[v][co] x[v + off(tap)][ci], gm = g * (y > 0),
 // one 16 (co) x 16 (ci) tile of one tap per warp task; the CTA covers taps
 // [tap0, tap0 + ntaps) for all channels over bricks split, split + nsplit, ...
@@ -629,6 +850,26 @@ int launch_conv(const el_nn_conv_args* a, cudaStream_t s) {
 }
 
 template <int CIN, int COUT>
+int launch_conv_tc(const el_nn_conv_args* a, cudaStream_t s) {
+    using S = tc::Shape<CIN, COUT>;
+    if (cudaFuncSetAttribute(tc::conv3_tc_kernel<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM) !=
+        cudaSuccess)
+        return EL_ERR_CUDA;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc::conv3_tc_kernel<CIN, COUT>, tc::kThreads,
+                                                      S::SMEM) != cudaSuccess ||
+        per_sm < 1)
+        return EL_ERR_CUDA;
+    const long long bricks =
+        (long long)((a->nx + tc::TX - 1) / tc::TX) * ((a->ny + tc::TY - 1) / tc::TY) * a->nz;
+    const int grid = (int)std::max<long long>(1, std::min<long long>(bricks, (long long)num_sms_current() * per_sm));
+    tc::conv3_tc_kernel<CIN, COUT><<<grid, tc::kThreads, S::SMEM, s>>>(
+        a->nx, a->ny, a->nz, conv_in(a), static_cast<const uint4*>(a->weights_tc), a->bias, a->relu,
+        static_cast<__nv_bfloat16*>(a->out_a), a->out_a_channels, static_cast<__nv_bfloat16*>(a->out_b));
+    return cudaGetLastError() == cudaSuccess ? EL_OK : EL_ERR_CUDA;
+}
+
+template <int CIN, int COUT>
 int wgrad_splits(int nx, int ny, int nz) {
     const long long bricks = (long long)((nx + kTX - 1) / kTX) * ((ny + kTY - 1) / kTY) * nz;
     const int want = (2 * num_sms_current() + WGrad<CIN, COUT>::GROUPS - 1) / WGrad<CIN, COUT>::GROUPS;
@@ -665,6 +906,9 @@ int launch_wgrad(const el_nn_conv_args* a, const void* grad_out, float* dw, floa
 #define EL_NN_CONV_PAIRS(X)                                                                                      \
     X(16, 16) X(16, 32) X(32, 32) X(32, 64) X(64, 64) X(128, 64) X(96, 32) X(48, 16) X(32, 16) X(64, 32) X(64, 128) \
         X(32, 96) X(16, 48)
+// pairs whose 27 taps of weights fit in shared memory with the input brick: the tcgen05 kernel
+#define EL_NN_TC_PAIRS(X) \
+    X(16, 16) X(16, 32) X(32, 32) X(32, 64) X(48, 16) X(32, 16) X(64, 32) X(16, 48) X(32, 96)
 // forward pairs (backward weight)
 #define EL_NN_FWD_PAIRS(X) X(16, 16) X(16, 32) X(32, 32) X(32, 64) X(64, 64) X(128, 64) X(96, 32) X(48, 16)
 
@@ -680,7 +924,32 @@ bool valid_conv(const el_nn_conv_args* a) {
 
 #define EL_API extern "C" __attribute__((visibility("default")))
 
+EL_API int el_nn_tc_supported(int cin, int cout) {
+#define EL_NN_CASE(CI, CO) \
+    if (cin == CI && cout == CO) return 1;
+    EL_NN_TC_PAIRS(EL_NN_CASE)
+#undef EL_NN_CASE
+    return 0;
+}
+
+EL_API int el_nn_take_error(void) {
+    int e = 0;
+    const int zero = 0;
+    if (cudaMemcpyFromSymbol(&e, tc::g_error, sizeof(int)) != cudaSuccess) return -1;
+    if (e && cudaMemcpyToSymbol(tc::g_error, &zero, sizeof(int)) != cudaSuccess) return -1;
+    return e;
+}
+
 EL_API int el_nn_conv3_forward(const el_nn_conv_args* a, void* stream) {
+    if (a && a->weights_tc && el_nn_tc_supported(a->cin, a->cout) && valid_conv(a) && a->out_a &&
+        a->out_a_channels > 0 && a->out_a_channels <= a->cout && a->out_a_channels % 8 == 0 &&
+        (a->out_a_channels == a->cout || a->out_b)) {
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+#define EL_NN_CASE(CI, CO) \
+        if (a->cin == CI && a->cout == CO) return launch_conv_tc<CI, CO>(a, s);
+        EL_NN_TC_PAIRS(EL_NN_CASE)
+#undef EL_NN_CASE
+    }
     if (!valid_conv(a) || !a->weights || !a->out_a || a->out_a_channels <= 0 || a->out_a_channels > a->cout ||
         a->out_a_channels % 8 || (a->out_a_channels < a->cout && !a->out_b))
         return EL_ERR_INVALID_ARGUMENT;
@@ -717,6 +986,15 @@ EL_API int el_nn_pack_weights(int cin, int cout, const float* w, void* packed_fw
     if (cin % 16 || cout % 16 || cin <= 0 || cout <= 0 || !w || !packed_fwd) return EL_ERR_INVALID_ARGUMENT;
     const long long n = 27LL * cin * cout;
     pack_weights_kernel<<<grid_elems(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        cin, cout, w, static_cast<__nv_bfloat16*>(packed_fwd), static_cast<__nv_bfloat16*>(packed_bwd));
+    return cudaGetLastError() == cudaSuccess ? EL_OK : EL_ERR_CUDA;
+}
+
+EL_API int el_nn_pack_weights_tc(int cin, int cout, const float* w, void* packed_fwd, void* packed_bwd,
+                                  void* stream) {
+    if (cin % 16 || cout % 16 || cin <= 0 || cout <= 0 || !w || !packed_fwd) return EL_ERR_INVALID_ARGUMENT;
+    const long long n = 27LL * cin * cout;
+    tc::pack_weights_tc_kernel<<<grid_elems(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
         cin, cout, w, static_cast<__nv_bfloat16*>(packed_fwd), static_cast<__nv_bfloat16*>(packed_bwd));
     return cudaGetLastError() == cudaSuccess ? EL_OK : EL_ERR_CUDA;
 }

@@ -63,7 +63,8 @@ class ConvArgs(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("cin", C.c_int), ("cout", C.c_int),
                 ("in_a", C.c_void_p), ("ca", C.c_int), ("upsample_a", C.c_int), ("in_b", C.c_void_p),
                 ("cb", C.c_int), ("mask", C.c_void_p), ("weights", C.c_void_p), ("bias", C.c_void_p),
-                ("relu", C.c_int), ("out_a", C.c_void_p), ("out_a_channels", C.c_int), ("out_b", C.c_void_p)]
+                ("relu", C.c_int), ("out_a", C.c_void_p), ("out_a_channels", C.c_int), ("out_b", C.c_void_p),
+                ("weights_tc", C.c_void_p)]
 
 
 _declared = False
@@ -81,6 +82,9 @@ def lib():
         L.el_nn_packed_weight_bytes.argtypes = [i, i]
         L.el_nn_packed_weight_bytes.restype = sz
         L.el_nn_pack_weights.argtypes = [i, i, vp, vp, vp, vp]
+        L.el_nn_pack_weights_tc.argtypes = [i, i, vp, vp, vp, vp]
+        L.el_nn_tc_supported.argtypes = [i, i]
+        L.el_nn_take_error.argtypes = []
         L.el_nn_pool.argtypes = [i, i, i, i, vp, vp, vp]
         L.el_nn_spread.argtypes = [i, i, i, i, vp, vp, f, i, vp]
         L.el_nn_gather8.argtypes = [i, i, i, i, vp, vp, vp]
@@ -110,8 +114,9 @@ class WarmStartNet:
     """The network's parameters (FP32 masters, Adam moments, packed bf16 copies) and, per grid
     size, its activation and gradient buffers."""
 
-    def __init__(self, torch, device="cuda", seed=0, lr=1e-3):
+    def __init__(self, torch, device="cuda", seed=0, lr=1e-3, tensor_cores=True):
         self.torch = torch
+        self.tensor_cores = tensor_cores
         self.dev = torch.device(device)
         self.L = lib()
         self.lr = lr
@@ -140,10 +145,15 @@ class WarmStartNet:
         self.m = torch.zeros_like(self.params)
         self.v = torch.zeros_like(self.params)
         self.packed = {}
+        self.packed_tc = {}  # forward / backward-data weights for the tcgen05 kernel, where it applies
         for name, cin, cout in sizes:
             nb = self.L.el_nn_packed_weight_bytes(cin, cout) // 2
             self.packed[name] = (torch.empty(nb, dtype=torch.bfloat16, device=self.dev),
                                  torch.empty(nb, dtype=torch.bfloat16, device=self.dev))
+            fwd_tc, bwd_tc = self.L.el_nn_tc_supported(cin, cout), self.L.el_nn_tc_supported(cout, cin)
+            if tensor_cores and (fwd_tc or bwd_tc):
+                self.packed_tc[name] = (torch.empty(nb, dtype=torch.bfloat16, device=self.dev) if fwd_tc else None,
+                                        torch.empty(nb, dtype=torch.bfloat16, device=self.dev) if bwd_tc else None)
         self.buffers = {}
         self.pack()
 
@@ -182,6 +192,16 @@ class WarmStartNet:
         for name, _, _, _, cin, cout, _ in CONVS:
             fwd, bwd = self.packed[name]
             _ok(self.L.el_nn_pack_weights(cin, cout, _p(self.weight(name)), _p(fwd), _p(bwd), s), "pack_weights")
+            if name in self.packed_tc:
+                tf, tb = self.packed_tc[name]
+                scratch = tf if tf is not None else self._scratch(tb)
+                _ok(self.L.el_nn_pack_weights_tc(cin, cout, _p(self.weight(name)), _p(scratch), _p(tb), s),
+                    "pack_weights_tc")
+
+    def _scratch(self, like):
+        if getattr(self, "_pack_scratch", None) is None or self._pack_scratch.numel() < like.numel():
+            self._pack_scratch = self.torch.empty_like(like)
+        return self._pack_scratch
 
     def state_dict(self):
         return {"params": self.params.detach().cpu().numpy().copy(), "step": self.step_count}
@@ -250,6 +270,8 @@ class WarmStartNet:
                 self._pool(b, 2, s)
             args = self._conv_args(b, name, a_name, up, b_name, cin, cout, level)
             args.weights = self.packed[name][0].data_ptr()
+            if name in self.packed_tc and self.packed_tc[name][0] is not None:
+                args.weights_tc = self.packed_tc[name][0].data_ptr()
             args.bias = self.bias(name).data_ptr()
             args.relu = 1
             args.out_a = A[name].data_ptr()
@@ -300,6 +322,8 @@ class WarmStartNet:
             d.in_b, d.cb = None, 0
             d.mask = A[name].data_ptr()
             d.weights = self.packed[name][1].data_ptr()
+            if name in self.packed_tc and self.packed_tc[name][1] is not None:
+                d.weights_tc = self.packed_tc[name][1].data_ptr()
             d.bias, d.relu = None, 0
             if up:
                 d.out_a, d.out_a_channels, d.out_b = b["gup"][name].data_ptr(), CHANNELS[a_name], G[b_name].data_ptr()

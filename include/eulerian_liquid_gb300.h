@@ -346,6 +346,8 @@ typedef struct el_nn_conv_args {
     void* out_a;             /* bf16 [.., out_a_channels]: output channels [0, out_a_channels)    */
     int out_a_channels;
     void* out_b;             /* bf16 [.., cout - out_a_channels]: the rest (may be NULL if none)  */
+    const void* weights_tc;  /* NULL, or the same weights packed by el_nn_pack_weights_tc: then
+                                pairs with el_nn_tc_supported run on the tcgen05 kernel          */
 } el_nn_conv_args;
 
 /* y = act(conv(x, W) + bias).  The backward-data pass is the same call with the gradient of the
@@ -363,6 +365,15 @@ int el_nn_conv3_backward_weight(const el_nn_conv_args* args, const void* grad_ou
  * the backward-data packing of the transposed, tap-mirrored kernel); each 27*cin*cout*2 bytes. */
 size_t el_nn_packed_weight_bytes(int cin, int cout);
 int el_nn_pack_weights(int cin, int cout, const float* w, void* packed_fwd, void* packed_bwd, void* stream);
+/* The same weights in the tcgen05 kernel's shared-memory operand layout (27*cin*cout*2 bytes
+ * each), forward and (if packed_bwd is not NULL) backward data.  el_nn_tc_supported(cin, cout)
+ * says whether a (cin, cout) call can use them: (16,16) (16,32) (32,32) (32,64) (48,16) (32,16)
+ * (64,32) (16,48) (32,96), the pairs whose 27 taps fit in shared memory with the input brick.
+ * el_nn_take_error returns (and clears) 1 if a tcgen05 kernel's bounded wait for its MMAs gave
+ * up, 0 otherwise, -1 if it could not be read. */
+int el_nn_pack_weights_tc(int cin, int cout, const float* w, void* packed_fwd, void* packed_bwd, void* stream);
+int el_nn_tc_supported(int cin, int cout);
+int el_nn_take_error(void);
 /* 2x2x2 average pooling; its backward is el_nn_spread(scale 1/8, accumulate 1) */
 int el_nn_pool(int nx, int ny, int nz, int c, const void* in, void* out, void* stream);
 /* fine[v] = (accumulate ? fine[v] : 0) + scale * coarse[v / 2] ; (nx, ny, nz) = fine grid */

@@ -352,3 +352,57 @@ def test_network_gradients_match_autograd():
         assert rel_err(gw, wv.grad.numpy()) < TOL_NET, (name, rel_err(gw, wv.grad.numpy()))
     ghw, ghb = net.head_grads()
     assert rel_err(ghw.cpu().numpy(), hw.grad.numpy()) < 1e-2
+
+
+TC_PAIRS = [(16, 16), (16, 32), (32, 32), (32, 64), (48, 16), (32, 16), (64, 32), (16, 48), (32, 96)]
+
+
+@pytest.mark.parametrize("cin,cout", TC_PAIRS)
+def test_tcgen05_conv_matches_conv3d_and_mma_sync(cin, cout):
+    """The tcgen05 kernel (operands in shared memory, accumulator in TMEM) against torch-CPU conv3d
+    and against the mma.sync kernel, on a grid with partial bricks; (48, 16) with the decoder's
+    upsampled concatenation, (32, 96) with a ReLU mask as in the backward-data pass."""
+    W = _ws()
+    L = W.lib()
+    assert L.el_nn_tc_supported(cin, cout) == 1
+    rng = np.random.default_rng(cin * 7 + cout)
+    nx, ny, nz = 20, 34, 4
+    w = bf(_rand(rng, cout, 27, cin, scale=(2.0 / (27 * cin)) ** 0.5))
+    bias = torch.from_numpy(_rand(rng, cout, scale=0.1))
+    fwd, _ = _pack(L, w.numpy(), cin, cout)
+    nb = L.el_nn_packed_weight_bytes(cin, cout) // 2
+    tcw = torch.empty(nb, dtype=torch.bfloat16, device="cuda")
+    wd = torch.from_numpy(np.asarray(w.numpy(), np.float32)).cuda()
+    assert L.el_nn_pack_weights_tc(cin, cout, wd.data_ptr(), tcw.data_ptr(), None, None) == 0
+    mask = None
+    if cin == 48:
+        a = bf(_rand(rng, nz // 2, ny // 2, nx // 2, 32))
+        b = bf(_rand(rng, nz, ny, nx, 16))
+        inp = torch.cat([up2(a), b], dim=3)
+        args_in = (dev(a), 32, 1, dev(b), 16)
+    else:
+        x = bf(_rand(rng, nz, ny, nx, cin))
+        inp = x
+        args_in = (dev(x), cin, 0, None, 0)
+        if cin == 32 and cout == 96:
+            m = bf(_rand(rng, nz, ny, nx, cin))
+            mask = dev(m)
+            inp = x * (m > 0).double()
+    ref = torch.relu(conv_ref(inp, w, bias.double()))
+    outs = []
+    for use_tc in (True, False):
+        out = torch.empty((nz, ny, nx, cout), dtype=torch.bfloat16, device="cuda")
+        bd = bias.cuda()
+        args = _args(W, (nx, ny, nz), cin, cout, args_in[0], args_in[1], args_in[2], args_in[3], args_in[4])
+        args.weights, args.bias, args.relu = fwd.data_ptr(), bd.data_ptr(), 1
+        if mask is not None:
+            args.mask = mask.data_ptr()
+        args.out_a, args.out_a_channels = out.data_ptr(), cout
+        if use_tc:
+            args.weights_tc = tcw.data_ptr()
+        assert L.el_nn_conv3_forward(C.byref(args), None) == 0
+        torch.cuda.synchronize()
+        outs.append(out.float().cpu().numpy())
+    assert L.el_nn_take_error() == 0
+    assert rel_err(outs[0], ref.numpy()) < TOL_ACT, rel_err(outs[0], ref.numpy())
+    assert rel_err(outs[0], outs[1]) < TOL_ACT
