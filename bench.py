@@ -819,7 +819,7 @@ def run_warmstart(args, dist):
                                f"{args.tol}", "n": n, "samples": len(ds), "parallelism": "single GPU"},
         "warmstart": {"solvers": summary, "record_s": record_s, "train_s": train_s, "train_steps": tr["steps"],
                       "loss_history": tr["history"][-5:], "fwd_ms": fwd_ms, "bwd_ms": bwd_ms},
-        "roofline": {"kernel": "network forward (all 3x3x3 convolutions, mma.sync bf16)", "bound": "tensor",
+        "roofline": {"kernel": "network forward (the 3x3x3 convolutions: tcgen05 on the small-cin layers, mma.sync on the rest)", "bound": "tensor",
                      "achieved": achieved, "peak": tflops_peak, "unit": "TFLOP/s", "frac": achieved / tflops_peak,
                      "peak_kind": peak_kind, "traffic": None, "flops_per_launch": F,
                      "backward_tflops": (2 * F - first) / (bwd_ms / 1e3) / 1e12},

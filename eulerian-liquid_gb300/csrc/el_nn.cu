@@ -380,6 +380,229 @@ __global__ void __launch_bounds__(kThreads) conv3_tc_kernel(int X, int Y, int Z,
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(S::NCOL) : "memory");
 }
 
+// Pipelined variant, for the layers where two input bricks fit next to the weights: the copy of
+// brick i+1 (cp.async, 16 bytes per thread and chunk, zero-filled outside the grid) and the
+// epilogue of brick i-1 run while the tensor cores work on brick i, with two input buffers and
+// two accumulators (2 * cout TMEM columns) used in turn.  A ReLU mask (backward data) is applied
+// while staging, so that case stages with ordinary loads at the same point.
+template <int CIN, int COUT>
+struct PipeShape {
+    static constexpr int KC = CIN / 8;
+    static constexpr int WB = 27 * KC * COUT * 16;
+    static constexpr int HB = KC * HV * 16;
+    static constexpr int SMEM = WB + 2 * HB + 32;
+    static constexpr uint32_t NCOL = 2 * COUT <= 32 ? 32u : (2 * COUT <= 64 ? 64u : (2 * COUT <= 128 ? 128u : 256u));
+    static constexpr bool FITS = SMEM <= 220 * 1024;
+};
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool valid) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+
+template <int CIN>
+__device__ __forceinline__ void stage_brick_async(unsigned char* hsm, const ConvIn& in, int X, int Y, int Z, int x0,
+                                                  int y0, int z0) {
+    if (in.mask) {  // needs the mask applied on the way: ordinary loads
+        stage_brick<CIN>(hsm, in, X, Y, Z, x0, y0, z0);
+        return;
+    }
+    constexpr int KC = CIN / 8;
+    const uint32_t base = smem_u32(hsm);
+    for (int idx = threadIdx.x; idx < HV * KC; idx += kThreads) {
+        const int hv = idx / KC, cv = idx - hv * KC;
+        const int hx = hv % HX, t = hv / HX, hy = t % HY, hz = t / HY;
+        const int x = x0 + hx - 1, y = y0 + hy - 1, z = z0 + hz - 1;
+        const bool inside = x >= 0 && x < X && y >= 0 && y < Y && z >= 0 && z < Z;
+        const int c = cv * 8;
+        const __nv_bfloat16* src = in.a;  // a valid address even when nothing is read
+        bool valid = false;
+        if (inside) {
+            const long long fine = ((long long)z * Y + y) * X + x;
+            if (c < in.ca) {
+                const long long va = in.up_a ? ((long long)(z >> 1) * in.ay + (y >> 1)) * in.ax + (x >> 1) : fine;
+                src = in.a + va * in.ca + c;
+                valid = true;
+            } else if (in.b) {
+                src = in.b + fine * in.cb + (c - in.ca);
+                valid = true;
+            }
+        }
+        cp_async16(base + (uint32_t)(((size_t)cv * HV + hv) * 16), src, valid);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// accumulator columns [col, col + COUT) of this warp's 32 lanes -> bias, ReLU, bf16, store
+template <int COUT>
+__device__ __forceinline__ void tc_epilogue(uint32_t tmem, uint32_t col, int X, int Y, int x0, int y0, int z0,
+                                            const float* __restrict__ bias, int relu, __nv_bfloat16* out_a, int oca,
+                                            __nv_bfloat16* out_b) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = warp * 32 + lane;
+    const int x = x0 + (r & 7), y = y0 + (r >> 3);
+    const bool live = x < X && y < Y;
+    const long long v = ((long long)z0 * Y + y) * X + x;
+#pragma unroll
+    for (int c0 = 0; c0 < COUT; c0 += 16) {
+        uint32_t q[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+            "[%16];\n"
+            : "=r"(q[0]), "=r"(q[1]), "=r"(q[2]), "=r"(q[3]), "=r"(q[4]), "=r"(q[5]), "=r"(q[6]), "=r"(q[7]),
+              "=r"(q[8]), "=r"(q[9]), "=r"(q[10]), "=r"(q[11]), "=r"(q[12]), "=r"(q[13]), "=r"(q[14]), "=r"(q[15])
+            : "r"(tmem + ((uint32_t)(warp * 32) << 16) + col + (uint32_t)c0));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        if (!live) continue;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            uint4 o;
+            __nv_bfloat162* op = reinterpret_cast<__nv_bfloat162*>(&o);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int co = c0 + h * 8 + 2 * e;
+                float f0 = __uint_as_float(q[h * 8 + 2 * e]), f1 = __uint_as_float(q[h * 8 + 2 * e + 1]);
+                if (bias) {
+                    f0 += bias[co];
+                    f1 += bias[co + 1];
+                }
+                if (relu) {
+                    f0 = fmaxf(f0, 0.f);
+                    f1 = fmaxf(f1, 0.f);
+                }
+                op[e] = __floats2bfloat162_rn(f0, f1);
+            }
+            const int cb = c0 + h * 8;
+            if (cb < oca)
+                *reinterpret_cast<uint4*>(out_a + v * oca + cb) = o;
+            else
+                *reinterpret_cast<uint4*>(out_b + v * (COUT - oca) + (cb - oca)) = o;
+        }
+    }
+}
+
+template <int CIN, int COUT>
+__device__ __forceinline__ void tc_issue(uint32_t tmem_acc, uint32_t hbase, uint32_t wbase, uint32_t mbar) {
+    using S = PipeShape<CIN, COUT>;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+#pragma unroll 1
+    for (int tap = 0; tap < 27; ++tap) {
+        const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+        const uint32_t a0 = hbase + (uint32_t)(((dz * HY + dy) * HX + dx) * 16);
+        const uint32_t b0 = wbase + (uint32_t)(tap * S::KC * COUT * 16);
+#pragma unroll
+        for (int s = 0; s < S::KC / 2; ++s) {
+            const uint64_t da = smem_desc(a0 + (uint32_t)(2 * s * HV * 16), HV * 16, HX * 16);
+            const uint64_t db = smem_desc(b0 + (uint32_t)(2 * s * COUT * 16), COUT * 16, 128);
+            const uint32_t acc = (tap | s) ? 1u : 0u;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\t"
+                "setp.ne.b32 p, %4, 0;\n\t"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_acc),
+                "l"(da), "l"(db), "r"(Shape<CIN, COUT>::IDESC), "r"(acc)
+                : "memory");
+        }
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+                 : "memory");
+}
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(kThreads) conv3_tc_pipe_kernel(int X, int Y, int Z, ConvIn in,
+                                                                 const uint4* __restrict__ wtc,
+                                                                 const float* __restrict__ bias, int relu,
+                                                                 __nv_bfloat16* __restrict__ out_a, int oca,
+                                                                 __nv_bfloat16* __restrict__ out_b) {
+    using S = PipeShape<CIN, COUT>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char* wsm = smem_raw;
+    unsigned char* hsm[2] = {smem_raw + S::WB, smem_raw + S::WB + S::HB};
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw + S::WB + 2 * S::HB);  // two
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + S::WB + 2 * S::HB + 16);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int q = tid; q < S::WB / 16; q += kThreads) reinterpret_cast<uint4*>(wsm)[q] = __ldg(wtc + q);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tslot)),
+                     "r"(S::NCOL)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(mbar)), "r"(1) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(mbar + 1)), "r"(1) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tslot;
+    const uint32_t wbase = smem_u32(wsm), hb[2] = {smem_u32(hsm[0]), smem_u32(hsm[1])};
+    const uint32_t mb[2] = {smem_u32(mbar), smem_u32(mbar + 1)};
+    const int bx = (X + TX - 1) / TX, by = (Y + TY - 1) / TY;
+    const long long nbricks = (long long)bx * by * Z;
+    const long long mine = nbricks > blockIdx.x ? (nbricks - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    auto origin = [&](long long i, int& x0, int& y0, int& z0) {
+        const long long br = blockIdx.x + i * gridDim.x;
+        x0 = (int)(br % bx) * TX;
+        const long long rest = br / bx;
+        y0 = (int)(rest % by) * TY;
+        z0 = (int)(rest / by);
+    };
+    uint32_t phase[2] = {0u, 0u};
+    bool ok = true;
+    int x0, y0, z0;
+    if (mine > 0) {
+        origin(0, x0, y0, z0);
+        stage_brick_async<CIN>(hsm[0], in, X, Y, Z, x0, y0, z0);
+    }
+    for (long long i = 0; i < mine && ok; ++i) {
+        const int b = (int)(i & 1);
+        cp_async_wait_all();
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // brick i visible to the tensor cores
+        __syncthreads();
+        if (tid == 0) tc_issue<CIN, COUT>(tmem + (uint32_t)(b * COUT), hb[b], wbase, mb[b]);
+        if (i > 0) {
+            // brick i-1: its MMAs are done, so its buffer takes brick i+1 while its result is stored
+            const bool mine_ok = mbar_wait(mb[b ^ 1], phase[b ^ 1]);
+            phase[b ^ 1] ^= 1u;
+            ok = __syncthreads_and(mine_ok) != 0;  // uniform across the block
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        }
+        if (i + 1 < mine) {
+            int x1, y1, z1;
+            origin(i + 1, x1, y1, z1);
+            stage_brick_async<CIN>(hsm[b ^ 1], in, X, Y, Z, x1, y1, z1);
+        }
+        if (i > 0) {
+            int xp, yp, zp;
+            origin(i - 1, xp, yp, zp);
+            tc_epilogue<COUT>(tmem, (uint32_t)((b ^ 1) * COUT), X, Y, xp, yp, zp, bias, relu, out_a, oca, out_b);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();  // the accumulator just read is free for brick i+1
+    }
+    if (ok && mine > 0) {  // ok is uniform here
+        const long long i = mine - 1;
+        const int b = (int)(i & 1);
+        ok = __syncthreads_and(mbar_wait(mb[b], phase[b])) != 0;
+        if (ok) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            origin(i, x0, y0, z0);
+            tc_epilogue<COUT>(tmem, (uint32_t)(b * COUT), X, Y, x0, y0, z0, bias, relu, out_a, oca, out_b);
+        }
+    }
+    if (!ok && tid == 0) atomicExch(&g_error, 1);
+    cp_async_wait_all();
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(S::NCOL) : "memory");
+}
+
 // FP32 master [co][27][ci] -> the B layout above: [tap][ci / 8][co][ci % 8]
 __global__ void pack_weights_tc_kernel(int cin, int cout, const float* __restrict__ w, __nv_bfloat16* __restrict__ tf,
                                        __nv_bfloat16* __restrict__ tb) {
@@ -820,6 +1043,18 @@ int num_sms_current() {
     return sms;
 }
 
+// resident CTAs per SM for a kernel of `threads` threads and `smem` dynamic shared bytes, from the
+// device's shared memory per SM (the occupancy query alone reported one CTA per SM for these)
+int resident_per_sm(int threads, int smem) {
+    int dev = 0, per_sm_smem = 0, reserved = 0, max_threads = 2048;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&per_sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    cudaDeviceGetAttribute(&max_threads, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+    const int by_smem = per_sm_smem / (smem + reserved);
+    return std::max(1, std::min(by_smem, max_threads / threads));
+}
+
 int grid_elems(long long n) { return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152LL * 16)); }
 
 ConvIn conv_in(const el_nn_conv_args* a) {
@@ -850,16 +1085,45 @@ int launch_conv(const el_nn_conv_args* a, cudaStream_t s) {
 }
 
 template <int CIN, int COUT>
+int launch_conv_tc_pipe(const el_nn_conv_args* a, cudaStream_t s) {
+    using S = tc::PipeShape<CIN, COUT>;
+    // the largest shared-memory carve-out, so that the occupancy below (and the launch) get it
+    if (cudaFuncSetAttribute(tc::conv3_tc_pipe_kernel<CIN, COUT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+        return EL_ERR_CUDA;
+    if (cudaFuncSetAttribute(tc::conv3_tc_pipe_kernel<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             S::SMEM) != cudaSuccess)
+        return EL_ERR_CUDA;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc::conv3_tc_pipe_kernel<CIN, COUT>, tc::kThreads,
+                                                      S::SMEM) != cudaSuccess)
+        return EL_ERR_CUDA;
+    per_sm = std::max(per_sm, resident_per_sm(tc::kThreads, S::SMEM));
+    const long long bricks =
+        (long long)((a->nx + tc::TX - 1) / tc::TX) * ((a->ny + tc::TY - 1) / tc::TY) * a->nz;
+    const int grid = (int)std::max<long long>(1, std::min<long long>(bricks, (long long)num_sms_current() * per_sm));
+    tc::conv3_tc_pipe_kernel<CIN, COUT><<<grid, tc::kThreads, S::SMEM, s>>>(
+        a->nx, a->ny, a->nz, conv_in(a), static_cast<const uint4*>(a->weights_tc), a->bias, a->relu,
+        static_cast<__nv_bfloat16*>(a->out_a), a->out_a_channels, static_cast<__nv_bfloat16*>(a->out_b));
+    return cudaGetLastError() == cudaSuccess ? EL_OK : EL_ERR_CUDA;
+}
+
+template <int CIN, int COUT>
 int launch_conv_tc(const el_nn_conv_args* a, cudaStream_t s) {
+    if constexpr (tc::PipeShape<CIN, COUT>::FITS) return launch_conv_tc_pipe<CIN, COUT>(a, s);
     using S = tc::Shape<CIN, COUT>;
+    // the largest shared-memory carve-out, so that the occupancy below (and the launch) get it
+    if (cudaFuncSetAttribute(tc::conv3_tc_kernel<CIN, COUT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+        return EL_ERR_CUDA;
     if (cudaFuncSetAttribute(tc::conv3_tc_kernel<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM) !=
         cudaSuccess)
         return EL_ERR_CUDA;
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc::conv3_tc_kernel<CIN, COUT>, tc::kThreads,
-                                                      S::SMEM) != cudaSuccess ||
-        per_sm < 1)
+                                                      S::SMEM) != cudaSuccess)
         return EL_ERR_CUDA;
+    per_sm = std::max(per_sm, resident_per_sm(tc::kThreads, S::SMEM));
     const long long bricks =
         (long long)((a->nx + tc::TX - 1) / tc::TX) * ((a->ny + tc::TY - 1) / tc::TY) * a->nz;
     const int grid = (int)std::max<long long>(1, std::min<long long>(bricks, (long long)num_sms_current() * per_sm));
@@ -930,6 +1194,13 @@ EL_API int el_nn_tc_supported(int cin, int cout) {
     EL_NN_TC_PAIRS(EL_NN_CASE)
 #undef EL_NN_CASE
     return 0;
+}
+
+// pairs where the tcgen05 kernel measured faster than the mma.sync one on GB300 (128^3 network
+// grids): the small-cin layers; with cin >= 32 and cout <= 64 the persistent tcgen05 CTAs are
+// limited to one or two per SM by the staged weights and lose to the register-tiled kernel
+EL_API int el_nn_tc_preferred(int cin, int cout) {
+    return (cin == 16 && (cout == 16 || cout == 32 || cout == 48)) || (cin == 32 && cout == 96);
 }
 
 EL_API int el_nn_take_error(void) {

@@ -84,6 +84,7 @@ def lib():
         L.el_nn_pack_weights.argtypes = [i, i, vp, vp, vp, vp]
         L.el_nn_pack_weights_tc.argtypes = [i, i, vp, vp, vp, vp]
         L.el_nn_tc_supported.argtypes = [i, i]
+        L.el_nn_tc_preferred.argtypes = [i, i]
         L.el_nn_take_error.argtypes = []
         L.el_nn_pool.argtypes = [i, i, i, i, vp, vp, vp]
         L.el_nn_spread.argtypes = [i, i, i, i, vp, vp, f, i, vp]
@@ -114,7 +115,9 @@ class WarmStartNet:
     """The network's parameters (FP32 masters, Adam moments, packed bf16 copies) and, per grid
     size, its activation and gradient buffers."""
 
-    def __init__(self, torch, device="cuda", seed=0, lr=1e-3, tensor_cores=True):
+    def __init__(self, torch, device="cuda", seed=0, lr=1e-3, tensor_cores="auto"):
+        """tensor_cores: "auto" runs the tcgen05 kernel on the layers where it is the faster one,
+        True on every layer it supports, False never."""
         self.torch = torch
         self.tensor_cores = tensor_cores
         self.dev = torch.device(device)
@@ -150,7 +153,8 @@ class WarmStartNet:
             nb = self.L.el_nn_packed_weight_bytes(cin, cout) // 2
             self.packed[name] = (torch.empty(nb, dtype=torch.bfloat16, device=self.dev),
                                  torch.empty(nb, dtype=torch.bfloat16, device=self.dev))
-            fwd_tc, bwd_tc = self.L.el_nn_tc_supported(cin, cout), self.L.el_nn_tc_supported(cout, cin)
+            pick = self.L.el_nn_tc_preferred if tensor_cores == "auto" else self.L.el_nn_tc_supported
+            fwd_tc, bwd_tc = pick(cin, cout), pick(cout, cin)
             if tensor_cores and (fwd_tc or bwd_tc):
                 self.packed_tc[name] = (torch.empty(nb, dtype=torch.bfloat16, device=self.dev) if fwd_tc else None,
                                         torch.empty(nb, dtype=torch.bfloat16, device=self.dev) if bwd_tc else None)

@@ -373,6 +373,8 @@ int el_nn_pack_weights(int cin, int cout, const float* w, void* packed_fwd, void
  * up, 0 otherwise, -1 if it could not be read. */
 int el_nn_pack_weights_tc(int cin, int cout, const float* w, void* packed_fwd, void* packed_bwd, void* stream);
 int el_nn_tc_supported(int cin, int cout);
+/* 1 where the tcgen05 kernel measured faster than the mma.sync one on GB300 (small cin) */
+int el_nn_tc_preferred(int cin, int cout);
 int el_nn_take_error(void);
 /* 2x2x2 average pooling; its backward is el_nn_spread(scale 1/8, accumulate 1) */
 int el_nn_pool(int nx, int ny, int nz, int c, const void* in, void* out, void* stream);
