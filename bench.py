@@ -897,11 +897,44 @@ def run_reference_batch(args, dist):
             "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_reference_warmstart(args, dist):
+    """The reference solves from zero only (Eigen's solve(), simulator.cpp:102-109): its speed-up
+    from a learned guess is 1 by definition; the line carries the CPU path's solve rate on the same
+    128^3 scenes (one step of a held-out spheres_pool scene, MIC(0)-PCG to the same tolerance)."""
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    import oracle as O
+    from oracle import step as S
+
+    n = args.ws_n
+    spec = _scenes_module().spheres_pool(n, 90000)
+    phi, solid = O.rasterise(spec, np.float32)
+    wts = O.compute_weights(solid)
+    st = S.initial_state(phi, wts, O.cell_solid_phi(solid), O.float_dx(n, np.float32))
+    dt = min(O.calc_time_step(st["u"], st["v"], st["w"], st["dx"], 1.0), 1.0 / 60.0)
+    t0 = time.perf_counter()
+    st, _ = S.step(st, dt, 0, 1, 1, 0, 9.8, tol=args.tol, maxit=20000)
+    elapsed = time.perf_counter() - t0
+    rate = 1.0 / elapsed
+    return {"metric": WS_METRIC, "value": 1.0, "unit": "x", "n_gpus": dist.world, "steps": 1, "warmup": 0,
+            "ms_per_step": elapsed * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 fields; pressure f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"learned warm start at {n}^3 (the reference solves from zero: speed-up 1)",
+                       "n": n, "parallelism": "host cores"},
+            "cpu_baseline": {"kind": "port", "cores": os.cpu_count(), "value": rate, "unit": "steps/s",
+                             "sample": f"one full {n}^3 step (held-out spheres_pool scene) on the CPU oracle, "
+                                       f"MIC(0)-PCG from zero to {args.tol} ({st['pcg_iterations']} iterations), "
+                                       f"{elapsed:.1f} s"},
+            "e2e": {"value": 1.0, "unit": "x", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def run_reference(args, dist):
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
     os.environ.setdefault("OMP_PROC_BIND", "close")
     if args.workload == "batch32":
         return run_reference_batch(args, dist)
+    if args.workload == "warmstart128":
+        return run_reference_warmstart(args, dist)
     if args.workload in ("dam64", "dam128"):
         n, weno = dam_setup(args)
         base = cpu_baseline_dam(args, steps=max(1, min(args.steps, 3 if n == 128 else 10)))
