@@ -77,6 +77,172 @@ __global__ void __launch_bounds__(256) advect_kernel(GridView<T> src, T* __restr
     out[lin3(i, j, k, src.n0, src.n1)] = r;
 }
 
+// ---------------------------------------------------------------------------------------
+// Tiled variants.  Under the CFL limit (cfl <= 1) the foot point and every RK stage lie within
+// one cell of the sample, so every trilinear velocity sample of a 32 x 8 x 8 tile of outputs
+// reads indices within [tile - 2, tile + 1] of each MAC grid: a CTA stages those boxes of u, v
+// and w (36 x 12 x 12 values each) in shared memory once and samples them there.  A sample
+// whose 8 points are not all in the box (a larger dt) reads global memory instead, with the
+// same arithmetic, so the results do not depend on which path a sample took.  The velocity
+// advection computes u, v and w of a tile in one CTA (when the advected field is the advecting
+// velocity, as in advect_velocity), sharing the staged boxes; the level set samples phi from
+// global memory at the foot point.
+constexpr int kTileX = 32, kTileY = 8, kTileZ = 8, kHalo = 2;
+constexpr int kBoxX = kTileX + 2 * kHalo, kBoxY = kTileY + 2 * kHalo, kBoxZ = kTileZ + 2 * kHalo;
+constexpr int kBoxN = kBoxX * kBoxY * kBoxZ;
+
+template <typename T>
+struct Staged {
+    const T* box;         // shared memory, [z][y][x] over the box
+    int bx0, by0, bz0;    // grid index of the box's first entry
+};
+
+template <typename T>
+__device__ __forceinline__ T sample_staged(const GridView<T>& g, const Staged<T>& b, T x, T y, T z, T dx, T inv) {
+    const TriIdx<T> t = tri_index(g, x, y, z, dx, inv);
+    const int a0 = t.i0 - b.bx0, a1 = t.i1 - b.bx0, c0 = t.j0 - b.by0, c1 = t.j1 - b.by0;
+    const int e0 = t.k0 - b.bz0, e1 = t.k1 - b.bz0;
+    if (a0 >= 0 && a1 < kBoxX && c0 >= 0 && c1 < kBoxY && e0 >= 0 && e1 < kBoxZ) {
+        const T* r00 = b.box + (e0 * kBoxY + c0) * kBoxX;
+        const T* r10 = b.box + (e0 * kBoxY + c1) * kBoxX;
+        const T* r01 = b.box + (e1 * kBoxY + c0) * kBoxX;
+        const T* r11 = b.box + (e1 * kBoxY + c1) * kBoxX;
+        return tri_combine(t, r00[a0], r00[a1], r10[a0], r10[a1], r01[a0], r01[a1], r11[a0], r11[a1]);
+    }
+    return tri_global(g, t);
+}
+
+template <typename T>
+struct StagedMac {
+    Staged<T> u, v, w;
+};
+
+template <typename T>
+__device__ __forceinline__ void velocity_at_staged(const Mac<T>& m, const StagedMac<T>& s, T x, T y, T z, T dx, T inv,
+                                                   T& vx, T& vy, T& vz) {
+    vx = sample_staged(m.u, s.u, x, y, z, dx, inv);
+    vy = sample_staged(m.v, s.v, x, y, z, dx, inv);
+    vz = sample_staged(m.w, s.w, x, y, z, dx, inv);
+}
+
+// backtrace with the staged velocity: the same stages and arithmetic as backtrace()
+template <typename T, int TRACE>
+__device__ __forceinline__ void backtrace_staged(const Mac<T>& m, const StagedMac<T>& sm, T& x, T& y, T& z, T h, T dx,
+                                                 T inv) {
+    T ax, ay, az;
+    velocity_at_staged(m, sm, x, y, z, dx, inv, ax, ay, az);
+    const T h2 = T(0.5) * h;
+    T bx, by, bz;
+    velocity_at_staged(m, sm, x + h2 * ax, y + h2 * ay, z + h2 * az, dx, inv, bx, by, bz);
+    if constexpr (TRACE == EL_TRACE_RK2) {
+        x = x + h * bx;
+        y = y + h * by;
+        z = z + h * bz;
+    } else {
+        const T h3 = T(0.75) * h;
+        T cx, cy, cz;
+        velocity_at_staged(m, sm, x + h3 * bx, y + h3 * by, z + h3 * bz, dx, inv, cx, cy, cz);
+        const T w1 = h * (T(2) / T(9)), w2 = h * (T(1) / T(3)), w3 = h * (T(4) / T(9));
+        x = x + w1 * ax + w2 * bx + w3 * cx;
+        y = y + w1 * ay + w2 * by + w3 * cy;
+        z = z + w1 * az + w2 * bz + w3 * cz;
+    }
+}
+
+// stages the boxes of u, v, w around tile (x0, y0, z0): rows of kBoxX along x, one warp per row
+template <typename T>
+__device__ __forceinline__ StagedMac<T> stage_mac(const Mac<T>& m, T* smem, int x0, int y0, int z0) {
+    const int bx0 = x0 - kHalo, by0 = y0 - kHalo, bz0 = z0 - kHalo;
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    const int lane = tid & 31, warp = tid >> 5, nwarps = (blockDim.x * blockDim.y) >> 5;
+    for (int row = warp; row < 3 * kBoxY * kBoxZ; row += nwarps) {
+        const int comp = row / (kBoxY * kBoxZ), r = row - comp * (kBoxY * kBoxZ);
+        const int bz = r / kBoxY, by = r - bz * kBoxY;
+        const GridView<T>& g = comp == 0 ? m.u : (comp == 1 ? m.v : m.w);
+        T* dst = smem + comp * kBoxN + (bz * kBoxY + by) * kBoxX;
+        const int gy = by0 + by, gz = bz0 + bz;
+        if (gy < 0 || gy >= g.n1 || gz < 0 || gz >= g.n2) continue;
+        const T* src = g.d + (long long)g.n0 * (gy + (long long)g.n1 * gz);
+        const int gx = bx0 + lane;
+        if (gx >= 0 && gx < g.n0) dst[lane] = __ldg(src + gx);
+        if (lane < kBoxX - 32) {
+            const int gx2 = bx0 + 32 + lane;
+            if (gx2 >= 0 && gx2 < g.n0) dst[32 + lane] = __ldg(src + gx2);
+        }
+    }
+    return StagedMac<T>{{smem, bx0, by0, bz0}, {smem + kBoxN, bx0, by0, bz0}, {smem + 2 * kBoxN, bx0, by0, bz0}};
+}
+
+// u, v, w of a tile, each advected through the (old) velocity itself
+template <typename T, int TRACE>
+__global__ void __launch_bounds__(kTileX * kTileY) advect_velocity_tiled_kernel(Mac<T> mac, T* __restrict__ ou,
+                                                                                T* __restrict__ ov,
+                                                                                T* __restrict__ ow, DtArg dt, T dx,
+                                                                                T inv_dx) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* smem = reinterpret_cast<T*>(smem_raw);
+    const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * kTileY, z0 = blockIdx.z * kTileZ;
+    const StagedMac<T> sm = stage_mac(mac, smem, x0, y0, z0);
+    __syncthreads();
+    const T h = -(T)dt_value(dt);
+    const int i = x0 + threadIdx.x, j = y0 + threadIdx.y;
+#pragma unroll 1
+    for (int kk = 0; kk < kTileZ; ++kk) {
+        const int k = z0 + kk;
+#pragma unroll 1
+        for (int c = 0; c < 3; ++c) {
+            // the component's grid, box and output, picked by value (no local arrays)
+            GridView<T> g = mac.u;
+            Staged<T> b = sm.u;
+            T* o = ou;
+            if (c == 1) {
+                g = mac.v;
+                b = sm.v;
+                o = ov;
+            } else if (c == 2) {
+                g = mac.w;
+                b = sm.w;
+                o = ow;
+            }
+            if (i >= g.n0 || j >= g.n1 || k >= g.n2) continue;
+            T x = (i + T(0.5)) * dx + g.ox;
+            T y = (j + T(0.5)) * dx + g.oy;
+            T z = (k + T(0.5)) * dx + g.oz;
+            backtrace_staged<T, TRACE>(mac, sm, x, y, z, h, dx, inv_dx);
+            o[lin3(i, j, k, g.n0, g.n1)] = sample_staged(g, b, x, y, z, dx, inv_dx);
+        }
+    }
+}
+
+// the level set (cells) through the staged velocity; phi itself from global memory
+template <typename T, int TRACE, int SAMPLE>
+__global__ void __launch_bounds__(kTileX * kTileY) advect_phi_tiled_kernel(GridView<T> src, T* __restrict__ out,
+                                                                           Mac<T> mac, DtArg dt, T dx, T inv_dx) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* smem = reinterpret_cast<T*>(smem_raw);
+    const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * kTileY, z0 = blockIdx.z * kTileZ;
+    const StagedMac<T> sm = stage_mac(mac, smem, x0, y0, z0);
+    __syncthreads();
+    const T h = -(T)dt_value(dt);
+    const int i = x0 + threadIdx.x, j = y0 + threadIdx.y;
+    if (i >= src.n0 || j >= src.n1) return;
+#pragma unroll 1
+    for (int kk = 0; kk < kTileZ; ++kk) {
+        const int k = z0 + kk;
+        if (k >= src.n2) break;
+        T x = (i + T(0.5)) * dx + src.ox;
+        T y = (j + T(0.5)) * dx + src.oy;
+        T z = (k + T(0.5)) * dx + src.oz;
+        backtrace_staged<T, TRACE>(mac, sm, x, y, z, h, dx, inv_dx);
+        T r;
+        if constexpr (SAMPLE == EL_SAMPLE_WENO6)
+            r = sample_weno6(src, x, y, z, dx, inv_dx);
+        else
+            r = sample_trilinear(src, x, y, z, dx, inv_dx);
+        out[lin3(i, j, k, src.n0, src.n1)] = r;
+    }
+}
+
 // Grid views of the scene's grids (staggered_grid.h:100-112): comp 0 = cells, 1/2/3 = u/v/w.
 template <typename T>
 GridView<T> make_view(const void* d, int ni, int nj, int nk, T dx, int comp) {
@@ -122,6 +288,76 @@ static int advect_launch(int ni, int nj, int nk, double dx_d, int comp, void* ou
     GridView<T> src = make_view<T>(in, ni, nj, nk, dx, comp);
     launch_dispatch<T>(src, out, mac, dt, dx, trace, sample, rows, s);
     return 1;
+}
+
+// the tiled kernels: the level set (any scheme), and the velocity advecting itself (trilinear)
+template <typename T, int TRACE, int SAMPLE>
+static int launch_phi_tiled(const GridView<T>& src, void* out, const Mac<T>& mac, DtArg dt, T dx, cudaStream_t s) {
+    const int smem = 3 * kBoxN * (int)sizeof(T);
+    if (cudaFuncSetAttribute(advect_phi_tiled_kernel<T, TRACE, SAMPLE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess)
+        return -1;
+    const dim3 grid((src.n0 + kTileX - 1) / kTileX, (src.n1 + kTileY - 1) / kTileY, (src.n2 + kTileZ - 1) / kTileZ);
+    advect_phi_tiled_kernel<T, TRACE, SAMPLE><<<grid, dim3(kTileX, kTileY, 1), smem, s>>>(
+        src, static_cast<T*>(out), mac, dt, dx, T(1) / dx);
+    return 1;
+}
+
+template <typename T, int TRACE>
+static int launch_velocity_tiled(const Mac<T>& mac, void* ou, void* ov, void* ow, DtArg dt, T dx, cudaStream_t s) {
+    const int smem = 3 * kBoxN * (int)sizeof(T);
+    if (cudaFuncSetAttribute(advect_velocity_tiled_kernel<T, TRACE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess)
+        return -1;
+    // tiles over the largest extent of the three face grids
+    const dim3 grid((mac.u.n0 + kTileX - 1) / kTileX, (mac.v.n1 + kTileY - 1) / kTileY,
+                    (mac.w.n2 + kTileZ - 1) / kTileZ);
+    advect_velocity_tiled_kernel<T, TRACE><<<grid, dim3(kTileX, kTileY, 1), smem, s>>>(
+        mac, static_cast<T*>(ou), static_cast<T*>(ov), static_cast<T*>(ow), dt, dx, T(1) / dx);
+    return 1;
+}
+
+template <typename T>
+static int advect_phi_tiled_t(int ni, int nj, int nk, double dx_d, void* out, const void* in, const void* vu,
+                              const void* vv, const void* vw, DtArg dt, int trace, int sample, cudaStream_t s) {
+    const T dx = (T)dx_d;
+    Mac<T> mac{make_view<T>(vu, ni, nj, nk, dx, 1), make_view<T>(vv, ni, nj, nk, dx, 2),
+               make_view<T>(vw, ni, nj, nk, dx, 3)};
+    GridView<T> src = make_view<T>(in, ni, nj, nk, dx, 0);
+    if (trace == EL_TRACE_RK2 && sample == EL_SAMPLE_TRILINEAR)
+        return launch_phi_tiled<T, EL_TRACE_RK2, EL_SAMPLE_TRILINEAR>(src, out, mac, dt, dx, s);
+    if (trace == EL_TRACE_RK2 && sample == EL_SAMPLE_WENO6)
+        return launch_phi_tiled<T, EL_TRACE_RK2, EL_SAMPLE_WENO6>(src, out, mac, dt, dx, s);
+    if (trace == EL_TRACE_RK3 && sample == EL_SAMPLE_TRILINEAR)
+        return launch_phi_tiled<T, EL_TRACE_RK3, EL_SAMPLE_TRILINEAR>(src, out, mac, dt, dx, s);
+    return launch_phi_tiled<T, EL_TRACE_RK3, EL_SAMPLE_WENO6>(src, out, mac, dt, dx, s);
+}
+
+template <typename T>
+static int advect_velocity_tiled_t(int ni, int nj, int nk, double dx_d, void* ou, void* ov, void* ow, const void* vu,
+                                   const void* vv, const void* vw, DtArg dt, int trace, cudaStream_t s) {
+    const T dx = (T)dx_d;
+    Mac<T> mac{make_view<T>(vu, ni, nj, nk, dx, 1), make_view<T>(vv, ni, nj, nk, dx, 2),
+               make_view<T>(vw, ni, nj, nk, dx, 3)};
+    if (trace == EL_TRACE_RK2) return launch_velocity_tiled<T, EL_TRACE_RK2>(mac, ou, ov, ow, dt, dx, s);
+    return launch_velocity_tiled<T, EL_TRACE_RK3>(mac, ou, ov, ow, dt, dx, s);
+}
+
+// Level set through the tiled kernel; returns kernels launched, -1 on a launch set-up failure.
+int advect_phi_tiled(int dtype, int ni, int nj, int nk, double dx, void* out, const void* in, const void* vu,
+                     const void* vv, const void* vw, const Scalars* dts, double dtv, int trace, int sample,
+                     cudaStream_t s) {
+    DtArg dt{dts, dtv};
+    if (dtype == EL_F64) return advect_phi_tiled_t<double>(ni, nj, nk, dx, out, in, vu, vv, vw, dt, trace, sample, s);
+    return advect_phi_tiled_t<float>(ni, nj, nk, dx, out, in, vu, vv, vw, dt, trace, sample, s);
+}
+
+// u, v, w advected through themselves with trilinear sampling, one tiled launch
+int advect_velocity_tiled(int dtype, int ni, int nj, int nk, double dx, void* ou, void* ov, void* ow, const void* vu,
+                          const void* vv, const void* vw, const Scalars* dts, double dtv, int trace, cudaStream_t s) {
+    DtArg dt{dts, dtv};
+    if (dtype == EL_F64) return advect_velocity_tiled_t<double>(ni, nj, nk, dx, ou, ov, ow, vu, vv, vw, dt, trace, s);
+    return advect_velocity_tiled_t<float>(ni, nj, nk, dx, ou, ov, ow, vu, vv, vw, dt, trace, s);
 }
 
 int advect_any(int dtype, int ni, int nj, int nk, double dx, int comp, void* out, const void* in,

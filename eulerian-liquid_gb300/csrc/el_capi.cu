@@ -13,6 +13,11 @@ namespace el {
 int advect_any(int dtype, int ni, int nj, int nk, double dx, int comp, void* out, const void* in, const void* vu,
                const void* vv, const void* vw, const Scalars* dts, double dtv, int trace, int sample,
                cudaStream_t s, int rows = 4);
+int advect_phi_tiled(int dtype, int ni, int nj, int nk, double dx, void* out, const void* in, const void* vu,
+                     const void* vv, const void* vw, const Scalars* dts, double dtv, int trace, int sample,
+                     cudaStream_t s);
+int advect_velocity_tiled(int dtype, int ni, int nj, int nk, double dx, void* ou, void* ov, void* ow, const void* vu,
+                          const void* vv, const void* vw, const Scalars* dts, double dtv, int trace, cudaStream_t s);
 int launch_weights(int dtype, int ni, int nj, int nk, const void* solid, void* wu, void* wv, void* ww,
                    cudaStream_t s);
 int launch_cell_solid(el_ctx* ctx);
@@ -234,13 +239,15 @@ EL_API int el_ctx_set_tuning(el_ctx* ctx, const el_tuning* t) {
     CHECK_CTX(ctx);
     if (!t || t->seg_blocks_per_sm < 1 || t->seg_blocks_per_sm > 8 || t->stencil_blocks_per_sm < 1 ||
         t->stencil_blocks_per_sm > 8 || t->extrapolate_blocks_per_sm < 1 || t->extrapolate_blocks_per_sm > 16 ||
-        (t->advect_rows != 1 && t->advect_rows != 2 && t->advect_rows != 4 && t->advect_rows != 8))
+        (t->advect_rows != 1 && t->advect_rows != 2 && t->advect_rows != 4 && t->advect_rows != 8) ||
+        (t->advect_tiled != 0 && t->advect_tiled != 1))
         return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "tuning out of range");
     // the reduction partials are sized for 8 blocks per SM (el_ctx_create)
     ctx->seg_per_sm = t->seg_blocks_per_sm;
     ctx->stencil_per_sm = t->stencil_blocks_per_sm;
     ctx->extrap_per_sm = t->extrapolate_blocks_per_sm;
     ctx->advect_rows = t->advect_rows;
+    ctx->advect_tiled = t->advect_tiled;
     // cached PCG iteration graphs hold the old launch shapes
     cudaStreamSynchronize(ctx->stream);
     for (auto& g : ctx->iter_graph)
@@ -257,6 +264,7 @@ EL_API int el_ctx_get_tuning(const el_ctx* ctx, el_tuning* t) {
     t->stencil_blocks_per_sm = ctx->stencil_per_sm;
     t->extrapolate_blocks_per_sm = ctx->extrap_per_sm;
     t->advect_rows = ctx->advect_rows;
+    t->advect_tiled = ctx->advect_tiled;
     return EL_OK;
 }
 
@@ -391,7 +399,16 @@ static int advect_level_set_impl(el_ctx* ctx, const Scalars* dts, double dt, int
     // reads phi, u, v, w; writes phi
     ProfScope prof(ctx, EL_KC_ADVECT_PHI, 2 * nbytes(ctx, EL_FIELD_PHI) + nbytes(ctx, EL_FIELD_U) +
                                               nbytes(ctx, EL_FIELD_V) + nbytes(ctx, EL_FIELD_W));
-    int n = advect_any(ctx->dtype, ctx->ni, ctx->nj, ctx->nk, ctx->dx, 0, ctx->tmp[0], ctx->field[EL_FIELD_PHI],
+    // the tiled kernel (velocity staged in shared memory) for trilinear sampling, unless
+    // launch-shape tuning asked for the per-sample one; WENO6 is arithmetic-bound and measured
+    // faster one thread per sample
+    int n = (ctx->advect_tiled && sample == EL_SAMPLE_TRILINEAR) ? advect_phi_tiled(ctx->dtype, ctx->ni, ctx->nj, ctx->nk, ctx->dx, ctx->tmp[0],
+                                                 ctx->field[EL_FIELD_PHI], ctx->field[EL_FIELD_U],
+                                                 ctx->field[EL_FIELD_V], ctx->field[EL_FIELD_W], dts, dt, trace,
+                                                 sample, ctx->stream)
+                              : -1;
+    if (n < 0)
+        n = advect_any(ctx->dtype, ctx->ni, ctx->nj, ctx->nk, ctx->dx, 0, ctx->tmp[0], ctx->field[EL_FIELD_PHI],
                        ctx->field[EL_FIELD_U], ctx->field[EL_FIELD_V], ctx->field[EL_FIELD_W], dts, dt, trace,
                        sample, ctx->stream, ctx->advect_rows);
     std::swap(ctx->tmp[0], ctx->field[EL_FIELD_PHI]);
@@ -402,12 +419,22 @@ static int advect_level_set_impl(el_ctx* ctx, const Scalars* dts, double dt, int
 static int advect_velocity_impl(el_ctx* ctx, const Scalars* dts, double dt, int trace, int sample) {
     int n = 0;
     const double vel_bytes = nbytes(ctx, EL_FIELD_U) + nbytes(ctx, EL_FIELD_V) + nbytes(ctx, EL_FIELD_W);
-    for (int comp = 0; comp < 3; ++comp) {
-        // reads u, v, w (the advected component among them); writes the component
-        ProfScope prof(ctx, EL_KC_ADVECT_VEL, vel_bytes + nbytes(ctx, EL_FIELD_U + comp));
-        n += advect_any(ctx->dtype, ctx->ni, ctx->nj, ctx->nk, ctx->dx, comp + 1, ctx->tmp[1 + comp],
-                        ctx->field[EL_FIELD_U + comp], ctx->field[EL_FIELD_U], ctx->field[EL_FIELD_V],
-                        ctx->field[EL_FIELD_W], dts, dt, trace, sample, ctx->stream, ctx->advect_rows);
+    if (ctx->advect_tiled && sample == EL_SAMPLE_TRILINEAR) {
+        // one launch for the three components: reads u, v, w once; writes the three components
+        ProfScope prof(ctx, EL_KC_ADVECT_VEL, 2 * vel_bytes);
+        n = advect_velocity_tiled(ctx->dtype, ctx->ni, ctx->nj, ctx->nk, ctx->dx, ctx->tmp[1], ctx->tmp[2],
+                                  ctx->tmp[3], ctx->field[EL_FIELD_U], ctx->field[EL_FIELD_V],
+                                  ctx->field[EL_FIELD_W], dts, dt, trace, ctx->stream);
+    }
+    if (n <= 0) {  // one launch per component
+        n = 0;
+        for (int comp = 0; comp < 3; ++comp) {
+            // reads u, v, w (the advected component among them); writes the component
+            ProfScope prof(ctx, EL_KC_ADVECT_VEL, vel_bytes + nbytes(ctx, EL_FIELD_U + comp));
+            n += advect_any(ctx->dtype, ctx->ni, ctx->nj, ctx->nk, ctx->dx, comp + 1, ctx->tmp[1 + comp],
+                            ctx->field[EL_FIELD_U + comp], ctx->field[EL_FIELD_U], ctx->field[EL_FIELD_V],
+                            ctx->field[EL_FIELD_W], dts, dt, trace, sample, ctx->stream, ctx->advect_rows);
+        }
     }
     for (int comp = 0; comp < 3; ++comp) std::swap(ctx->tmp[1 + comp], ctx->field[EL_FIELD_U + comp]);
     return n;

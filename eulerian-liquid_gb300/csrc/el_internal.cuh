@@ -103,6 +103,7 @@ struct el_ctx {
     // of the grid-wide stencil / element-wise kernels and of the extrapolation, and the rows of
     // the advection tile (32 x rows cells per block)
     int seg_per_sm = 6, stencil_per_sm = 8, extrap_per_sm = 6, advect_rows = 4;
+    int advect_tiled = 1;  // advection through the staged-tile kernels
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int64_t launches = 0;
@@ -337,28 +338,54 @@ __device__ __forceinline__ T lerp1(T a, T b, T f) {
     return (T(1) - f) * a + f * b;
 }
 
-// lerp(x, grid): clamped 8-point gather, x then y then z (interpolation.h:35-72, grid.h:369-377)
+// lerp(x, grid): clamped 8-point gather, x then y then z (interpolation.h:35-72, grid.h:369-377).
+// Split in three so that every sampler (global or shared-memory data) rounds identically.
+template <typename T>
+struct TriIdx {
+    int i0, i1, j0, j1, k0, k1;
+    T fx, fy, fz;
+};
+
+template <typename T>
+__device__ __forceinline__ TriIdx<T> tri_index(const GridView<T>& g, T x, T y, T z, T dx, T inv_dx) {
+    int i, j, k;
+    TriIdx<T> t;
+    index_fraction(x, g.ox, dx, inv_dx, i, t.fx);
+    index_fraction(y, g.oy, dx, inv_dx, j, t.fy);
+    index_fraction(z, g.oz, dx, inv_dx, k, t.fz);
+    t.i0 = clampi(i, 0, g.n0 - 1);
+    t.i1 = clampi(i + 1, 0, g.n0 - 1);
+    t.j0 = clampi(j, 0, g.n1 - 1);
+    t.j1 = clampi(j + 1, 0, g.n1 - 1);
+    t.k0 = clampi(k, 0, g.n2 - 1);
+    t.k1 = clampi(k + 1, 0, g.n2 - 1);
+    return t;
+}
+
+template <typename T>
+__device__ __forceinline__ T tri_combine(const TriIdx<T>& t, T c000, T c100, T c010, T c110, T c001, T c101, T c011,
+                                         T c111) {
+    const T lo = lerp1(lerp1(c000, c100, t.fx), lerp1(c010, c110, t.fx), t.fy);
+    const T hi = lerp1(lerp1(c001, c101, t.fx), lerp1(c011, c111, t.fx), t.fy);
+    return lerp1(lo, hi, t.fz);
+}
+
+template <typename T>
+__device__ __forceinline__ T tri_global(const GridView<T>& g, const TriIdx<T>& t) {
+    const long long r00 = (long long)g.n0 * (t.j0 + (long long)g.n1 * t.k0);
+    const long long r10 = (long long)g.n0 * (t.j1 + (long long)g.n1 * t.k0);
+    const long long r01 = (long long)g.n0 * (t.j0 + (long long)g.n1 * t.k1);
+    const long long r11 = (long long)g.n0 * (t.j1 + (long long)g.n1 * t.k1);
+    const T c000 = __ldg(g.d + r00 + t.i0), c100 = __ldg(g.d + r00 + t.i1);
+    const T c010 = __ldg(g.d + r10 + t.i0), c110 = __ldg(g.d + r10 + t.i1);
+    const T c001 = __ldg(g.d + r01 + t.i0), c101 = __ldg(g.d + r01 + t.i1);
+    const T c011 = __ldg(g.d + r11 + t.i0), c111 = __ldg(g.d + r11 + t.i1);
+    return tri_combine(t, c000, c100, c010, c110, c001, c101, c011, c111);
+}
+
 template <typename T>
 __device__ __forceinline__ T sample_trilinear(const GridView<T>& g, T x, T y, T z, T dx, T inv_dx) {
-    int i, j, k;
-    T fx, fy, fz;
-    index_fraction(x, g.ox, dx, inv_dx, i, fx);
-    index_fraction(y, g.oy, dx, inv_dx, j, fy);
-    index_fraction(z, g.oz, dx, inv_dx, k, fz);
-    const int i0 = clampi(i, 0, g.n0 - 1), i1 = clampi(i + 1, 0, g.n0 - 1);
-    const int j0 = clampi(j, 0, g.n1 - 1), j1 = clampi(j + 1, 0, g.n1 - 1);
-    const int k0 = clampi(k, 0, g.n2 - 1), k1 = clampi(k + 1, 0, g.n2 - 1);
-    const long long r00 = (long long)g.n0 * (j0 + (long long)g.n1 * k0);
-    const long long r10 = (long long)g.n0 * (j1 + (long long)g.n1 * k0);
-    const long long r01 = (long long)g.n0 * (j0 + (long long)g.n1 * k1);
-    const long long r11 = (long long)g.n0 * (j1 + (long long)g.n1 * k1);
-    const T c000 = __ldg(g.d + r00 + i0), c100 = __ldg(g.d + r00 + i1);
-    const T c010 = __ldg(g.d + r10 + i0), c110 = __ldg(g.d + r10 + i1);
-    const T c001 = __ldg(g.d + r01 + i0), c101 = __ldg(g.d + r01 + i1);
-    const T c011 = __ldg(g.d + r11 + i0), c111 = __ldg(g.d + r11 + i1);
-    const T lo = lerp1(lerp1(c000, c100, fx), lerp1(c010, c110, fx), fy);
-    const T hi = lerp1(lerp1(c001, c101, fx), lerp1(c011, c111, fx), fy);
-    return lerp1(lo, hi, fz);
+    return tri_global(g, tri_index(g, x, y, z, dx, inv_dx));
 }
 
 // Six-point WENO interpolation on nodes -2..3 at x = f in [0,1) (interpolation.h:74-111):

@@ -141,7 +141,7 @@ def test_autotune_picks_and_caches(el, tmp_path, monkeypatch):
     sims = _scene_set(el, specs)
     params = _params(el, el.SAMPLE_TRILINEAR)
     before = [s.download("phi") for s in sims]
-    cands = [(6, 8, 6, 4), (2, 4, 3, 2)]
+    cands = [(6, 8, 6, 4, 1), (2, 4, 3, 2, 0)]
     r = el.autotune.tune_batch(el, sims, params, device_name="test", steps=2, candidates=cands)
     assert not r["cached"] and len(r["trials"]) == 2 and cache.exists()
     # the scenes are back where they started and carry the chosen shapes
