@@ -26,15 +26,17 @@ __global__ void valid_from_stamps_kernel(long long n, const uint8_t* __restrict_
 }
 
 // One layer over the active tiles.  Tiles are 32 x 8 x 8 cells (i, j, k); a persistent grid
-// walks them, skipping those not flagged in act_in.  A cell can only become valid in layer
-// l+1 next to a cell that became valid in layer l (otherwise it would have become valid in
-// layer l already), so layer l+1 only visits tiles whose 3x3x3 tile neighbourhood changed in
-// layer l; layer 0 visits the tiles that hold an invalid cell and have a valid cell in their
-// tile neighbourhood.  A visited tile loads the stamps of its cells plus a one-cell halo
-// (10 x 10 x 34 bytes) into shared memory behind one barrier, so the 3x3x3 validity test runs
-// on shared memory; only cells with a valid neighbour read field values, and the sum walks the
-// neighbours in z, y, x order like the reference loop.  Stamps of cells updated in this layer
-// become layer + 1, which reads as "not yet valid" whether a block sees the old or new byte.
+// walks them, skipping those not flagged in act_in and those with no invalid cell left.  A cell
+// can only become valid in layer l+1 next to a cell that became valid in layer l (otherwise it
+// would have become valid in layer l already), so layer l+1 visits a tile only if a cell made
+// valid in layer l lies in it or on the face, edge or corner it shares with it; layer 0 visits
+// the tiles that hold an invalid cell and have a valid cell in their tile neighbourhood.  A
+// visited tile turns the stamps of its cells plus a one-cell halo into one 34-bit "valid before
+// this layer" mask per (y, z) row (warp ballots over coalesced byte loads) behind one barrier,
+// so a cell's 3x3x3 validity test is nine shared-memory words and a shift; only cells with a
+// valid neighbour read field values, and the sum walks the neighbours in z, y, x order like
+// the reference loop.  Stamps of cells updated in this layer become layer + 1, which reads as
+// "not yet valid" whether a block sees the old or new byte.
 constexpr int kExBX = 32, kExBY = 8, kExBZ = 8;
 
 struct TileGrid {
@@ -90,6 +92,7 @@ __global__ void __launch_bounds__(kExBX * kExBY) extrapolate_layer_kernel(int n0
     // (y, z) row: bit hx <-> cell i0 - 1 + hx
     constexpr int kRows = (kExBZ + 2) * (kExBY + 2);
     __shared__ unsigned long long rows[kExBZ + 2][kExBY + 2];
+    __shared__ unsigned int touched;  // bit (dz+1)*9 + (dy+1)*3 + (dx+1): that neighbour tile may change next
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int warp = ty, lane = tx;  // blocks are 32 x 8: one warp per y row of threads
     const int ntiles = tg.tx * tg.ty * tg.tz;
@@ -100,6 +103,7 @@ __global__ void __launch_bounds__(kExBX * kExBY) extrapolate_layer_kernel(int n0
         const int bx = t % tg.tx, by = (t / tg.tx) % tg.ty, bz = t / (tg.tx * tg.ty);
         const int i0 = bx * kExBX, j0 = by * kExBY, k0 = bz * kExBZ;
         const int i = i0 + tx, j = j0 + ty;
+        if (tx == 0 && ty == 0) touched = 0u;
         // each warp ballots whole rows: lanes read cells i0-1+lane, lanes 0 and 1 also the two
         // beyond; out-of-grid cells count as invalid
         for (int r = warp; r < kRows; r += kExBY) {
@@ -114,7 +118,8 @@ __global__ void __launch_bounds__(kExBX * kExBY) extrapolate_layer_kernel(int n0
             if (lane == 0) rows[hz][hy] = (unsigned long long)lo | ((unsigned long long)(hi & 3u) << 32);
         }
         __syncthreads();
-        bool changed = false, left = false;
+        unsigned int dirs = 0u;
+        bool left = false;
         if (i < n0 && j < n1) {
             for (int kk = 0; kk < kExBZ; ++kk) {
                 const int k = k0 + kk;
@@ -146,19 +151,27 @@ __global__ void __launch_bounds__(kExBX * kExBY) extrapolate_layer_kernel(int n0
                 const long long c = lin3(i, j, k, n0, n1);
                 g[c] = sum / (T)count;
                 stamp[c] = (uint8_t)(layer + 1);
-                changed = true;
+                // next layer: this tile, and the neighbour tiles this cell touches
+                const int xl = tx == 0 ? -1 : 0, xh = tx == kExBX - 1 ? 1 : 0;
+                const int yl = ty == 0 ? -1 : 0, yh = ty == kExBY - 1 ? 1 : 0;
+                const int zl = kk == 0 ? -1 : 0, zh = kk == kExBZ - 1 ? 1 : 0;
+                for (int dz = zl; dz <= zh; ++dz)
+                    for (int dy = yl; dy <= yh; ++dy)
+                        for (int dx = xl; dx <= xh; ++dx) dirs |= 1u << ((dz + 1) * 9 + (dy + 1) * 3 + (dx + 1));
             }
         }
-        // a tile whose cells are all valid now is never visited again; flag this tile's 3x3x3
-        // tile neighbourhood for the next layer (the barriers also keep the row masks intact
-        // until every thread is done with them)
+        if (dirs) atomicOr(&touched, dirs);
+        // a tile whose cells are all valid now is never visited again; flag the tiles a cell
+        // made valid here touches for the next layer (the barriers also keep the row masks
+        // intact until every thread is done with them)
         const int tid = tx + kExBX * ty;
         if (!__syncthreads_or(left) && tid == 0) tile_bits[t] &= (uint8_t)~2u;
-        if (__syncthreads_or(changed) && tid < 27) {
+        if (tid < 27 && ((touched >> tid) & 1u)) {
             const int ox = bx + tid % 3 - 1, oy = by + (tid / 3) % 3 - 1, oz = bz + tid / 9 - 1;
             if (ox >= 0 && ox < tg.tx && oy >= 0 && oy < tg.ty && oz >= 0 && oz < tg.tz)
                 act_out[ox + tg.tx * (oy + tg.ty * oz)] = 1;
         }
+        __syncthreads();  // `touched` is read before the next tile resets it
     }
 }
 
