@@ -171,9 +171,10 @@ EL_API int el_ctx_create(int ni, int nj, int nk, double dx, int dtype, int devic
     for (int f = EL_FIELD_VALID_U; f <= EL_FIELD_VALID_PHI; ++f)
         biggest_face = std::max(biggest_face, ctx->field_bytes[f]);
     ctx->valid_tmp = (uint8_t*)ctx_alloc(ctx, biggest_face);
-    // tiles of 32 x 8 x 8 cells over the largest face grid, three maps
-    const size_t tiles = (size_t)((ni + 1 + 31) / 32) * ((nj + 1 + 7) / 8) * ((nk + 1 + 7) / 8);
-    ctx->ex_tiles = (uint8_t*)ctx_alloc(ctx, 3 * tiles);
+    // extrapolation tiles of 32 x 4 x 4 cells over the largest face grid
+    const size_t tiles = (size_t)((ni + 1 + 31) / 32) * ((nj + 1 + 3) / 4) * ((nk + 1 + 3) / 4);
+    // per-tile bits (bytes, padded to 16), two flag words and two lists per tile, two counts
+    ctx->ex_tiles = (uint8_t*)ctx_alloc(ctx, ((tiles + 15) & ~size_t(15)) + 4 * tiles * 4 + 64);
     ctx->dscal = (Scalars*)ctx_alloc(ctx, 4 * sizeof(Scalars));
     Geom g = stencil_geom(ni, nj, nk, ctx->num_sms);
     ctx->max_partials = std::max(g.blocks(), ctx->num_sms * 8) * 2 + 64;

@@ -102,7 +102,7 @@ struct el_ctx {
     // launch-shape tuning (el_ctx_set_tuning): resident blocks per SM of the segment kernels,
     // of the grid-wide stencil / element-wise kernels and of the extrapolation, and the rows of
     // the advection tile (32 x rows cells per block)
-    int seg_per_sm = 6, stencil_per_sm = 8, extrap_per_sm = 6, advect_rows = 4;
+    int seg_per_sm = 6, stencil_per_sm = 8, extrap_per_sm = 12, advect_rows = 4;
     int advect_tiled = 1;  // advection through the staged-tile kernels
     cudaStream_t stream = nullptr;
     bool own_stream = false;

@@ -25,8 +25,9 @@ __global__ void valid_from_stamps_kernel(long long n, const uint8_t* __restrict_
         valid[c] = stamp[c] != 255 ? 1 : 0;
 }
 
-// One layer over the active tiles.  Tiles are 32 x 8 x 8 cells (i, j, k); a persistent grid
-// walks them, skipping those not flagged in act_in and those with no invalid cell left.  A cell
+// One layer over the active tiles.  Tiles are 32 x 4 x 4 cells (i, j, k); a persistent grid
+// walks the layer's list of tiles (built by the layer before), skipping those with no invalid
+// cell left.  A cell
 // can only become valid in layer l+1 next to a cell that became valid in layer l (otherwise it
 // would have become valid in layer l already), so layer l+1 visits a tile only if a cell made
 // valid in layer l lies in it or on the face, edge or corner it shares with it; layer 0 visits
@@ -37,7 +38,7 @@ __global__ void valid_from_stamps_kernel(long long n, const uint8_t* __restrict_
 // valid neighbour read field values, and the sum walks the neighbours in z, y, x order like
 // the reference loop.  Stamps of cells updated in this layer become layer + 1, which reads as
 // "not yet valid" whether a block sees the old or new byte.
-constexpr int kExBX = 32, kExBY = 8, kExBZ = 8;
+constexpr int kExBX = 32, kExBY = 4, kExBZ = 4;
 
 struct TileGrid {
     int tx, ty, tz;  // tiles per axis
@@ -65,8 +66,9 @@ __global__ void __launch_bounds__(kExBX * kExBY) stamps_init_kernel(int n0, int 
     if (threadIdx.x == 0 && threadIdx.y == 0) tile_bits[t] = (uint8_t)((bv ? 1 : 0) | (bi ? 2 : 0));
 }
 
-// layer-0 activity: tiles with an invalid cell and a valid cell in their tile neighbourhood
-__global__ void tiles_layer0_kernel(TileGrid tg, const uint8_t* __restrict__ tile_bits, uint8_t* __restrict__ act) {
+// layer 0's list: tiles with an invalid cell and a valid cell in their tile neighbourhood
+__global__ void tiles_layer0_kernel(TileGrid tg, const uint8_t* __restrict__ tile_bits, int* __restrict__ list,
+                                    int* __restrict__ count) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int ntiles = tg.tx * tg.ty * tg.tz;
     if (t >= ntiles) return;
@@ -79,14 +81,17 @@ __global__ void tiles_layer0_kernel(TileGrid tg, const uint8_t* __restrict__ til
                 if (x < 0 || y < 0 || z < 0 || x >= tg.tx || y >= tg.ty || z >= tg.tz) continue;
                 near_valid = near_valid || (tile_bits[x + tg.tx * (y + tg.ty * z)] & 1);
             }
-    act[t] = ((tile_bits[t] & 2) && near_valid) ? 1 : 0;
+    if ((tile_bits[t] & 2) && near_valid) list[atomicAdd(count, 1)] = t;
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kExBX * kExBY) extrapolate_layer_kernel(int n0, int n1, int n2, T* __restrict__ g,
                                                                           uint8_t* __restrict__ stamp, int layer,
-                                                                          TileGrid tg, const uint8_t* __restrict__ act_in,
-                                                                          uint8_t* __restrict__ act_out,
+                                                                          TileGrid tg, const int* __restrict__ list_in,
+                                                                          const int* __restrict__ count_in,
+                                                                          uint8_t* __restrict__ flags_out,
+                                                                          int* __restrict__ list_out,
+                                                                          int* __restrict__ count_out,
                                                                           uint8_t* __restrict__ tile_bits) {
     // validity before this layer of the tile and its one-cell halo, one 34-bit row mask per
     // (y, z) row: bit hx <-> cell i0 - 1 + hx
@@ -95,11 +100,11 @@ __global__ void __launch_bounds__(kExBX * kExBY) extrapolate_layer_kernel(int n0
     __shared__ unsigned int touched;  // bit (dz+1)*9 + (dy+1)*3 + (dx+1): that neighbour tile may change next
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int warp = ty, lane = tx;  // blocks are 32 x 8: one warp per y row of threads
-    const int ntiles = tg.tx * tg.ty * tg.tz;
     const unsigned full = 0xffffffffu;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        // block-uniform: tiles not flagged for this layer, and tiles with no invalid cell left
-        if (!act_in[t] || !(tile_bits[t] & 2)) continue;
+    const int nlist = *count_in;
+    for (int q = blockIdx.x; q < nlist; q += gridDim.x) {
+        const int t = list_in[q];
+        if (!(tile_bits[t] & 2)) continue;  // block-uniform: no invalid cell left
         const int bx = t % tg.tx, by = (t / tg.tx) % tg.ty, bz = t / (tg.tx * tg.ty);
         const int i0 = bx * kExBX, j0 = by * kExBY, k0 = bz * kExBZ;
         const int i = i0 + tx, j = j0 + ty;
@@ -168,8 +173,12 @@ __global__ void __launch_bounds__(kExBX * kExBY) extrapolate_layer_kernel(int n0
         if (!__syncthreads_or(left) && tid == 0) tile_bits[t] &= (uint8_t)~2u;
         if (tid < 27 && ((touched >> tid) & 1u)) {
             const int ox = bx + tid % 3 - 1, oy = by + (tid / 3) % 3 - 1, oz = bz + tid / 9 - 1;
-            if (ox >= 0 && ox < tg.tx && oy >= 0 && oy < tg.ty && oz >= 0 && oz < tg.tz)
-                act_out[ox + tg.tx * (oy + tg.ty * oz)] = 1;
+            if (ox >= 0 && ox < tg.tx && oy >= 0 && oy < tg.ty && oz >= 0 && oz < tg.tz) {
+                const int nt = ox + tg.tx * (oy + tg.ty * oz);
+                // the first to flag a tile lists it for the next layer
+                if (atomicExch(reinterpret_cast<unsigned int*>(flags_out) + nt, 1u) == 0u)
+                    list_out[atomicAdd(count_out, 1)] = nt;
+            }
         }
         __syncthreads();  // `touched` is read before the next tile resets it
     }
@@ -350,24 +359,31 @@ int launch_extrapolate(el_ctx* ctx, int field, uint8_t* valid, int layers, bool 
     dim3 block(kExBX, kExBY, 1);
     const TileGrid tg{(n0 + kExBX - 1) / kExBX, (n1 + kExBY - 1) / kExBY, (n2 + kExBZ - 1) / kExBZ};
     const int ntiles = tg.tx * tg.ty * tg.tz;
-    // three tile maps in the context's tile buffer: per-tile bits, and the layer's input and output
+    // the context's tile buffer: per-tile bits, and per layer parity a flag word per tile and a
+    // list of the tiles to visit (with its length)
     uint8_t* bits = ctx->ex_tiles;
-    uint8_t* act[2] = {ctx->ex_tiles + ntiles, ctx->ex_tiles + 2 * ntiles};
+    unsigned int* flags_base = reinterpret_cast<unsigned int*>(ctx->ex_tiles + ((ntiles + 15) & ~15));
+    unsigned int* flag[2] = {flags_base, flags_base + ntiles};
+    int* list[2] = {reinterpret_cast<int*>(flags_base + 2 * ntiles), reinterpret_cast<int*>(flags_base + 3 * ntiles)};
+    int* count[2] = {reinterpret_cast<int*>(flags_base + 4 * ntiles), reinterpret_cast<int*>(flags_base + 4 * ntiles) + 1};
+    cudaMemsetAsync(count[0], 0, 2 * sizeof(int), ctx->stream);
     stamps_init_kernel<<<ntiles, block, 0, ctx->stream>>>(n0, n1, n2, valid, stamp, tg, bits);
-    tiles_layer0_kernel<<<(ntiles + 255) / 256, 256, 0, ctx->stream>>>(tg, bits, act[0]);
+    tiles_layer0_kernel<<<(ntiles + 255) / 256, 256, 0, ctx->stream>>>(tg, bits, list[0], count[0]);
     int launched = 2;
     const int grid = std::max(1, std::min(ntiles, ctx->num_sms * ctx->extrap_per_sm));
     const int L = std::min(layers, 254);  // stamps are bytes: 255 marks "still invalid"
     for (int l = 0; l < L; ++l) {
-        uint8_t* in = act[l & 1];
-        uint8_t* out = act[(l + 1) & 1];
-        cudaMemsetAsync(out, 0, ntiles, ctx->stream);
+        const int in = l & 1, out = (l + 1) & 1;
+        cudaMemsetAsync(flag[out], 0, ntiles * sizeof(unsigned int), ctx->stream);
+        cudaMemsetAsync(count[out], 0, sizeof(int), ctx->stream);
         if (ctx->dtype == EL_F64)
-            extrapolate_layer_kernel<double><<<grid, block, 0, ctx->stream>>>(n0, n1, n2, (double*)ctx->field[field],
-                                                                              stamp, l, tg, in, out, bits);
+            extrapolate_layer_kernel<double><<<grid, block, 0, ctx->stream>>>(
+                n0, n1, n2, (double*)ctx->field[field], stamp, l, tg, list[in], count[in],
+                reinterpret_cast<uint8_t*>(flag[out]), list[out], count[out], bits);
         else
-            extrapolate_layer_kernel<float><<<grid, block, 0, ctx->stream>>>(n0, n1, n2, (float*)ctx->field[field],
-                                                                             stamp, l, tg, in, out, bits);
+            extrapolate_layer_kernel<float><<<grid, block, 0, ctx->stream>>>(
+                n0, n1, n2, (float*)ctx->field[field], stamp, l, tg, list[in], count[in],
+                reinterpret_cast<uint8_t*>(flag[out]), list[out], count[out], bits);
         ++launched;
     }
     if (write_back) {
