@@ -171,7 +171,8 @@ EL_API int el_ctx_create(int ni, int nj, int nk, double dx, int dtype, int devic
     for (int f = EL_FIELD_VALID_U; f <= EL_FIELD_VALID_PHI; ++f)
         biggest_face = std::max(biggest_face, ctx->field_bytes[f]);
     ctx->valid_tmp = (uint8_t*)ctx_alloc(ctx, biggest_face);
-    // extrapolation tiles of 32 x 4 x 4 cells over the largest face grid
+    // extrapolation tiles over the largest face grid (counted as 32 x 4 x 4: at least as many
+    // as the 32 x 8 x 4 tiles used)
     const size_t tiles = (size_t)((ni + 1 + 31) / 32) * ((nj + 1 + 3) / 4) * ((nk + 1 + 3) / 4);
     // per-tile bits (bytes, padded to 16), two flag words and two lists per tile, two counts
     ctx->ex_tiles = (uint8_t*)ctx_alloc(ctx, ((tiles + 15) & ~size_t(15)) + 4 * tiles * 4 + 64);

@@ -25,7 +25,7 @@ __global__ void valid_from_stamps_kernel(long long n, const uint8_t* __restrict_
         valid[c] = stamp[c] != 255 ? 1 : 0;
 }
 
-// One layer over the active tiles.  Tiles are 32 x 4 x 4 cells (i, j, k); a persistent grid
+// One layer over the active tiles.  Tiles are 32 x 8 x 4 cells (i, j, k); a persistent grid
 // walks the layer's list of tiles (built by the layer before), skipping those with no invalid
 // cell left.  A cell
 // can only become valid in layer l+1 next to a cell that became valid in layer l (otherwise it
@@ -38,7 +38,7 @@ __global__ void valid_from_stamps_kernel(long long n, const uint8_t* __restrict_
 // valid neighbour read field values, and the sum walks the neighbours in z, y, x order like
 // the reference loop.  Stamps of cells updated in this layer become layer + 1, which reads as
 // "not yet valid" whether a block sees the old or new byte.
-constexpr int kExBX = 32, kExBY = 4, kExBZ = 4;
+constexpr int kExBX = 32, kExBY = 8, kExBZ = 4;
 
 struct TileGrid {
     int tx, ty, tz;  // tiles per axis
