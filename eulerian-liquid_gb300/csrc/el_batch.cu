@@ -19,9 +19,10 @@ using namespace el;
 
 namespace el {
 int enqueue_step_device(el_ctx* ctx, const el_step_params& p, double cfl, double dt_frame, const BatchRecord* rec,
-                        int kernels[3]);
+                        int kernels[3], bool fork);
 int ensure_solver(el_ctx* ctx, int solver);
 int prepare_device_solve(el_ctx* ctx);
+int prepare_device_step(el_ctx* ctx);
 }  // namespace el
 
 namespace {
@@ -89,6 +90,10 @@ struct el_batch {
     BatchRecord* rec = nullptr;                // device, one per scene
     std::vector<std::array<int, 3>> kernels;   // per scene: outside loops, per sweep, per pass
     int64_t graph_kernels = 0;
+    // a scene's independent pieces (extrapolations, advections) as parallel graph branches: pays
+    // for one or two scenes; with more, the scenes' own branches already fill the GPU and the
+    // extra branches cost more than they overlap (a 32-scene step ran 1.5x slower with them)
+    bool fork_steps = false;
     std::string error;
 };
 
@@ -127,7 +132,7 @@ static int capture(el_batch* b, cudaGraphExec_t* out, bool count_kernels) {
         cudaStream_t own = c->stream;
         c->stream = b->branch[q];
         int k[3] = {0, 0, 0};
-        rc = enqueue_step_device(c, b->params, b->cfl, b->dt_frame, b->rec + q, k);
+        rc = enqueue_step_device(c, b->params, b->cfl, b->dt_frame, b->rec + q, k, b->fork_steps);
         if (rc == EL_OK) {
             if (c->dtype == EL_F64)
                 record_kernel<double><<<1, 1, 0, c->stream>>>(c->dscal, b->rec + q, b->dt_frame);
@@ -203,6 +208,7 @@ EL_API int el_batch_create(el_ctx* const* scenes, int count, const el_step_param
     b->device = scenes[0]->device;
     b->scenes.assign(scenes, scenes + count);
     b->params = *p;
+    b->fork_steps = count <= 2;
     b->cfl = cfl;
     b->dt_frame = dt_frame;
     b->kernels.assign(count, {0, 0, 0});
@@ -215,6 +221,7 @@ EL_API int el_batch_create(el_ctx* const* scenes, int count, const el_step_param
     for (el_ctx* c : b->scenes) {
         rc = ensure_solver(c, EL_SOLVER_MIXED);
         if (rc == EL_OK) rc = prepare_device_solve(c);
+        if (rc == EL_OK && b->fork_steps) rc = prepare_device_step(c);
         if (rc != EL_OK) return fail(rc);
         if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(EL_ERR_CUDA);
     }

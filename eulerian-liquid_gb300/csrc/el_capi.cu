@@ -25,7 +25,7 @@ int launch_flags_build(el_ctx* ctx, bool inner32, bool build = true);
 int launch_assign_indices(el_ctx* ctx, int* d_chunks, int* d_total);
 int launch_scatter_pressure(el_ctx* ctx);
 int launch_update_velocity(el_ctx* ctx, const Scalars* s, double dtv);
-int launch_extrapolate(el_ctx* ctx, int field, uint8_t* valid, int layers, bool write_back);
+int launch_extrapolate(el_ctx* ctx, int field, uint8_t* valid, int layers, bool write_back, int slot = 0);
 int launch_masks(el_ctx* ctx, bool gravity, double g, const Scalars* s, double dtv, bool zero);
 int launch_gravity(el_ctx* ctx, double g, const Scalars* s, double dtv);
 int launch_zero_invalid(el_ctx* ctx);
@@ -37,7 +37,8 @@ int setup_solver_storage(el_ctx* ctx, int solver);
 int launch_substep(el_ctx* ctx, double cfl, double dt_frame, const BatchRecord* rec, unsigned long long* scratch_max);
 int enqueue_solve_device(el_ctx* ctx, const el_solve_params& prm, int kernels[3]);
 int enqueue_step_device(el_ctx* ctx, const el_step_params& p, double cfl, double dt_frame, const BatchRecord* rec,
-                        int kernels[3]);
+                        int kernels[3], bool fork);
+int prepare_device_step(el_ctx* ctx);
 
 int set_error(el_ctx* ctx, int code, const std::string& msg) {
     if (ctx) ctx->last_error = msg;
@@ -170,12 +171,14 @@ EL_API int el_ctx_create(int ni, int nj, int nk, double dx, int dtype, int devic
     size_t biggest_face = 0;
     for (int f = EL_FIELD_VALID_U; f <= EL_FIELD_VALID_PHI; ++f)
         biggest_face = std::max(biggest_face, ctx->field_bytes[f]);
+    ctx->ex_stamp_bytes = biggest_face;
     ctx->valid_tmp = (uint8_t*)ctx_alloc(ctx, biggest_face);
     // extrapolation tiles over the largest face grid (counted as 32 x 4 x 4: at least as many
     // as the 32 x 8 x 4 tiles used)
     const size_t tiles = (size_t)((ni + 1 + 31) / 32) * ((nj + 1 + 3) / 4) * ((nk + 1 + 3) / 4);
     // per-tile bits (bytes, padded to 16), two flag words and two lists per tile, two counts
-    ctx->ex_tiles = (uint8_t*)ctx_alloc(ctx, ((tiles + 15) & ~size_t(15)) + 4 * tiles * 4 + 64);
+    ctx->ex_tiles_bytes = ((tiles + 15) & ~size_t(15)) + 4 * tiles * 4 + 64;
+    ctx->ex_tiles = (uint8_t*)ctx_alloc(ctx, ctx->ex_tiles_bytes);
     ctx->dscal = (Scalars*)ctx_alloc(ctx, 4 * sizeof(Scalars));
     Geom g = stencil_geom(ni, nj, nk, ctx->num_sms);
     ctx->max_partials = std::max(g.blocks(), ctx->num_sms * 8) * 2 + 64;
@@ -207,6 +210,11 @@ EL_API int el_ctx_destroy(el_ctx* ctx) {
         if (g) cudaGraphExecDestroy(g);
     for (auto& bs : ctx->body_stream)
         if (bs) cudaStreamDestroy(bs);
+    for (auto& ss : ctx->side)
+        if (ss) cudaStreamDestroy(ss);
+    for (auto& e : ctx->side_join)
+        if (e) cudaEventDestroy(e);
+    if (ctx->side_fork) cudaEventDestroy(ctx->side_fork);
     if (ctx->hscal) cudaFreeHost(ctx->hscal);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -597,17 +605,66 @@ EL_API int el_step(el_ctx* ctx, double dt, const el_step_params* p, el_step_stat
 // One sub-step of a scene with nothing decided on the host, for capture into a batch graph:
 // device dt (cut at the frame end), el_step's work, the solve with both loops on the device.
 // kernels[0]: kernels outside the solver loops; [1] per refinement sweep; [2] per PCG pass.
+// Streams, events and extrapolation scratch of the captured step's side branches (outside any
+// capture: they allocate).
+int el::prepare_device_step(el_ctx* ctx) {
+    for (int q = 0; q < 3; ++q) {
+        if (!ctx->side[q]) EL_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->side[q], cudaStreamNonBlocking));
+        if (!ctx->side_join[q]) EL_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->side_join[q], cudaEventDisableTiming));
+        if (!ctx->ex_stamp_extra[q]) {
+            ctx->ex_stamp_extra[q] = (uint8_t*)ctx_alloc(ctx, ctx->ex_stamp_bytes);
+            ctx->ex_tiles_extra[q] = (uint8_t*)ctx_alloc(ctx, ctx->ex_tiles_bytes);
+            if (!ctx->ex_stamp_extra[q] || !ctx->ex_tiles_extra[q])
+                return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "step branches");
+        }
+    }
+    if (!ctx->side_fork) EL_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->side_fork, cudaEventDisableTiming));
+    return EL_OK;
+}
+
+// Runs f(q) for q = 0..nwork-1 on nbranch streams (1 or nwork): with nbranch = nwork, f(q) runs
+// with ctx->stream switched to branch q's stream (q = 0 is the context's own), forked from and
+// joined back into the context's stream -- under capture these become parallel branches of the
+// graph; with nbranch = 1 all of them run in order on the context's stream.
+template <typename F>
+static int branches(el_ctx* ctx, int nbranch, int nwork, F&& f) {
+    int n = 0;
+    if (nbranch <= 1) {
+        for (int q = 0; q < nwork; ++q) n += f(q);
+        return n;
+    }
+    cudaStream_t own = ctx->stream;
+    EL_CUDA_TRY(ctx, cudaEventRecord(ctx->side_fork, own));
+    for (int q = 1; q < nbranch; ++q) EL_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->side[q - 1], ctx->side_fork, 0));
+    for (int q = 0; q < nbranch; ++q) {
+        ctx->stream = q == 0 ? own : ctx->side[q - 1];
+        n += f(q);
+        if (q > 0) EL_CUDA_TRY(ctx, cudaEventRecord(ctx->side_join[q - 1], ctx->stream));
+    }
+    ctx->stream = own;
+    for (int q = 1; q < nbranch; ++q) EL_CUDA_TRY(ctx, cudaStreamWaitEvent(own, ctx->side_join[q - 1], 0));
+    return n;
+}
+
 int el::enqueue_step_device(el_ctx* ctx, const el_step_params& p, double cfl, double dt_frame,
-                            const BatchRecord* rec, int kernels[3]) {
+                            const BatchRecord* rec, int kernels[3], bool fork) {
     int n = launch_substep(ctx, cfl, dt_frame, rec, (unsigned long long*)(ctx->dscal + 3));
     const Scalars* dts = ctx->dscal;
-    for (int comp = 0; comp < 3; ++comp)
-        n += launch_extrapolate(ctx, EL_FIELD_U + comp, (uint8_t*)ctx->field[EL_FIELD_VALID_U + comp],
-                                p.extrapolation_layers, true);
-    n += launch_extrapolate(ctx, EL_FIELD_PHI, (uint8_t*)ctx->field[EL_FIELD_VALID_PHI], p.extrapolation_layers,
-                            false);
-    n += advect_level_set_impl(ctx, dts, 0.0, p.trace_phi, p.sample_phi);
-    n += advect_velocity_impl(ctx, dts, 0.0, p.trace_vel, p.sample_vel);
+    // the four extrapolations are independent: four branches, each with its own scratch
+    n += branches(ctx, fork ? 4 : 1, 4, [&](int q) {
+        if (q < 3)
+            return launch_extrapolate(ctx, EL_FIELD_U + q, (uint8_t*)ctx->field[EL_FIELD_VALID_U + q],
+                                      p.extrapolation_layers, true, fork ? q : 0);
+        return launch_extrapolate(ctx, EL_FIELD_PHI, (uint8_t*)ctx->field[EL_FIELD_VALID_PHI], p.extrapolation_layers,
+                                  false, fork ? 3 : 0);
+    });
+    // the level set and the velocity advect independently (both read the old velocity); the
+    // level set is enqueued first because enqueueing the velocity's advection swaps the
+    // context's velocity buffers on the host
+    n += branches(ctx, fork ? 2 : 1, 2, [&](int q) {
+        return q == 0 ? advect_level_set_impl(ctx, dts, 0.0, p.trace_phi, p.sample_phi)
+                      : advect_velocity_impl(ctx, dts, 0.0, p.trace_vel, p.sample_vel);
+    });
     n += launch_masks(ctx, true, p.gravity, dts, 0.0, true);
     n += launch_flags_build(ctx, true);
     int rc = check_launch(ctx, "captured step");

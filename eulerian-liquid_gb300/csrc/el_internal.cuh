@@ -147,6 +147,13 @@ struct el_ctx {
     // captured CUDA graphs of PCG iteration batches, one per solver (index EL_SOLVER_*)
     cudaGraphExec_t iter_graph[3] = {nullptr, nullptr, nullptr};
     cudaStream_t body_stream[2] = {nullptr, nullptr};  // capture of conditional-node bodies
+    // branches of a captured step (independent extrapolations and advections run side by side),
+    // each extra branch with its own extrapolation scratch
+    cudaStream_t side[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t side_fork = nullptr, side_join[3] = {nullptr, nullptr, nullptr};
+    uint8_t* ex_stamp_extra[3] = {nullptr, nullptr, nullptr};
+    uint8_t* ex_tiles_extra[3] = {nullptr, nullptr, nullptr};
+    size_t ex_stamp_bytes = 0, ex_tiles_bytes = 0;
     int iter_graph_len[3] = {0, 0, 0};
     int iter_graph_kernels[3] = {0, 0, 0};
     bool use_graphs = true;

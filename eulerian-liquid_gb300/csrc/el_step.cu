@@ -351,18 +351,20 @@ static void field_dims(el_ctx* ctx, int field, int& n0, int& n1, int& n2) {
 
 // extrapolate `field` over `layers` Jacobi layers using the mask `valid`; when write_back the
 // mask is updated like extrapolate() (velocity), else left alone like extrapolate_const().
-int launch_extrapolate(el_ctx* ctx, int field, uint8_t* valid, int layers, bool write_back) {
+// slot 0 uses the context's extrapolation scratch, slots 1-3 the step branches' own
+int launch_extrapolate(el_ctx* ctx, int field, uint8_t* valid, int layers, bool write_back, int slot) {
     int n0, n1, n2;
     field_dims(ctx, field, n0, n1, n2);
     const long long n = (long long)n0 * n1 * n2;
-    uint8_t* stamp = ctx->valid_tmp;
+    uint8_t* stamp = slot ? ctx->ex_stamp_extra[slot - 1] : ctx->valid_tmp;
+    uint8_t* tiles = slot ? ctx->ex_tiles_extra[slot - 1] : ctx->ex_tiles;
     dim3 block(kExBX, kExBY, 1);
     const TileGrid tg{(n0 + kExBX - 1) / kExBX, (n1 + kExBY - 1) / kExBY, (n2 + kExBZ - 1) / kExBZ};
     const int ntiles = tg.tx * tg.ty * tg.tz;
     // the context's tile buffer: per-tile bits, and per layer parity a flag word per tile and a
     // list of the tiles to visit (with its length)
-    uint8_t* bits = ctx->ex_tiles;
-    unsigned int* flags_base = reinterpret_cast<unsigned int*>(ctx->ex_tiles + ((ntiles + 15) & ~15));
+    uint8_t* bits = tiles;
+    unsigned int* flags_base = reinterpret_cast<unsigned int*>(tiles + ((ntiles + 15) & ~15));
     unsigned int* flag[2] = {flags_base, flags_base + ntiles};
     int* list[2] = {reinterpret_cast<int*>(flags_base + 2 * ntiles), reinterpret_cast<int*>(flags_base + 3 * ntiles)};
     int* count[2] = {reinterpret_cast<int*>(flags_base + 4 * ntiles), reinterpret_cast<int*>(flags_base + 4 * ntiles) + 1};
