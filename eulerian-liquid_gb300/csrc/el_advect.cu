@@ -87,9 +87,80 @@ __global__ void __launch_bounds__(256) advect_kernel(GridView<T> src, T* __restr
 // advection computes u, v and w of a tile in one CTA (when the advected field is the advecting
 // velocity, as in advect_velocity), sharing the staged boxes; the level set samples phi from
 // global memory at the foot point.
+//
+// The box holds the clamped grid (entry p = value at clamp(box origin + p)), so a sample reads
+// its 8 points at the unclamped indices i, i+1 (j, k likewise) with no clamping and gets exactly
+// the values of the clamped gather lerp() makes; the 8 reads sit at fixed offsets from one
+// address.  The floor of the cell coordinate is taken without conversions (floor_index), and
+// the three components at one position share their cell-centred and face coordinates.
 constexpr int kTileX = 32, kTileY = 8, kTileZ = 8, kHalo = 2;
 constexpr int kBoxX = kTileX + 2 * kHalo, kBoxY = kTileY + 2 * kHalo, kBoxZ = kTileZ + 2 * kHalo;
 constexpr int kBoxN = kBoxX * kBoxY * kBoxZ;
+
+// floor(t) and t - floor(t), the same values as index_fraction.  FP32: t + 1.5 * 2^23 rounded
+// toward -inf holds floor(t) in its low mantissa bits (exact for |t| < 2^22); outside that range
+// (and for NaN) the index lands millions of cells away, i.e. outside every staged box, and the
+// sample takes the exact global path.
+template <typename T>
+__device__ __forceinline__ void floor_index(T t, int& idx, T& frac) {
+    if constexpr (sizeof(T) == 4) {
+        const float big = 12582912.0f;  // 1.5 * 2^23, bit pattern 0x4B400000
+        const float r = __fadd_rd(t, big);
+        idx = (int)((unsigned)__float_as_int(r) - 0x4B400000u);
+        frac = t - (r - big);
+    } else {
+        const T fl = floor(t);
+        idx = (int)fl;
+        frac = t - fl;
+    }
+}
+
+// the cell coordinate of index_fraction: (pos - origin - dx / 2) / dx
+template <typename T>
+__device__ __forceinline__ T cell_coord(T pos, T origin, T dx, T inv_dx) {
+    if constexpr (sizeof(T) == 8)
+        return (pos - origin - T(0.5) * dx) / dx;
+    else
+        return (pos - origin - T(0.5) * dx) * inv_dx;
+}
+
+// one axis of a position: box-relative floor index and fraction
+template <typename T>
+struct AxisPos {
+    int a;
+    T f;
+};
+
+template <typename T>
+__device__ __forceinline__ AxisPos<T> axis_pos(T pos, T origin, int box0, T dx, T inv_dx) {
+    AxisPos<T> p;
+    int idx;
+    floor_index(cell_coord(pos, origin, dx, inv_dx), idx, p.f);
+    p.a = (int)((unsigned)idx - (unsigned)box0);
+    return p;
+}
+
+template <typename T>
+__device__ __forceinline__ T lerp_combine(T fx, T fy, T fz, T c000, T c100, T c010, T c110, T c001, T c101, T c011,
+                                          T c111) {
+    const T lo = lerp1(lerp1(c000, c100, fx), lerp1(c010, c110, fx), fy);
+    const T hi = lerp1(lerp1(c001, c101, fx), lerp1(c011, c111, fx), fy);
+    return lerp1(lo, hi, fz);
+}
+
+// trilinear sample from a staged box at box-relative (x, y, z); false when the 8 points are not
+// all inside the box
+template <typename T>
+__device__ __forceinline__ bool staged_lerp(const T* box, const AxisPos<T>& x, const AxisPos<T>& y,
+                                            const AxisPos<T>& z, T& out) {
+    if ((unsigned)x.a >= (unsigned)(kBoxX - 1) || (unsigned)y.a >= (unsigned)(kBoxY - 1) ||
+        (unsigned)z.a >= (unsigned)(kBoxZ - 1))
+        return false;
+    const T* p = box + (z.a * kBoxY + y.a) * kBoxX + x.a;
+    constexpr int SY = kBoxX, SZ = kBoxX * kBoxY;
+    out = lerp_combine(x.f, y.f, z.f, p[0], p[1], p[SY], p[SY + 1], p[SZ], p[SZ + 1], p[SZ + SY], p[SZ + SY + 1]);
+    return true;
+}
 
 template <typename T>
 struct Staged {
@@ -99,17 +170,11 @@ struct Staged {
 
 template <typename T>
 __device__ __forceinline__ T sample_staged(const GridView<T>& g, const Staged<T>& b, T x, T y, T z, T dx, T inv) {
-    const TriIdx<T> t = tri_index(g, x, y, z, dx, inv);
-    const int a0 = t.i0 - b.bx0, a1 = t.i1 - b.bx0, c0 = t.j0 - b.by0, c1 = t.j1 - b.by0;
-    const int e0 = t.k0 - b.bz0, e1 = t.k1 - b.bz0;
-    if (a0 >= 0 && a1 < kBoxX && c0 >= 0 && c1 < kBoxY && e0 >= 0 && e1 < kBoxZ) {
-        const T* r00 = b.box + (e0 * kBoxY + c0) * kBoxX;
-        const T* r10 = b.box + (e0 * kBoxY + c1) * kBoxX;
-        const T* r01 = b.box + (e1 * kBoxY + c0) * kBoxX;
-        const T* r11 = b.box + (e1 * kBoxY + c1) * kBoxX;
-        return tri_combine(t, r00[a0], r00[a1], r10[a0], r10[a1], r01[a0], r01[a1], r11[a0], r11[a1]);
-    }
-    return tri_global(g, t);
+    T r;
+    if (staged_lerp(b.box, axis_pos(x, g.ox, b.bx0, dx, inv), axis_pos(y, g.oy, b.by0, dx, inv),
+                    axis_pos(z, g.oz, b.bz0, dx, inv), r))
+        return r;
+    return sample_trilinear(g, x, y, z, dx, inv);
 }
 
 template <typename T>
@@ -117,12 +182,17 @@ struct StagedMac {
     Staged<T> u, v, w;
 };
 
+// u at (face x, cell y, cell z), v at (cell, face, cell), w at (cell, cell, face): six axis
+// positions serve all three (the cell origins are those of the other components' grids)
 template <typename T>
 __device__ __forceinline__ void velocity_at_staged(const Mac<T>& m, const StagedMac<T>& s, T x, T y, T z, T dx, T inv,
                                                    T& vx, T& vy, T& vz) {
-    vx = sample_staged(m.u, s.u, x, y, z, dx, inv);
-    vy = sample_staged(m.v, s.v, x, y, z, dx, inv);
-    vz = sample_staged(m.w, s.w, x, y, z, dx, inv);
+    const AxisPos<T> xf = axis_pos(x, m.u.ox, s.u.bx0, dx, inv), xc = axis_pos(x, m.v.ox, s.u.bx0, dx, inv);
+    const AxisPos<T> yf = axis_pos(y, m.v.oy, s.u.by0, dx, inv), yc = axis_pos(y, m.u.oy, s.u.by0, dx, inv);
+    const AxisPos<T> zf = axis_pos(z, m.w.oz, s.u.bz0, dx, inv), zc = axis_pos(z, m.u.oz, s.u.bz0, dx, inv);
+    if (!staged_lerp(s.u.box, xf, yc, zc, vx)) vx = sample_trilinear(m.u, x, y, z, dx, inv);
+    if (!staged_lerp(s.v.box, xc, yf, zc, vy)) vy = sample_trilinear(m.v, x, y, z, dx, inv);
+    if (!staged_lerp(s.w.box, xc, yc, zf, vz)) vz = sample_trilinear(m.w, x, y, z, dx, inv);
 }
 
 // backtrace with the staged velocity: the same stages and arithmetic as backtrace()
@@ -149,7 +219,8 @@ __device__ __forceinline__ void backtrace_staged(const Mac<T>& m, const StagedMa
     }
 }
 
-// stages the boxes of u, v, w around tile (x0, y0, z0): rows of kBoxX along x, one warp per row
+// stages the clamped boxes of u, v, w around tile (x0, y0, z0): rows of kBoxX along x, one warp
+// per row
 template <typename T>
 __device__ __forceinline__ StagedMac<T> stage_mac(const Mac<T>& m, T* smem, int x0, int y0, int z0) {
     const int bx0 = x0 - kHalo, by0 = y0 - kHalo, bz0 = z0 - kHalo;
@@ -160,15 +231,10 @@ __device__ __forceinline__ StagedMac<T> stage_mac(const Mac<T>& m, T* smem, int 
         const int bz = r / kBoxY, by = r - bz * kBoxY;
         const GridView<T>& g = comp == 0 ? m.u : (comp == 1 ? m.v : m.w);
         T* dst = smem + comp * kBoxN + (bz * kBoxY + by) * kBoxX;
-        const int gy = by0 + by, gz = bz0 + bz;
-        if (gy < 0 || gy >= g.n1 || gz < 0 || gz >= g.n2) continue;
+        const int gy = clampi(by0 + by, 0, g.n1 - 1), gz = clampi(bz0 + bz, 0, g.n2 - 1);
         const T* src = g.d + (long long)g.n0 * (gy + (long long)g.n1 * gz);
-        const int gx = bx0 + lane;
-        if (gx >= 0 && gx < g.n0) dst[lane] = __ldg(src + gx);
-        if (lane < kBoxX - 32) {
-            const int gx2 = bx0 + 32 + lane;
-            if (gx2 >= 0 && gx2 < g.n0) dst[32 + lane] = __ldg(src + gx2);
-        }
+        dst[lane] = __ldg(src + clampi(bx0 + lane, 0, g.n0 - 1));
+        if (lane < kBoxX - 32) dst[32 + lane] = __ldg(src + clampi(bx0 + 32 + lane, 0, g.n0 - 1));
     }
     return StagedMac<T>{{smem, bx0, by0, bz0}, {smem + kBoxN, bx0, by0, bz0}, {smem + 2 * kBoxN, bx0, by0, bz0}};
 }
@@ -243,6 +309,101 @@ __global__ void __launch_bounds__(kTileX * kTileY) advect_phi_tiled_kernel(GridV
     }
 }
 
+// ---------------------------------------------------------------------------------------
+// WENO6 level set, tiled.  Under the CFL limit the foot point of a cell lies within one cell
+// of it, so the 6^3 stencils of a 32 x 8 x 4 tile of cells read phi within [tile - 3, tile + 4]:
+// the CTA stages that clamped box (39 x 15 x 11) once.  The smoothness indicators of an x-pass
+// depend only on the six values it reads, not on the sample's fraction, so they are formed once
+// per (row, floor index) of the box -- (eps + IS_s)^2 for the 34 floor indices of each of the
+// 165 rows -- and shared by every sample whose stencil uses that row segment, instead of being
+// recomputed by all 36 x-passes of every sample.  The y- and z-passes combine per-sample values
+// and are evaluated in full.  The backtrace reads the velocity from global memory (L1-served).
+// A foot point outside the box (a larger dt) takes the global sample_weno6 path, with the same
+// arithmetic.
+constexpr int kWX = 32, kWY = 8, kWZ = 4;
+constexpr int kWBX = kWX + 7, kWBY = kWY + 7, kWBZ = kWZ + 7;  // nodes [tile - 3, tile + 4]
+constexpr int kWRows = kWBY * kWBZ;
+constexpr int kWBases = kWX + 2;                 // floor indices [tile - 1, tile + 32]
+constexpr int kWBoxN = (kWBX * kWRows + 3) & ~3;  // phi box, padded to 16 bytes (float)
+constexpr int kWQ = kWRows * kWBases;            // one indicator plane
+
+template <typename T, int TRACE>
+__global__ void __launch_bounds__(kWX * kWY, sizeof(T) == 4 ? 2 : 1) advect_phi_weno_tiled_kernel(GridView<T> src, T* __restrict__ out,
+                                                                           Mac<T> mac, DtArg dt, T dx, T inv_dx) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* pbox = reinterpret_cast<T*>(smem_raw);  // [z][y][x]
+    T* qbox = pbox + kWBoxN;                    // [s][row][floor index]
+    const int x0 = blockIdx.x * kWX, y0 = blockIdx.y * kWY, z0 = blockIdx.z * kWZ;
+    const int bx0 = x0 - 3, by0 = y0 - 3, bz0 = z0 - 3;
+    const int tid = threadIdx.x + kWX * threadIdx.y;
+    const int lane = tid & 31, warp = tid >> 5;
+    for (int row = warp; row < kWRows; row += (kWX * kWY) / 32) {
+        const int bz = row / kWBY, by = row - bz * kWBY;
+        const int gy = clampi(by0 + by, 0, src.n1 - 1), gz = clampi(bz0 + bz, 0, src.n2 - 1);
+        const T* s = src.d + (long long)src.n0 * (gy + (long long)src.n1 * gz);
+        T* d = pbox + row * kWBX;
+        d[lane] = __ldg(s + clampi(bx0 + lane, 0, src.n0 - 1));
+        if (lane < kWBX - 32) d[32 + lane] = __ldg(s + clampi(bx0 + 32 + lane, 0, src.n0 - 1));
+    }
+    __syncthreads();
+    for (int e = tid; e < kWQ; e += kWX * kWY) {
+        const int row = e / kWBases, b = e - row * kWBases;
+        const T* v = pbox + row * kWBX + b;
+        T qa, qb, qc;
+        weno6_sq(v[0], v[1], v[2], v[3], v[4], v[5], qa, qb, qc);
+        qbox[e] = qa;
+        qbox[kWQ + e] = qb;
+        qbox[2 * kWQ + e] = qc;
+    }
+    __syncthreads();
+    const int i = x0 + threadIdx.x, j = y0 + threadIdx.y;
+    if (i >= src.n0 || j >= src.n1) return;
+    const T h = -(T)dt_value(dt);
+#pragma unroll 1
+    for (int kk = 0; kk < kWZ; ++kk) {
+        const int k = z0 + kk;
+        if (k >= src.n2) break;
+        T x = (i + T(0.5)) * dx + src.ox;
+        T y = (j + T(0.5)) * dx + src.oy;
+        T z = (k + T(0.5)) * dx + src.oz;
+        backtrace<T, TRACE>(mac, x, y, z, h, dx, inv_dx);
+        // stencil origin (floor - 2) relative to the box, per axis
+        const AxisPos<T> px = axis_pos(x, src.ox, x0 - 1, dx, inv_dx);
+        const AxisPos<T> py = axis_pos(y, src.oy, y0 - 1, dx, inv_dx);
+        const AxisPos<T> pz = axis_pos(z, src.oz, z0 - 1, dx, inv_dx);
+        T r;
+        if ((unsigned)px.a < (unsigned)kWBases && (unsigned)py.a < (unsigned)(kWY + 2) &&
+            (unsigned)pz.a < (unsigned)(kWZ + 2)) {
+            const WenoAxis<T> wx = weno_axis(px.f);
+            const WenoAxis<T> wy = weno_axis(py.f);
+            T zl[6];
+#pragma unroll 1
+            for (int dk = 0; dk < 6; ++dk) {
+                const int row0 = (pz.a + dk) * kWBY + py.a;
+                T yl[6];
+#pragma unroll
+                for (int dj = 0; dj < 6; ++dj) {
+                    const int row = row0 + dj;
+                    const T* v = pbox + row * kWBX + px.a;
+                    const T* q = qbox + row * kWBases + px.a;
+                    yl[dj] = weno6_combine(wx, v[0], v[1], v[2], v[3], v[4], v[5], q[0], q[kWQ], q[2 * kWQ]);
+                }
+                const T zv = weno6_eval(wy, yl[0], yl[1], yl[2], yl[3], yl[4], yl[5]);
+                zl[0] = dk == 0 ? zv : zl[0];
+                zl[1] = dk == 1 ? zv : zl[1];
+                zl[2] = dk == 2 ? zv : zl[2];
+                zl[3] = dk == 3 ? zv : zl[3];
+                zl[4] = dk == 4 ? zv : zl[4];
+                zl[5] = dk == 5 ? zv : zl[5];
+            }
+            r = weno6_eval(weno_axis(pz.f), zl[0], zl[1], zl[2], zl[3], zl[4], zl[5]);
+        } else {
+            r = sample_weno6(src, x, y, z, dx, inv_dx);
+        }
+        out[lin3(i, j, k, src.n0, src.n1)] = r;
+    }
+}
+
 // Grid views of the scene's grids (staggered_grid.h:100-112): comp 0 = cells, 1/2/3 = u/v/w.
 template <typename T>
 GridView<T> make_view(const void* d, int ni, int nj, int nk, T dx, int comp) {
@@ -304,6 +465,18 @@ static int launch_phi_tiled(const GridView<T>& src, void* out, const Mac<T>& mac
 }
 
 template <typename T, int TRACE>
+static int launch_phi_weno_tiled(const GridView<T>& src, void* out, const Mac<T>& mac, DtArg dt, T dx, cudaStream_t s) {
+    const int smem = (kWBoxN + 3 * kWQ) * (int)sizeof(T);
+    if (cudaFuncSetAttribute(advect_phi_weno_tiled_kernel<T, TRACE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess)
+        return -1;
+    const dim3 grid((src.n0 + kWX - 1) / kWX, (src.n1 + kWY - 1) / kWY, (src.n2 + kWZ - 1) / kWZ);
+    advect_phi_weno_tiled_kernel<T, TRACE><<<grid, dim3(kWX, kWY, 1), smem, s>>>(src, static_cast<T*>(out), mac, dt,
+                                                                                  dx, T(1) / dx);
+    return 1;
+}
+
+template <typename T, int TRACE>
 static int launch_velocity_tiled(const Mac<T>& mac, void* ou, void* ov, void* ow, DtArg dt, T dx, cudaStream_t s) {
     const int smem = 3 * kBoxN * (int)sizeof(T);
     if (cudaFuncSetAttribute(advect_velocity_tiled_kernel<T, TRACE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -324,13 +497,11 @@ static int advect_phi_tiled_t(int ni, int nj, int nk, double dx_d, void* out, co
     Mac<T> mac{make_view<T>(vu, ni, nj, nk, dx, 1), make_view<T>(vv, ni, nj, nk, dx, 2),
                make_view<T>(vw, ni, nj, nk, dx, 3)};
     GridView<T> src = make_view<T>(in, ni, nj, nk, dx, 0);
-    if (trace == EL_TRACE_RK2 && sample == EL_SAMPLE_TRILINEAR)
-        return launch_phi_tiled<T, EL_TRACE_RK2, EL_SAMPLE_TRILINEAR>(src, out, mac, dt, dx, s);
-    if (trace == EL_TRACE_RK2 && sample == EL_SAMPLE_WENO6)
-        return launch_phi_tiled<T, EL_TRACE_RK2, EL_SAMPLE_WENO6>(src, out, mac, dt, dx, s);
-    if (trace == EL_TRACE_RK3 && sample == EL_SAMPLE_TRILINEAR)
-        return launch_phi_tiled<T, EL_TRACE_RK3, EL_SAMPLE_TRILINEAR>(src, out, mac, dt, dx, s);
-    return launch_phi_tiled<T, EL_TRACE_RK3, EL_SAMPLE_WENO6>(src, out, mac, dt, dx, s);
+    if (sample == EL_SAMPLE_WENO6)
+        return trace == EL_TRACE_RK2 ? launch_phi_weno_tiled<T, EL_TRACE_RK2>(src, out, mac, dt, dx, s)
+                                     : launch_phi_weno_tiled<T, EL_TRACE_RK3>(src, out, mac, dt, dx, s);
+    if (trace == EL_TRACE_RK2) return launch_phi_tiled<T, EL_TRACE_RK2, EL_SAMPLE_TRILINEAR>(src, out, mac, dt, dx, s);
+    return launch_phi_tiled<T, EL_TRACE_RK3, EL_SAMPLE_TRILINEAR>(src, out, mac, dt, dx, s);
 }
 
 template <typename T>

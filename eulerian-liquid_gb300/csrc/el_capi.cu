@@ -409,10 +409,10 @@ static int advect_level_set_impl(el_ctx* ctx, const Scalars* dts, double dt, int
     // reads phi, u, v, w; writes phi
     ProfScope prof(ctx, EL_KC_ADVECT_PHI, 2 * nbytes(ctx, EL_FIELD_PHI) + nbytes(ctx, EL_FIELD_U) +
                                               nbytes(ctx, EL_FIELD_V) + nbytes(ctx, EL_FIELD_W));
-    // the tiled kernel (velocity staged in shared memory) for trilinear sampling, unless
-    // launch-shape tuning asked for the per-sample one; WENO6 is arithmetic-bound and measured
-    // faster one thread per sample
-    int n = (ctx->advect_tiled && sample == EL_SAMPLE_TRILINEAR) ? advect_phi_tiled(ctx->dtype, ctx->ni, ctx->nj, ctx->nk, ctx->dx, ctx->tmp[0],
+    // the tiled kernels (trilinear: the velocity staged in shared memory; WENO6: phi and the
+    // x-pass smoothness indicators staged), unless launch-shape tuning asked for the
+    // per-sample one
+    int n = ctx->advect_tiled ? advect_phi_tiled(ctx->dtype, ctx->ni, ctx->nj, ctx->nk, ctx->dx, ctx->tmp[0],
                                                  ctx->field[EL_FIELD_PHI], ctx->field[EL_FIELD_U],
                                                  ctx->field[EL_FIELD_V], ctx->field[EL_FIELD_W], dts, dt, trace,
                                                  sample, ctx->stream)

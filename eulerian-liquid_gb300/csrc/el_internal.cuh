@@ -433,13 +433,11 @@ __device__ __forceinline__ WenoAxis<T> weno_axis(T x) {
     return w;
 }
 
+// (eps + IS_s)^2 of the three candidates: data only, independent of x
 template <typename T>
-__device__ __forceinline__ T weno6_eval(const WenoAxis<T>& w, T v0, T v1, T v2, T v3, T v4, T v5) {
+__device__ __forceinline__ void weno6_sq(T v0, T v1, T v2, T v3, T v4, T v5, T& qa, T& qb, T& qc) {
     const T eps = T(1e-6);
     const T d1 = v1 - v0, d2 = v2 - v1, d3 = v3 - v2, d4 = v4 - v3, d5 = v5 - v4;
-    const T pa = w.L[0][0] * v0 + w.L[0][1] * v1 + w.L[0][2] * v2 + w.L[0][3] * v3;
-    const T pb = w.L[1][0] * v1 + w.L[1][1] * v2 + w.L[1][2] * v3 + w.L[1][3] * v4;
-    const T pc = w.L[2][0] * v2 + w.L[2][1] * v3 + w.L[2][2] * v4 + w.L[2][3] * v5;
     const T k = T(1.0 / 180.0);
     const T ia = (d1 * (T(244) * d1 - T(1171) * d2 + T(683) * d3) + d2 * (T(1561) * d2 - T(1951) * d3) +
                   T(814) * d3 * d3) * k;
@@ -448,14 +446,33 @@ __device__ __forceinline__ T weno6_eval(const WenoAxis<T>& w, T v0, T v1, T v2, 
     const T ic = (d3 * (T(814) * d3 - T(1951) * d4 + T(683) * d5) + d4 * (T(1561) * d4 - T(1171) * d5) +
                   T(244) * d5 * d5) * k;
     const T sa = eps + ia, sb = eps + ib, sc = eps + ic;
+    qa = sa * sa;
+    qb = sb * sb;
+    qc = sc * sc;
+}
+
+// the candidates at x and their nonlinear combination, given weno6_sq of the same values
+template <typename T>
+__device__ __forceinline__ T weno6_combine(const WenoAxis<T>& w, T v0, T v1, T v2, T v3, T v4, T v5, T qa, T qb,
+                                           T qc) {
+    const T pa = w.L[0][0] * v0 + w.L[0][1] * v1 + w.L[0][2] * v2 + w.L[0][3] * v3;
+    const T pb = w.L[1][0] * v1 + w.L[1][1] * v2 + w.L[1][2] * v3 + w.L[1][3] * v4;
+    const T pc = w.L[2][0] * v2 + w.L[2][1] * v3 + w.L[2][2] * v4 + w.L[2][3] * v5;
     if constexpr (sizeof(T) == 8) {
-        const T aa = w.C[0] / (sa * sa), ab = w.C[1] / (sb * sb), ac = w.C[2] / (sc * sc);
+        const T aa = w.C[0] / qa, ab = w.C[1] / qb, ac = w.C[2] / qc;
         return (aa * pa + ab * pb + ac * pc) / (aa + ab + ac);
     } else {
         // FP32: fast divisions (within 2 ulp)
-        const T aa = __fdividef(w.C[0], sa * sa), ab = __fdividef(w.C[1], sb * sb), ac = __fdividef(w.C[2], sc * sc);
+        const T aa = __fdividef(w.C[0], qa), ab = __fdividef(w.C[1], qb), ac = __fdividef(w.C[2], qc);
         return __fdividef(aa * pa + ab * pb + ac * pc, aa + ab + ac);
     }
+}
+
+template <typename T>
+__device__ __forceinline__ T weno6_eval(const WenoAxis<T>& w, T v0, T v1, T v2, T v3, T v4, T v5) {
+    T qa, qb, qc;
+    weno6_sq(v0, v1, v2, v3, v4, v5, qa, qb, qc);
+    return weno6_combine(w, v0, v1, v2, v3, v4, v5, qa, qb, qc);
 }
 
 // weno6_interp(x, grid) in 3-D: 6^3 clamped gather at offsets -2..3; x-passes, then y, then z
