@@ -168,6 +168,9 @@ struct el_ctx {
     std::vector<cudaEvent_t> ev_pool;
     size_t ev_used = 0;
     std::vector<ProfRec> prof;
+    // while profiling: cells covered by the active segments of each multigrid level of the
+    // current solve (read back once per solve), for the byte counts of the segment kernels
+    std::vector<double> prof_active;
 };
 
 namespace el {

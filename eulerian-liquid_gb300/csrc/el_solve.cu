@@ -633,6 +633,17 @@ __global__ void __launch_bounds__(kSegThreads) residual_kernel(LGeom g, SegArg s
 // MODE 1: one sweep from x_in + P e (e = coarse correction, formed on the fly)
 // MODE 2: one sweep from x_in.   DOT (finest level, last sweep): rz = b . x_out and beta.
 enum { SM_ZERO2 = 0, SM_PROLONG = 1, SM_PLAIN = 2 };
+
+// a / b inside the multigrid preconditioner: FP32 takes the fast division (within 2 ulp; the
+// preconditioner only has to be a fixed symmetric operator, not correctly rounded), FP64 the
+// exact one
+template <typename V>
+__device__ __forceinline__ V mg_div(V a, V b) {
+    if constexpr (sizeof(V) == 4)
+        return __fdividef(a, b);
+    else
+        return a / b;
+}
 enum { DOT_NONE = 0, DOT_INIT = 1, DOT_BETA = 2 };
 
 template <typename V, typename R, int MODE, int DOT>
@@ -654,14 +665,14 @@ __global__ void __launch_bounds__(kSegThreads) smooth_kernel(LGeom g, SegArg seg
     };
     auto valf = [&](V raw, const Co<V>& rec) -> V {
         if (!(rec.d > V(0))) return V(0);
-        return MODE == SM_ZERO2 ? omega * raw / rec.d : raw;
+        return MODE == SM_ZERO2 ? mg_div(omega * raw, rec.d) : raw;
     };
     SEG_LOOP_ALL_BEGIN(seg, g)
     const St7<V> st = gather7<V, true>(g, c, i, j, k, live, lane, recf, rawf, valf);
     if (live) {
         const V bc = b[c];
         V xo = V(0);
-        if (st.d > V(0)) xo = st.v0 + omega * (bc - apply7(st)) / st.d;
+        if (st.d > V(0)) xo = st.v0 + mg_div(omega * (bc - apply7(st)), st.d);
         x_out[c] = xo;
         if (DOT != DOT_NONE) acc[0] += (double)bc * (double)xo;
     }
@@ -679,9 +690,10 @@ __global__ void __launch_bounds__(kSegThreads) smooth_kernel(LGeom g, SegArg seg
     }
 }
 
-// Residual of the fine level summed onto the coarse right-hand side (R = P^T), one warp per
-// active coarse segment: the warp walks the 64 x 2 x 2 fine cells under it one fine row
-// segment at a time (one fine cell per lane, coalesced), the i-pairs are summed by shuffle.
+// Residual of a level summed onto the coarse right-hand side (R = P^T), one warp per active
+// coarse segment: the warp walks the 64 x 2 x 2 fine cells under it one fine row segment at a
+// time (one fine cell per lane, coalesced), the i-pairs are summed by shuffle.  Used from the
+// finest level, where the grid of warps is capped well below the number of coarse segments.
 template <typename V, typename R>
 __global__ void __launch_bounds__(kSegThreads, 4) restrict_kernel(LGeom g, const R* __restrict__ A, const V* __restrict__ b,
                                                                const V* __restrict__ x, LGeom gc, SegArg cseg,
@@ -723,6 +735,65 @@ __global__ void __launch_bounds__(kSegThreads, 4) restrict_kernel(LGeom g, const
     }
 }
 
+// The same below the finest level, where the coarse segments are few: a quad of four
+// warps takes one active coarse segment: warp (kk, jj) of the quad walks the fine row
+// (2J + jj, 2K + kk) under it, 64 fine cells as two 32-cell halves (one fine cell per lane,
+// coalesced), and sums the i-pairs by shuffle; the quad then adds its four rows in a fixed order
+// through shared memory (deterministic).  Four rows in flight per coarse segment instead of
+// eight gathers in sequence: the kernel is bound by the latency of the gathers.
+constexpr int kQuadsPerBlock = kSegThreads / 128;
+
+template <typename V, typename R>
+__global__ void __launch_bounds__(kSegThreads, 4) restrict_quad_kernel(LGeom g, const R* __restrict__ A,
+                                                                    const V* __restrict__ b, const V* __restrict__ x,
+                                                                    LGeom gc, SegArg cseg, V* __restrict__ bc,
+                                                                    const Scalars* s) {
+    if (s->done) return;
+    __shared__ V part[kQuadsPerBlock][4][2][16];
+    const RecLoad<V, R> recf{A};
+    auto rawf = [&](int q, int, int, int) -> V { return x[q]; };
+    auto valf = [](V raw, const Co<V>&) -> V { return raw; };
+    const int lane = threadIdx.x & 31;
+    const int wb = threadIdx.x >> 5;                  // warp in the block
+    const int quad_b = wb >> 2, sub = wb & 3;         // quad in the block, row of the quad
+    const int kk = sub >> 1, jj = sub & 1;
+    const int quad = blockIdx.x * kQuadsPerBlock + quad_b;
+    const int nquads = gridDim.x * kQuadsPerBlock;
+    const int nseg = *cseg.count;
+    for (int qs = quad; qs < nseg; qs += nquads) {
+        const int4 sd = cseg.desc[qs];
+        const int I0 = sd.y, J = sd.z, K = sd.w;
+        const int j = 2 * J + jj, k = 2 * K + kk;
+        V sum[2] = {V(0), V(0)};  // fine i in [2*I0, 2*I0+32) and [2*I0+32, 2*I0+64)
+        // warp-uniform: the row exists for all lanes or for none
+        if (j < g.n1 && k < g.n2) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int i = 2 * I0 + 32 * h + lane;
+                const bool live = i < g.n0;
+                const int c = i + g.s1 * j + g.s2 * k;
+                const St7<V> st = gather7<V, false>(g, c, i, j, k, live, lane, recf, rawf, valf);
+                if (live && st.d > V(0)) sum[h] = b[c] - apply7(st);
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const V pair = sum[h] + __shfl_down_sync(kFull, sum[h], 1);
+            if ((lane & 1) == 0) part[quad_b][sub][h][lane >> 1] = pair;
+        }
+        // the quad's four warps meet on their own named barrier (1 + quad in the block)
+        asm volatile("bar.sync %0, %1;" ::"r"(1 + quad_b), "r"(128) : "memory");
+        if (sub == 0) {
+            const int h = lane >> 4, q = lane & 15;
+            const V tot = ((part[quad_b][0][h][q] + part[quad_b][1][h][q]) + part[quad_b][2][h][q]) +
+                          part[quad_b][3][h][q];
+            const int I = I0 + 16 * h + q;
+            if (I < gc.n0) bc[I + gc.s1 * J + gc.s2 * K] = tot;
+        }
+        asm volatile("bar.sync %0, %1;" ::"r"(1 + quad_b), "r"(128) : "memory");
+    }
+}
+
 
 // Coarsest level: omega-Jacobi sweeps from zero in one block's shared memory.
 template <typename V, typename R>
@@ -742,7 +813,7 @@ __global__ void __launch_bounds__(kCoarsestMaxCells) coarsest_kernel(LGeom g, co
         sy[c] = (V)r.y;
         sz[c] = (V)r.z;
         sb[c] = b[c];
-        xa[c] = sd[c] > V(0) ? omega * sb[c] / sd[c] : V(0);
+        xa[c] = sd[c] > V(0) ? mg_div(omega * sb[c], sd[c]) : V(0);
     }
     __syncthreads();
     const int i = c % g.n0, j = (c / g.n0) % g.n1, k = c / (g.n0 * g.n1);
@@ -761,7 +832,7 @@ __global__ void __launch_bounds__(kCoarsestMaxCells) coarsest_kernel(LGeom g, co
                 if (j < g.n1 - 1) a += sy[c] * cur[c + s1];
                 if (k > 0) a += sz[c - s2] * cur[c - s2];
                 if (k < g.n2 - 1) a += sz[c] * cur[c + s2];
-                xo = cur[c] + omega * (sb[c] - a) / d;
+                xo = cur[c] + mg_div(omega * (sb[c] - a), d);
             }
             nxt[c] = xo;
         }
@@ -783,6 +854,34 @@ static int seg_blocks(el_ctx* ctx, long long total_segments) {
 }
 
 static SegArg seg_arg(const SegList& l) { return SegArg{l.desc, l.count}; }
+
+// Cells a segment kernel of multigrid level `level` visits (for the byte counts of profiled
+// launches): the active segments' cells, as read back by record_active(), else `full`.
+static double active_cells(const el_ctx* ctx, int level, double full) {
+    if (level >= 0 && level < (int)ctx->prof_active.size() && ctx->prof_active[level] >= 0)
+        return ctx->prof_active[level];
+    return full;
+}
+
+// While profiling, reads back the active segment counts of the finest level (seg0) and of the
+// coarse levels (one synchronisation per solve; not used outside profiling).
+template <typename V>
+static int record_active(el_ctx* ctx, const SegList& seg0, int n0, const std::vector<MGLevel<V>>* mg) {
+    ctx->prof_active.clear();
+    if (!ctx->prof_mask) return EL_OK;
+    const size_t levels = mg ? mg->size() : 1;
+    std::vector<int> counts(levels, 0);
+    for (size_t l = 0; l < levels; ++l) {
+        const int* c = l == 0 ? seg0.count : (*mg)[l].seg.count;
+        EL_CUDA_TRY(ctx, cudaMemcpyAsync(&counts[l], c, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    EL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    for (size_t l = 0; l < levels; ++l) {
+        const int w = l == 0 ? n0 : (*mg)[l].n0;
+        ctx->prof_active.push_back((double)counts[l] * std::min(32, w));
+    }
+    return EL_OK;
+}
 
 static int alloc_seglist(el_ctx* ctx, SegList& l, int n0, int n1, int n2) {
     l.nsr = (n0 + 31) / 32;
@@ -885,6 +984,7 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
     const int L = (int)mg.size();
     auto segof = [&](int l) -> const SegList& { return l == 0 ? seg0 : mg[l].seg; };
     auto cells = [](const MGLevel<V>& X) { return (double)X.n0 * X.n1 * X.n2; };
+    auto act = [&](int l, const MGLevel<V>& X) { return active_cells(ctx, l, cells(X)); };
     const double vs = sizeof(V);
     if (L == 1) {
         // too small to coarsen: the coarsest sweeps solve it, one more sweep gives the dot
@@ -903,7 +1003,7 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
         const double rb = l == 0 ? sizeof(R0) : sizeof(RC);
         {
             // reads b and records; writes x
-            ProfScope prof(ctx, l == 0 ? EL_KC_SMOOTH : EL_KC_MG_COARSE, cells(F) * (2 * vs + rb));
+            ProfScope prof(ctx, l == 0 ? EL_KC_SMOOTH : EL_KC_MG_COARSE, act(l, F) * (2 * vs + rb));
             if (l == 0)
                 launch_smooth<V, R0, SM_ZERO2, DOT_NONE>(ctx, F, segof(l), nullptr, nullptr, F.x, s);
             else
@@ -911,13 +1011,13 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
         }
         {
             // reads b, x and records; writes the coarse b
-            ProfScope prof(ctx, l == 0 ? EL_KC_RESTRICT : EL_KC_MG_COARSE, cells(F) * (2 * vs + rb) + cells(C) * vs);
+            ProfScope prof(ctx, l == 0 ? EL_KC_RESTRICT : EL_KC_MG_COARSE, act(l, F) * (2 * vs + rb) + act(l + 1, C) * vs);
             const LGeom gf = make_geom(F.n0, F.n1, F.n2), gc = make_geom(C.n0, C.n1, C.n2);
             if (l == 0)
                 restrict_kernel<V, R0><<<seg_blocks(ctx, C.seg.total), kSegThreads, 0, ctx->stream>>>(
                     gf, (const R0*)F.rec, F.b, F.x, gc, seg_arg(C.seg), C.b, s);
             else
-                restrict_kernel<V, RC><<<seg_blocks(ctx, C.seg.total), kSegThreads, 0, ctx->stream>>>(
+                restrict_quad_kernel<V, RC><<<seg_blocks(ctx, 4 * C.seg.total), kSegThreads, 0, ctx->stream>>>(
                     gf, (const RC*)F.rec, F.b, F.x, gc, seg_arg(C.seg), C.b, s);
         }
         launched += 2;
@@ -935,7 +1035,7 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
         const double rb = l == 0 ? sizeof(R0) : sizeof(RC);
         // prolongation sweep: b, x, records, coarse x read, t written; last sweep: b, t,
         // records read, x written
-        ProfScope prof(ctx, l == 0 ? EL_KC_SMOOTH : EL_KC_MG_COARSE, cells(F) * (6 * vs + 2 * rb) + cells(C) * vs);
+        ProfScope prof(ctx, l == 0 ? EL_KC_SMOOTH : EL_KC_MG_COARSE, act(l, F) * (6 * vs + 2 * rb) + act(l + 1, C) * vs);
         if (l == 0) {
             launch_smooth<V, R0, SM_PROLONG, DOT_NONE>(ctx, F, segof(l), F.x, &C, F.t, s);
             if (dot == DOT_INIT)
@@ -964,7 +1064,7 @@ static int enqueue_mg_iteration(el_ctx* ctx, const RA* A, V* x, V* r, V* z, V*& 
                                 int first, std::vector<MGLevel<V>>& mg) {
     const LGeom g = make_geom(ctx->ni, ctx->nj, ctx->nk);
     const SegList& seg = ctx->seg0;
-    const double N = (double)ctx->ni * ctx->nj * ctx->nk, vs = sizeof(V);
+    const double N = active_cells(ctx, 0, (double)ctx->ni * ctx->nj * ctx->nk), vs = sizeof(V);
     {
         // reads z, p (not on the first iteration), records; writes p, Ap
         ProfScope prof(ctx, EL_KC_DIR_SPMV, N * (vs * (first ? 3 : 4) + sizeof(RA)));
@@ -986,7 +1086,7 @@ static int enqueue_jacobi_iteration(el_ctx* ctx, const SplitOp<OT>& A, double*& 
                                     int first) {
     const LGeom g = make_geom(ctx->ni, ctx->nj, ctx->nk);
     const SegList& seg = ctx->seg0;
-    const double N = (double)ctx->ni * ctx->nj * ctx->nk;
+    const double N = active_cells(ctx, 0, (double)ctx->ni * ctx->nj * ctx->nk);
     {
         // reads r, p (not on the first iteration), diag, 3 couplings; writes p, Ap
         ProfScope prof(ctx, EL_KC_DIR_SPMV, N * (8.0 * (first ? 4 : 5) + 3 * sizeof(OT)));
@@ -1099,14 +1199,17 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
             g, ctx->diag64, ctx->seg0.total, ctx->seg0.flags);
     }
     ctx->launches += 1 + enqueue_compact(ctx, ctx->seg0, g);
+    int rc = record_active<double>(ctx, ctx->seg0, ctx->ni, nullptr);
+    if (rc != EL_OK) return rc;
+    const double na = active_cells(ctx, 0, (double)n);
     {
-        ProfScope prof(ctx, EL_KC_OTHER, (double)n * 24);
+        ProfScope prof(ctx, EL_KC_OTHER, na * 24);
         solve_init_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
             g, seg_arg(ctx->seg0), ctx->rhs64, ctx->x64, ctx->r64, s0, prm.tol);
     }
     ctx->launches += 1;
     if (prm.initial_guess) {
-        ProfScope prof(ctx, EL_KC_OTHER, (double)n * 56);
+        ProfScope prof(ctx, EL_KC_OTHER, na * 56);
         const int nb = seg_blocks(ctx, ctx->seg0.total);
         guess_load_kernel<T><<<nb, kSegThreads, 0, ctx->stream>>>(g, seg_arg(ctx->seg0),
                                                                   (const T*)ctx->field[EL_FIELD_PRESSURE], ctx->diag64,
@@ -1119,7 +1222,6 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
                                                                 s0, ctx->partials, ctx->counter);
         ctx->launches += 4;
     }
-    int rc = EL_OK;
     st->outer_iterations = 1;
     if (prm.solver == EL_SOLVER_JACOBI_FP64) {
         jacobi_rz_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
@@ -1138,6 +1240,8 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
         mg[0].x = ctx->z64;
         pack64_kernel<T><<<grid1d(ctx, n), 256, 0, ctx->stream>>>(n, ctx->diag64, A64.x, A64.y, A64.z, ctx->A64rec);
         ctx->launches += 1 + enqueue_coarsen<double, Rec64, Rec64>(ctx, mg);
+        rc = record_active(ctx, ctx->seg0, ctx->ni, &mg);
+        if (rc != EL_OK) return rc;
         ctx->launches += enqueue_vcycle<double, Rec64, Rec64>(ctx, mg, ctx->seg0, s0, DOT_INIT);
         double* p = ctx->p64;
         double* p_alt = ctx->p64b;
@@ -1159,6 +1263,8 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
                                                                       ctx->A16);
         }
         ctx->launches += 1 + enqueue_coarsen<float, ushort4, float4>(ctx, mg);
+        rc = record_active(ctx, ctx->seg0, ctx->ni, &mg);
+        if (rc != EL_OK) return rc;
         Scalars* s1 = ctx->dscal + 1;
         Scalars hi;
         rc = poll(ctx, h, 0);
@@ -1167,7 +1273,7 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
         float* p_alt = ctx->p32b;
         while (rc == EL_OK && !h->done && outer < std::max(1, prm.max_outer) && inner_total < prm.max_iter) {
             {
-                ProfScope prof(ctx, EL_KC_OTHER, (double)n * 16);
+                ProfScope prof(ctx, EL_KC_OTHER, na * 16);
                 inner_init_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
                     g, seg_arg(ctx->seg0), ctx->r64, ctx->r32, ctx->x32, s0, s1, prm.tol, prm.inner_floor,
                     ctx->partials, ctx->counter);
@@ -1185,13 +1291,13 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
                 break;
             }
             {
-                ProfScope prof(ctx, EL_KC_OTHER, (double)n * 20);
+                ProfScope prof(ctx, EL_KC_OTHER, na * 20);
                 accumulate_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
                     g, seg_arg(ctx->seg0), ctx->x64, ctx->x32, s1);
             }
             {
                 // reads x, b, diag (f64), 3 couplings; writes r (f64)
-                ProfScope prof(ctx, EL_KC_RESIDUAL, (double)n * (32 + 3 * sizeof(T)));
+                ProfScope prof(ctx, EL_KC_RESIDUAL, na * (32 + 3 * sizeof(T)));
                 residual_kernel<T><<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
                     g, seg_arg(ctx->seg0), A64, ctx->rhs64, ctx->x64, ctx->r64, s0, ctx->partials, ctx->counter);
             }
