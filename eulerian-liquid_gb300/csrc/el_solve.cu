@@ -695,7 +695,7 @@ __global__ void __launch_bounds__(kSegThreads) smooth_kernel(LGeom g, SegArg seg
 // time (one fine cell per lane, coalesced), the i-pairs are summed by shuffle.  Used from the
 // finest level, where the grid of warps is capped well below the number of coarse segments.
 template <typename V, typename R>
-__global__ void __launch_bounds__(kSegThreads, 4) restrict_kernel(LGeom g, const R* __restrict__ A, const V* __restrict__ b,
+__global__ void __launch_bounds__(kSegThreads, sizeof(V) == 4 ? 5 : 4) restrict_kernel(LGeom g, const R* __restrict__ A, const V* __restrict__ b,
                                                                const V* __restrict__ x, LGeom gc, SegArg cseg,
                                                                V* __restrict__ bc, const Scalars* s) {
     if (s->done) return;
@@ -854,6 +854,15 @@ static int seg_blocks(el_ctx* ctx, long long total_segments) {
 }
 
 static SegArg seg_arg(const SegList& l) { return SegArg{l.desc, l.count}; }
+
+// The finest level's restriction is bound by the latency of its gathers: as many warps as can
+// be resident (five CTAs of 256 threads per SM at its FP32 register budget), so that each walks a
+// short chain of coarse segments.
+static int restrict_blocks(el_ctx* ctx, long long total_segments) {
+    const long long warps = (long long)ctx->num_sms * 5 * (kSegThreads / 32);
+    const long long need = std::max<long long>(1, std::min<long long>(total_segments, warps));
+    return (int)((need * 32 + kSegThreads - 1) / kSegThreads);
+}
 
 // Cells a segment kernel of multigrid level `level` visits (for the byte counts of profiled
 // launches): the active segments' cells, as read back by record_active(), else `full`.
@@ -1014,7 +1023,7 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
             ProfScope prof(ctx, l == 0 ? EL_KC_RESTRICT : EL_KC_MG_COARSE, act(l, F) * (2 * vs + rb) + act(l + 1, C) * vs);
             const LGeom gf = make_geom(F.n0, F.n1, F.n2), gc = make_geom(C.n0, C.n1, C.n2);
             if (l == 0)
-                restrict_kernel<V, R0><<<seg_blocks(ctx, C.seg.total), kSegThreads, 0, ctx->stream>>>(
+                restrict_kernel<V, R0><<<restrict_blocks(ctx, C.seg.total), kSegThreads, 0, ctx->stream>>>(
                     gf, (const R0*)F.rec, F.b, F.x, gc, seg_arg(C.seg), C.b, s);
             else
                 restrict_quad_kernel<V, RC><<<seg_blocks(ctx, 4 * C.seg.total), kSegThreads, 0, ctx->stream>>>(
