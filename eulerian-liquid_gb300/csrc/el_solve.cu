@@ -39,7 +39,7 @@
 
 namespace el {
 
-constexpr double kOmega = 0.8;
+constexpr double kOmega = 6.0 / 7.0;  // the damping that balances the smoothing of the 3-D 7-point Laplacian
 constexpr int kCoarsestSweeps = 30;
 constexpr int kCoarsestMaxDim = 8;
 constexpr int kCoarsestMaxCells = 512;
