@@ -4,6 +4,8 @@
 // src/project/3d/eulerian_liquid/simulator.cpp:90-178 (add_gravity, find_valid_velocity,
 // set_invalid_velocity_zero), src/project/3d/fluid/time_stepping.cpp:5-7 (calc_time_step),
 // src/project/3d/fluid/levelset_emitter.cpp:10-79 (emitters).
+#include <type_traits>
+
 #include "el_internal.cuh"
 
 namespace el {
@@ -234,14 +236,39 @@ __device__ __forceinline__ void atomic_max_abs(unsigned long long* m, double v) 
     atomicMax(m, (unsigned long long)__double_as_longlong(fabs(v)));
 }
 
+// max |a| over one array, in the field type (a maximum of magnitudes is exact in any type, and
+// fmax ignores NaN in both), 16-byte loads for the bulk
 template <typename T>
-__global__ void maxabs_kernel(long long n, const T* __restrict__ a, unsigned long long* out) {
-    double m = 0.0;
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
-        m = fmax(m, fabs((double)a[c]));
+__device__ __forceinline__ T maxabs_run(const T* __restrict__ a, long long n, long long t0, long long stride, T m) {
+    using V2 = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+    constexpr int per = (int)(sizeof(V2) / sizeof(T));
+    const long long nv = n / per;
+    const V2* av = reinterpret_cast<const V2*>(a);
+    for (long long c = t0; c < nv; c += stride) {
+        const V2 x = __ldg(av + c);
+        if constexpr (sizeof(T) == 4)
+            m = fmaxf(fmaxf(fmaxf(m, fabsf(x.x)), fmaxf(fabsf(x.y), fabsf(x.z))), fabsf(x.w));
+        else
+            m = fmax(m, fmax(fabs(x.x), fabs(x.y)));
+    }
+    for (long long c = nv * per + t0; c < n; c += stride) m = (T)fmax(m, fabs(a[c]));
+    return m;
+}
+
+// max(|u|, |v|, |w|) over the three face grids, one launch (the fields are 256-byte aligned)
+template <typename T>
+__global__ void maxabs3_kernel(const T* __restrict__ u, long long nu, const T* __restrict__ v, long long nv,
+                               const T* __restrict__ w, long long nw, unsigned long long* out) {
+    const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    T m = T(0);
+    m = maxabs_run(u, nu, t0, stride, m);
+    m = maxabs_run(v, nv, t0, stride, m);
+    m = maxabs_run(w, nw, t0, stride, m);
+    double md = (double)m;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) atomic_max_abs(out, m);
+    for (int o = 16; o > 0; o >>= 1) md = fmax(md, __shfl_down_sync(0xffffffffu, md, o));
+    if ((threadIdx.x & 31) == 0) atomic_max_abs(out, md);
 }
 
 // dt = cfl * dx / max(max|u|, 1e-4) in the field type (time_stepping.cpp:5-7)
@@ -439,42 +466,45 @@ int launch_zero_invalid(el_ctx* ctx) {
 }
 
 // Computes dt into ctx->dscal[0].dt on the device.
-int launch_time_step(el_ctx* ctx, double cfl, unsigned long long* scratch_max) {
+// max |u|, |v|, |w| into scratch_max (as the bits of a non-negative double)
+static void launch_maxabs(el_ctx* ctx, unsigned long long* scratch_max) {
     cudaMemsetAsync(scratch_max, 0, sizeof(unsigned long long), ctx->stream);
+    long long n[3];
     for (int comp = 0; comp < 3; ++comp) {
         int n0, n1, n2;
         field_dims(ctx, EL_FIELD_U + comp, n0, n1, n2);
-        const long long n = (long long)n0 * n1 * n2;
-        if (ctx->dtype == EL_F64)
-            maxabs_kernel<double><<<g1(ctx, n), 256, 0, ctx->stream>>>(n, (const double*)ctx->field[EL_FIELD_U + comp], scratch_max);
-        else
-            maxabs_kernel<float><<<g1(ctx, n), 256, 0, ctx->stream>>>(n, (const float*)ctx->field[EL_FIELD_U + comp], scratch_max);
+        n[comp] = (long long)n0 * n1 * n2;
     }
+    const int per = ctx->dtype == EL_F64 ? 2 : 4;
+    const int grid = g1(ctx, n[0] / per);
+    if (ctx->dtype == EL_F64)
+        maxabs3_kernel<double><<<grid, 256, 0, ctx->stream>>>(
+            (const double*)ctx->field[EL_FIELD_U], n[0], (const double*)ctx->field[EL_FIELD_V], n[1],
+            (const double*)ctx->field[EL_FIELD_W], n[2], scratch_max);
+    else
+        maxabs3_kernel<float><<<grid, 256, 0, ctx->stream>>>(
+            (const float*)ctx->field[EL_FIELD_U], n[0], (const float*)ctx->field[EL_FIELD_V], n[1],
+            (const float*)ctx->field[EL_FIELD_W], n[2], scratch_max);
+}
+
+int launch_time_step(el_ctx* ctx, double cfl, unsigned long long* scratch_max) {
+    launch_maxabs(ctx, scratch_max);
     if (ctx->dtype == EL_F64)
         time_step_kernel<double><<<1, 1, 0, ctx->stream>>>(scratch_max, cfl, ctx->dx, ctx->dscal);
     else
         time_step_kernel<float><<<1, 1, 0, ctx->stream>>>(scratch_max, (float)cfl, (float)ctx->dx, ctx->dscal);
-    return 4;
+    return 2;
 }
 
 // dt of a batch sub-step into ctx->dscal[0].dt on the device (no host involvement).
 int launch_substep(el_ctx* ctx, double cfl, double dt_frame, const BatchRecord* rec, unsigned long long* scratch_max) {
-    cudaMemsetAsync(scratch_max, 0, sizeof(unsigned long long), ctx->stream);
-    for (int comp = 0; comp < 3; ++comp) {
-        int n0, n1, n2;
-        field_dims(ctx, EL_FIELD_U + comp, n0, n1, n2);
-        const long long n = (long long)n0 * n1 * n2;
-        if (ctx->dtype == EL_F64)
-            maxabs_kernel<double><<<g1(ctx, n), 256, 0, ctx->stream>>>(n, (const double*)ctx->field[EL_FIELD_U + comp], scratch_max);
-        else
-            maxabs_kernel<float><<<g1(ctx, n), 256, 0, ctx->stream>>>(n, (const float*)ctx->field[EL_FIELD_U + comp], scratch_max);
-    }
+    launch_maxabs(ctx, scratch_max);
     if (ctx->dtype == EL_F64)
         substep_kernel<double><<<1, 1, 0, ctx->stream>>>(scratch_max, cfl, ctx->dx, dt_frame, rec, ctx->dscal);
     else
         substep_kernel<float><<<1, 1, 0, ctx->stream>>>(scratch_max, (float)cfl, (float)ctx->dx, (float)dt_frame, rec,
                                                         ctx->dscal);
-    return 4;
+    return 2;
 }
 
 int launch_set_dt(el_ctx* ctx, double dt) {
