@@ -314,10 +314,10 @@ __global__ void __launch_bounds__(kTileX * kTileY) advect_phi_tiled_kernel(GridV
 // of it, so the 6^3 stencils of a 32 x 8 x 4 tile of cells read phi within [tile - 3, tile + 4]:
 // the CTA stages that clamped box (39 x 15 x 11) once.  The smoothness indicators of an x-pass
 // depend only on the six values it reads, not on the sample's fraction, so they are formed once
-// per (row, floor index) of the box -- (eps + IS_s)^2 for the 34 floor indices of each of the
-// 165 rows -- and shared by every sample whose stencil uses that row segment, instead of being
-// recomputed by all 36 x-passes of every sample.  The y- and z-passes combine per-sample values
-// and are evaluated in full.  The backtrace reads the velocity from global memory (L1-served).
+// per (row, floor index) of the box -- (eps + IS_s)^2, in FP32 its reciprocal, for the 34 floor
+// indices of each of the 165 rows -- and shared by every sample whose stencil uses that row
+// segment, instead of being recomputed by all 36 x-passes of every sample.  The y- and z-passes
+// combine per-sample values and are evaluated in full.  The backtrace reads the velocity from global memory (L1-served).
 // A foot point outside the box (a larger dt) takes the global sample_weno6 path, with the same
 // arithmetic.
 constexpr int kWX = 32, kWY = 8, kWZ = 4;

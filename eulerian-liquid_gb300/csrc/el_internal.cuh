@@ -436,7 +436,9 @@ __device__ __forceinline__ WenoAxis<T> weno_axis(T x) {
     return w;
 }
 
-// (eps + IS_s)^2 of the three candidates: data only, independent of x
+// The data-only part of the nonlinear weights, independent of x: (eps + IS_s)^2 of the three
+// candidates (FP64), or its reciprocal (FP32, fast reciprocal: the weights are then one
+// multiplication each, alpha_s = C_s * q_s)
 template <typename T>
 __device__ __forceinline__ void weno6_sq(T v0, T v1, T v2, T v3, T v4, T v5, T& qa, T& qb, T& qc) {
     const T eps = T(1e-6);
@@ -449,9 +451,15 @@ __device__ __forceinline__ void weno6_sq(T v0, T v1, T v2, T v3, T v4, T v5, T& 
     const T ic = (d3 * (T(814) * d3 - T(1951) * d4 + T(683) * d5) + d4 * (T(1561) * d4 - T(1171) * d5) +
                   T(244) * d5 * d5) * k;
     const T sa = eps + ia, sb = eps + ib, sc = eps + ic;
-    qa = sa * sa;
-    qb = sb * sb;
-    qc = sc * sc;
+    if constexpr (sizeof(T) == 8) {
+        qa = sa * sa;
+        qb = sb * sb;
+        qc = sc * sc;
+    } else {
+        qa = __fdividef(1.f, sa * sa);
+        qb = __fdividef(1.f, sb * sb);
+        qc = __fdividef(1.f, sc * sc);
+    }
 }
 
 // the candidates at x and their nonlinear combination, given weno6_sq of the same values
@@ -465,8 +473,8 @@ __device__ __forceinline__ T weno6_combine(const WenoAxis<T>& w, T v0, T v1, T v
         const T aa = w.C[0] / qa, ab = w.C[1] / qb, ac = w.C[2] / qc;
         return (aa * pa + ab * pb + ac * pc) / (aa + ab + ac);
     } else {
-        // FP32: fast divisions (within 2 ulp)
-        const T aa = __fdividef(w.C[0], qa), ab = __fdividef(w.C[1], qb), ac = __fdividef(w.C[2], qc);
+        // FP32: qa, qb, qc hold the reciprocals; fast division for the normalisation (within 2 ulp)
+        const T aa = w.C[0] * qa, ab = w.C[1] * qb, ac = w.C[2] * qc;
         return __fdividef(aa * pa + ab * pb + ac * pc, aa + ab + ac);
     }
 }
