@@ -35,6 +35,8 @@
 // entry, so the host polls only every `check_every` iterations.
 #include <cuda_fp16.h>
 
+#include <type_traits>
+
 #include "el_internal.cuh"
 
 namespace el {
@@ -117,8 +119,23 @@ struct SegArg {
         const int c = sd.x + lane;                                                \
         const bool live = i < (g).n0;
 
+// the same, with the next segment's descriptor loaded while the current one is processed (for
+// the kernels whose registers leave room for it)
+#define SEG_LOOP_ALL_PF_BEGIN(seg, g)                                             \
+    const int lane = threadIdx.x & 31;                                            \
+    const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;         \
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;                             \
+    const int nseg = *(seg).count;                                                \
+    int4 sd_next = warp_global < nseg ? (seg).desc[warp_global] : make_int4(0, 0, 0, 0); \
+    for (int qs = warp_global; qs < nseg; qs += nwarps) {                         \
+        const int4 sd = sd_next;                                                  \
+        if (qs + nwarps < nseg) sd_next = (seg).desc[qs + nwarps];                \
+        const int i = sd.y + lane, j = sd.z, k = sd.w;                            \
+        const int c = sd.x + lane;                                                \
+        const bool live = i < (g).n0;
+
 #define SEG_LOOP_BEGIN(seg, g) \
-    SEG_LOOP_ALL_BEGIN(seg, g) \
+    SEG_LOOP_ALL_PF_BEGIN(seg, g) \
     if (!live) continue;
 
 #define SEG_LOOP_END }
@@ -285,6 +302,12 @@ __global__ void coarsen_kernel(LGeom F, const RF* __restrict__ fr, LGeom C, RC* 
 // formed, so a lane waits for memory once; the i-neighbours of the other lanes come by shuffle.
 // ALL: every neighbour's record is needed (for its diagonal); else only those carrying a
 // coupling (-x, -y, -z) are loaded.  Must be called by all 32 lanes.
+// Per-thread partial sums of a dot product: FP32 for the FP32 solver (a thread sums a few
+// dozen products; FP64 arithmetic runs at a small fraction of the FP32 rate on this GPU), FP64
+// otherwise; the grid reduction is FP64 either way.
+template <typename V>
+using DotAcc = typename std::conditional<sizeof(V) == 4, float, double>::type;
+
 template <typename V>
 struct St7 {
     V v0, vxm, vxp, vym, vyp, vzm, vzp;  // values at the centre and the six neighbours
@@ -370,11 +393,11 @@ __global__ void __launch_bounds__(kSegThreads) dir_spmv_rec_kernel(LGeom g, SegA
                                                                    unsigned* counter) {
     if (s->done) return;
     const V beta = first ? V(0) : (V)s->beta;
-    double acc[1] = {0.0};
+    DotAcc<V> part = 0;
     const RecLoad<V, R> recf{A};
     auto rawf = [&](int q, int, int, int) -> V { return first ? z[q] : z[q] + beta * p_in[q]; };
     auto valf = [](V raw, const Co<V>&) -> V { return raw; };
-    SEG_LOOP_ALL_BEGIN(seg, g)
+    SEG_LOOP_ALL_PF_BEGIN(seg, g)
     const St7<V> st = gather7<V, false>(g, c, i, j, k, live, lane, recf, rawf, valf);
     if (live) {
         V pc = V(0), apc = V(0);
@@ -384,9 +407,10 @@ __global__ void __launch_bounds__(kSegThreads) dir_spmv_rec_kernel(LGeom g, SegA
         }
         p_out[c] = pc;
         ap[c] = apc;
-        acc[0] += (double)pc * (double)apc;
+        part += (DotAcc<V>)pc * (DotAcc<V>)apc;
     }
     SEG_LOOP_END
+    double acc[1] = {(double)part};
     double tot[1];
     if (grid_sum<1>(acc, partials, counter, tot)) {
         const double alpha = s->rz / tot[0];
@@ -444,17 +468,46 @@ __global__ void __launch_bounds__(kSegThreads) update_kernel(LGeom g, SegArg seg
     if (s->done) return;
     const V alpha = (V)s->alpha;
     double acc[2] = {0.0, 0.0};
-    SEG_LOOP_BEGIN(seg, g)
-    const V pc = p[c], apc = ap[c], xc = x[c], rc0 = r[c];
-    const V rc = rc0 - alpha * apc;
-    x[c] = xc + alpha * pc;
-    r[c] = rc;
-    acc[0] += (double)rc * (double)rc;
-    if (JAC) {
-        const double d = diag[c];
-        if (d > 0.0) acc[1] += (double)rc * ((double)rc / d);
+    DotAcc<V> part = 0;
+    // two segments per warp and iteration, all eight loads issued before any use: the kernel is
+    // pure streaming and bound by the loads in flight
+    const int lane = threadIdx.x & 31;
+    const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int nseg = *seg.count;
+    auto finish = [&](int c, V pc, V apc, V xc, V rc0) {
+        const V rc = rc0 - alpha * apc;
+        x[c] = xc + alpha * pc;
+        r[c] = rc;
+        part += (DotAcc<V>)rc * (DotAcc<V>)rc;
+        if (JAC) {
+            const double d = diag[c];
+            if (d > 0.0) acc[1] += (double)rc * ((double)rc / d);
+        }
+    };
+    for (int qs = warp_global; qs < nseg; qs += 2 * nwarps) {
+        const int q2 = qs + nwarps;
+        const int4 sa = seg.desc[qs];
+        const int4 sb = q2 < nseg ? seg.desc[q2] : sa;
+        const bool la = sa.y + lane < g.n0, lb = q2 < nseg && sb.y + lane < g.n0;
+        const int ca = sa.x + lane, cb = sb.x + lane;
+        V pa = V(0), apa = V(0), xa = V(0), ra = V(0), pb = V(0), apb = V(0), xb = V(0), rb = V(0);
+        if (la) {
+            pa = p[ca];
+            apa = ap[ca];
+            xa = x[ca];
+            ra = r[ca];
+        }
+        if (lb) {
+            pb = p[cb];
+            apb = ap[cb];
+            xb = x[cb];
+            rb = r[cb];
+        }
+        if (la) finish(ca, pa, apa, xa, ra);
+        if (lb) finish(cb, pb, apb, xb, rb);
     }
-    SEG_LOOP_END
+    acc[0] = (double)part;
     double tot[2];
     if (grid_sum<2>(acc, partials, counter, tot)) {
         s->rr = tot[0];
@@ -566,13 +619,14 @@ __global__ void inner_init_kernel(LGeom g, SegArg seg, const double* __restrict_
     const double tau = fmin(0.5, fmax(tau_floor, want));
     const double norm = sqrt(so->rr);
     const double inv = norm > 0.0 ? 1.0 / norm : 0.0;
-    double acc[1] = {0.0};
+    float part = 0.f;
     SEG_LOOP_BEGIN(seg, g)
     const float v = (float)(r64[c] * inv);
     r32[c] = v;
     x32[c] = 0.0f;
-    acc[0] += (double)v * (double)v;
+    part += v * v;
     SEG_LOOP_END
+    double acc[1] = {(double)part};
     double tot[1];
     if (grid_sum<1>(acc, partials, counter, tot)) {
         si->bb = tot[0];
@@ -654,7 +708,7 @@ __global__ void __launch_bounds__(kSegThreads) smooth_kernel(LGeom g, SegArg seg
                                                              unsigned* counter) {
     if (s->done) return;
     const V omega = V(kOmega);
-    double acc[1] = {0.0};
+    DotAcc<V> part = 0;
     const RecLoad<V, R> recf{A};
     // value of the current iterate at a cell, zero on inactive cells
     auto rawf = [&](int q, int qi, int qj, int qk) -> V {
@@ -674,10 +728,11 @@ __global__ void __launch_bounds__(kSegThreads) smooth_kernel(LGeom g, SegArg seg
         V xo = V(0);
         if (st.d > V(0)) xo = st.v0 + mg_div(omega * (bc - apply7(st)), st.d);
         x_out[c] = xo;
-        if (DOT != DOT_NONE) acc[0] += (double)bc * (double)xo;
+        if (DOT != DOT_NONE) part += (DotAcc<V>)bc * (DotAcc<V>)xo;
     }
     SEG_LOOP_END
     if (DOT != DOT_NONE) {
+        double acc[1] = {(double)part};
         double tot[1];
         if (grid_sum<1>(acc, partials, counter, tot)) {
             if (DOT == DOT_BETA) s->beta = tot[0] / s->rz;
