@@ -1097,18 +1097,24 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
         MGLevel<V>& F = mg[l];
         MGLevel<V>& C = mg[l + 1];
         const double rb = l == 0 ? sizeof(R0) : sizeof(RC);
-        // prolongation sweep: b, x, records, coarse x read, t written; last sweep: b, t,
-        // records read, x written
-        ProfScope prof(ctx, l == 0 ? EL_KC_SMOOTH : EL_KC_MG_COARSE, act(l, F) * (6 * vs + 2 * rb) + act(l + 1, C) * vs);
-        if (l == 0) {
-            launch_smooth<V, R0, SM_PROLONG, DOT_NONE>(ctx, F, segof(l), F.x, &C, F.t, s);
-            if (dot == DOT_INIT)
-                launch_smooth<V, R0, SM_PLAIN, DOT_INIT>(ctx, F, segof(l), F.t, nullptr, F.x, s);
+        const int cls = l == 0 ? EL_KC_SMOOTH : EL_KC_MG_COARSE;
+        {
+            // prolongation sweep: b, x, records, coarse x read, t written
+            ProfScope prof(ctx, cls, act(l, F) * (3 * vs + rb) + act(l + 1, C) * vs);
+            if (l == 0)
+                launch_smooth<V, R0, SM_PROLONG, DOT_NONE>(ctx, F, segof(l), F.x, &C, F.t, s);
             else
+                launch_smooth<V, RC, SM_PROLONG, DOT_NONE>(ctx, F, segof(l), F.x, &C, F.t, s);
+        }
+        {
+            // last sweep: b, t, records read, x written
+            ProfScope prof(ctx, cls, act(l, F) * (3 * vs + rb));
+            if (l == 0 && dot == DOT_INIT)
+                launch_smooth<V, R0, SM_PLAIN, DOT_INIT>(ctx, F, segof(l), F.t, nullptr, F.x, s);
+            else if (l == 0)
                 launch_smooth<V, R0, SM_PLAIN, DOT_BETA>(ctx, F, segof(l), F.t, nullptr, F.x, s);
-        } else {
-            launch_smooth<V, RC, SM_PROLONG, DOT_NONE>(ctx, F, segof(l), F.x, &C, F.t, s);
-            launch_smooth<V, RC, SM_PLAIN, DOT_NONE>(ctx, F, segof(l), F.t, nullptr, F.x, s);
+            else
+                launch_smooth<V, RC, SM_PLAIN, DOT_NONE>(ctx, F, segof(l), F.t, nullptr, F.x, s);
         }
         launched += 2;
     }
