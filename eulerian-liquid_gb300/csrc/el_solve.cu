@@ -900,6 +900,169 @@ __global__ void __launch_bounds__(kCoarsestMaxCells) coarsest_kernel(LGeom g, co
 }
 
 // ---------------------------------------------------------------------------------------
+// The bottom of the FP32 V-cycle in one CTA.  Coarsening stops once the largest dimension is
+// at most 8, so the level above the coarsest holds at most 16^3 = 4096 cells: that level and
+// the coarsest fit in one CTA's shared memory (126 KB with float4 records).  One launch of 1024
+// threads does what the segment kernels do in five: the two sweeps from zero, the restriction,
+// the coarsest level's 30 sweeps, the prolongation sweep and the last sweep -- the same
+// expressions in the same order, over the dense level (cells with no diagonal come out 0, as
+// they contribute nothing to their neighbours), with barriers between the passes instead of
+// kernel boundaries.  Only the level's final x goes back to global memory (the finer level's
+// prolongation reads it).
+constexpr int kBottomMaxCells = 4096;
+constexpr int kBottomThreads = 1024;
+
+// the 7-point stencil of cell c of a dense level held in shared memory (float4 records)
+__device__ __forceinline__ St7<float> dense_st7(const float4* rec, const float* v, int c, int i, int j, int k,
+                                                const LGeom& g) {
+    St7<float> st;
+    const float4 r0 = rec[c];
+    st.d = r0.x;
+    st.cxp = r0.y;
+    st.cyp = r0.z;
+    st.czp = r0.w;
+    st.cxm = i > 0 ? rec[c - 1].y : 0.f;
+    st.cym = j > 0 ? rec[c - g.s1].z : 0.f;
+    st.czm = k > 0 ? rec[c - g.s2].w : 0.f;
+    st.v0 = v[c];
+    st.vxm = i > 0 ? v[c - 1] : 0.f;
+    st.vxp = i < g.n0 - 1 ? v[c + 1] : 0.f;
+    st.vym = j > 0 ? v[c - g.s1] : 0.f;
+    st.vyp = j < g.n1 - 1 ? v[c + g.s1] : 0.f;
+    st.vzm = k > 0 ? v[c - g.s2] : 0.f;
+    st.vzp = k < g.n2 - 1 ? v[c + g.s2] : 0.f;
+    return st;
+}
+
+constexpr int bottom_smem_bytes() {
+    return kBottomMaxCells * (int)(sizeof(float4) + 3 * sizeof(float)) +
+           kCoarsestMaxCells * (int)(sizeof(float4) + 3 * sizeof(float));
+}
+
+__global__ void __launch_bounds__(kBottomThreads) mg_bottom_kernel(LGeom gf, const float4* __restrict__ recf,
+                                                                   const float* __restrict__ bf,
+                                                                   float* __restrict__ xf, LGeom gc,
+                                                                   const float4* __restrict__ recc, int sweeps,
+                                                                   const Scalars* s) {
+    if (s->done) return;
+    extern __shared__ __align__(16) unsigned char bottom_smem[];
+    float4* sr = reinterpret_cast<float4*>(bottom_smem);
+    float* sb = reinterpret_cast<float*>(sr + kBottomMaxCells);
+    float* s1 = sb + kBottomMaxCells;
+    float* s2 = s1 + kBottomMaxCells;
+    float4* cr = reinterpret_cast<float4*>(s2 + kBottomMaxCells);
+    float* cb = reinterpret_cast<float*>(cr + kCoarsestMaxCells);
+    float* c1 = cb + kCoarsestMaxCells;
+    float* c2 = c1 + kCoarsestMaxCells;
+    const float omega = (float)kOmega;
+    const int nf = gf.n0 * gf.n1 * gf.n2, nc = gc.n0 * gc.n1 * gc.n2;
+    const int tid = threadIdx.x;
+    auto fine_ijk = [&](int c, int& i, int& j, int& k) {
+        i = c % gf.n0;
+        j = (c / gf.n0) % gf.n1;
+        k = c / (gf.n0 * gf.n1);
+    };
+    for (int c = tid; c < nf; c += kBottomThreads) {
+        sr[c] = recf[c];
+        sb[c] = bf[c];
+    }
+    for (int c = tid; c < nc; c += kBottomThreads) cr[c] = recc[c];
+    __syncthreads();
+    // two sweeps from zero: the first is pointwise
+    for (int c = tid; c < nf; c += kBottomThreads) {
+        const float d = sr[c].x;
+        s1[c] = d > 0.f ? mg_div(omega * sb[c], d) : 0.f;
+    }
+    __syncthreads();
+    for (int c = tid; c < nf; c += kBottomThreads) {
+        int i, j, k;
+        fine_ijk(c, i, j, k);
+        const St7<float> st = dense_st7(sr, s1, c, i, j, k, gf);
+        float xo = 0.f;
+        if (st.d > 0.f) xo = st.v0 + mg_div(omega * (sb[c] - apply7(st)), st.d);
+        s2[c] = xo;
+    }
+    __syncthreads();
+    // residual, then its 2 x 2 x 2 sums onto the coarsest level (order of the segment kernels:
+    // i-pairs of the rows (jj, kk) = (0,0), (1,0), (0,1), (1,1), summed in that order)
+    for (int c = tid; c < nf; c += kBottomThreads) {
+        int i, j, k;
+        fine_ijk(c, i, j, k);
+        const St7<float> st = dense_st7(sr, s2, c, i, j, k, gf);
+        s1[c] = st.d > 0.f ? sb[c] - apply7(st) : 0.f;
+    }
+    __syncthreads();
+    for (int q = tid; q < nc; q += kBottomThreads) {
+        const int I = q % gc.n0, J = (q / gc.n0) % gc.n1, K = q / (gc.n0 * gc.n1);
+        auto res = [&](int i, int j, int k) -> float {
+            return (i < gf.n0 && j < gf.n1 && k < gf.n2) ? s1[i + gf.s1 * j + gf.s2 * k] : 0.f;
+        };
+        float part[4];
+#pragma unroll
+        for (int sub = 0; sub < 4; ++sub) {
+            const int jj = sub & 1, kk = sub >> 1;
+            part[sub] = res(2 * I, 2 * J + jj, 2 * K + kk) + res(2 * I + 1, 2 * J + jj, 2 * K + kk);
+        }
+        cb[q] = ((part[0] + part[1]) + part[2]) + part[3];
+    }
+    __syncthreads();
+    // the coarsest level: damped Jacobi from zero, as coarsest_kernel
+    for (int q = tid; q < nc; q += kBottomThreads) {
+        const float d = cr[q].x;
+        c1[q] = d > 0.f ? mg_div(omega * cb[q], d) : 0.f;
+    }
+    __syncthreads();
+    float* cur = c1;
+    float* nxt = c2;
+    for (int it = 1; it < sweeps; ++it) {
+        for (int q = tid; q < nc; q += kBottomThreads) {
+            const int i = q % gc.n0, j = (q / gc.n0) % gc.n1, k = q / (gc.n0 * gc.n1);
+            float xo = 0.f;
+            const float d = cr[q].x;
+            if (d > 0.f) {
+                float a = d * cur[q];
+                if (i > 0) a += cr[q - 1].y * cur[q - 1];
+                if (i < gc.n0 - 1) a += cr[q].y * cur[q + 1];
+                if (j > 0) a += cr[q - gc.s1].z * cur[q - gc.s1];
+                if (j < gc.n1 - 1) a += cr[q].z * cur[q + gc.s1];
+                if (k > 0) a += cr[q - gc.s2].w * cur[q - gc.s2];
+                if (k < gc.n2 - 1) a += cr[q].w * cur[q + gc.s2];
+                xo = cur[q] + mg_div(omega * (cb[q] - a), d);
+            }
+            nxt[q] = xo;
+        }
+        __syncthreads();
+        float* t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+    // prolongation (x + P e) and a sweep, then the last sweep into global memory
+    for (int c = tid; c < nf; c += kBottomThreads) {
+        int i, j, k;
+        fine_ijk(c, i, j, k);
+        s1[c] = s2[c] + cur[(i >> 1) + gc.s1 * (j >> 1) + gc.s2 * (k >> 1)];
+    }
+    __syncthreads();
+    for (int c = tid; c < nf; c += kBottomThreads) {
+        int i, j, k;
+        fine_ijk(c, i, j, k);
+        const St7<float> st = dense_st7(sr, s1, c, i, j, k, gf);
+        float xo = 0.f;
+        if (st.d > 0.f) xo = st.v0 + mg_div(omega * (sb[c] - apply7(st)), st.d);
+        s2[c] = xo;
+    }
+    __syncthreads();
+    for (int c = tid; c < nf; c += kBottomThreads) {
+        int i, j, k;
+        fine_ijk(c, i, j, k);
+        const St7<float> st = dense_st7(sr, s2, c, i, j, k, gf);
+        float xo = 0.f;
+        if (st.d > 0.f) xo = st.v0 + mg_div(omega * (sb[c] - apply7(st)), st.d);
+        xf[c] = xo;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
 // host side
 
 static int seg_blocks(el_ctx* ctx, long long total_segments) {
@@ -1061,7 +1224,12 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
             launch_smooth<V, R0, SM_PLAIN, DOT_BETA>(ctx, C, seg0, C.t, nullptr, C.x, s);
         return 2;
     }
-    for (int l = 0; l < L - 1; ++l) {
+    // the FP32 hierarchy's last two levels in one CTA (mg_bottom_kernel)
+    constexpr bool kBottomType = std::is_same<V, float>::value && std::is_same<RC, float4>::value;
+    const bool fused_bottom = kBottomType && L >= 3 && cells(mg[L - 2]) <= kBottomMaxCells &&
+                              cells(mg[L - 1]) <= kCoarsestMaxCells;
+    const int pre_end = fused_bottom ? L - 2 : L - 1;  // levels smoothed and restricted by the loops
+    for (int l = 0; l < pre_end; ++l) {
         MGLevel<V>& F = mg[l];
         MGLevel<V>& C = mg[l + 1];
         const double rb = l == 0 ? sizeof(R0) : sizeof(RC);
@@ -1086,14 +1254,25 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
         }
         launched += 2;
     }
-    {
+    if (fused_bottom) {
+        if constexpr (kBottomType) {
+            MGLevel<V>& F = mg[L - 2];
+            MGLevel<V>& C = mg[L - 1];
+            // reads the level's records and b and the coarsest records; writes the level's x
+            ProfScope prof(ctx, EL_KC_MG_COARSE, cells(F) * (sizeof(RC) + 2 * vs) + cells(C) * sizeof(RC));
+            mg_bottom_kernel<<<1, kBottomThreads, bottom_smem_bytes(), ctx->stream>>>(
+                make_geom(F.n0, F.n1, F.n2), (const float4*)F.rec, F.b, F.x, make_geom(C.n0, C.n1, C.n2),
+                (const float4*)C.rec, kCoarsestSweeps, s);
+            ++launched;
+        }
+    } else {
         MGLevel<V>& C = mg[L - 1];
         ProfScope prof(ctx, EL_KC_MG_COARSE, cells(C) * (3 * vs + sizeof(RC)));
         coarsest_kernel<V, RC><<<1, kCoarsestMaxCells, 0, ctx->stream>>>(make_geom(C.n0, C.n1, C.n2), (const RC*)C.rec,
                                                                          C.b, C.x, kCoarsestSweeps, s);
         ++launched;
     }
-    for (int l = L - 2; l >= 0; --l) {
+    for (int l = pre_end - 1; l >= 0; --l) {
         MGLevel<V>& F = mg[l];
         MGLevel<V>& C = mg[l + 1];
         const double rb = l == 0 ? sizeof(R0) : sizeof(RC);
@@ -1569,6 +1748,8 @@ int setup_solver_storage(el_ctx* ctx, int solver) {
         if (rc != EL_OK) return rc;
     }
     if (solver == EL_SOLVER_MIXED && !ctx->x32) {
+        EL_CUDA_TRY(ctx, cudaFuncSetAttribute(mg_bottom_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              bottom_smem_bytes()));
         ctx->x32 = (float*)ctx_alloc(ctx, n * 4);
         ctx->r32 = (float*)ctx_alloc(ctx, n * 4);
         ctx->z32 = (float*)ctx_alloc(ctx, n * 4);
