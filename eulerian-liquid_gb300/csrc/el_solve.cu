@@ -264,14 +264,18 @@ __global__ void pack64_kernel(long long n, const double* __restrict__ d, const O
         a[c] = Rec64{d[c], (double)ox[c], (double)oy[c], (double)oz[c]};
 }
 
-// Coarse records A_c = 1/2 P^T A P over 2x2x2 blocks.
+// Coarse records A_c = 1/2 P^T A P over 2x2x2 blocks.  The FP32 hierarchy (float4 coarse
+// records, built from half4 or float4 records) sums in FP32 -- the eight children's values
+// carry at most 24 significant bits, and FP64 arithmetic runs at a small fraction of the FP32
+// rate on this GPU -- the FP64 hierarchy in FP64.
 template <typename RF, typename RC>
 __global__ void coarsen_kernel(LGeom F, const RF* __restrict__ fr, LGeom C, RC* __restrict__ cr) {
+    using A = typename std::conditional<sizeof(RC) == sizeof(float4), float, double>::type;
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
     const int K = blockIdx.z;
     if (I >= C.n0 || J >= C.n1) return;
-    double d = 0, sx = 0, sy = 0, sz = 0, inner = 0;
+    A d = 0, sx = 0, sy = 0, sz = 0, inner = 0;
     for (int kk = 0; kk < 2; ++kk)
         for (int jj = 0; jj < 2; ++jj)
             for (int ii = 0; ii < 2; ++ii) {
@@ -283,13 +287,13 @@ __global__ void coarsen_kernel(LGeom F, const RF* __restrict__ fr, LGeom C, RC* 
                 if (jj == 0) inner += r.y; else sy += r.y;
                 if (kk == 0) inner += r.z; else sz += r.z;
             }
-    double dc = 0.5 * (d + 2.0 * inner);
+    A dc = A(0.5) * (d + A(2) * inner);
     // an aggregate coupled to nothing outside it (an enclosed Neumann pocket) has a zero row
     // sum; its diagonal is raised to half the children's, which keeps the operator SPD
-    if (d > 0 && !(dc > 1e-6 * d)) dc = 0.5 * d;
+    if (d > A(0) && !(dc > A(1e-6) * d)) dc = A(0.5) * d;
     const long long q = I + C.s1 * J + C.s2 * K;
     if constexpr (sizeof(RC) == sizeof(float4))
-        cr[q] = make_float4((float)dc, (float)(0.5 * sx), (float)(0.5 * sy), (float)(0.5 * sz));
+        cr[q] = make_float4(dc, A(0.5) * sx, A(0.5) * sy, A(0.5) * sz);
     else
         cr[q] = Rec64{dc, 0.5 * sx, 0.5 * sy, 0.5 * sz};
 }
