@@ -1,5 +1,5 @@
 """Pressure projection on the GPU vs the oracle (a7-a13): weights, cell flags and numbering,
-ghost-fluid coefficients (bit-exact), the three solvers (to the solve tolerance, judged with the
+ghost-fluid coefficients (bit-exact), the three solvers (to the solve tolerance, measured with the
 oracle's own matrix) and the velocity update (bit-exact), plus the error paths."""
 
 import numpy as np
@@ -107,7 +107,7 @@ def test_solvers_reach_tolerance_on_oracle_matrix(el, orc, dtype, solver, n):
     assert stats["status"] == 0, stats
     mats = orc.build_matrix(phi, u, v, w, *wts, sim.dx, dt)
     p = sim.download("pressure")
-    # the GPU pressure, judged by the oracle's own matrix in FP64
+    # the GPU pressure, checked against the oracle's own matrix in FP64
     slack = 5.0 if dtype == np.float64 else 50.0  # FP32 pressure grid rounding
     assert residual_rel(orc, mats, p) <= slack * tol
     # against a tight oracle solve, the error is bounded by the conditioning times the residual
