@@ -193,28 +193,31 @@ __global__ void __launch_bounds__(kExBX * kExBY) extrapolate_layer_kernel(int n0
 template <typename T>
 __global__ void masks_kernel(int ni, int nj, int nk, int comp, T* __restrict__ f, const T* __restrict__ wt,
                              const T* __restrict__ phi, uint8_t* __restrict__ valid, int apply_gravity,
-                             T gravity, const Scalars* s, double dt_value, int zero_invalid) {
+                             T gravity, const Scalars* s, double dt_value, int zero_invalid, int kz) {
     const int f0 = ni + (comp == 0), f1 = nj + (comp == 1), f2 = nk + (comp == 2);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
-    if (i >= f0 || j >= f1 || k >= f2) return;
-    const long long fi = lin3(i, j, k, f0, f1);
-    T val = f[fi];
-    if (apply_gravity) {
-        const T dt = (T)(s ? s->dt : dt_value);
-        val = val - mul_rn2(gravity, dt);
-    }
-    bool ok = wt[fi] != T(0);
+    if (i >= f0 || j >= f1) return;
+    const T dt = apply_gravity ? (T)(s ? s->dt : dt_value) : T(0);
     const int ei = comp == 0 ? ni : ni - 1, ej = comp == 1 ? nj : nj - 1, ek = comp == 2 ? nk : nk - 1;
-    if (ok && i >= 1 && j >= 1 && k >= 1 && i < ei && j < ej && k < ek) {
-        const long long b = lin3(i, j, k, ni, nj);
-        const long long a = comp == 0 ? b - 1 : (comp == 1 ? b - ni : b - (long long)ni * nj);
-        if (phi[a] >= T(0) && phi[b] >= T(0)) ok = false;
+    // a column of kz faces per thread (independent: the loads of several are in flight)
+#pragma unroll 4
+    for (int kk = 0; kk < kz; ++kk) {
+        const int k = blockIdx.z * kz + kk;
+        if (k >= f2) break;
+        const long long fi = lin3(i, j, k, f0, f1);
+        T val = f[fi];
+        if (apply_gravity) val = val - mul_rn2(gravity, dt);
+        bool ok = wt[fi] != T(0);
+        if (ok && i >= 1 && j >= 1 && k >= 1 && i < ei && j < ej && k < ek) {
+            const long long b = lin3(i, j, k, ni, nj);
+            const long long a = comp == 0 ? b - 1 : (comp == 1 ? b - ni : b - (long long)ni * nj);
+            if (phi[a] >= T(0) && phi[b] >= T(0)) ok = false;
+        }
+        valid[fi] = ok ? 1 : 0;
+        if (zero_invalid && !ok) val = T(0);
+        if (apply_gravity || (zero_invalid && !ok)) f[fi] = val;
     }
-    valid[fi] = ok ? 1 : 0;
-    if (zero_invalid && !ok) val = T(0);
-    if (apply_gravity || (zero_invalid && !ok)) f[fi] = val;
 }
 
 template <typename T>
@@ -424,15 +427,16 @@ int launch_extrapolate(el_ctx* ctx, int field, uint8_t* valid, int layers, bool 
 
 template <typename T>
 static int launch_masks_t(el_ctx* ctx, bool gravity, double g, const Scalars* s, double dtv, bool zero) {
-    dim3 block(32, 4, 1);
+    dim3 block(32, 8, 1);
+    constexpr int kz = 8;
     for (int comp = 0; comp < 3; ++comp) {
         int n0, n1, n2;
         field_dims(ctx, EL_FIELD_U + comp, n0, n1, n2);
-        masks_kernel<T><<<pgrid(n0, n1, n2, block), block, 0, ctx->stream>>>(
+        masks_kernel<T><<<pgrid(n0, n1, (n2 + kz - 1) / kz, block), block, 0, ctx->stream>>>(
             ctx->ni, ctx->nj, ctx->nk, comp, (T*)ctx->field[EL_FIELD_U + comp],
             (const T*)ctx->field[EL_FIELD_WEIGHT_U + comp], (const T*)ctx->field[EL_FIELD_PHI],
             (uint8_t*)ctx->field[EL_FIELD_VALID_U + comp], (gravity && comp == 1) ? 1 : 0, (T)g, s, dtv,
-            zero ? 1 : 0);
+            zero ? 1 : 0, kz);
     }
     return 3;
 }
