@@ -2,11 +2,13 @@
 //
 // Reference: src/project/3d/fluid/advection.cpp:9-27 (loop drivers), include/nama/math/ode.h
 // (StaggeredGridField, trace_rk2), include/nama/math/interpolation.h (lerp, weno6_interp).
-// One thread per output sample: sample position -> backtrace through the old velocity
-// (trilinear MAC interpolation at every RK stage) -> trilinear or WENO6 sample of the old
-// field at the foot point.  Reads go through the read-only path; the foot point moves at most
-// about one cell per step under the CFL limit, so neighbouring threads gather overlapping
-// stencils and the L1/L2 serve most of them.
+// Per output sample: sample position -> backtrace through the old velocity (trilinear MAC
+// interpolation at every RK stage) -> trilinear or WENO6 sample of the old field at the foot
+// point.  Two forms: advect_kernel, one thread per sample reading global memory (the stateless
+// operators; any dt), and the tiled kernels below, which stage what a tile of samples reads
+// (the velocity boxes; for WENO6 the level-set box and its x-pass smoothness terms) in shared
+// memory once -- under the CFL limit the foot point moves at most about one cell -- and fall
+// back to the global reads for a sample whose stencil leaves the box.
 #include "el_internal.cuh"
 
 namespace el {
