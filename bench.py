@@ -312,6 +312,10 @@ def peaks():
 # launches (the coarse multigrid levels, kernels of a few microseconds) is listed in the
 # breakdown but not taken as the roofline's kernel.
 ROOFLINE_MIN_LAUNCH_US = 20.0
+# Classes whose profiled records each time exactly one kernel launch (the roofline is per
+# launch); extrapolate, masks, build and other time groups of kernels and memsets.
+SINGLE_KERNEL_CLASSES = ("advect_phi", "advect_vel", "dir_spmv", "update", "mg_smooth_fine", "mg_restrict_fine",
+                         "mg_coarse", "residual_fp64")
 
 # DRAM traffic per launch of a kernel class, from one ncu capture of the 256^3 workload
 # (dram__bytes_read.sum + dram__bytes_write.sum of the finest level's three smoother kernels of
@@ -320,10 +324,10 @@ NCU_TRAFFIC_PER_LAUNCH = {"mg_smooth_fine": (96_948_480 + 125_156_096 + 121_205_
 
 
 def dominant_class(breakdown):
-    """The kernel class with the most device time among those whose launches average at least
-    ROOFLINE_MIN_LAUNCH_US (all classes if none does)."""
+    """The single-kernel class with the most device time among those whose launches average at
+    least ROOFLINE_MIN_LAUNCH_US (all classes if none does)."""
     big = {k: v for k, v in breakdown.items()
-           if v["launches"] and v["ms"] * 1e3 / v["launches"] >= ROOFLINE_MIN_LAUNCH_US}
+           if k in SINGLE_KERNEL_CLASSES and v["launches"] and v["ms"] * 1e3 / v["launches"] >= ROOFLINE_MIN_LAUNCH_US}
     pool = big or breakdown
     return max(pool, key=lambda k: pool[k]["ms"])
 
