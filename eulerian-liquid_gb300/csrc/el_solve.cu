@@ -24,9 +24,10 @@
 // Multigrid: coarse operators by aggregation of 2x2x2 blocks scaled by 1/2
 // (A_c = 1/2 P^T A P, piecewise-constant P; it reproduces the rediscretised Laplacian for
 // constant coefficients and carries the ghost-fluid Dirichlet terms down by summation),
-// restriction R = P^T, damped Jacobi (omega = 0.8) with two sweeps before and two after, and
-// 30 sweeps on the coarsest level (at most 8 cells per axis) in one block's shared memory.
-// Same smoother on both legs and R = P^T make the V-cycle symmetric, as PCG needs.
+// restriction R = P^T, two Jacobi sweeps before and two after with Chebyshev weights (see
+// kSweep1 / kSweep2), and 30 damped-Jacobi sweeps on the coarsest level (at most 8 cells per
+// axis) in one block's shared memory.  The same polynomial smoother on both legs and R = P^T
+// make the V-cycle symmetric, as PCG needs.
 //
 // Per PCG iteration:  K1  p = z + beta p ; Ap = A p ; alpha = rz / p.Ap
 //                     K2  x += alpha p ; r -= alpha Ap ; rr = r.r (; rz = r.D^-1 r for Jacobi)
