@@ -298,24 +298,29 @@ __global__ void scatter_pressure_kernel(long long n, const double* __restrict__ 
 template <typename T>
 __global__ void update_velocity_kernel(int ni, int nj, int nk, T* __restrict__ f, int comp,
                                        const T* __restrict__ p, const T* __restrict__ phi, T dx,
-                                       const Scalars* s, double dt_value) {
+                                       const Scalars* s, double dt_value, int kz) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int k = blockIdx.z + 1;
     const int ei = comp == 0 ? ni : ni - 1, ej = comp == 1 ? nj : nj - 1, ek = comp == 2 ? nk : nk - 1;
-    if (i >= ei || j >= ej || k >= ek) return;
+    if (i >= ei || j >= ej) return;
     const T dt = (T)(s ? s->dt : dt_value);
-    const long long b = lin3(i, j, k, ni, nj);
-    const long long a = comp == 0 ? b - 1 : (comp == 1 ? b - ni : b - (long long)ni * nj);
     const int f0 = ni + (comp == 0), f1 = nj + (comp == 1);
-    if (phi[b] < T(0) || phi[a] < T(0)) {
-        T theta = T(1);
-        if (phi[b] >= T(0) || phi[a] >= T(0)) theta = fraction_inside(phi[a], phi[b]);
-        theta = theta < T(0.01) ? T(0.01) : theta;
-        const T num = mul_rn(dt, p[b] - p[a]);
-        const T den = mul_rn(dx, theta);
-        const long long fi = lin3(i, j, k, f0, f1);
-        f[fi] = f[fi] - num / den;
+    // a column of kz faces per thread (independent: the loads of several are in flight)
+#pragma unroll 4
+    for (int kk = 0; kk < kz; ++kk) {
+        const int k = blockIdx.z * kz + kk + 1;
+        if (k >= ek) break;
+        const long long b = lin3(i, j, k, ni, nj);
+        const long long a = comp == 0 ? b - 1 : (comp == 1 ? b - ni : b - (long long)ni * nj);
+        if (phi[b] < T(0) || phi[a] < T(0)) {
+            T theta = T(1);
+            if (phi[b] >= T(0) || phi[a] >= T(0)) theta = fraction_inside(phi[a], phi[b]);
+            theta = theta < T(0.01) ? T(0.01) : theta;
+            const T num = mul_rn(dt, p[b] - p[a]);
+            const T den = mul_rn(dx, theta);
+            const long long fi = lin3(i, j, k, f0, f1);
+            f[fi] = f[fi] - num / den;
+        }
     }
 }
 
@@ -413,7 +418,8 @@ int launch_scatter_pressure(el_ctx* ctx) {
 template <typename T>
 static int launch_update_velocity_t(el_ctx* ctx, const Scalars* s, double dtv) {
     const int ni = ctx->ni, nj = ctx->nj, nk = ctx->nk;
-    dim3 block(32, 4, 1);
+    dim3 block(32, 8, 1);
+    constexpr int kz = 8;
     const T* p = (const T*)ctx->field[EL_FIELD_PRESSURE];
     const T* phi = (const T*)ctx->field[EL_FIELD_PHI];
     const T dx = (T)ctx->dx;
@@ -421,9 +427,9 @@ static int launch_update_velocity_t(el_ctx* ctx, const Scalars* s, double dtv) {
     for (int comp = 0; comp < 3; ++comp) {
         const int ei = comp == 0 ? ni : ni - 1, ej = comp == 1 ? nj : nj - 1, ek = comp == 2 ? nk : nk - 1;
         if (ei <= 1 || ej <= 1 || ek <= 1) continue;
-        dim3 grid = plane_grid(ei - 1, ej - 1, ek - 1, block);
+        dim3 grid = plane_grid(ei - 1, ej - 1, (ek - 1 + kz - 1) / kz, block);
         update_velocity_kernel<T><<<grid, block, 0, ctx->stream>>>(
-            ni, nj, nk, (T*)ctx->field[EL_FIELD_U + comp], comp, p, phi, dx, s, dtv);
+            ni, nj, nk, (T*)ctx->field[EL_FIELD_U + comp], comp, p, phi, dx, s, dtv, kz);
         ++launched;
     }
     return launched;
