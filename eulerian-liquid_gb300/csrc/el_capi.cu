@@ -181,7 +181,7 @@ EL_API int el_ctx_create(int ni, int nj, int nk, double dx, int dtype, int devic
     ctx->ex_tiles = (uint8_t*)ctx_alloc(ctx, ctx->ex_tiles_bytes);
     ctx->dscal = (Scalars*)ctx_alloc(ctx, 4 * sizeof(Scalars));
     Geom g = stencil_geom(ni, nj, nk, ctx->num_sms);
-    ctx->max_partials = std::max(g.blocks(), ctx->num_sms * 8) * 2 + 64;
+    ctx->max_partials = std::max(g.blocks(), ctx->num_sms * 16) * 2 + 64;
     ctx->partials = (double*)ctx_alloc(ctx, ctx->max_partials * sizeof(double));
     ctx->counter = (unsigned*)ctx_alloc(ctx, 64);
     ok = ok && ctx->valid_tmp && ctx->ex_tiles && ctx->dscal && ctx->partials && ctx->counter;
@@ -248,11 +248,11 @@ EL_API int64_t el_ctx_kernel_launches(const el_ctx* ctx) { return ctx ? ctx->lau
 EL_API int el_ctx_set_tuning(el_ctx* ctx, const el_tuning* t) {
     CHECK_CTX(ctx);
     if (!t || t->seg_blocks_per_sm < 1 || t->seg_blocks_per_sm > 8 || t->stencil_blocks_per_sm < 1 ||
-        t->stencil_blocks_per_sm > 8 || t->extrapolate_blocks_per_sm < 1 || t->extrapolate_blocks_per_sm > 16 ||
+        t->stencil_blocks_per_sm > 16 || t->extrapolate_blocks_per_sm < 1 || t->extrapolate_blocks_per_sm > 16 ||
         (t->advect_rows != 1 && t->advect_rows != 2 && t->advect_rows != 4 && t->advect_rows != 8) ||
         (t->advect_tiled != 0 && t->advect_tiled != 1))
         return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "tuning out of range");
-    // the reduction partials are sized for 8 blocks per SM (el_ctx_create)
+    // the reduction partials are sized for 16 stencil blocks per SM (el_ctx_create)
     ctx->seg_per_sm = t->seg_blocks_per_sm;
     ctx->stencil_per_sm = t->stencil_blocks_per_sm;
     ctx->extrap_per_sm = t->extrapolate_blocks_per_sm;

@@ -134,7 +134,7 @@ int64_t el_ctx_kernel_launches(const el_ctx* ctx);
  * shapes its scenes have when it is created. */
 typedef struct el_tuning {
     int seg_blocks_per_sm;       /* solver kernels over active row segments, 1..8 (default 6)   */
-    int stencil_blocks_per_sm;   /* matrix build, masks, element-wise kernels, 1..8 (default 8) */
+    int stencil_blocks_per_sm;   /* matrix build, masks, element-wise kernels, 1..16 (default 8) */
     int extrapolate_blocks_per_sm; /* extrapolation tiles in flight per SM, 1..16 (default 12)  */
     int advect_rows;             /* per-sample advection: 32 x rows cells per block, 1, 2, 4 or 8 */
     int advect_tiled;            /* 1 (default): advection kernels that stage the velocity of a
