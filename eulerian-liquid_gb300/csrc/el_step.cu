@@ -330,7 +330,8 @@ __global__ void emit_kernel(int n0, int n1, int n2, T* __restrict__ g, T ox, T d
     T val;
     if (e.kind == EMIT_SPHERE) {
         const T qx = px - (T)e.a[0], qy = py - (T)e.a[1], qz = pz - (T)e.a[2];
-        const T ss = add_rn2(add_rn2(mul_rn2(qx, qx), mul_rn2(qy, qy)), mul_rn2(qz, qz));
+        // (x - c).norm() of an Eigen::Vector3f: x^2 + (y^2 + z^2)  (levelset_emitter.cpp:10-12)
+        const T ss = add_rn2(mul_rn2(qx, qx), add_rn2(mul_rn2(qy, qy), mul_rn2(qz, qz)));
         val = sqrt(ss) - (T)e.a[3];
     } else if (e.kind == EMIT_POOL) {
         val = py - (T)e.a[0];

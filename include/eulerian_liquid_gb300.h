@@ -424,7 +424,9 @@ int el_nn_adam(int64_t n, float* w, float* g, float* m, float* v, float lr, floa
  *   - the work goes on `stream` (a cudaStream_t, NULL = the default stream); the call returns
  *     after the solve, because it reads the convergence scalars back on the host;
  *   - the first call on a device looks up the scratch array's device address, once per device,
- *     with that device current; make that first call before any stream capture;
+ *     with that device current, and keeps it for the life of the process; make that first call
+ *     before any stream capture, and do not use this entry point after a cudaDeviceReset of
+ *     that device (the reset unloads the library's device memory, so the kept address is stale);
  *   - all calls share the one array, which keeps the last call's contents: calls that overlap
  *     on the GPU (from several threads or streams) race, and the caller must serialise them. */
 #define EL_ERR_TOO_LARGE 8

@@ -355,3 +355,208 @@ def rasterise(spec, dtype=np.float64):
             else:
                 raise ValueError(e[0])
     return phi, solid
+
+
+# ----------------------------------------------------------------------------------------
+# The reference's own simulator code (oracle/_ref, built from the reference tree by
+# oracle/build.py against oracle/eigen_min).  FP32, as the reference.  Every wrapper raises
+# RuntimeError when the library is absent; tests skip on ref_sim_available() == False.
+
+_refsim = None
+
+
+def ref_sim_available():
+    return _ref_sim_lib() is not None
+
+
+def _ref_sim_lib():
+    global _refsim
+    if _refsim is None:
+        L = ref_lib()
+        if L is None or not hasattr(L, "refsim_new"):
+            return None
+        vp, i, d, ll, cp = C.c_void_p, C.c_int, C.c_double, C.c_longlong, C.c_char_p
+        L.refsim_compute_weights.argtypes = [i, i, i, d, vp, vp, vp, vp]
+        L.refsim_assign_indices.argtypes = [i, i, i, d, vp, vp, vp, vp, vp]
+        L.refsim_assign_indices.restype = i
+        L.refsim_build_matrix.argtypes = [i, i, i, d] + [vp] * 7 + [d] + [vp] * 6
+        L.refsim_build_matrix.restype = i
+        L.refsim_build_grid_from_vector.argtypes = [i, i, i, d, vp, i, vp, d, vp]
+        L.refsim_update_velocity.argtypes = [i, i, i, d, vp, vp, vp, vp, vp, d]
+        L.refsim_extrapolate.argtypes = [vp, vp, i, i, i, i, i]
+        L.refsim_calc_time_step.argtypes = [i, i, i, d, vp, vp, vp, d]
+        L.refsim_calc_time_step.restype = C.c_float
+        L.refsim_advect_collocated.argtypes = [i, i, i, d, vp, vp, vp, vp, vp, d]
+        L.refsim_advect_staggered.argtypes = [i, i, i, d, vp, vp, vp, vp, vp, vp, d]
+        L.refsim_new.argtypes = [i, i, i, d]
+        L.refsim_new.restype = vp
+        L.refsim_free.argtypes = [vp]
+        L.refsim_dx.argtypes = [vp]
+        L.refsim_dx.restype = d
+        L.refsim_add_sphere.argtypes = [vp, i, d, d, d, d]
+        L.refsim_add_pool.argtypes = [vp, d]
+        L.refsim_add_room.argtypes = [vp]
+        L.refsim_init_scene.argtypes = [vp]
+        L.refsim_field.argtypes = [vp, cp, C.POINTER(ll), C.POINTER(i)]
+        L.refsim_field.restype = vp
+        L.refsim_call.argtypes = [vp, cp, d]
+        L.refsim_call.restype = i
+        L.refsim_mesh_obj.argtypes = [vp, i, i, i, d, d, d, d, d, i, cp, vp]
+        L.refsim_mesh_obj.restype = i
+        _refsim = L
+    return _refsim
+
+
+def _rs():
+    L = _ref_sim_lib()
+    if L is None:
+        raise RuntimeError("the reference library oracle/_ref/libnama_ref.so is not built")
+    return L
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def ref_compute_weights(solid_nodal):
+    nk1, nj1, ni1 = solid_nodal.shape
+    ni, nj, nk = ni1 - 1, nj1 - 1, nk1 - 1
+    s = _f32(solid_nodal)
+    outs = [np.empty(face_shape(ni, nj, nk, c), np.float32) for c in range(3)]
+    _rs().refsim_compute_weights(ni, nj, nk, float_dx(ni, np.float32), _p(s), *[_p(o) for o in outs])
+    return tuple(outs)
+
+
+def ref_assign_indices(phi, wu, wv, ww):
+    nk, nj, ni = phi.shape
+    arrs = [_f32(a) for a in (phi, wu, wv, ww)]
+    idx = np.empty(phi.shape, np.int32)
+    n = _rs().refsim_assign_indices(ni, nj, nk, float_dx(ni, np.float32), *[_p(a) for a in arrs], _p(idx))
+    return n, idx
+
+
+def ref_build_matrix(phi, u, v, w, wu, wv, ww, dx, dt):
+    """The reference's build_matrix laid out on the grid: (diag, offx, offy, offz, rhs, odd, nnz)."""
+    nk, nj, ni = phi.shape
+    arrs = [_f32(a) for a in (phi, u, v, w, wu, wv, ww)]
+    outs = [np.empty(phi.shape, np.float64) for _ in range(5)]
+    nnz = C.c_longlong()
+    odd = _rs().refsim_build_matrix(ni, nj, nk, dx, *[_p(a) for a in arrs], dt, *[_p(o) for o in outs],
+                                    C.byref(nnz))
+    return (*outs, odd, nnz.value)
+
+
+def ref_build_grid_from_vector(vec, indices, background=0.0):
+    nk, nj, ni = indices.shape
+    vec = np.ascontiguousarray(vec, np.float64)
+    idx = np.ascontiguousarray(indices, np.int32)
+    out = np.empty(indices.shape, np.float32)
+    _rs().refsim_build_grid_from_vector(ni, nj, nk, float_dx(ni, np.float32), _p(vec), vec.size, _p(idx),
+                                        background, _p(out))
+    return out
+
+
+def ref_update_velocity(u, v, w, pressure, phi, dx, dt):
+    nk, nj, ni = phi.shape
+    u, v, w = (np.array(a, dtype=np.float32, copy=True, order="C") for a in (u, v, w))
+    p, phi = _f32(pressure), _f32(phi)
+    _rs().refsim_update_velocity(ni, nj, nk, dx, _p(u), _p(v), _p(w), _p(p), _p(phi), dt)
+    return u, v, w
+
+
+def ref_extrapolate(grid, valid, layers=10, keep_valid=False):
+    n2, n1, n0 = grid.shape
+    g = np.array(grid, dtype=np.float32, copy=True, order="C")
+    m = np.array(valid, dtype=np.uint8, copy=True, order="C")
+    _rs().refsim_extrapolate(_p(g), _p(m), n0, n1, n2, layers, int(keep_valid))
+    return g, m
+
+
+def ref_calc_time_step(u, v, w, dx, cfl):
+    nk, nj, ni1 = u.shape
+    u, v, w = (_f32(a) for a in (u, v, w))
+    return float(_rs().refsim_calc_time_step(ni1 - 1, nj, nk, dx, _p(u), _p(v), _p(w), cfl))
+
+
+def ref_advect_collocated(phi, u, v, w, dx, dt):
+    nk, nj, ni = phi.shape
+    arrs = [_f32(a) for a in (phi, u, v, w)]
+    out = np.empty(phi.shape, np.float32)
+    _rs().refsim_advect_collocated(ni, nj, nk, dx, _p(out), *[_p(a) for a in arrs], dt)
+    return out
+
+
+def ref_advect_staggered(u, v, w, dx, dt):
+    nk, nj, ni1 = u.shape
+    u, v, w = (_f32(a) for a in (u, v, w))
+    outs = [np.empty(a.shape, np.float32) for a in (u, v, w)]
+    _rs().refsim_advect_staggered(ni1 - 1, nj, nk, dx, *[_p(o) for o in outs], _p(u), _p(v), _p(w), dt)
+    return tuple(outs)
+
+
+def ref_mesh_obj(phi, dx, origin=(0.0, 0.0, 0.0), isolevel=0.0, method=0, path=""):
+    """The reference's get_mesh + Mesh::save: returns (vertices, faces, vertices per face)."""
+    nk, nj, ni = phi.shape
+    counts = np.zeros(3, np.int64)
+    phi = _f32(phi)
+    rc = _rs().refsim_mesh_obj(_p(phi), ni, nj, nk, dx, *origin, isolevel, method, path.encode(), _p(counts))
+    if rc != 0:
+        raise OSError(f"cannot write {path}")
+    return tuple(int(c) for c in counts)
+
+
+class RefSimulator:
+    """The reference's Simulator (simulator.cpp) on an (ni, nj, nk) grid of width 1."""
+
+    _SHAPES = {"phi": 0, "phi_valid": 0, "pressure": 0, "indices": 0, "solid_cell": 0,
+               "u": 1, "weight_u": 1, "valid_u": 1, "v": 2, "weight_v": 2, "valid_v": 2,
+               "w": 3, "weight_w": 3, "valid_w": 3, "solid_nodal": 4}
+
+    def __init__(self, ni, nj, nk, cfl=1.0):
+        self.shape3 = (ni, nj, nk)
+        self.h = _rs().refsim_new(ni, nj, nk, cfl)
+        self.dx = _rs().refsim_dx(self.h)
+
+    def close(self):
+        if self.h:
+            _rs().refsim_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_sphere(self, center, radius, liquid=True):
+        _rs().refsim_add_sphere(self.h, int(liquid), *center, radius)
+
+    def add_pool(self, height):
+        _rs().refsim_add_pool(self.h, height)
+
+    def add_room(self):
+        _rs().refsim_add_room(self.h)
+
+    def init_scene(self):
+        _rs().refsim_init_scene(self.h)
+
+    def field(self, name):
+        """A numpy view (nk, nj, ni)-shaped onto the reference's own storage of a field."""
+        ni, nj, nk = self.shape3
+        comp = self._SHAPES[name]
+        shape = (nk + 1, nj + 1, ni + 1) if comp == 4 else ((nk, nj, ni) if comp == 0 else
+                                                             face_shape(ni, nj, nk, comp - 1))
+        count, elem = C.c_longlong(), C.c_int()
+        ptr = _rs().refsim_field(self.h, name.encode(), C.byref(count), C.byref(elem))
+        dt = {4: np.float32, 1: np.uint8}[elem.value]
+        if name == "indices":
+            dt = np.int32
+        buf = (C.c_char * (count.value * elem.value)).from_address(ptr)
+        return np.frombuffer(buf, dtype=dt).reshape(shape)
+
+    def call(self, method, dt=0.0):
+        rc = _rs().refsim_call(self.h, method.encode(), dt)
+        if rc == -1:
+            raise RuntimeError("No fluid")
+        if rc == -2:
+            raise ValueError(method)

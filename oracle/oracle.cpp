@@ -672,10 +672,12 @@ static int pcg(const GridMatrix& A, const double* b, double* x, int precond, dou
 // ---------------------------------------------------------------------------------------
 // Level-set emitters (src/project/3d/fluid/levelset_emitter.cpp:10-79): each writes
 // min(grid, f(x)) at its grid's sample positions; the list starts from FLT_MAX.
+// sphere: (x - c).norm() - r with Eigen::Vector3f, whose unrolled three-term reduction sums
+// x^2 + (y^2 + z^2) (pinned against the reference's levelset_emitter.cpp:10-12 compiled here)
 template <typename T>
 inline T sphere_sdf(const Vec3<T>& p, T cx, T cy, T cz, T r) {
     T dx = p.x - cx, dy = p.y - cy, dz = p.z - cz;
-    return std::sqrt(dx * dx + dy * dy + dz * dz) - r;
+    return std::sqrt(dx * dx + (dy * dy + dz * dz)) - r;
 }
 
 // Exact signed distance to an axis-aligned box [lo, hi] (new: the reference has no box).

@@ -11,6 +11,13 @@ Run here, where the reference tree exists:
 Fixtures: advect_<dtype>.npz -- semi-Lagrangian advection (RK2 backtrace, trilinear and WENO6
 sampling, cell-centred and staggered) of seeded fields on a 12 x 10 x 8 grid, and
 interp_<dtype>.npz -- point samples, RK2 traces and 1-D WENO6 evaluations.
+
+step_ref_f32.npz -- one sub-step of update_second_order without reinitialize() run piece by
+piece on the reference's own Simulator (simulator.cpp, projection.cpp, boundary.cpp,
+extrapolation.cpp, advection.cpp, levelset_emitter.cpp, compiled by oracle/build.py against
+oracle/eigen_min) on a 20 x 16 x 18 scene: spheres and a pool in a room with a solid box
+obstacle, seeded velocity.  Every intermediate field is stored, the matrix in grid form, and
+the velocity update of a seeded pressure.
 """
 
 import ctypes as C
@@ -79,7 +86,62 @@ def main():
                             dt=np.float64(dt), points=pts, trilinear=np.array(tri, dtype),
                             weno6=np.array(weno, dtype), traces=np.array(traces), weno1d_values=vals,
                             weno1d_fractions=fr, weno1d=np.array(w1, dtype))
+    step_fixture()
     print("wrote fixtures to", HERE)
+
+
+def step_fixture():
+    if not O.ref_sim_available():
+        raise SystemExit("oracle/_ref/libnama_ref.so lacks the simulator sources: rebuild with oracle/build.py")
+    ni, nj, nk = 20, 16, 18
+    sim = O.RefSimulator(ni, nj, nk)
+    sim.add_sphere((0.3, 0.55, 0.35), 0.16)
+    sim.add_sphere((0.7, 0.6, 0.6), 0.12)
+    sim.add_pool(0.22)
+    sim.add_room()
+    sim.init_scene()
+    dx = sim.dx
+    solid = sim.field("solid_nodal")
+    # a solid box obstacle (not one of the reference's emitters), composed with min
+    O.emit_box(solid, (-0.5 * dx,) * 3, dx, (0.45, 0.05, 0.3), (0.62, 0.3, 0.55))
+    sim.call("calc_cell_centered_solid_phi")
+    sim.call("compute_weights")
+    sim.call("find_valid_level_set")
+    rng = np.random.default_rng(20261204)
+    out = {"shape": np.array([ni, nj, nk]), "dx": np.float64(dx)}
+    for f in ("u", "v", "w"):
+        sim.field(f)[...] = (0.4 * rng.standard_normal(sim.field(f).shape)).astype(np.float32)
+    for f in ("phi", "solid_nodal", "solid_cell", "phi_valid", "u", "v", "w", "weight_u", "weight_v", "weight_w"):
+        out[f"in_{f}"] = sim.field(f).copy()
+    dt = O.ref_calc_time_step(sim.field("u"), sim.field("v"), sim.field("w"), dx, 1.0)
+    out["dt"] = np.float64(dt)
+
+    def record(tag, fields):
+        for f in fields:
+            out[f"{tag}_{f}"] = sim.field(f).copy()
+
+    sim.call("extrapolate_velocity")
+    record("extrap", ("u", "v", "w", "valid_u", "valid_v", "valid_w"))
+    sim.call("extrapolate_level_set")
+    record("extrap", ("phi",))
+    sim.call("advect_level_set", dt)
+    sim.call("advect_velocity", dt)
+    record("advect", ("phi", "u", "v", "w"))
+    sim.call("add_gravity", dt)
+    record("gravity", ("v",))
+    sim.call("find_valid_velocity")
+    sim.call("set_invalid_velocity_zero")
+    record("masks", ("u", "v", "w", "valid_u", "valid_v", "valid_w"))
+    args = [sim.field(f) for f in ("phi", "u", "v", "w", "weight_u", "weight_v", "weight_w")]
+    n, idx = O.ref_assign_indices(args[0], *args[4:])
+    D, X, Y, Z, B, odd, _ = O.ref_build_matrix(*args, dx, dt)
+    assert odd == 0
+    out.update(indices=idx, mat_size=np.int64(n), diag=D, offx=X, offy=Y, offz=Z, rhs=B)
+    p = np.where(D > 0, rng.standard_normal(D.shape), 0).astype(np.float32)
+    uu, vv, ww = O.ref_update_velocity(args[1], args[2], args[3], p, args[0], dx, dt)
+    out.update(update_pressure=p, update_u=uu, update_v=vv, update_w=ww)
+    sim.close()
+    np.savez_compressed(os.path.join(HERE, "step_ref_f32.npz"), **out)
 
 
 if __name__ == "__main__":

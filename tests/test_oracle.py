@@ -176,3 +176,42 @@ def test_extrapolation_known_layers(orc):
     valid[0, 0, 0] = 1
     out, m = orc.extrapolate(g, valid, layers=3)
     assert list(out[0, 0]) == [2, 2, 2, 2, 0, 0] and list(m[0, 0]) == [1, 1, 1, 1, 0, 0]
+
+
+def test_oracle_reproduces_reference_step_fixture(orc):
+    """tests/golden/step_ref_f32.npz holds one sub-step of the reference's own Simulator, piece
+    by piece (tests/golden/make_golden.py); the FP32 restatement reproduces every piece exactly."""
+    g = np.load(os.path.join(GOLDEN, "step_ref_f32.npz"))
+    dx, dt = float(g["dx"]), float(g["dt"])
+    solid = g["in_solid_nodal"]
+    wts = orc.compute_weights(solid)
+    for f, w in zip(("weight_u", "weight_v", "weight_w"), wts):
+        np.testing.assert_array_equal(w, g[f"in_{f}"])
+    np.testing.assert_array_equal(orc.cell_solid_phi(solid), g["in_solid_cell"])
+    np.testing.assert_array_equal((g["in_solid_cell"] >= 0).astype(np.uint8), g["in_phi_valid"])
+    assert orc.calc_time_step(g["in_u"], g["in_v"], g["in_w"], dx, 1.0) == dt
+    ex = {}
+    for f in "uvw":
+        ex[f], m = orc.extrapolate(g[f"in_{f}"], np.ones(g[f"in_{f}"].shape, np.uint8), 10)
+        np.testing.assert_array_equal(ex[f], g[f"extrap_{f}"])
+        np.testing.assert_array_equal(m, g[f"extrap_valid_{f}"])
+    phi_x, _ = orc.extrapolate(g["in_phi"], g["in_phi_valid"], 10)
+    np.testing.assert_array_equal(phi_x, g["extrap_phi"])
+    phi1 = orc.advect_collocated(phi_x, ex["u"], ex["v"], ex["w"], dx, dt)
+    np.testing.assert_array_equal(phi1, g["advect_phi"])
+    for f, a in zip("uvw", orc.advect_staggered(ex["u"], ex["v"], ex["w"], dx, dt)):
+        np.testing.assert_array_equal(a, g[f"advect_{f}"])
+    t = np.float32
+    np.testing.assert_array_equal((g["advect_v"] - t(t(9.80665) * t(dt))).astype(np.float32), g["gravity_v"])
+    masks = orc.find_valid_velocity(phi1, *wts)
+    for f, m in zip("uvw", masks):
+        np.testing.assert_array_equal(m, g[f"masks_valid_{f}"])
+    n, idx = orc.assign_indices(g["advect_phi"], *wts)
+    assert n == int(g["mat_size"])
+    np.testing.assert_array_equal(idx, g["indices"])
+    mats = orc.build_matrix(g["advect_phi"], g["masks_u"], g["masks_v"], g["masks_w"], *wts, dx, dt)
+    for a, key in zip(mats, ("diag", "offx", "offy", "offz", "rhs")):
+        np.testing.assert_array_equal(a, g[key])
+    upd = orc.update_velocity(g["masks_u"], g["masks_v"], g["masks_w"], g["update_pressure"], g["advect_phi"], dx, dt)
+    for a, f in zip(upd, "uvw"):
+        np.testing.assert_array_equal(a, g[f"update_{f}"])

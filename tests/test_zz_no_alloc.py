@@ -27,7 +27,7 @@ def _declare(lib, el):
     return f
 
 
-def test_noalloc_matches_solve_pressure_on_two_calls(el):
+def test_noalloc_matches_solve_pressure_on_two_calls(el, orc):
     torch = pytest.importorskip("torch")
     lib = el.load()
     solve_noalloc = _declare(lib, el)
@@ -68,6 +68,12 @@ def test_noalloc_matches_solve_pressure_on_two_calls(el):
             got = dev[f].cpu().numpy()
             assert np.all(np.isfinite(got)), (call, f)
             assert rel_err(got, want[f]) <= MATCH, (call, f, rel_err(got, want[f]))
+        # and the pressure solves the CPU oracle's own system for these inputs: the residual is
+        # that of the FP64 solution rounded to the FP32 pressure grid
+        mats = orc.build_matrix(phi, *vel, *weights, sim.dx, dt)
+        p = dev["pressure"].cpu().numpy().astype(np.float64)
+        r = mats[4] - orc.spmv(*mats[:4], np.where(mats[0] > 0, p, 0.0))
+        assert np.linalg.norm(r) / np.linalg.norm(mats[4]) <= 5e-5, call
     sim.close()
 
 
