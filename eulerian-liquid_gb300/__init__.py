@@ -37,6 +37,12 @@ EL_F32, EL_F64 = 0, 1
 TRACE_RK2, TRACE_RK3 = 0, 1
 SAMPLE_TRILINEAR, SAMPLE_WENO6 = 0, 1
 SOLVER_JACOBI_FP64, SOLVER_MG_FP64, SOLVER_MIXED = 0, 1, 2
+# kernel classes of el_ctx_profile_* (enum el_kernel_class)
+KERNEL_CLASSES = ("advect_phi", "advect_vel", "extrapolate", "masks", "build", "dir_spmv", "update",
+                  "mg_smooth_fine", "mg_restrict_fine", "mg_coarse", "residual_fp64", "other")
+(EL_KC_ADVECT_PHI, EL_KC_ADVECT_VEL, EL_KC_EXTRAPOLATE, EL_KC_MASKS, EL_KC_BUILD, EL_KC_DIR_SPMV, EL_KC_UPDATE,
+ EL_KC_SMOOTH, EL_KC_RESTRICT, EL_KC_MG_COARSE, EL_KC_RESIDUAL, EL_KC_OTHER) = range(12)
+EL_KC_COUNT = 12
 
 FIELDS = {
     "phi": 0, "u": 1, "v": 2, "w": 3, "solid_nodal": 4, "weight_u": 5, "weight_v": 6,
@@ -88,7 +94,8 @@ class Grid(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("seg_blocks_per_sm", C.c_int), ("stencil_blocks_per_sm", C.c_int),
-                ("extrapolate_blocks_per_sm", C.c_int), ("advect_rows", C.c_int), ("advect_tiled", C.c_int)]
+                ("extrapolate_blocks_per_sm", C.c_int), ("advect_rows", C.c_int), ("advect_tiled", C.c_int),
+                ("solver_tiles", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -102,6 +109,10 @@ class BatchStats(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ProfileEntry(C.Structure):
+    _fields_ = [("launches", C.c_int64), ("ms", C.c_double), ("bytes", C.c_double)]
 
 
 _lib = None
@@ -145,6 +156,8 @@ def _declare(L):
     L.el_state_save.argtypes = [ctxp, C.c_char_p, d]
     L.el_state_load.argtypes = [ctxp, C.c_char_p, C.POINTER(C.c_double)]
     L.el_ctx_set_tuning.argtypes = [ctxp, C.POINTER(Tuning)]
+    L.el_ctx_profile_begin.argtypes = [ctxp, C.c_uint32]
+    L.el_ctx_profile_end.argtypes = [ctxp, C.POINTER(ProfileEntry)]
     L.el_ctx_get_tuning.argtypes = [ctxp, C.POINTER(Tuning)]
     L.el_upload.argtypes = [ctxp, i, vp, sz]
     L.el_download.argtypes = [ctxp, i, vp, sz]
@@ -316,6 +329,17 @@ class Simulator:
 
     def kernel_launches(self):
         return int(self.lib.el_ctx_kernel_launches(self.h))
+
+    # -- per-kernel-class timing (el_ctx_profile_begin / _end) ------------------------------
+    def profile_begin(self, class_mask=(1 << EL_KC_COUNT) - 1):
+        self._check(self.lib.el_ctx_profile_begin(self.h, class_mask), "profile_begin")
+
+    def profile_end(self):
+        """{class name: {launches, ms, bytes}} for the classes that launched while profiling."""
+        out = (ProfileEntry * EL_KC_COUNT)()
+        self._check(self.lib.el_ctx_profile_end(self.h, out), "profile_end")
+        return {KERNEL_CLASSES[c]: {"launches": int(out[c].launches), "ms": out[c].ms, "bytes": out[c].bytes}
+                for c in range(EL_KC_COUNT) if out[c].launches}
 
     # -- scene set-up (levelset_emitter.cpp, boundary.cpp, simulator.cpp:72-76, 160-200) ----
     def emit(self, target, item):

@@ -6,6 +6,7 @@
 // entries of non-fluid cells are zero and their matrix rows are empty (diag = 0).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -48,6 +49,7 @@ struct Scalars {
     int outer;       // mixed solver: refinement sweeps done
     int inner_total; // mixed solver: inner iterations summed over the sweeps
     int inner_passes;// device-driven mixed solver: passes of its PCG loop
+    int fault;       // a bounded device wait gave up (the solve reports EL_ERR_TIMEOUT)
 };
 
 // Per-scene running totals of a batch (el_batch_stats on the device).
@@ -85,6 +87,40 @@ struct MGLevel {
     SegList seg;
 };
 
+// The smoother: two Jacobi sweeps with weights 1/t1 and 1/t2, t1,2 the roots of the degree-2
+// Chebyshev polynomial on [1/3, 2] -- the high-frequency part of the spectrum of D^-1 A (a
+// 7-point operator with D >= the sum of its couplings' magnitudes has its spectrum in [0, 2];
+// modes with a wave number past pi/2 on any axis have lambda >= 1/3).  Two sweeps apply
+// (1 - w1 D^-1 A)(1 - w2 D^-1 A), which reduces that band by at most 1/T2(7/5) = 0.34, against
+// 0.51 for two sweeps at 6/7, for the same work; and, a polynomial in D^-1 A, the smoother is
+// self-adjoint in the A inner product and contracts on (0, 2], so the V-cycle stays a
+// symmetric positive definite preconditioner.  The first sweep of a pair takes w1, the second
+// w2 (before and after the coarse correction alike).
+constexpr double kChebMid = 7.0 / 6.0, kChebHalf = 5.0 / 6.0;
+constexpr double kSweep1 = 1.0 / (kChebMid + kChebHalf * 0.70710678118654752);  // 0.5695
+constexpr double kSweep2 = 1.0 / (kChebMid - kChebHalf * 0.70710678118654752);  // 1.7319
+
+// The finest level of the FP32 multigrid as z-marching tile kernels (el_march.cu): work items
+// of 32 x 16 cells x up to kMarchPlanes planes holding an active cell, and the TMA tensor maps
+// of the arrays those kernels stage.  `on` when the grid meets the kernels' conditions (row
+// pitch a multiple of 16 bytes on the finest and the next level, at least three levels).
+constexpr int kMarchPlanes = 16;  // planes per work item (tiles are 32 x 16 cells)
+struct MarchPlan {
+    bool on = false;
+    int nib = 0, njb = 0, nkc = 0;  // tiles along i, j and plane chunks along k
+    int4* items = nullptr;          // {i0, j0, k0, k1}, ordered i-tile fastest, then j, then k
+    int* count = nullptr;           // number of items (device)
+    uint8_t* flags = nullptr;
+    // tensor maps: 40 x 18 halo boxes of the vectors, 32 x 16 centre boxes, the records' halo
+    // boxes and the coarse level's 24 x 10 box
+    enum { Z, P, PB, AP, R, RB, T, NHALO };
+    enum { CX, CP, CPB, CR, CRB, NCENTRE };
+    CUtensorMap halo[NHALO];
+    CUtensorMap centre[NCENTRE];
+    CUtensorMap rec32, rec16, coarse_x;
+    int per_sm[6] = {};  // resident CTAs per SM of each tile kernel
+};
+
 struct DeviceBuffer {
     void* ptr = nullptr;
     size_t bytes = 0;
@@ -104,6 +140,7 @@ struct el_ctx {
     // the advection tile (32 x rows cells per block)
     int seg_per_sm = 6, stencil_per_sm = 8, extrap_per_sm = 12, advect_rows = 4;
     int advect_tiled = 1;  // advection through the staged-tile kernels
+    int solver_tiles = 1;  // the mixed solver's finest level on the tile kernels (where supported)
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int64_t launches = 0;
@@ -130,6 +167,8 @@ struct el_ctx {
     ushort4* A16 = nullptr;
     float *x32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *ap32 = nullptr;
     float* p32b = nullptr;
+    float* r32b = nullptr;  // second residual buffer (the fused update writes r out of place)
+    el::MarchPlan march;    // finest-level tile kernels of the mixed solver
     el::Rec64* A64rec = nullptr;  // level-0 records of the FP64 multigrid
     el::SegList seg0;             // active segments of the finest level
     std::vector<el::MGLevel<float>> mg32;
@@ -215,6 +254,18 @@ int check_launch(el_ctx* ctx, const char* what);
 void* ctx_alloc(el_ctx* ctx, size_t bytes);  // zero-filled, owned by the context
 int ensure_projection(el_ctx* ctx);
 int ensure_solver(el_ctx* ctx, int solver);
+
+// finest-level tile kernels of the FP32 multigrid (el_march.cu); each returns its launches
+bool march_supported(const el_ctx* ctx);
+int march_setup(el_ctx* ctx);
+int march_enqueue_items(el_ctx* ctx);
+int march_dir_spmv(el_ctx* ctx, const float* z, const float* p_in, float* p_out, float* ap, Scalars* s, int first);
+int march_update_smooth(el_ctx* ctx, float* x, const float* p, const float* r_in, float* r_out, const float* ap,
+                        float* z, Scalars* s);
+int march_zero2(el_ctx* ctx, const float* b, float* z, Scalars* s);
+int march_restrict(el_ctx* ctx, const float* x, const float* b, float* coarse_b, Scalars* s);
+int march_prolong(el_ctx* ctx, const float* x, const float* b, float* t, Scalars* s);
+int march_last(el_ctx* ctx, const float* t, const float* b, float* x, Scalars* s, int dot);
 
 // ---------------------------------------------------------------------------------------
 // launch geometry: stencil kernels use blocks of 32 x 8 threads over (i, j) marching a chunk

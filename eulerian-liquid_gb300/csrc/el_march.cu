@@ -1,0 +1,800 @@
+// el_march.cu -- the finest level of the FP32 multigrid PCG (the mixed-precision solver's inner
+// iterations) as z-marching tile kernels with TMA-staged halo planes.
+//
+// The segment kernels of el_solve.cu give every warp one 32-cell row and fetch its +-y and +-z
+// rows again from L2; those rows are shared with four other warps, so each stencil value is
+// read about five times and the kernels wait on L2 latency.  Here a CTA owns a tile of 32 (i) x
+// 16 (j) cells and marches it along k: every plane of every staged array arrives once, by one
+// cp.async.bulk.tensor copy of a 40 x 18 box (the tile, one row above and below, four cells left
+// and right so that the box starts on a 16-byte boundary; a record box one or two cells, its
+// nearest boundary) into a ring of shared-memory plane buffers, and the 7-point stencil reads its -z / centre / +z planes and its +-y rows from
+// shared memory.  Copies of the next planes are in flight while a plane is computed (one
+// mbarrier per ring slot, transaction-counted); the box's parts outside the grid arrive as
+// zeros, which is the zero value and zero coupling the segment kernels use there.
+//
+// A CTA is eight compute warps (one per tile row) and a producer warp whose one thread issues
+// the copies: full / empty mbarrier pairs per ring slot, no CTA-wide barrier per plane.  CTAs
+// take the work items round robin, so the CTAs running at any moment hold neighbouring tiles of
+// the same planes and read each other's halo rows from L2 rather than from DRAM; a CTA's planes
+// stream in one sequence across its items.
+//
+// Kernels (one launch each, over the work items of el::MarchPlan):
+//   DIRSPMV   p' = z + beta p ; Ap' ; p'.Ap'                            (K1 of a PCG iteration)
+//   UPDZ      x += alpha p ; r' = r - alpha Ap ; |r'|^2 ; and the first two smoothing sweeps of
+//             the V-cycle on r', from zero (update fused with the pre-smoother: r' is formed
+//             from r and Ap in shared memory wherever the stencil needs it)
+//   ZERO2     the two sweeps from zero alone (the V-cycle that starts a refinement sweep)
+//   RESTRICT  residual of the pre-smoothed level summed over 2x2x2 blocks onto the coarse rhs
+//   PROLONG   one sweep from x + P e (e = the coarse correction)
+//   LAST      the last sweep, and r.z for beta
+// The expressions and their order are those of el_solve.cu's dir_spmv_rec_kernel,
+// update_kernel, smooth_kernel and restrict_kernel; only the dot products' summation order
+// differs (per CTA instead of per segment warp).
+//
+// Conditions (el::march_supported): the finest level's rows are a multiple of 16 bytes (ni a
+// multiple of 8, so that the next level's rows are too) -- a tensor map's strides must be.
+// Other grids keep the segment kernels.
+
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "el_internal.cuh"
+
+namespace el {
+
+namespace {
+
+constexpr int kTI = 32;          // tile cells along i (one warp's lanes)
+constexpr int kTJ = 16;          // tile rows along j (two per compute warp)
+constexpr int kHX = 40;          // staged row: i0 - 4 .. i0 + 35
+constexpr int kHY = kTJ + 2;     // staged rows: j0 - 1 .. j0 + 16
+constexpr int kCX = 24;          // staged coarse row: i0/2 - 4 .. i0/2 + 19
+constexpr int kCY = kTJ / 2 + 2; // staged coarse rows: j0/2 - 1 .. j0/2 + 8
+constexpr int kComputeWarps = kTJ / 2;             // rows 2w and 2w + 1 each
+constexpr int kThreads = 32 * (kComputeWarps + 1);  // and one producer warp
+constexpr int kStages = 6;       // plane buffers in the ring: three in use, three in flight
+constexpr unsigned kFull = 0xffffffffu;
+// a bounded wait: this many polls (each try_wait may itself suspend for a while) before the
+// kernel gives up, records the fault and stops
+constexpr long long kWaitPolls = 1ll << 24;
+
+enum Mode { DIRSPMV = 0, UPDZ = 1, ZERO2 = 2, RESTRICT = 3, PROLONG = 4, LAST = 5 };
+
+// staged arrays of a mode: halo f32 arrays (40 x 18), the record halo (float4 or half4 records,
+// 34 / 36 x 18), centre f32 arrays (32 x 16), the coarse box (24 x 10)
+template <int M>
+struct Layout {
+    static constexpr int nhalo = M == DIRSPMV ? 2 : (M == UPDZ ? 2 : 1);
+    static constexpr int ncentre = M == UPDZ ? 2 : (M == ZERO2 || M == DIRSPMV ? 0 : 1);
+    static constexpr bool coarse = M == PROLONG;
+    static constexpr int rec_bytes = M == DIRSPMV ? 16 : 8;
+    // the record box starts one (float4) or two (half4) cells left of the tile, the nearest
+    // 16-byte boundary, and ends as far right of it
+    static constexpr int rec_x0 = M == DIRSPMV ? 1 : 2;
+    static constexpr int rec_w = kTI + 2 * rec_x0;                // 34 / 36
+    static constexpr int halo_bytes = kHX * kHY * 4;             // 2880
+    static constexpr int rec_box_bytes = rec_w * kHY * rec_bytes; // 9792 / 5184
+    static constexpr int centre_bytes = kTI * kTJ * 4;           // 2048
+    static constexpr int coarse_bytes = kCX * kCY * 4;           // 960
+    static constexpr int al(int b) { return (b + 127) / 128 * 128; }
+    static constexpr int off_rec = 0;
+    static constexpr int off_halo = al(rec_box_bytes);
+    static constexpr int off_centre = off_halo + nhalo * al(halo_bytes);
+    static constexpr int off_coarse = off_centre + ncentre * al(centre_bytes);
+    static constexpr int stage = al(off_coarse + (coarse ? coarse_bytes : 0));
+    static constexpr int smem = 128 + kStages * stage + 128;  // barriers first; alignment slack
+    static_assert(2 * kStages * 8 <= 128, "barriers fit in front of the ring");
+};
+
+struct Maps {
+    CUtensorMap halo[2];
+    CUtensorMap rec;
+    CUtensorMap centre[2];
+    CUtensorMap coarse;
+};
+
+struct Args {
+    int n0, n1, n2;             // the level
+    int c0, c1, c2;             // the next coarser level (RESTRICT, PROLONG)
+    const int4* items;
+    const int* count;
+    float* out0;
+    float* out1;
+    float* out2;
+    Scalars* s;
+    double* partials;
+    unsigned* counter;
+    int first;                  // DIRSPMV: first iteration (p' = z)
+    int dot;                    // LAST: DOT_INIT (1) or DOT_BETA (2)
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait for the completion of the phase with the given parity
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+    for (long long n = 0; n < kWaitPolls; ++n)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ float mg_divf(float a, float b) { return __fdividef(a, b); }
+
+// records of a staged plane: {diagonal, +x, +y, +z couplings}
+struct Rc {
+    float d, x, y, z;
+};
+__device__ __forceinline__ Rc ld_rec(const unsigned char* base, int idx, int bytes) {
+    if (bytes == 16) {
+        const float4 v = reinterpret_cast<const float4*>(base)[idx];
+        return {v.x, v.y, v.z, v.w};
+    }
+    const ushort4 v = reinterpret_cast<const ushort4*>(base)[idx];
+    return {__half2float(__ushort_as_half(v.x)), __half2float(__ushort_as_half(v.y)),
+            __half2float(__ushort_as_half(v.z)), __half2float(__ushort_as_half(v.w))};
+}
+
+// the 7 values and couplings of one cell's stencil; value(plane, y, x) is a staged value with
+// plane 0 = k-1, 1 = k, 2 = k+1 and (y, x) staged-box coordinates
+struct S7 {
+    float v0, vxm, vxp, vym, vyp, vzm, vzp;
+    float d, cxm, cxp, cym, cyp, czm, czp;
+};
+__device__ __forceinline__ float apply7(const S7& st) {
+    return st.d * st.v0 + st.cxm * st.vxm + st.cxp * st.vxp + st.cym * st.vym + st.cyp * st.vyp + st.czm * st.vzm +
+           st.czp * st.vzp;
+}
+
+template <int M>
+__device__ __forceinline__ unsigned char* stage_ptr(unsigned char* smem, int slot) {
+    return smem + 128 + slot * Layout<M>::stage;
+}
+
+// the dynamic shared memory, rounded up to a 128-byte boundary (the launch reserves the slack)
+__device__ __forceinline__ unsigned char* aligned_smem(unsigned char* raw) {
+    const unsigned a = smem_u32(raw);
+    return raw + ((128u - (a & 127u)) & 127u);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+
+// a half record's diagonal is positive: sign bit clear and not zero
+__device__ __forceinline__ bool dpos(const unsigned char* rec, int idx, int bytes) {
+    if (bytes == 16) return reinterpret_cast<const float4*>(rec)[idx].x > 0.f;
+    return static_cast<short>(reinterpret_cast<const ushort4*>(rec)[idx].x) > 0;
+}
+
+template <int M>
+__global__ void __launch_bounds__(kThreads) march_kernel(const __grid_constant__ Maps maps, const Args a) {
+    using L = Layout<M>;
+    Scalars* s = a.s;
+    if (s->done) return;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char* smem = aligned_smem(smem_raw);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem);   // a plane landed (transaction count)
+    uint64_t* empty = full + kStages;                     // every compute warp is done with it
+    __shared__ volatile int abort_flag;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, w = tid >> 5;
+    const int n = *a.count;
+    const int G = gridDim.x, b = blockIdx.x;
+    if (tid == 0) {
+        abort_flag = 0;
+        for (int q = 0; q < kStages; ++q) {
+            mbar_init(&full[q], 1);
+            mbar_init(&empty[q], kComputeWarps);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    float part = 0.f;  // this thread's share of the mode's dot product
+
+    if (w == kComputeWarps) {
+        // ---- producer warp: one thread streams the planes of this CTA's items ------------
+        if (lane == 0) {
+            const int nhalo = (M == DIRSPMV && a.first) ? 1 : L::nhalo;
+            const unsigned tx = (unsigned)(L::rec_box_bytes + nhalo * L::halo_bytes + L::ncentre * L::centre_bytes +
+                                           (L::coarse ? L::coarse_bytes : 0));
+            int slot = 0, round = 0, issued = 0;
+            for (int it = b; it < n && !abort_flag; it += G) {
+                const int4 d = a.items[it];
+                const int i0 = d.x, j0 = d.y;
+                for (int k = d.z - 1; k <= d.w; ++k) {
+                    // the slot's previous plane must have been released by every compute warp
+                    if (round > 0 && !mbar_wait(&empty[slot], (unsigned)((round - 1) & 1))) {
+                        abort_flag = 1;
+                        break;
+                    }
+                    unsigned char* st = stage_ptr<M>(smem, slot);
+                    uint64_t* bar = &full[slot];
+                    mbar_expect_tx(bar, tx);
+                    tma_load_3d(st + L::off_rec, &maps.rec, bar, 4 * (i0 - L::rec_x0), j0 - 1, k);
+                    for (int h = 0; h < nhalo; ++h)
+                        tma_load_3d(st + L::off_halo + h * L::al(L::halo_bytes), &maps.halo[h], bar, i0 - 4, j0 - 1, k);
+                    for (int c = 0; c < L::ncentre; ++c)
+                        tma_load_3d(st + L::off_centre + c * L::al(L::centre_bytes), &maps.centre[c], bar, i0, j0, k);
+                    if (L::coarse) tma_load_3d(st + L::off_coarse, &maps.coarse, bar, i0 / 2 - 4, j0 / 2 - 1, k >> 1);
+                    ++issued;
+                    if (++slot == kStages) {
+                        slot = 0;
+                        ++round;
+                    }
+                }
+            }
+            if (abort_flag) {
+                // a fault: no copy may still be in flight when the CTA's shared memory goes
+                for (int q = (issued > kStages ? issued - kStages : 0); q < issued; ++q)
+                    mbar_wait(&full[q % kStages], (unsigned)((q / kStages) & 1));
+            }
+        }
+    } else {
+        // ---- compute warps: warp w owns rows j0 + 2w and j0 + 2w + 1, lane l cell i0 + l ---
+        const float alpha = (M == UPDZ) ? (float)s->alpha : 0.f;
+        const float beta = (M == DIRSPMV && !a.first) ? (float)s->beta : 0.f;
+        const float w1 = (float)kSweep1, w2 = (float)kSweep2;
+        bool ok = true;
+        int wslot = 0;        // the next plane to wait for: its slot and phase parity
+        unsigned wpar = 0;
+        int rslot = 0;        // the next plane to release
+        auto wait_next = [&]() -> int {
+            const int sl = wslot;
+            if (ok && !mbar_wait(&full[sl], wpar)) {
+                ok = false;
+                abort_flag = 1;
+            }
+            if (++wslot == kStages) {
+                wslot = 0;
+                wpar ^= 1u;
+            }
+            return sl;
+        };
+        auto release_next = [&]() {
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[rslot]);
+            if (++rslot == kStages) rslot = 0;
+        };
+        for (int it = b; it < n && ok; it += G) {
+            const int4 d = a.items[it];
+            const int i0 = d.x, j0 = d.y, k0 = d.z, k1 = d.w;
+            const int i = i0 + lane;
+            int sa = wait_next(), sb = wait_next();  // planes k0 - 1 and k0
+            float racc0 = 0.f;                     // RESTRICT: this lane's 2x2 (j, k) sum
+            for (int k = k0; k < k1; ++k) {
+                const int sc = wait_next();        // plane k + 1
+                if (!ok) break;
+                const unsigned char* P[3] = {stage_ptr<M>(smem, sa), stage_ptr<M>(smem, sb), stage_ptr<M>(smem, sc)};
+                auto H = [&](int pl, int h, int idx) -> float {
+                    return reinterpret_cast<const float*>(P[pl] + L::off_halo + h * L::al(L::halo_bytes))[idx];
+                };
+                auto Cn = [&](int c, int row) -> float {
+                    return reinterpret_cast<const float*>(P[1] + L::off_centre + c * L::al(L::centre_bytes))[row * kTI + lane];
+                };
+                auto R = [&](int pl, int idx) -> Rc { return ld_rec(P[pl] + L::off_rec, idx, L::rec_bytes); };
+                auto D = [&](int pl, int idx) -> bool { return dpos(P[pl] + L::off_rec, idx, L::rec_bytes); };
+                float res[2];  // RESTRICT: the two rows' residuals
+#pragma unroll
+                for (int r = 0; r < 2; ++r) {
+                    const int row = 2 * w + r;
+                    const int j = j0 + row;
+                    const bool live = i < a.n0 && j < a.n1;
+                    const int hc = (row + 1) * kHX + lane + 4;               // in a staged value box
+                    const int rc = (row + 1) * L::rec_w + lane + L::rec_x0;  // in the staged record box
+                    // records of the stencil: the cell's own ({d, +x, +y, +z}), and the -x, -y,
+                    // -z neighbours' (their +x/+y/+z couplings are the cell's -x/-y/-z ones)
+                    const Rc r0 = R(1, rc);
+                    S7 st;
+                    st.d = r0.d;
+                    st.cxp = r0.x;
+                    st.cyp = r0.y;
+                    st.czp = r0.z;
+                    st.cxm = R(1, rc - 1).x;
+                    st.cym = R(1, rc - L::rec_w).y;
+                    st.czm = R(0, rc).z;
+                    // stencil points: centre, -x, +x, -y, +y (plane k), -z (k - 1), +z (k + 1)
+                    const int vo[7] = {0, -1, 1, -kHX, kHX, 0, 0};
+                    const int ro[7] = {0, -1, 1, -L::rec_w, L::rec_w, 0, 0};
+                    const int pq[7] = {1, 1, 1, 1, 1, 0, 2};
+                    const int c = i + a.n0 * (j + a.n1 * k);
+                    if (M == DIRSPMV) {
+                        // p' = z + beta p at every stencil point; Ap' and p'.Ap' at the cell
+                        float v[7];
+#pragma unroll
+                        for (int q = 0; q < 7; ++q) {
+                            const float zq = H(pq[q], 0, hc + vo[q]);
+                            v[q] = a.first ? zq : zq + beta * H(pq[q], 1, hc + vo[q]);
+                        }
+                        st.v0 = v[0];
+                        st.vxm = v[1];
+                        st.vxp = v[2];
+                        st.vym = v[3];
+                        st.vyp = v[4];
+                        st.vzm = v[5];
+                        st.vzp = v[6];
+                        float pc = 0.f, apc = 0.f;
+                        if (st.d > 0.f) {
+                            pc = st.v0;
+                            apc = apply7(st);
+                        }
+                        if (live) {
+                            a.out0[c] = pc;
+                            a.out1[c] = apc;
+                            part += pc * apc;
+                        }
+                    } else {
+                        // every other mode masks the stencil's values by the points' diagonals
+                        bool dp[7];
+#pragma unroll
+                        for (int q = 0; q < 7; ++q) dp[q] = q == 0 ? (r0.d > 0.f) : D(pq[q], rc + ro[q]);
+                        if (M == UPDZ || M == ZERO2) {
+                            // b = r' = r - alpha Ap (UPDZ) or b (ZERO2) at every stencil point; the
+                            // first sweep from zero is pointwise, x1 = w1 b / D on cells with D > 0
+                            float x1[7];
+                            float bc = 0.f;
+#pragma unroll
+                            for (int q = 0; q < 7; ++q) {
+                                const int idx = hc + vo[q];
+                                const float bq =
+                                    M == UPDZ ? H(pq[q], 0, idx) - alpha * H(pq[q], 1, idx) : H(pq[q], 0, idx);
+                                if (q == 0) bc = bq;
+                                x1[q] = dp[q] ? mg_divf(w1 * bq, q == 0 ? r0.d : R(pq[q], rc + ro[q]).d) : 0.f;
+                            }
+                            st.v0 = x1[0];
+                            st.vxm = x1[1];
+                            st.vxp = x1[2];
+                            st.vym = x1[3];
+                            st.vyp = x1[4];
+                            st.vzm = x1[5];
+                            st.vzp = x1[6];
+                            float x2 = 0.f;
+                            if (dp[0]) x2 = st.v0 + mg_divf(w2 * (bc - apply7(st)), st.d);
+                            if (live) {
+                                if (M == UPDZ) {
+                                    // x += alpha p; r' out of place.  A tile also covers cells
+                                    // outside the system (diagonal 0), whose r may still hold an
+                                    // earlier solve's values: their r' is 0 and they stay out of
+                                    // |r'|^2, as in the segment kernels (where r is 0 on every
+                                    // such cell of an active segment).
+                                    const float rn = dp[0] ? bc : 0.f;
+                                    a.out0[c] = Cn(0, row) + alpha * Cn(1, row);
+                                    a.out1[c] = rn;
+                                    part += rn * rn;
+                                    a.out2[c] = x2;
+                                } else {
+                                    a.out0[c] = x2;
+                                }
+                            }
+                        } else {
+                            // RESTRICT / PROLONG / LAST: the level's values at the stencil points
+                            float v[7];
+#pragma unroll
+                            for (int q = 0; q < 7; ++q) {
+                                float raw = H(pq[q], 0, hc + vo[q]);
+                                if (M == PROLONG) {
+                                    // + the coarse parent's correction; each ring slot holds the
+                                    // coarse plane of its fine plane
+                                    const int fi = lane + (q == 1 ? -1 : (q == 2 ? 1 : 0));
+                                    const int fj = row + (q == 3 ? -1 : (q == 4 ? 1 : 0));
+                                    const int cx = (fi >> 1) + 4, cy = (fj >> 1) + 1;
+                                    raw += reinterpret_cast<const float*>(P[pq[q]] + L::off_coarse)[cy * kCX + cx];
+                                }
+                                v[q] = dp[q] ? raw : 0.f;
+                            }
+                            st.v0 = v[0];
+                            st.vxm = v[1];
+                            st.vxp = v[2];
+                            st.vym = v[3];
+                            st.vyp = v[4];
+                            st.vzm = v[5];
+                            st.vzp = v[6];
+                            const float bc = Cn(0, row);
+                            if (M == RESTRICT) {
+                                res[r] = dp[0] ? bc - apply7(st) : 0.f;
+                            } else {
+                                const float omega = M == PROLONG ? w1 : w2;
+                                float xo = 0.f;
+                                if (dp[0]) xo = st.v0 + mg_divf(omega * (bc - apply7(st)), st.d);
+                                if (live) {
+                                    a.out0[c] = xo;
+                                    if (M == LAST) part += bc * xo;
+                                }
+                            }
+                        }
+                    }
+                }
+                if (M == RESTRICT) {
+                    // the residuals summed over 2x2x2 blocks onto the coarse rhs: the thread's two
+                    // rows are a j pair, the k pairs add in registers, the i pairs by shuffle
+                    racc0 = (k & 1) ? (racc0 + res[0]) + res[1] : res[0] + res[1];
+                    if ((k & 1) || k + 1 == a.n2) {
+                        const float pr = racc0 + __shfl_down_sync(kFull, racc0, 1);
+                        const int I = i0 / 2 + (lane >> 1), J = j0 / 2 + w, K = k >> 1;
+                        if (!(lane & 1) && I < a.c0 && J < a.c1) a.out0[I + a.c0 * (J + a.c1 * K)] = pr;
+                        racc0 = 0.f;
+                    }
+                }
+                release_next();  // plane k - 1 is not read again
+                sa = sb;
+                sb = sc;
+            }
+            if (!ok) break;
+            // the item's last two planes are not needed any more
+            release_next();
+            release_next();
+        }
+    }
+    __syncthreads();
+    if (abort_flag && tid == 0) {
+        s->fault = 1;
+        s->bad = 1;
+        s->done = 1;
+    }
+    if (M == DIRSPMV || M == UPDZ || M == LAST) {
+        double acc[1] = {(double)part};
+        double tot[1];
+        if (grid_sum<1>(acc, a.partials, a.counter, tot)) {
+            if (M == DIRSPMV) {
+                const double al = s->rz / tot[0];
+                s->alpha = al;
+                if (!isfinite(al)) {
+                    s->bad = 1;
+                    s->done = 1;
+                }
+            } else if (M == UPDZ) {
+                s->rr = tot[0];
+                s->iter += 1;
+                if (!isfinite(tot[0])) {
+                    s->bad = 1;
+                    s->done = 1;
+                } else if (tot[0] < s->thresh) {
+                    s->done = 1;
+                }
+            } else {
+                if (a.dot == 2) s->beta = tot[0] / s->rz;
+                s->rz = tot[0];
+                if (!isfinite(tot[0])) {
+                    s->bad = 1;
+                    s->done = 1;
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// work items: tiles of 32 x 16 cells x kMarchPlanes planes holding a cell with a positive
+// diagonal, in the order i-tile fastest, then j-tile, then plane chunk
+
+__global__ void march_flags_kernel(int n0, int n1, int n2, int nib, int njb, const ushort4* __restrict__ rec,
+                                   uint8_t* __restrict__ flags) {
+    const int item = blockIdx.x;
+    const int ib = item % nib, jb = (item / nib) % njb, kc = item / (nib * njb);
+    const int i = ib * kTI + (threadIdx.x & 31), j = jb * kTJ + (threadIdx.x >> 5);
+    const int k0 = kc * kMarchPlanes, k1 = min(n2, k0 + kMarchPlanes);
+    int act = 0;
+    if (i < n0 && j < n1)
+        for (int k = k0; k < k1 && !act; ++k)
+            act = __half2float(__ushort_as_half(rec[i + n0 * (j + n1 * k)].x)) > 0.f;
+    act = __syncthreads_or(act);
+    if (threadIdx.x == 0) flags[item] = act ? 1 : 0;
+}
+
+// ordered compaction of the flags (one block)
+__global__ void march_compact_kernel(int total, int nib, int njb, int n2, const uint8_t* __restrict__ flags,
+                                     int4* __restrict__ items, int* __restrict__ count) {
+    __shared__ int scan[1024];
+    const int t = threadIdx.x;
+    const int per = (total + blockDim.x - 1) / blockDim.x;
+    const int lo = min(total, t * per), hi = min(total, lo + per);
+    int c = 0;
+    for (int q = lo; q < hi; ++q) c += flags[q];
+    scan[t] = c;
+    __syncthreads();
+    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+        const int v = t >= o ? scan[t - o] : 0;
+        __syncthreads();
+        scan[t] += v;
+        __syncthreads();
+    }
+    int run = scan[t] - c;
+    for (int q = lo; q < hi; ++q)
+        if (flags[q]) {
+            const int ib = q % nib, jb = (q / nib) % njb, kc = q / (nib * njb);
+            const int k0 = kc * kMarchPlanes;
+            items[run++] = make_int4(ib * kTI, jb * kTJ, k0, min(n2, k0 + kMarchPlanes));
+        }
+    if (t == blockDim.x - 1) *count = scan[t];
+}
+
+// ---------------------------------------------------------------------------------------
+// host side
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// a 3-D tensor map over an i-fastest array of (d0 elements of `type`) x n1 x n2
+bool encode(CUtensorMap* map, CUtensorMapDataType type, int esize, const void* base, long long d0, int n1, int n2,
+            long long row_elems, unsigned bx, unsigned by) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)d0, (cuuint64_t)n1, (cuuint64_t)n2};
+    const cuuint64_t strides[2] = {(cuuint64_t)(row_elems * esize), (cuuint64_t)(row_elems * esize * n1)};
+    const cuuint32_t box[3] = {bx, by, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return fn(map, type, 3, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int M>
+int smem_bytes() {
+    return Layout<M>::smem;
+}
+
+// dynamic shared memory, and the CTAs of the mode one SM holds (the grid is that many per SM,
+// or the number of tiles when smaller)
+template <int M>
+int set_smem(el_ctx* ctx) {
+    EL_CUDA_TRY(ctx, cudaFuncSetAttribute(march_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          smem_bytes<M>()));
+    int per_sm = 0;
+    EL_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_kernel<M>, kThreads, smem_bytes<M>()));
+    ctx->march.per_sm[M] = std::max(1, per_sm);
+    return EL_OK;
+}
+
+template <int M>
+int march_grid(el_ctx* ctx) {
+    const MarchPlan& mp = ctx->march;
+    const long long total = (long long)mp.nib * mp.njb * mp.nkc;
+    return (int)std::max<long long>(1, std::min<long long>(total, (long long)ctx->num_sms * mp.per_sm[M]));
+}
+
+template <int M>
+void launch(el_ctx* ctx, const Maps& maps, const Args& a) {
+    march_kernel<M><<<march_grid<M>(ctx), kThreads, smem_bytes<M>(), ctx->stream>>>(maps, a);
+}
+
+Args base_args(el_ctx* ctx, Scalars* s) {
+    Args a{};
+    a.n0 = ctx->ni;
+    a.n1 = ctx->nj;
+    a.n2 = ctx->nk;
+    const auto& mg = ctx->mg32;
+    if (mg.size() > 1) {
+        a.c0 = mg[1].n0;
+        a.c1 = mg[1].n1;
+        a.c2 = mg[1].n2;
+    }
+    a.items = ctx->march.items;
+    a.count = ctx->march.count;
+    a.s = s;
+    a.partials = ctx->partials;
+    a.counter = ctx->counter;
+    return a;
+}
+
+int halo_index(el_ctx* ctx, const float* v) {
+    if (v == ctx->z32) return MarchPlan::Z;
+    if (v == ctx->p32) return MarchPlan::P;
+    if (v == ctx->p32b) return MarchPlan::PB;
+    if (v == ctx->ap32) return MarchPlan::AP;
+    if (v == ctx->r32) return MarchPlan::R;
+    if (v == ctx->r32b) return MarchPlan::RB;
+    if (!ctx->mg32.empty() && v == ctx->mg32[0].t) return MarchPlan::T;
+    return -1;
+}
+
+int centre_index(el_ctx* ctx, const float* v) {
+    if (v == ctx->x32) return MarchPlan::CX;
+    if (v == ctx->p32) return MarchPlan::CP;
+    if (v == ctx->p32b) return MarchPlan::CPB;
+    if (v == ctx->r32) return MarchPlan::CR;
+    if (v == ctx->r32b) return MarchPlan::CRB;
+    return -1;
+}
+
+}  // namespace
+
+bool march_supported(const el_ctx* ctx) {
+    return ctx->dtype == EL_F32 && ctx->ni % 8 == 0 && ctx->ni >= 64 && ctx->nj >= 16 && ctx->nk >= 16 &&
+           ctx->mg32.size() >= 3 && encode_fn() != nullptr;
+}
+
+// Tensor maps and the work-item storage, once per context (the arrays never move).
+int march_setup(el_ctx* ctx) {
+    MarchPlan& mp = ctx->march;
+    mp.on = false;
+    if (!march_supported(ctx)) return EL_OK;
+    const int ni = ctx->ni, nj = ctx->nj, nk = ctx->nk;
+    mp.nib = (ni + kTI - 1) / kTI;
+    mp.njb = (nj + kTJ - 1) / kTJ;
+    mp.nkc = (nk + kMarchPlanes - 1) / kMarchPlanes;
+    const long long total = (long long)mp.nib * mp.njb * mp.nkc;
+    mp.items = (int4*)ctx_alloc(ctx, total * sizeof(int4));
+    mp.count = (int*)ctx_alloc(ctx, sizeof(int));
+    mp.flags = (uint8_t*)ctx_alloc(ctx, total);
+    if (!mp.items || !mp.count || !mp.flags) return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "march items");
+    const float* halo_src[MarchPlan::NHALO] = {ctx->z32,   ctx->p32, ctx->p32b, ctx->ap32,
+                                               ctx->r32,   ctx->r32b, ctx->mg32[0].t};
+    bool ok = true;
+    for (int h = 0; h < MarchPlan::NHALO; ++h)
+        ok = ok && encode(&mp.halo[h], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, halo_src[h], ni, nj, nk, ni, kHX, kHY);
+    const float* centre_src[MarchPlan::NCENTRE] = {ctx->x32, ctx->p32, ctx->p32b, ctx->r32, ctx->r32b};
+    for (int c = 0; c < MarchPlan::NCENTRE; ++c)
+        ok = ok && encode(&mp.centre[c], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, centre_src[c], ni, nj, nk, ni, kTI, kTJ);
+    // records: four components per cell as the innermost dimension
+    ok = ok && encode(&mp.rec32, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, ctx->A32, 4ll * ni, nj, nk, 4ll * ni,
+                      4 * Layout<DIRSPMV>::rec_w, kHY);
+    ok = ok && encode(&mp.rec16, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, ctx->A16, 4ll * ni, nj, nk, 4ll * ni,
+                      4 * Layout<LAST>::rec_w, kHY);
+    const auto& C = ctx->mg32[1];
+    ok = ok && encode(&mp.coarse_x, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, C.x, C.n0, C.n1, C.n2, C.n0, kCX, kCY);
+    if (!ok) return EL_OK;  // the segment kernels stay in use
+    int rc;
+    if ((rc = set_smem<DIRSPMV>(ctx)) != EL_OK || (rc = set_smem<UPDZ>(ctx)) != EL_OK ||
+        (rc = set_smem<ZERO2>(ctx)) != EL_OK || (rc = set_smem<RESTRICT>(ctx)) != EL_OK ||
+        (rc = set_smem<PROLONG>(ctx)) != EL_OK || (rc = set_smem<LAST>(ctx)) != EL_OK)
+        return rc;
+    mp.on = true;
+    return EL_OK;
+}
+
+// Work items of the system just packed (A16 written): 2 launches.
+int march_enqueue_items(el_ctx* ctx) {
+    const MarchPlan& mp = ctx->march;
+    const int total = mp.nib * mp.njb * mp.nkc;
+    march_flags_kernel<<<total, kTI * kTJ, 0, ctx->stream>>>(ctx->ni, ctx->nj, ctx->nk, mp.nib, mp.njb, ctx->A16,
+                                                            mp.flags);
+    march_compact_kernel<<<1, 1024, 0, ctx->stream>>>(total, mp.nib, mp.njb, ctx->nk, mp.flags, mp.items, mp.count);
+    return 2;
+}
+
+// K1: p_out = z + beta p_in, ap = A p_out, alpha
+int march_dir_spmv(el_ctx* ctx, const float* z, const float* p_in, float* p_out, float* ap, Scalars* s, int first) {
+    const MarchPlan& mp = ctx->march;
+    Maps maps;
+    std::memset(&maps, 0, sizeof(maps));
+    maps.halo[0] = mp.halo[halo_index(ctx, z)];
+    maps.halo[1] = mp.halo[halo_index(ctx, p_in)];
+    maps.rec = mp.rec32;
+    Args a = base_args(ctx, s);
+    a.out0 = p_out;
+    a.out1 = ap;
+    a.first = first;
+    launch<DIRSPMV>(ctx, maps, a);
+    return 1;
+}
+
+// K2 fused with the pre-smoother: x += alpha p; r_out = r_in - alpha ap; |r_out|^2; z = two
+// sweeps from zero on r_out
+int march_update_smooth(el_ctx* ctx, float* x, const float* p, const float* r_in, float* r_out, const float* ap,
+                        float* z, Scalars* s) {
+    const MarchPlan& mp = ctx->march;
+    Maps maps;
+    std::memset(&maps, 0, sizeof(maps));
+    maps.halo[0] = mp.halo[halo_index(ctx, r_in)];
+    maps.halo[1] = mp.halo[halo_index(ctx, ap)];
+    maps.rec = mp.rec16;
+    maps.centre[0] = mp.centre[centre_index(ctx, x)];
+    maps.centre[1] = mp.centre[centre_index(ctx, p)];
+    Args a = base_args(ctx, s);
+    a.out0 = x;
+    a.out1 = r_out;
+    a.out2 = z;
+    launch<UPDZ>(ctx, maps, a);
+    return 1;
+}
+
+// two sweeps from zero: z = S(b)
+int march_zero2(el_ctx* ctx, const float* b, float* z, Scalars* s) {
+    const MarchPlan& mp = ctx->march;
+    Maps maps;
+    std::memset(&maps, 0, sizeof(maps));
+    maps.halo[0] = mp.halo[halo_index(ctx, b)];
+    maps.rec = mp.rec16;
+    Args a = base_args(ctx, s);
+    a.out0 = z;
+    launch<ZERO2>(ctx, maps, a);
+    return 1;
+}
+
+// coarse rhs = P^T (b - A x)
+int march_restrict(el_ctx* ctx, const float* x, const float* b, float* coarse_b, Scalars* s) {
+    const MarchPlan& mp = ctx->march;
+    Maps maps;
+    std::memset(&maps, 0, sizeof(maps));
+    maps.halo[0] = mp.halo[halo_index(ctx, x)];
+    maps.rec = mp.rec16;
+    maps.centre[0] = mp.centre[centre_index(ctx, b)];
+    Args a = base_args(ctx, s);
+    a.out0 = coarse_b;
+    launch<RESTRICT>(ctx, maps, a);
+    return 1;
+}
+
+// t = one sweep from x + P e (e = the next level's x)
+int march_prolong(el_ctx* ctx, const float* x, const float* b, float* t, Scalars* s) {
+    const MarchPlan& mp = ctx->march;
+    Maps maps;
+    std::memset(&maps, 0, sizeof(maps));
+    maps.halo[0] = mp.halo[halo_index(ctx, x)];
+    maps.rec = mp.rec16;
+    maps.centre[0] = mp.centre[centre_index(ctx, b)];
+    maps.coarse = mp.coarse_x;
+    Args a = base_args(ctx, s);
+    a.out0 = t;
+    launch<PROLONG>(ctx, maps, a);
+    return 1;
+}
+
+// x = the last sweep from t, and b.x (dot = 1: rz; 2: beta and rz)
+int march_last(el_ctx* ctx, const float* t, const float* b, float* x, Scalars* s, int dot) {
+    const MarchPlan& mp = ctx->march;
+    Maps maps;
+    std::memset(&maps, 0, sizeof(maps));
+    maps.halo[0] = mp.halo[halo_index(ctx, t)];
+    maps.rec = mp.rec16;
+    maps.centre[0] = mp.centre[centre_index(ctx, b)];
+    Args a = base_args(ctx, s);
+    a.out0 = x;
+    a.dot = dot;
+    launch<LAST>(ctx, maps, a);
+    return 1;
+}
+
+}  // namespace el

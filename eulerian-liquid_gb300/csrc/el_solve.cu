@@ -45,18 +45,7 @@ namespace el {
 // Damped Jacobi on the coarsest level (a solve): the damping that balances the 3-D 7-point
 // Laplacian's high-frequency error reduction.
 constexpr double kOmega = 6.0 / 7.0;
-// The smoother: two Jacobi sweeps with weights 1/t1 and 1/t2, t1,2 the roots of the degree-2
-// Chebyshev polynomial on [1/3, 2] -- the high-frequency part of the spectrum of D^-1 A (a
-// 7-point operator with D >= the sum of its couplings' magnitudes has its spectrum in [0, 2];
-// modes with a wave number past pi/2 on any axis have lambda >= 1/3).  Two sweeps apply
-// (1 - w1 D^-1 A)(1 - w2 D^-1 A), which reduces that band by at most 1/T2(7/5) = 0.34, against
-// 0.51 for two sweeps at 6/7, for the same work; and, a polynomial in D^-1 A, the smoother is
-// self-adjoint in the A inner product and contracts on (0, 2], so the V-cycle stays a
-// symmetric positive definite preconditioner.  The first sweep of a pair takes w1, the second
-// w2 (before and after the coarse correction alike).
-constexpr double kChebMid = 7.0 / 6.0, kChebHalf = 5.0 / 6.0;
-constexpr double kSweep1 = 1.0 / (kChebMid + kChebHalf * 0.70710678118654752);  // 0.5695
-constexpr double kSweep2 = 1.0 / (kChebMid - kChebHalf * 0.70710678118654752);  // 1.7319
+// The smoother's sweep weights kSweep1 / kSweep2 are defined in el_internal.cuh.
 constexpr int kCoarsestSweeps = 30;
 constexpr int kCoarsestMaxDim = 8;
 constexpr int kCoarsestMaxCells = 512;
@@ -574,6 +563,7 @@ __global__ void solve_init_kernel(LGeom g, SegArg seg, const double* __restrict_
         s->outer = 0;
         s->inner_total = 0;
         s->inner_passes = 0;
+        s->fault = 0;
     }
 }
 
@@ -654,6 +644,7 @@ __global__ void inner_init_kernel(LGeom g, SegArg seg, const double* __restrict_
         si->norm = norm;
         si->iter = 0;
         si->bad = 0;
+        si->fault = 0;
         si->beta = 0.0;
         si->done = (tot[0] == 0.0 || tot[0] < si->thresh) ? 1 : 0;
     }
@@ -1226,9 +1217,11 @@ static void launch_smooth(el_ctx* ctx, const MGLevel<V>& F, const SegList& seg, 
 }
 
 // z = M^-1 r with r = mg[0].b and z = mg[0].x; dot = DOT_INIT or DOT_BETA.  R0 / RC are the
-// record types of the finest / coarse levels.
+// record types of the finest / coarse levels.  from > 0: the levels below `from` only (level
+// from - 1 restricted onto mg[from].b before, and prolonged from mg[from].x after, by the caller).
 template <typename V, typename R0, typename RC>
-static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegList& seg0, Scalars* s, int dot) {
+static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegList& seg0, Scalars* s, int dot,
+                          int from = 0) {
     int launched = 0;
     const int L = (int)mg.size();
     auto segof = [&](int l) -> const SegList& { return l == 0 ? seg0 : mg[l].seg; };
@@ -1251,7 +1244,7 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
     const bool fused_bottom = kBottomType && L >= 3 && cells(mg[L - 2]) <= kBottomMaxCells &&
                               cells(mg[L - 1]) <= kCoarsestMaxCells;
     const int pre_end = fused_bottom ? L - 2 : L - 1;  // levels smoothed and restricted by the loops
-    for (int l = 0; l < pre_end; ++l) {
+    for (int l = from; l < pre_end; ++l) {
         MGLevel<V>& F = mg[l];
         MGLevel<V>& C = mg[l + 1];
         const double rb = l == 0 ? sizeof(R0) : sizeof(RC);
@@ -1294,7 +1287,7 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
                                                                          C.b, C.x, kCoarsestSweeps, s);
         ++launched;
     }
-    for (int l = pre_end - 1; l >= 0; --l) {
+    for (int l = pre_end - 1; l >= from; --l) {
         MGLevel<V>& F = mg[l];
         MGLevel<V>& C = mg[l + 1];
         const double rb = l == 0 ? sizeof(R0) : sizeof(RC);
@@ -1320,6 +1313,70 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
         launched += 2;
     }
     return launched;
+}
+
+// The finest level of the FP32 V-cycle by the tile kernels (el_march.cu), from the pre-smoothed
+// level on: restriction, the coarse levels (the segment kernels), prolongation sweep, last sweep
+// with the dot product (dot = DOT_INIT or DOT_BETA).
+static int enqueue_march_vcycle_rest(el_ctx* ctx, std::vector<MGLevel<float>>& mg, Scalars* s, int dot) {
+    MGLevel<float>& F = mg[0];
+    MGLevel<float>& C = mg[1];
+    const double na = active_cells(ctx, 0, (double)F.n0 * F.n1 * F.n2);
+    const double nc = active_cells(ctx, 1, (double)C.n0 * C.n1 * C.n2);
+    int n = 0;
+    {
+        // reads x, b and half4 records; writes the coarse b
+        ProfScope prof(ctx, EL_KC_RESTRICT, na * 16 + nc * 4);
+        n += march_restrict(ctx, F.x, F.b, C.b, s);
+    }
+    n += enqueue_vcycle<float, ushort4, float4>(ctx, mg, ctx->seg0, s, DOT_NONE, 1);
+    {
+        // reads x, b, records and the coarse x; writes t
+        ProfScope prof(ctx, EL_KC_SMOOTH, na * 20 + nc * 4);
+        n += march_prolong(ctx, F.x, F.b, F.t, s);
+    }
+    {
+        // reads t, b, records; writes x
+        ProfScope prof(ctx, EL_KC_SMOOTH, na * 20);
+        n += march_last(ctx, F.t, F.b, F.x, s, dot);
+    }
+    return n;
+}
+
+// z = M^-1 r by the tile kernels on the finest level (the V-cycle that opens a refinement sweep)
+static int enqueue_march_vcycle(el_ctx* ctx, std::vector<MGLevel<float>>& mg, Scalars* s, int dot) {
+    const double na = active_cells(ctx, 0, (double)mg[0].n0 * mg[0].n1 * mg[0].n2);
+    int n = 0;
+    {
+        // reads b and records; writes x
+        ProfScope prof(ctx, EL_KC_SMOOTH, na * 16);
+        n += march_zero2(ctx, mg[0].b, mg[0].x, s);
+    }
+    return n + enqueue_march_vcycle_rest(ctx, mg, s, dot);
+}
+
+// One PCG iteration of the mixed solver's inner system with the finest level on the tile
+// kernels: K1 (direction, A p, alpha), then the update fused with the pre-smoother (x, r out of
+// place, |r|^2, z's first two sweeps), then the rest of the V-cycle.  The direction and the
+// residual each alternate between two buffers; mg[0].b follows r.
+static int enqueue_march_iteration(el_ctx* ctx, float*& p, float*& p_alt, float*& r, float*& r_alt, Scalars* s,
+                                   int first, std::vector<MGLevel<float>>& mg) {
+    const double na = active_cells(ctx, 0, (double)ctx->ni * ctx->nj * ctx->nk);
+    int n = 0;
+    {
+        // reads z, p (not on the first iteration), float4 records; writes p, Ap
+        ProfScope prof(ctx, EL_KC_DIR_SPMV, na * (4.0 * (first ? 3 : 4) + 16));
+        n += march_dir_spmv(ctx, ctx->z32, p, p_alt, ctx->ap32, s, first);
+    }
+    std::swap(p, p_alt);
+    {
+        // reads r, Ap, x, p, half4 records; writes x, r, z
+        ProfScope prof(ctx, EL_KC_UPDATE, na * 36);
+        n += march_update_smooth(ctx, ctx->x32, p, r, r_alt, ctx->ap32, ctx->z32, s);
+    }
+    std::swap(r, r_alt);
+    mg[0].b = r;
+    return n + enqueue_march_vcycle_rest(ctx, mg, s, DOT_BETA);
 }
 
 static int poll(el_ctx* ctx, Scalars* host_copy, int which) {
@@ -1440,7 +1497,7 @@ static void reset_vectors(el_ctx* ctx) {
     const size_t n = (size_t)ctx->ni * ctx->nj * ctx->nk;
     for (double* v : {ctx->x64, ctx->r64, ctx->z64, ctx->p64, ctx->p64b, ctx->ap64})
         if (v) cudaMemsetAsync(v, 0, n * 8, ctx->stream);
-    for (float* v : {ctx->x32, ctx->r32, ctx->z32, ctx->p32, ctx->p32b, ctx->ap32})
+    for (float* v : {ctx->x32, ctx->r32, ctx->r32b, ctx->z32, ctx->p32, ctx->p32b, ctx->ap32})
         if (v) cudaMemsetAsync(v, 0, n * 4, ctx->stream);
     for (auto& L : ctx->mg32) {
         const size_t m = (size_t)L.n0 * L.n1 * L.n2 * 4;
@@ -1452,6 +1509,11 @@ static void reset_vectors(el_ctx* ctx) {
         for (double* v : {L.t, L.rec ? L.b : nullptr, L.rec ? L.x : nullptr})
             if (v) cudaMemsetAsync(v, 0, m, ctx->stream);
     }
+}
+
+// mg[0].b follows the residual buffer during a solve; between solves it is r32 again
+static void mg_restore_pointers(el_ctx* ctx) {
+    if (!ctx->mg32.empty()) ctx->mg32[0].b = ctx->r32;
 }
 
 // Solve A x64 = rhs64 (matrix already built, s0.bb set).  Fills stats.
@@ -1534,15 +1596,26 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
                                                                       ctx->A16);
         }
         ctx->launches += 1 + enqueue_coarsen<float, ushort4, float4>(ctx, mg);
+        const bool march = ctx->march.on && ctx->solver_tiles;
+        if (march) {
+            ProfScope prof(ctx, EL_KC_OTHER, (double)n * 8);
+            ctx->launches += march_enqueue_items(ctx);
+        }
         rc = record_active(ctx, ctx->seg0, ctx->ni, &mg);
         if (rc != EL_OK) return rc;
         Scalars* s1 = ctx->dscal + 1;
         Scalars hi;
         rc = poll(ctx, h, 0);
         int inner_total = 0, outer = 0;
-        float* p = ctx->p32;
-        float* p_alt = ctx->p32b;
+        float *p = ctx->p32, *p_alt = ctx->p32b, *r = ctx->r32, *r_alt = ctx->r32b;
         while (rc == EL_OK && !h->done && outer < std::max(1, prm.max_outer) && inner_total < prm.max_iter) {
+            // every sweep starts from the same buffer assignment, so that the captured iteration
+            // batches (run_iterations) see the pointers they were captured with
+            p = ctx->p32;
+            p_alt = ctx->p32b;
+            r = ctx->r32;
+            r_alt = ctx->r32b;
+            mg[0].b = ctx->r32;
             {
                 ProfScope prof(ctx, EL_KC_OTHER, na * 16);
                 inner_init_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
@@ -1550,13 +1623,18 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
                     ctx->partials, ctx->counter);
             }
             ctx->launches += 1;
-            ctx->launches += enqueue_vcycle<float, ushort4, float4>(ctx, mg, ctx->seg0, s1, DOT_INIT);
+            if (march)
+                ctx->launches += enqueue_march_vcycle(ctx, mg, s1, DOT_INIT);
+            else
+                ctx->launches += enqueue_vcycle<float, ushort4, float4>(ctx, mg, ctx->seg0, s1, DOT_INIT);
             rc = run_iterations(ctx, EL_SOLVER_MIXED, 1, prm.max_iter - inner_total, check, &hi, [&](int first) {
+                if (march) return enqueue_march_iteration(ctx, p, p_alt, r, r_alt, s1, first, mg);
                 return enqueue_mg_iteration<float, float4, ushort4, float4>(ctx, ctx->A32, ctx->x32, ctx->r32, ctx->z32,
                                                                             p, p_alt, ctx->ap32, s1, first, mg);
             });
             if (rc != EL_OK) break;
             inner_total += hi.iter;
+            if (hi.fault) h->fault = 1;
             if (hi.bad) {
                 h->bad = 1;
                 break;
@@ -1580,11 +1658,13 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
         st->outer_iterations = outer;
         st->relres = h->bb > 0 ? sqrt(h->rr / h->bb) : 0.0;
     }
+    mg_restore_pointers(ctx);
     if (rc != EL_OK) return rc;
     if (h->bad) {
         // entries outside the active segments are never rewritten and must stay finite (they
         // meet zero couplings), so a failed solve leaves every solver vector cleared
         reset_vectors(ctx);
+        if (h->fault) return set_error(ctx, EL_ERR_TIMEOUT, "a bounded wait of the pressure solve gave up");
         return set_error(ctx, EL_ERR_NAN, "non-finite value in the pressure solve");
     }
     st->status = h->done ? EL_OK : EL_ERR_NOT_CONVERGED;
@@ -1611,6 +1691,7 @@ __global__ void outer_cond_kernel(cudaGraphConditionalHandle h, Scalars* so, con
         so->outer += 1;
         so->inner_total += si->iter;
         if (si->bad) so->bad = 1;
+        if (si->fault) so->fault = 1;
     }
     const bool go = !so->done && !so->bad && so->outer < max_outer && so->inner_total < max_iter;
     cudaGraphSetConditional(h, go ? 1u : 0u);
@@ -1684,8 +1765,10 @@ static int enqueue_solve_device_t(el_ctx* ctx, const el_solve_params& prm, int k
         g, seg_arg(ctx->seg0), ctx->rhs64, ctx->x64, ctx->r64, s0, prm.tol);
     pack32_kernel<T><<<grid1d(ctx, n), 256, 0, ctx->stream>>>(n, ctx->diag64, A64.x, A64.y, A64.z, ctx->A32, ctx->A16);
     nk += 2 + enqueue_coarsen<float, ushort4, float4>(ctx, mg);
-    float* p = ctx->p32;
-    float* p_alt = ctx->p32b;
+    const bool march = ctx->march.on && ctx->solver_tiles;
+    if (march) nk += march_enqueue_items(ctx);
+    float *p = ctx->p32, *p_alt = ctx->p32b, *r = ctx->r32, *r_alt = ctx->r32b;
+    mg[0].b = ctx->r32;
     cudaGraphConditionalHandle h_outer, h_inner;
     cudaStream_t parent_outer, parent_inner;
     int rc = new_handle(ctx, &h_outer);
@@ -1697,9 +1780,14 @@ static int enqueue_solve_device_t(el_ctx* ctx, const el_solve_params& prm, int k
     inner_init_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
         g, seg_arg(ctx->seg0), ctx->r64, ctx->r32, ctx->x32, s0, s1, prm.tol, prm.inner_floor, ctx->partials,
         ctx->counter);
-    int body = 1 + enqueue_vcycle<float, ushort4, float4>(ctx, mg, ctx->seg0, s1, DOT_INIT);
-    body += enqueue_mg_iteration<float, float4, ushort4, float4>(ctx, ctx->A32, ctx->x32, ctx->r32, ctx->z32, p,
-                                                                p_alt, ctx->ap32, s1, 1, mg);
+    auto iteration = [&](int first) {
+        if (march) return enqueue_march_iteration(ctx, p, p_alt, r, r_alt, s1, first, mg);
+        return enqueue_mg_iteration<float, float4, ushort4, float4>(ctx, ctx->A32, ctx->x32, ctx->r32, ctx->z32, p,
+                                                                   p_alt, ctx->ap32, s1, first, mg);
+    };
+    int body = 1 + (march ? enqueue_march_vcycle(ctx, mg, s1, DOT_INIT)
+                          : enqueue_vcycle<float, ushort4, float4>(ctx, mg, ctx->seg0, s1, DOT_INIT));
+    body += iteration(1);
     rc = new_handle(ctx, &h_inner);
     if (rc == EL_OK) {
         inner_cond_kernel<<<1, 1, 0, ctx->stream>>>(h_inner, s0, s1, prm.max_iter, 0);
@@ -1710,9 +1798,7 @@ static int enqueue_solve_device_t(el_ctx* ctx, const el_solve_params& prm, int k
         return rc;
     }
     int inner = 0;
-    for (int q = 0; q < 2; ++q)
-        inner += enqueue_mg_iteration<float, float4, ushort4, float4>(ctx, ctx->A32, ctx->x32, ctx->r32, ctx->z32, p,
-                                                                     p_alt, ctx->ap32, s1, 0, mg);
+    for (int q = 0; q < 2; ++q) inner += iteration(0);
     inner_cond_kernel<<<1, 1, 0, ctx->stream>>>(h_inner, s0, s1, prm.max_iter, 1);
     rc = end_while(ctx, parent_inner);
     accumulate_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
@@ -1721,6 +1807,7 @@ static int enqueue_solve_device_t(el_ctx* ctx, const el_solve_params& prm, int k
         g, seg_arg(ctx->seg0), A64, ctx->rhs64, ctx->x64, ctx->r64, s0, ctx->partials, ctx->counter);
     outer_cond_kernel<<<1, 1, 0, ctx->stream>>>(h_outer, s0, s1, max_outer, prm.max_iter, 1);
     const int rc2 = end_while(ctx, parent_outer);
+    mg_restore_pointers(ctx);
     if (rc != EL_OK) return rc;
     if (rc2 != EL_OK) return rc2;
     // kernels outside the loops, per refinement sweep, per pass of the PCG loop
@@ -1778,11 +1865,18 @@ int setup_solver_storage(el_ctx* ctx, int solver) {
         ctx->p32 = (float*)ctx_alloc(ctx, n * 4);
         ctx->p32b = (float*)ctx_alloc(ctx, n * 4);
         ctx->ap32 = (float*)ctx_alloc(ctx, n * 4);
+        ctx->r32b = (float*)ctx_alloc(ctx, n * 4);
         ctx->A32 = (float4*)ctx_alloc(ctx, n * sizeof(float4));
         ctx->A16 = (ushort4*)ctx_alloc(ctx, n * sizeof(ushort4));
-        if (!ctx->x32 || !ctx->r32 || !ctx->z32 || !ctx->p32 || !ctx->p32b || !ctx->ap32 || !ctx->A32 || !ctx->A16)
+        if (!ctx->x32 || !ctx->r32 || !ctx->r32b || !ctx->z32 || !ctx->p32 || !ctx->p32b || !ctx->ap32 || !ctx->A32 ||
+            !ctx->A16)
             return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "mixed solver vectors");
         int rc = build_hierarchy<float>(ctx, ctx->mg32, sizeof(float4));
+        if (rc != EL_OK) return rc;
+        ctx->mg32[0].rec = ctx->A16;
+        ctx->mg32[0].b = ctx->r32;
+        ctx->mg32[0].x = ctx->z32;
+        rc = march_setup(ctx);
         if (rc != EL_OK) return rc;
     }
     return EL_OK;

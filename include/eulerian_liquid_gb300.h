@@ -139,6 +139,10 @@ typedef struct el_tuning {
     int advect_rows;             /* per-sample advection: 32 x rows cells per block, 1, 2, 4 or 8 */
     int advect_tiled;            /* 1 (default): advection kernels that stage the velocity of a
                                     32x8x8 tile in shared memory; 0: one thread per sample      */
+    int solver_tiles;            /* 1 (default): the mixed solver's finest level on the z-marching
+                                    tile kernels with TMA-staged planes, where the grid allows
+                                    (ni a multiple of 8, at least 64 x 16 x 16 cells); 0: the
+                                    row-segment kernels everywhere                              */
 } el_tuning;
 int el_ctx_set_tuning(el_ctx* ctx, const el_tuning* t);
 int el_ctx_get_tuning(const el_ctx* ctx, el_tuning* t);
