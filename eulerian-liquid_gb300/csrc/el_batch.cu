@@ -104,7 +104,7 @@ static int batch_error(el_batch* b, int code, const std::string& msg) {
 
 static void batch_free(el_batch* b) {
     if (!b) return;
-    cudaSetDevice(b->device);
+    DeviceGuard guard(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     for (auto& e : b->exec)
         if (e) cudaGraphExecDestroy(e);
@@ -217,7 +217,8 @@ EL_API int el_batch_create(el_ctx* const* scenes, int count, const el_step_param
         batch_free(b);
         return code;
     };
-    if (cudaSetDevice(b->device) != cudaSuccess) return fail(EL_ERR_CUDA);
+    DeviceGuard guard(b->device);
+    if (guard.err != cudaSuccess) return fail(EL_ERR_CUDA);
     for (el_ctx* c : b->scenes) {
         rc = ensure_solver(c, EL_SOLVER_MIXED);
         if (rc == EL_OK) rc = prepare_device_solve(c);
@@ -268,7 +269,8 @@ EL_API const char* el_batch_last_error(const el_batch* b) { return b ? b->error.
 EL_API int el_batch_step(el_batch* b, int steps) {
     if (!b || steps < 0) return EL_ERR_INVALID_ARGUMENT;
     if (steps == 0) return EL_OK;
-    cudaSetDevice(b->device);
+    DeviceGuard guard(b->device);
+    if (guard.err != cudaSuccess) return batch_error(b, EL_ERR_CUDA, cudaGetErrorString(guard.err));
     int parity = current_parity(b);
     if (parity < 0) return batch_error(b, EL_ERR_INVALID_ARGUMENT, "a scene was stepped outside the batch");
     int rc = order_with_scenes(b, true);

@@ -110,12 +110,13 @@ using namespace el;
 
 #define EL_API extern "C" __attribute__((visibility("default")))
 
-#define CHECK_CTX(ctx)                                                              \
-    do {                                                                            \
-        if (!(ctx)) return EL_ERR_INVALID_ARGUMENT;                                 \
-        cudaError_t _se = cudaSetDevice((ctx)->device);                             \
-        if (_se != cudaSuccess) return set_error(ctx, EL_ERR_CUDA, cudaGetErrorString(_se)); \
-    } while (0)
+// At the top of an entry point: the context is valid, and its device is current until the
+// entry point returns (the caller's device is restored then).
+#define CHECK_CTX(ctx)                                                                   \
+    if (!(ctx)) return EL_ERR_INVALID_ARGUMENT;                                          \
+    el::DeviceGuard _device_guard((ctx)->device);                                        \
+    if (_device_guard.err != cudaSuccess)                                                \
+    return set_error(ctx, EL_ERR_CUDA, cudaGetErrorString(_device_guard.err))
 
 EL_API const char* el_status_string(int status) {
     switch (status) {
@@ -142,7 +143,8 @@ EL_API int el_ctx_create(int ni, int nj, int nk, double dx, int dtype, int devic
     // the reference indexes with int and refuses sizes that overflow it (array.h:322-325)
     const long long biggest = (long long)(ni + 1) * (nj + 1) * (nk + 1);
     if (biggest >= 0x7fffffffLL) return EL_ERR_INVALID_ARGUMENT;
-    if (cudaSetDevice(device) != cudaSuccess) return EL_ERR_CUDA;
+    el::DeviceGuard guard(device);
+    if (guard.err != cudaSuccess) return EL_ERR_CUDA;
     el_ctx* ctx = new (std::nothrow) el_ctx();
     if (!ctx) return EL_ERR_OUT_OF_MEMORY;
     ctx->device = device;
@@ -202,7 +204,7 @@ EL_API int el_ctx_create(int ni, int nj, int nk, double dx, int dtype, int devic
 
 EL_API int el_ctx_destroy(el_ctx* ctx) {
     if (!ctx) return EL_ERR_INVALID_ARGUMENT;
-    cudaSetDevice(ctx->device);
+    el::DeviceGuard guard(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (void* p : ctx->allocations) cudaFree(p);
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);

@@ -121,6 +121,23 @@ struct MarchPlan {
     int per_sm[6] = {};  // resident CTAs per SM of each tile kernel
 };
 
+// Makes `device` current for the length of one entry point and gives the caller's current
+// device back on return, so that no call leaves a caller that works on another GPU switched.
+struct DeviceGuard {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceGuard(int device) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != device) err = cudaSetDevice(device);
+    }
+    ~DeviceGuard() {
+        int now = -1;
+        if (prev >= 0 && cudaGetDevice(&now) == cudaSuccess && now != prev) cudaSetDevice(prev);
+    }
+    DeviceGuard(const DeviceGuard&) = delete;
+    DeviceGuard& operator=(const DeviceGuard&) = delete;
+};
+
 struct DeviceBuffer {
     void* ptr = nullptr;
     size_t bytes = 0;

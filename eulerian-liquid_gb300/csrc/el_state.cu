@@ -65,7 +65,8 @@ struct File {
 
 EL_API int el_state_save(el_ctx* ctx, const char* path, double time) {
     if (!ctx || !path) return EL_ERR_INVALID_ARGUMENT;
-    if (cudaSetDevice(ctx->device) != cudaSuccess) return EL_ERR_CUDA;
+    DeviceGuard guard(ctx->device);
+    if (guard.err != cudaSuccess) return EL_ERR_CUDA;
     File out;
     out.f = fopen(path, "wb");
     if (!out.f) return set_error(ctx, EL_ERR_INVALID_ARGUMENT, std::string("cannot open ") + path);
@@ -98,7 +99,8 @@ EL_API int el_state_save(el_ctx* ctx, const char* path, double time) {
 
 EL_API int el_state_load(el_ctx* ctx, const char* path, double* time) {
     if (!ctx || !path) return EL_ERR_INVALID_ARGUMENT;
-    if (cudaSetDevice(ctx->device) != cudaSuccess) return EL_ERR_CUDA;
+    DeviceGuard guard(ctx->device);
+    if (guard.err != cudaSuccess) return EL_ERR_CUDA;
     File in;
     in.f = fopen(path, "rb");
     if (!in.f) return set_error(ctx, EL_ERR_INVALID_ARGUMENT, std::string("cannot open ") + path);

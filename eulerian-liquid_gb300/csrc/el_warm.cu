@@ -122,7 +122,8 @@ int reduce_blocks(el_ctx* ctx, long long n, int nv) {
 EL_API int el_warmstart_features(el_ctx* ctx, int build, double dt, void* features, void* couplings, float* target,
                                  uint8_t* fluid, double* scales) {
     if (!ctx || !features) return EL_ERR_INVALID_ARGUMENT;
-    if (cudaSetDevice(ctx->device) != cudaSuccess) return EL_ERR_CUDA;
+    DeviceGuard guard(ctx->device);
+    if (guard.err != cudaSuccess) return EL_ERR_CUDA;
     if (build) {
         if (!(dt > 0)) return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "warmstart_features: dt must be > 0");
         int rc = ensure_projection(ctx);
@@ -168,7 +169,8 @@ EL_API int el_warmstart_features(el_ctx* ctx, int build, double dt, void* featur
 
 EL_API int el_warmstart_set_guess(el_ctx* ctx, const float* pred) {
     if (!ctx || !pred) return EL_ERR_INVALID_ARGUMENT;
-    if (cudaSetDevice(ctx->device) != cudaSuccess) return EL_ERR_CUDA;
+    DeviceGuard guard(ctx->device);
+    if (guard.err != cudaSuccess) return EL_ERR_CUDA;
     if (!ctx->diag64) return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "warmstart_set_guess: no system built yet");
     const long long n = (long long)ctx->ni * ctx->nj * ctx->nk;
     if (ctx->dtype == EL_F64)

@@ -21,12 +21,48 @@ void check_ctx(el_ctx* ctx, int status) {
     raise(status, ctx ? el_ctx_last_error(ctx) : "eulerian_liquid_gb300");
 }
 
-// A scoped device context holding host grids for the free functions (no persistent state:
-// each call copies its inputs up and its outputs down, like the reference's by-reference grids).
+// The free functions' device context: one per thread, kept between calls and made again only
+// when the grid's shape or spacing or the caller's current device changes, so a call pays for
+// its copies and kernels, not for a context's allocations.  Each call copies up every input it
+// reads and copies down its outputs, like the reference's by-reference grids, so nothing a call
+// leaves on the device is read by the next one.  The context lives on the caller's current
+// device (the library gives that device back as current on return).
+struct Cached {
+    el_ctx* ctx = nullptr;
+    int ni = 0, nj = 0, nk = 0, device = -1;
+    float dx = 0;
+    void* faces[9] = {};   // advect_staggered_grid: device copies of three MAC grids
+    ~Cached() { release(); }
+    void release() {
+        for (void*& p : faces) {
+            if (p) cudaFree(p);
+            p = nullptr;
+        }
+        if (ctx) el_ctx_destroy(ctx);
+        ctx = nullptr;
+    }
+};
+
 struct Scoped {
     el_ctx* ctx = nullptr;
-    Scoped(int ni, int nj, int nk, float dx) { check_ctx(nullptr, el_ctx_create(ni, nj, nk, dx, EL_F32, 0, &ctx)); }
-    ~Scoped() { el_ctx_destroy(ctx); }
+    Cached* cache = nullptr;
+    Scoped(int ni, int nj, int nk, float dx) {
+        static thread_local Cached cached;
+        int device = 0;
+        if (cudaGetDevice(&device) != cudaSuccess) raise(EL_ERR_CUDA, "cudaGetDevice");
+        if (!cached.ctx || cached.ni != ni || cached.nj != nj || cached.nk != nk || cached.dx != dx ||
+            cached.device != device) {
+            cached.release();
+            check_ctx(nullptr, el_ctx_create(ni, nj, nk, dx, EL_F32, device, &cached.ctx));
+            cached.ni = ni;
+            cached.nj = nj;
+            cached.nk = nk;
+            cached.dx = dx;
+            cached.device = device;
+        }
+        ctx = cached.ctx;
+        cache = &cached;
+    }
     template <typename G>
     void up(int field, const G& g) {
         check_ctx(ctx, el_upload(ctx, field, g.data(), g.size() * sizeof(g[0])));
@@ -57,25 +93,28 @@ void advect_staggered_grid(StaggeredGrid3f& grid, const StaggeredGrid3f& grid_te
     const int ni = grid.ni(), nj = grid.nj(), nk = grid.nk();
     Scoped s(ni, nj, nk, grid_temp.dx());
     const el_grid g{ni, nj, nk, grid_temp.dx()};
-    // device copies of the three grids the kernels read and the three they write
-    void* d[9] = {};
+    // device copies of the three grids the kernels read and the three they write, kept with the
+    // cached context
+    void** d = s.cache->faces;
     const Grid3f* src[6] = {&grid_temp.u(), &grid_temp.v(), &grid_temp.w(), &velocity.u(), &velocity.v(),
                             &velocity.w()};
     for (int q = 0; q < 9; ++q) {
         const size_t bytes = src[q % 3]->size() * sizeof(float);
-        if (cudaMalloc(&d[q], bytes) != cudaSuccess) {
-            for (int r = 0; r < q; ++r) cudaFree(d[r]);
+        if (!d[q] && cudaMalloc(&d[q], bytes) != cudaSuccess) {
+            d[q] = nullptr;
             raise(EL_ERR_OUT_OF_MEMORY, "advect_staggered_grid");
         }
-        if (q < 6) cudaMemcpy(d[q], src[q]->data(), bytes, cudaMemcpyHostToDevice);
+        if (q < 6 && cudaMemcpy(d[q], src[q]->data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess)
+            raise(EL_ERR_CUDA, "advect_staggered_grid: copy to the device");
     }
     int st = el_advect_staggered_grid(&g, EL_F32, d[6], d[7], d[8], d[0], d[1], d[2], d[3], d[4], d[5], dt, trace,
                                       sample, nullptr);
-    cudaDeviceSynchronize();
+    if (st == EL_OK && cudaDeviceSynchronize() != cudaSuccess) st = EL_ERR_CUDA;
     Grid3f* dst[3] = {&grid.u(), &grid.v(), &grid.w()};
     for (int q = 0; q < 3 && st == EL_OK; ++q)
-        cudaMemcpy(dst[q]->data(), d[6 + q], dst[q]->size() * sizeof(float), cudaMemcpyDeviceToHost);
-    for (void* p : d) cudaFree(p);
+        if (cudaMemcpy(dst[q]->data(), d[6 + q], dst[q]->size() * sizeof(float), cudaMemcpyDeviceToHost) !=
+            cudaSuccess)
+            st = EL_ERR_CUDA;
     if (st != EL_OK) raise(st, "advect_staggered_grid");
 }
 
@@ -132,7 +171,10 @@ void Simulator::create_grid(float width, int ni, int nj, int nk) {
     m_dx = width / ni;
     if (m_ctx) el_ctx_destroy(m_ctx);
     m_ctx = nullptr;
-    check(el_ctx_create(ni, nj, nk, m_dx, EL_F32, 0, &m_ctx));
+    // the scene lives on the caller's current device
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) raise(EL_ERR_CUDA, "cudaGetDevice");
+    check(el_ctx_create(ni, nj, nk, m_dx, EL_F32, device, &m_ctx));
     m_velocity.create(ni, nj, nk, m_dx);
     m_velocity_weight.create(ni, nj, nk, m_dx);
     m_velocity_valid.create(ni, nj, nk, m_dx, 1);

@@ -40,10 +40,11 @@ def step(state, dt, trace_phi, sample_phi, trace_vel, sample_vel, gravity, layer
     u = np.where(vu == 0, t(0), u).astype(dtype)
     v = np.where(vv == 0, t(0), v).astype(dtype)
     w = np.where(vw == 0, t(0), w).astype(dtype)
+    pre_projection = (u, v, w)
     D, X, Y, Z, B = build_matrix(phi_new, u, v, w, wu, wv, ww, dx, dt)
     x, st, it, rr = pcg(D, X, Y, Z, B, precond=precond, tol=tol, maxit=maxit)
     p = np.where(D > 0, x, 0.0).astype(dtype)
     u, v, w = update_velocity(u, v, w, p, phi_new, dx, dt)
     s.update(phi=phi_new, u=u, v=v, w=w, valid_u=vu, valid_v=vv, valid_w=vw, pressure=p, pcg_iterations=it,
-             pcg_status=st, pcg_relres=rr)
+             pcg_status=st, pcg_relres=rr, pre_projection=pre_projection)
     return s, (D, X, Y, Z, B)

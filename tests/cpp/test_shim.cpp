@@ -1,7 +1,9 @@
 // C++ check of the host interface (eulerian-liquid_gb300/host/nama_gb300.h) driven the way the
 // reference's app drives its Simulator: update(update_second_order, 1/60, use_cfl) with the
 // reference's step order (apps/eulerian_liquid_3d.cpp:106-120), reinitialisation left out.
-// Prints "ok" and exits 0 when every check holds.
+// Prints "ok" and exits 0 when every check holds.  Given a directory, it also writes the state
+// before one more step of a fixed dt and the fields after it, as raw little-endian arrays, for a
+// comparison of the host interface's numbers with the oracle (tests/test_gpu_cpp_shim.py).
 #include <cmath>
 #include <cstdio>
 #include <stdexcept>
@@ -32,7 +34,15 @@ static void update_second_order(Simulator& sim, float dt) {
     sim.solve_pressure(dt);
 }
 
-int main() {
+template <typename G>
+static bool dump(const std::string& dir, const char* name, const G& g) {
+    FILE* f = std::fopen((dir + "/" + name).c_str(), "wb");
+    if (!f) return false;
+    const bool ok = std::fwrite(g.data(), sizeof(g[0]), g.size(), f) == g.size();
+    return std::fclose(f) == 0 && ok;
+}
+
+int main(int argc, char** argv) {
     const int n = 32;
     Simulator sim;
     sim.create_grid(1.0f, n, n, n);
@@ -109,6 +119,26 @@ int main() {
         threw = std::string(e.what()) == "No fluid";
     }
     CHECK(threw);
+
+    if (argc > 1) {
+        // one more step of a fixed dt: its input state, and the fields it leaves
+        const std::string dir = argv[1];
+        sim.sync_to_host();
+        bool ok = dump(dir, "in_phi", sim.m_level_set) && dump(dir, "in_valid_phi", sim.m_level_set_valid);
+        const char* comp[3] = {"u", "v", "w"};
+        for (int d = 0; d < 3; ++d) {
+            ok = ok && dump(dir, (std::string("in_") + comp[d]).c_str(), sim.m_velocity[d]);
+            ok = ok && dump(dir, (std::string("in_valid_") + comp[d]).c_str(), sim.m_velocity_valid[d]);
+            ok = ok && dump(dir, (std::string("weight_") + comp[d]).c_str(), sim.m_velocity_weight[d]);
+        }
+        sim.solve_params.tol = 1e-6;
+        update_second_order(sim, 1.0f / 240.0f);
+        CHECK(sim.last_solve.status == EL_OK);
+        sim.sync_to_host();
+        ok = ok && dump(dir, "out_phi", sim.m_level_set) && dump(dir, "out_pressure", sim.m_pressure);
+        for (int d = 0; d < 3; ++d) ok = ok && dump(dir, (std::string("out_") + comp[d]).c_str(), sim.m_velocity[d]);
+        CHECK(ok);
+    }
 
     if (failures == 0) std::printf("ok\n");
     return failures == 0 ? 0 : 1;
