@@ -17,7 +17,8 @@ roofline   the dominant kernel class, algorithmic bytes / device time over the t
 cpu_baseline  the CPU oracle (OpenMP restatement with MIC(0)-PCG) on one step of the workload.
 
 --impl reference times the reference's CPU path for the same workload: the oracle port (the
-reference itself cannot be built without Eigen).  Under torchrun rank 0 alone runs it.
+reference's own sources compile only against a stand-in Eigen from the reference tree, which
+is not present where the benchmark runs).  Under torchrun rank 0 alone runs it.
 """
 
 import argparse
@@ -316,20 +317,72 @@ ROOFLINE_MIN_LAUNCH_US = 20.0
 # launch); extrapolate, masks, build and other time groups of kernels and memsets.
 SINGLE_KERNEL_CLASSES = ("advect_phi", "advect_vel", "dir_spmv", "update", "mg_smooth_fine", "mg_restrict_fine",
                          "mg_coarse", "residual_fp64")
+# The finest level of the mixed solver: where the grid allows, every launch of these four classes
+# is the one z-marching tile kernel (march_kernel, csrc/el_march.cu) in one of its six modes
+# (direction + A p, update fused with the pre-smoother, the sweeps, restriction), so they are
+# taken together as one kernel: bytes and time summed over the modes.
+FINE_SOLVER = "finest_level_solver"
+FINE_SOLVER_CLASSES = ("dir_spmv", "update", "mg_smooth_fine", "mg_restrict_fine")
+# What bounds each class (from ncu): the HBM fraction is the roofline of the stencil and copy
+# classes; the advection kernels issue far more instructions than their bytes need (WENO6
+# weights, RK backtraces) and are bound by instruction issue, so their HBM fraction is listed
+# for completeness only.
+CLASS_BOUND = {"advect_phi": "issue", "advect_vel": "issue", "extrapolate": "latency"}
 
-# DRAM traffic per launch of a kernel class, from one ncu capture of the 256^3 workload
-# (dram__bytes_read.sum + dram__bytes_write.sum of the finest level's three smoother kernels of
-# one V-cycle, averaged).
-NCU_TRAFFIC_PER_LAUNCH = {"mg_smooth_fine": (96_948_480 + 125_156_096 + 121_205_760) / 3.0}
+# DRAM traffic per launch of a kernel class, from ncu captures of the 256^3 workload
+# (dram__bytes_read.sum + dram__bytes_write.sum; for the finest-level solver the six tile-kernel
+# modes of one PCG iteration and V-cycle, weighted by their launches per iteration).
+NCU_TRAFFIC_PER_LAUNCH = {"finest_level_solver": 163.4e6}
 
 
-def dominant_class(breakdown):
+def with_fine_solver(breakdown):
+    """The breakdown with the finest-level solver classes also summed into FINE_SOLVER."""
+    parts = [breakdown[k] for k in FINE_SOLVER_CLASSES if k in breakdown]
+    out = dict(breakdown)
+    if parts:
+        out[FINE_SOLVER] = {"launches": sum(p["launches"] for p in parts), "ms": sum(p["ms"] for p in parts),
+                            "bytes": sum(p["bytes"] for p in parts)}
+    return out
+
+
+def class_mask(name):
+    names = FINE_SOLVER_CLASSES if name == FINE_SOLVER else (name,)
+    m = 0
+    for k in names:
+        m |= 1 << KC_NAMES.index(k)
+    return m
+
+
+def dominant_class(breakdown, fine_solver_on=True):
     """The single-kernel class with the most device time among those whose launches average at
-    least ROOFLINE_MIN_LAUNCH_US (all classes if none does)."""
-    big = {k: v for k, v in breakdown.items()
-           if k in SINGLE_KERNEL_CLASSES and v["launches"] and v["ms"] * 1e3 / v["launches"] >= ROOFLINE_MIN_LAUNCH_US}
+    least ROOFLINE_MIN_LAUNCH_US (all classes if none does); with the finest-level tile kernels
+    on, their four classes compete as the one kernel FINE_SOLVER."""
+    b = with_fine_solver(breakdown) if fine_solver_on else dict(breakdown)
+    singles = set(SINGLE_KERNEL_CLASSES)
+    if fine_solver_on and FINE_SOLVER in b:
+        singles = (singles - set(FINE_SOLVER_CLASSES)) | {FINE_SOLVER}
+    big = {k: v for k, v in b.items()
+           if k in singles and v["launches"] and v["ms"] * 1e3 / v["launches"] >= ROOFLINE_MIN_LAUNCH_US}
     pool = big or breakdown
     return max(pool, key=lambda k: pool[k]["ms"])
+
+
+def class_fractions(breakdown, hbm):
+    """Per class of the breakdown: algorithmic GB/s, its fraction of the HBM peak, and the bound."""
+    out = {}
+    for k, v in with_fine_solver(breakdown).items():
+        if v["ms"] > 0:
+            gbs = v["bytes"] / (v["ms"] / 1e3) / 1e9
+            out[k] = {"gbs": gbs, "hbm_frac": gbs / hbm, "bound": CLASS_BOUND.get(k, "hbm"),
+                      "us_per_launch": v["ms"] * 1e3 / max(1, v["launches"])}
+    return out
+
+
+def headline_workload_name(n, seed, tol):
+    """The headline workload, named the same in both arms."""
+    return (f"spheres_pool {n}^3 seed {seed}: pool y<0.3 + 3 seeded spheres r in [0.08,0.2], room walls, "
+            f"seeded solid box 5-10% of cells; phi WENO6/RK2, velocity trilinear/RK3, g 9.8, CFL 1.0, "
+            f"pressure to rel. resid {tol}")
 
 
 def run_ours(args, dist):
@@ -354,7 +407,8 @@ def run_ours(args, dist):
     # class breakdown on two untimed, profiled steps (eager launches with CUDA events around each),
     # to pick the dominant kernel class
     _, _, _, breakdown, _ = timed_steps(el, torch, sim, stream, params, 2, dist, profile_mask=(1 << 12) - 1)
-    dominant = dominant_class(breakdown)
+    fine_on = sim.march_on()
+    dominant = dominant_class(breakdown, fine_on)
     # the timed region: one CUDA graph launch per step (the scene as a batch of one: dt, the
     # step and the solver's loops all decided on the device)
     batch = el.Batch([sim], params=params, cfl=1.0, dt_frame=1.0 / 60.0)
@@ -389,7 +443,7 @@ def run_ours(args, dist):
     batch.close()
     # roofline: the dominant class's launches over K eager steps, CUDA events around each launch
     _, stats, _, prof, _ = timed_steps(el, torch, sim, stream, params, K, dist,
-                                       profile_mask=1 << KC_NAMES.index(dominant))
+                                       profile_mask=class_mask(dominant))
     err = pressure_error(el, sim, params, args.error_steps) if args.error_steps else []
     sim.close()
     iters_mean = bst["iterations"] / max(1, bst["steps"])
@@ -416,7 +470,7 @@ def run_ours(args, dist):
             s2.close()
 
     hbm, peak_kind = peaks()
-    d = prof[dominant]
+    d = with_fine_solver(prof)[dominant]
     achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9
     traffic = NCU_TRAFFIC_PER_LAUNCH.get(dominant) if n == 256 else None
     roofline = {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
@@ -428,9 +482,7 @@ def run_ours(args, dist):
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": dist.world, "steps": K, "warmup": W,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 fields; pressure solve f32 inner / f64 refinement", "data": "synthetic",
-        "config": {"workload": f"spheres_pool {n}^3 seed {args.seed}: pool y<0.3 + 3 seeded spheres r in "
-                               f"[0.08,0.2], room walls, seeded solid box 5-10% of cells; phi WENO6/RK2, "
-                               f"velocity trilinear/RK3, g 9.8, CFL 1.0, mixed PCG to rel. resid {args.tol}",
+        "config": {"workload": headline_workload_name(n, args.seed, args.tol),
                    "n": n, "seed": args.seed, "parallelism": f"replicas x{dist.world}",
                    "l2": "inputs larger than L2 (fields + solver vectors > 2 GB), no flush",
                    "tuning": tuned},
@@ -439,7 +491,8 @@ def run_ours(args, dist):
                   "timed_path": "one CUDA graph launch per step (el_batch of one scene)"},
         "plain_fp64": plain, "mg_fp64": mgd,
         "mixed_over_plain": (value / plain["value"]) if plain else None,
-        "roofline": roofline, "kernel_breakdown_2_steps": breakdown, "gpu_launches": launches,
+        "roofline": roofline, "kernel_breakdown_2_steps": breakdown,
+        "class_rooflines_2_steps": class_fractions(breakdown, hbm), "gpu_launches": launches,
         "clocks": clocks, "e2e": e2e,
     }
     if dist.rank == 0 and not args.no_cpu_baseline:
@@ -874,6 +927,16 @@ def bf16_peak():
 
 # ---- the reference's CPU path (the oracle port) ------------------------------------------
 
+# How the CPU arm's sample differs from the GPU arm's timed region.
+REFERENCE_ARM_DIFFERENCES = (
+    "code: the oracle's C++ restatement of the reference's loops (bit-identical to the reference's own "
+    "sources compiled here, which cannot be built on the Arm GPU host), not the reference binary; "
+    "start: the initial scene at rest (the GPU arm times steps after warm-up steps); "
+    "steps: 1-2 (the GPU arm: 20); "
+    "solver: MIC(0)-PCG in FP64 to the same relative residual as the GPU arm, not the reference's own "
+    "1e-4 (Eigen IncompleteCholesky CG, simulator.cpp:102-107)")
+
+
 def cpu_baseline(n, seed, tol, steps):
     import numpy as np
 
@@ -894,8 +957,9 @@ def cpu_baseline(n, seed, tol, steps):
         its.append(st["pcg_iterations"])
     elapsed = time.perf_counter() - t0
     return {"value": steps / elapsed, "unit": "steps/s", "cores": cores, "kind": "port",
-            "sample": f"{steps} full step(s) of the {n}^3 workload from the initial scene on the CPU oracle "
-                      f"(OpenMP, FP32 fields, MIC(0)-PCG FP64 to {tol}; {its} iterations), {elapsed:.1f} s"}
+            "sample": f"{steps} full step(s) of the {n}^3 workload from the initial scene at rest on the CPU "
+                      f"oracle (a restatement of the reference's loops, OpenMP, FP32 fields, MIC(0)-PCG FP64 "
+                      f"to {tol}, not the reference's 1e-4; {its} iterations), {elapsed:.1f} s"}
 
 
 def _scenes_module():
@@ -985,8 +1049,9 @@ def run_reference(args, dist):
     return {"metric": METRIC, "value": base["value"], "unit": "steps/s", "n_gpus": dist.world, "steps": steps,
             "warmup": 0, "ms_per_step": 1e3 / base["value"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 fields; pressure f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"spheres_pool {args.n}^3 seed {args.seed} (same as our arm)",
-                       "n": args.n, "seed": args.seed, "parallelism": "host cores"},
+            "config": {"workload": headline_workload_name(args.n, args.seed, args.tol),
+                       "n": args.n, "seed": args.seed, "parallelism": "host cores",
+                       "differences_from_our_arm": REFERENCE_ARM_DIFFERENCES},
             "cpu_baseline": {"kind": base["kind"], "cores": base["cores"], "sample": base["sample"],
                              "value": base["value"], "unit": "steps/s"},
             "e2e": {"value": base["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

@@ -159,6 +159,7 @@ def _declare(L):
     L.el_ctx_profile_begin.argtypes = [ctxp, C.c_uint32]
     L.el_ctx_profile_end.argtypes = [ctxp, C.POINTER(ProfileEntry)]
     L.el_ctx_get_tuning.argtypes = [ctxp, C.POINTER(Tuning)]
+    L.el_ctx_solver_tiles_active.argtypes = [ctxp, C.POINTER(C.c_int)]
     L.el_upload.argtypes = [ctxp, i, vp, sz]
     L.el_download.argtypes = [ctxp, i, vp, sz]
     L.el_field_device_ptr.argtypes = [ctxp, i, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)]
@@ -280,6 +281,12 @@ class Simulator:
     def set_tuning(self, **kw):
         t = Tuning(**{**self.get_tuning(), **kw})
         self._check(self.lib.el_ctx_set_tuning(self.h, C.byref(t)), "set_tuning")
+
+    def march_on(self):
+        """True when the mixed solver's finest level runs on the z-marching tile kernels."""
+        on = C.c_int()
+        self._check(self.lib.el_ctx_solver_tiles_active(self.h, C.byref(on)), "solver_tiles_active")
+        return bool(on.value)
 
     # -- fields ---------------------------------------------------------------------------
     def shape(self, field):

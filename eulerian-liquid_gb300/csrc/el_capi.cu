@@ -282,6 +282,17 @@ EL_API int el_ctx_get_tuning(const el_ctx* ctx, el_tuning* t) {
     return EL_OK;
 }
 
+EL_API int el_ctx_solver_tiles_active(el_ctx* ctx, int* on) {
+    CHECK_CTX(ctx);
+    if (!on) return EL_ERR_INVALID_ARGUMENT;
+    *on = 0;
+    if (ctx->dtype != EL_F32) return EL_OK;  // the mixed solver's tile kernels are FP32-field only
+    const int rc = ensure_solver(ctx, EL_SOLVER_MIXED);
+    if (rc != EL_OK) return rc;
+    *on = (ctx->march.on && ctx->solver_tiles) ? 1 : 0;
+    return EL_OK;
+}
+
 EL_API int el_ctx_profile_begin(el_ctx* ctx, uint32_t class_mask) {
     CHECK_CTX(ctx);
     EL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));

@@ -146,6 +146,10 @@ typedef struct el_tuning {
 } el_tuning;
 int el_ctx_set_tuning(el_ctx* ctx, const el_tuning* t);
 int el_ctx_get_tuning(const el_ctx* ctx, el_tuning* t);
+/* *on = 1 when the mixed solver's finest level runs on the z-marching tile kernels on this
+ * context (solver_tiles set and the grid meets their conditions), else 0 (no counterpart in the
+ * reference).  Sets up the mixed solver's storage first if no mixed solve has run yet. */
+int el_ctx_solver_tiles_active(el_ctx* ctx, int* on);
 
 /* ---- per-kernel-class timing ---------------------------------------------------------
  * While profiling is on, every launch of a class in `class_mask` (bit = 1 << EL_KC_*) is

@@ -32,7 +32,13 @@ def test_roofline_class_skips_grouped_and_short_launches():
         "advect_phi": _rec(2, 3.6),
         "update": _rec(28, 0.9),
     }
-    assert bench.dominant_class(breakdown) == "mg_smooth_fine"
+    assert bench.dominant_class(breakdown, fine_solver_on=False) == "mg_smooth_fine"
+    # with the finest level on the tile kernels, its four classes are one kernel
+    assert bench.dominant_class(breakdown) == bench.FINE_SOLVER
+    merged = bench.with_fine_solver(breakdown)[bench.FINE_SOLVER]
+    assert merged["launches"] == 124 and abs(merged["ms"] - 5.1) < 1e-12
+    assert bench.class_mask(bench.FINE_SOLVER) == sum(1 << bench.KC_NAMES.index(k)
+                                                      for k in bench.FINE_SOLVER_CLASSES)
 
 
 def test_roofline_class_falls_back_to_the_largest():
@@ -42,7 +48,7 @@ def test_roofline_class_falls_back_to_the_largest():
 
 def test_ncu_traffic_is_per_launch_and_named_for_a_single_kernel_class():
     for cls, traffic in bench.NCU_TRAFFIC_PER_LAUNCH.items():
-        assert cls in bench.SINGLE_KERNEL_CLASSES
+        assert cls in bench.SINGLE_KERNEL_CLASSES or cls == bench.FINE_SOLVER
         assert 1e6 < traffic < 1e10
 
 
