@@ -95,7 +95,7 @@ class Grid(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("seg_blocks_per_sm", C.c_int), ("stencil_blocks_per_sm", C.c_int),
                 ("extrapolate_blocks_per_sm", C.c_int), ("advect_rows", C.c_int), ("advect_tiled", C.c_int),
-                ("solver_tiles", C.c_int)]
+                ("solver_tiles", C.c_int), ("coarse_fused", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -252,7 +252,8 @@ EL_API int el_ctx_set_tuning(el_ctx* ctx, const el_tuning* t) {
     if (!t || t->seg_blocks_per_sm < 1 || t->seg_blocks_per_sm > 8 || t->stencil_blocks_per_sm < 1 ||
         t->stencil_blocks_per_sm > 16 || t->extrapolate_blocks_per_sm < 1 || t->extrapolate_blocks_per_sm > 16 ||
         (t->advect_rows != 1 && t->advect_rows != 2 && t->advect_rows != 4 && t->advect_rows != 8) ||
-        (t->advect_tiled != 0 && t->advect_tiled != 1) || (t->solver_tiles != 0 && t->solver_tiles != 1))
+        (t->advect_tiled != 0 && t->advect_tiled != 1) || (t->solver_tiles != 0 && t->solver_tiles != 1) ||
+        (t->coarse_fused != 0 && t->coarse_fused != 1))
         return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "tuning out of range");
     // the reduction partials are sized for 16 stencil blocks per SM (el_ctx_create)
     ctx->seg_per_sm = t->seg_blocks_per_sm;
@@ -261,6 +262,7 @@ EL_API int el_ctx_set_tuning(el_ctx* ctx, const el_tuning* t) {
     ctx->advect_rows = t->advect_rows;
     ctx->advect_tiled = t->advect_tiled;
     ctx->solver_tiles = t->solver_tiles;
+    ctx->coarse_fused = t->coarse_fused;
     // cached PCG iteration graphs hold the old launch shapes
     cudaStreamSynchronize(ctx->stream);
     for (auto& g : ctx->iter_graph)
@@ -279,6 +281,7 @@ EL_API int el_ctx_get_tuning(const el_ctx* ctx, el_tuning* t) {
     t->advect_rows = ctx->advect_rows;
     t->advect_tiled = ctx->advect_tiled;
     t->solver_tiles = ctx->solver_tiles;
+    t->coarse_fused = ctx->coarse_fused;
     return EL_OK;
 }
 

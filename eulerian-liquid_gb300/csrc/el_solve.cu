@@ -123,6 +123,16 @@ struct SegArg {
         const int c = sd.x + lane;                                                \
         const bool live = i < (g).n0;
 
+// the same over an explicit warp numbering (warp wg of nw warps)
+#define SEG_LOOP_ALL_W_BEGIN(seg, g, wg, nw)                                      \
+    const int lane = threadIdx.x & 31;                                            \
+    const int nseg = *(seg).count;                                                \
+    for (int qs = (wg); qs < nseg; qs += (nw)) {                                  \
+        const int4 sd = (seg).desc[qs];                                           \
+        const int i = sd.y + lane, j = sd.z, k = sd.w;                            \
+        const int c = sd.x + lane;                                                \
+        const bool live = i < (g).n0;
+
 // the same, with the next segment's descriptor loaded while the current one is processed (for
 // the kernels whose registers leave room for it)
 #define SEG_LOOP_ALL_PF_BEGIN(seg, g)                                             \
@@ -710,6 +720,53 @@ __device__ __forceinline__ V mg_div(V a, V b) {
 }
 enum { DOT_NONE = 0, DOT_INIT = 1, DOT_BETA = 2 };
 
+// A value of an iterate or right-hand side.  COH: through L2 only (ld.global.cg), for arrays
+// that other CTAs of the same launch wrote (the fused coarse cycle); a read-only-cache load
+// would not see those writes.
+template <bool COH, typename V>
+__device__ __forceinline__ V ldv(const V* p, int q) {
+    if constexpr (COH)
+        return __ldcg(p + q);
+    else
+        return p[q];
+}
+
+// One smoothing sweep over the active segments of a level, warp wg of nw warps taking segments
+// wg, wg + nw, ...; returns the thread's share of b.x when DOT is set.
+// ZERO2: first sweep (formed on the fly) w1, this sweep w2; PROLONG: w1; PLAIN: w2
+template <typename V, typename R, int MODE, int DOT, bool COH = false>
+__device__ __forceinline__ DotAcc<V> smooth_segments(const LGeom& g, const SegArg& seg, const R* __restrict__ A,
+                                                     const V* __restrict__ b, const V* __restrict__ x_in,
+                                                     const LGeom& gc, const V* __restrict__ e, V* __restrict__ x_out,
+                                                     int wg, int nw) {
+    const V w_first = V(kSweep1);
+    const V omega = V(MODE == SM_PROLONG ? kSweep1 : kSweep2);
+    DotAcc<V> part = 0;
+    const RecLoad<V, R> recf{A};
+    // value of the current iterate at a cell, zero on inactive cells
+    auto rawf = [&](int q, int qi, int qj, int qk) -> V {
+        if (MODE == SM_ZERO2) return ldv<COH>(b, q);
+        V v = ldv<COH>(x_in, q);
+        if (MODE == SM_PROLONG) v += ldv<COH>(e, (qi >> 1) + gc.s1 * (qj >> 1) + gc.s2 * (qk >> 1));
+        return v;
+    };
+    auto valf = [&](V raw, const Co<V>& rec) -> V {
+        if (!(rec.d > V(0))) return V(0);
+        return MODE == SM_ZERO2 ? mg_div(w_first * raw, rec.d) : raw;
+    };
+    SEG_LOOP_ALL_W_BEGIN(seg, g, wg, nw)
+    const St7<V> st = gather7<V, true>(g, c, i, j, k, live, lane, recf, rawf, valf);
+    if (live) {
+        const V bc = ldv<COH>(b, c);
+        V xo = V(0);
+        if (st.d > V(0)) xo = st.v0 + mg_div(omega * (bc - apply7(st)), st.d);
+        x_out[c] = xo;
+        if (DOT != DOT_NONE) part += (DotAcc<V>)bc * (DotAcc<V>)xo;
+    }
+    SEG_LOOP_END
+    return part;
+}
+
 template <typename V, typename R, int MODE, int DOT>
 __global__ void __launch_bounds__(kSegThreads) smooth_kernel(LGeom g, SegArg seg, const R* __restrict__ A,
                                                              const V* __restrict__ b, const V* __restrict__ x_in,
@@ -717,32 +774,9 @@ __global__ void __launch_bounds__(kSegThreads) smooth_kernel(LGeom g, SegArg seg
                                                              V* __restrict__ x_out, Scalars* s, double* partials,
                                                              unsigned* counter) {
     if (s->done) return;
-    // ZERO2: first sweep (formed on the fly) w1, this sweep w2; PROLONG: w1; PLAIN: w2
-    const V w_first = V(kSweep1);
-    const V omega = V(MODE == SM_PROLONG ? kSweep1 : kSweep2);
-    DotAcc<V> part = 0;
-    const RecLoad<V, R> recf{A};
-    // value of the current iterate at a cell, zero on inactive cells
-    auto rawf = [&](int q, int qi, int qj, int qk) -> V {
-        if (MODE == SM_ZERO2) return b[q];
-        V v = x_in[q];
-        if (MODE == SM_PROLONG) v += e[(qi >> 1) + gc.s1 * (qj >> 1) + gc.s2 * (qk >> 1)];
-        return v;
-    };
-    auto valf = [&](V raw, const Co<V>& rec) -> V {
-        if (!(rec.d > V(0))) return V(0);
-        return MODE == SM_ZERO2 ? mg_div(w_first * raw, rec.d) : raw;
-    };
-    SEG_LOOP_ALL_BEGIN(seg, g)
-    const St7<V> st = gather7<V, true>(g, c, i, j, k, live, lane, recf, rawf, valf);
-    if (live) {
-        const V bc = b[c];
-        V xo = V(0);
-        if (st.d > V(0)) xo = st.v0 + mg_div(omega * (bc - apply7(st)), st.d);
-        x_out[c] = xo;
-        if (DOT != DOT_NONE) part += (DotAcc<V>)bc * (DotAcc<V>)xo;
-    }
-    SEG_LOOP_END
+    const DotAcc<V> part = smooth_segments<V, R, MODE, DOT>(g, seg, A, b, x_in, gc, e, x_out,
+                                                            (blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                                                            (gridDim.x * blockDim.x) >> 5);
     if (DOT != DOT_NONE) {
         double acc[1] = {(double)part};
         double tot[1];
@@ -810,22 +844,19 @@ __global__ void __launch_bounds__(kSegThreads, sizeof(V) == 4 ? 5 : 4) restrict_
 // eight gathers in sequence: the kernel is bound by the latency of the gathers.
 constexpr int kQuadsPerBlock = kSegThreads / 128;
 
-template <typename V, typename R>
-__global__ void __launch_bounds__(kSegThreads, 4) restrict_quad_kernel(LGeom g, const R* __restrict__ A,
-                                                                    const V* __restrict__ b, const V* __restrict__ x,
-                                                                    LGeom gc, SegArg cseg, V* __restrict__ bc,
-                                                                    const Scalars* s) {
-    if (s->done) return;
-    __shared__ V part[kQuadsPerBlock][4][2][16];
+// The quads' walk: quad `quad` of `nquads`, the block's quad quad_b (named barrier 1 + quad_b),
+// row `sub` of it; part = the block's [quads][4][2][16] sums in shared memory.
+template <typename V, typename R, bool COH = false>
+__device__ __forceinline__ void restrict_quad_segments(const LGeom& g, const R* __restrict__ A,
+                                                       const V* __restrict__ b, const V* __restrict__ x,
+                                                       const LGeom& gc, const SegArg& cseg, V* __restrict__ bc,
+                                                       V (*part)[4][2][16], int quad, int nquads, int quad_b,
+                                                       int sub) {
     const RecLoad<V, R> recf{A};
-    auto rawf = [&](int q, int, int, int) -> V { return x[q]; };
+    auto rawf = [&](int q, int, int, int) -> V { return ldv<COH>(x, q); };
     auto valf = [](V raw, const Co<V>&) -> V { return raw; };
     const int lane = threadIdx.x & 31;
-    const int wb = threadIdx.x >> 5;                  // warp in the block
-    const int quad_b = wb >> 2, sub = wb & 3;         // quad in the block, row of the quad
     const int kk = sub >> 1, jj = sub & 1;
-    const int quad = blockIdx.x * kQuadsPerBlock + quad_b;
-    const int nquads = gridDim.x * kQuadsPerBlock;
     const int nseg = *cseg.count;
     for (int qs = quad; qs < nseg; qs += nquads) {
         const int4 sd = cseg.desc[qs];
@@ -840,7 +871,7 @@ __global__ void __launch_bounds__(kSegThreads, 4) restrict_quad_kernel(LGeom g, 
                 const bool live = i < g.n0;
                 const int c = i + g.s1 * j + g.s2 * k;
                 const St7<V> st = gather7<V, false>(g, c, i, j, k, live, lane, recf, rawf, valf);
-                if (live && st.d > V(0)) sum[h] = b[c] - apply7(st);
+                if (live && st.d > V(0)) sum[h] = ldv<COH>(b, c) - apply7(st);
             }
         }
 #pragma unroll
@@ -859,6 +890,19 @@ __global__ void __launch_bounds__(kSegThreads, 4) restrict_quad_kernel(LGeom g, 
         }
         asm volatile("bar.sync %0, %1;" ::"r"(1 + quad_b), "r"(128) : "memory");
     }
+}
+
+template <typename V, typename R>
+__global__ void __launch_bounds__(kSegThreads, 4) restrict_quad_kernel(LGeom g, const R* __restrict__ A,
+                                                                    const V* __restrict__ b, const V* __restrict__ x,
+                                                                    LGeom gc, SegArg cseg, V* __restrict__ bc,
+                                                                    const Scalars* s) {
+    if (s->done) return;
+    __shared__ V part[kQuadsPerBlock][4][2][16];
+    const int wb = threadIdx.x >> 5;                  // warp in the block
+    const int quad_b = wb >> 2, sub = wb & 3;         // quad in the block, row of the quad
+    restrict_quad_segments<V, R>(g, A, b, x, gc, cseg, bc, part, blockIdx.x * kQuadsPerBlock + quad_b,
+                                 gridDim.x * kQuadsPerBlock, quad_b, sub);
 }
 
 
@@ -951,13 +995,11 @@ constexpr int bottom_smem_bytes() {
            kCoarsestMaxCells * (int)(sizeof(float4) + 3 * sizeof(float));
 }
 
-__global__ void __launch_bounds__(kBottomThreads) mg_bottom_kernel(LGeom gf, const float4* __restrict__ recf,
-                                                                   const float* __restrict__ bf,
-                                                                   float* __restrict__ xf, LGeom gc,
-                                                                   const float4* __restrict__ recc, int sweeps,
-                                                                   const Scalars* s) {
-    if (s->done) return;
-    extern __shared__ __align__(16) unsigned char bottom_smem[];
+// the bottom's passes by one CTA of kBottomThreads threads, staged in bottom_smem
+__device__ __forceinline__ void bottom_cycle(const LGeom& gf, const float4* __restrict__ recf,
+                                             const float* __restrict__ bf, float* __restrict__ xf, const LGeom& gc,
+                                             const float4* __restrict__ recc, int sweeps,
+                                             unsigned char* bottom_smem) {
     float4* sr = reinterpret_cast<float4*>(bottom_smem);
     float* sb = reinterpret_cast<float*>(sr + kBottomMaxCells);
     float* s1 = sb + kBottomMaxCells;
@@ -977,7 +1019,7 @@ __global__ void __launch_bounds__(kBottomThreads) mg_bottom_kernel(LGeom gf, con
     };
     for (int c = tid; c < nf; c += kBottomThreads) {
         sr[c] = recf[c];
-        sb[c] = bf[c];
+        sb[c] = __ldcg(bf + c);  // written by other CTAs of the fused coarse cycle
     }
     for (int c = tid; c < nc; c += kBottomThreads) cr[c] = recc[c];
     __syncthreads();
@@ -1072,6 +1114,126 @@ __global__ void __launch_bounds__(kBottomThreads) mg_bottom_kernel(LGeom gf, con
         float xo = 0.f;
         if (st.d > 0.f) xo = st.v0 + mg_div(w2 * (sb[c] - apply7(st)), st.d);
         xf[c] = xo;
+    }
+}
+
+__global__ void __launch_bounds__(kBottomThreads) mg_bottom_kernel(LGeom gf, const float4* __restrict__ recf,
+                                                                   const float* __restrict__ bf,
+                                                                   float* __restrict__ xf, LGeom gc,
+                                                                   const float4* __restrict__ recc, int sweeps,
+                                                                   const Scalars* s) {
+    if (s->done) return;
+    extern __shared__ __align__(16) unsigned char bottom_smem[];
+    bottom_cycle(gf, recf, bf, xf, gc, recc, sweeps, bottom_smem);
+}
+
+// ---------------------------------------------------------------------------------------
+// The coarse levels of one FP32 V-cycle in one cooperative launch.  Below the finest level the
+// segment kernels are launches of a few microseconds each (about 13 per V-cycle at 256^3:
+// two sweeps from zero and the restriction per level going down, the bottom, the prolongation
+// sweep and the last sweep per level coming up), so the V-cycle's coarse part was bound by
+// launch latency.  Here one launch of 1024-thread CTAs, all resident at once (a cooperative
+// launch), runs the same passes -- the same device functions, so the same expressions in the
+// same order and bit-identical results -- separated by grid barriers; the bottom pair (<= 16^3
+// and the coarsest level) runs in CTA 0's shared memory while the others wait at the next
+// barrier.  Arrays written by one pass and read by another are loaded through L2
+// (ld.global.cg).  Every barrier wait is bounded: a CTA that gives up marks the solve as failed
+// (fault, bad, done) and leaves; the other CTAs' waits then run out too.
+constexpr int kCoarseMaxLevels = 16;
+constexpr int kCoopQuads = kBottomThreads / 128;  // restriction quads per CTA
+constexpr long long kBarrierPolls = 1ll << 21;    // each poll sleeps ~100 ns: ~0.2 s per barrier
+
+struct CoarseLevel {
+    LGeom g;
+    const float4* rec;
+    float* b;
+    float* x;
+    float* t;
+    SegArg seg;
+};
+
+struct CoarseCycle {
+    CoarseLevel lv[kCoarseMaxLevels];  // by hierarchy level
+    int from, pre_end;                 // levels [from, pre_end) go down and up; pre_end, pre_end + 1: bottom
+    int sweeps;                        // coarsest-level sweeps
+    unsigned* bar;                     // grid barrier: arrivals, generation (arrivals 0 before a launch)
+};
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// all CTAs of the launch meet; false when this CTA's wait ran out
+__device__ __forceinline__ bool coarse_grid_barrier(unsigned* bar, unsigned nblocks) {
+    __shared__ int ok_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned gen = ld_acquire_gpu(bar + 1);  // cannot advance before this CTA arrives
+        __threadfence();
+        if (atomicAdd(bar, 1u) == nblocks - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            long long n = 0;
+            while (ld_acquire_gpu(bar + 1) == gen) {
+                if (++n > kBarrierPolls) {
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(100);
+            }
+        }
+        __threadfence();
+        ok_s = ok;
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+
+__global__ void __launch_bounds__(kBottomThreads, 1) mg_coarse_cycle_kernel(const __grid_constant__ CoarseCycle a,
+                                                                            Scalars* s) {
+    if (s->done) return;  // read by every CTA before any can change it: all leave, or none
+    extern __shared__ __align__(16) unsigned char bottom_smem[];
+    __shared__ float part[kCoopQuads][4][2][16];
+    const unsigned nblk = gridDim.x;
+    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const int wb = threadIdx.x >> 5, quad_b = wb >> 2, sub = wb & 3;
+    const int quad = blockIdx.x * kCoopQuads + quad_b, nquads = gridDim.x * kCoopQuads;
+    auto fail = [&]() {
+        if (threadIdx.x == 0) {
+            s->fault = 1;
+            s->bad = 1;
+            s->done = 1;
+        }
+    };
+    for (int l = a.from; l < a.pre_end; ++l) {
+        const CoarseLevel& F = a.lv[l];
+        const CoarseLevel& C = a.lv[l + 1];
+        smooth_segments<float, float4, SM_ZERO2, DOT_NONE, true>(F.g, F.seg, F.rec, F.b, nullptr, F.g, nullptr, F.x,
+                                                                 wg, nw);
+        if (!coarse_grid_barrier(a.bar, nblk)) return fail();
+        restrict_quad_segments<float, float4, true>(F.g, F.rec, F.b, F.x, C.g, C.seg, C.b, part, quad, nquads,
+                                                    quad_b, sub);
+        if (!coarse_grid_barrier(a.bar, nblk)) return fail();
+    }
+    if (blockIdx.x == 0) {
+        const CoarseLevel& F = a.lv[a.pre_end];
+        const CoarseLevel& C = a.lv[a.pre_end + 1];
+        bottom_cycle(F.g, F.rec, F.b, F.x, C.g, C.rec, a.sweeps, bottom_smem);
+    }
+    for (int l = a.pre_end - 1; l >= a.from; --l) {
+        const CoarseLevel& F = a.lv[l];
+        const CoarseLevel& C = a.lv[l + 1];
+        if (!coarse_grid_barrier(a.bar, nblk)) return fail();
+        smooth_segments<float, float4, SM_PROLONG, DOT_NONE, true>(F.g, F.seg, F.rec, F.b, F.x, C.g, C.x, F.t, wg,
+                                                                   nw);
+        if (!coarse_grid_barrier(a.bar, nblk)) return fail();
+        smooth_segments<float, float4, SM_PLAIN, DOT_NONE, true>(F.g, F.seg, F.rec, F.b, F.t, F.g, nullptr, F.x, wg,
+                                                                 nw);
     }
 }
 
@@ -1216,6 +1378,43 @@ static void launch_smooth(el_ctx* ctx, const MGLevel<V>& F, const SegList& seg, 
         g, seg_arg(seg), (const R*)F.rec, F.b, x_in, gc, C ? C->x : nullptr, x_out, s, ctx->partials, ctx->counter);
 }
 
+// The coarse part of an FP32 V-cycle, levels [from, pre_end) and the bottom pair, as one
+// cooperative launch of mg_coarse_cycle_kernel; the grid is one CTA per 32 rows of level
+// `from` (a warp per row segment), at most every resident CTA.
+static bool coarse_fused_usable(const el_ctx* ctx, int L) {
+    return ctx->coarse_fused && ctx->coarse_per_sm > 0 && ctx->coarse_bar && L <= kCoarseMaxLevels;
+}
+
+static int coarse_cycle_grid(const el_ctx* ctx, const SegList& seg_from) {
+    const long long cap = (long long)ctx->num_sms * ctx->coarse_per_sm;
+    const long long want = (seg_from.total + kBottomThreads / 32 - 1) / (kBottomThreads / 32);
+    return (int)std::max<long long>(1, std::min(cap, want));
+}
+
+static int launch_coarse_cycle(el_ctx* ctx, std::vector<MGLevel<float>>& mg, int from, int pre_end, Scalars* s) {
+    CoarseCycle a{};
+    for (int l = from; l <= pre_end + 1; ++l) {
+        const MGLevel<float>& X = mg[l];
+        a.lv[l] = CoarseLevel{make_geom(X.n0, X.n1, X.n2), (const float4*)X.rec, X.b, X.x, X.t, seg_arg(X.seg)};
+    }
+    a.from = from;
+    a.pre_end = pre_end;
+    a.sweeps = kCoarsestSweeps;
+    a.bar = ctx->coarse_bar;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(coarse_cycle_grid(ctx, mg[from].seg), 1, 1);
+    cfg.blockDim = dim3(kBottomThreads, 1, 1);
+    cfg.dynamicSmemBytes = bottom_smem_bytes();
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, mg_coarse_cycle_kernel, a, s);
+    return 1;
+}
+
 // z = M^-1 r with r = mg[0].b and z = mg[0].x; dot = DOT_INIT or DOT_BETA.  R0 / RC are the
 // record types of the finest / coarse levels.  from > 0: the levels below `from` only (level
 // from - 1 restricted onto mg[from].b before, and prolonged from mg[from].x after, by the caller).
@@ -1244,7 +1443,12 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
     const bool fused_bottom = kBottomType && L >= 3 && cells(mg[L - 2]) <= kBottomMaxCells &&
                               cells(mg[L - 1]) <= kCoarsestMaxCells;
     const int pre_end = fused_bottom ? L - 2 : L - 1;  // levels smoothed and restricted by the loops
-    for (int l = from; l < pre_end; ++l) {
+    // levels [coop_from, pre_end) and the bottom in one cooperative launch (the FP32 hierarchy)
+    int coop_from = -1;
+    if constexpr (kBottomType)
+        if (fused_bottom && coarse_fused_usable(ctx, L)) coop_from = std::max(from, 1);
+    const int down_end = coop_from >= 0 ? coop_from : pre_end;  // levels by per-level launches
+    for (int l = from; l < down_end; ++l) {
         MGLevel<V>& F = mg[l];
         MGLevel<V>& C = mg[l + 1];
         const double rb = l == 0 ? sizeof(R0) : sizeof(RC);
@@ -1269,7 +1473,17 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
         }
         launched += 2;
     }
-    if (fused_bottom) {
+    if (coop_from >= 0) {
+        if constexpr (kBottomType) {
+            // reads and writes what the per-level launches and the bottom would
+            double bytes = cells(mg[L - 2]) * (sizeof(RC) + 2 * vs) + cells(mg[L - 1]) * sizeof(RC);
+            for (int l = coop_from; l < pre_end; ++l)
+                bytes += act(l, mg[l]) * (2 * (2 * vs + sizeof(RC)) + 2 * (3 * vs + sizeof(RC))) +
+                         act(l + 1, mg[l + 1]) * 2 * vs;
+            ProfScope prof(ctx, EL_KC_MG_COARSE, bytes);
+            launched += launch_coarse_cycle(ctx, mg, coop_from, pre_end, s);
+        }
+    } else if (fused_bottom) {
         if constexpr (kBottomType) {
             MGLevel<V>& F = mg[L - 2];
             MGLevel<V>& C = mg[L - 1];
@@ -1287,7 +1501,7 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
                                                                          C.b, C.x, kCoarsestSweeps, s);
         ++launched;
     }
-    for (int l = pre_end - 1; l >= from; --l) {
+    for (int l = down_end - 1; l >= from; --l) {
         MGLevel<V>& F = mg[l];
         MGLevel<V>& C = mg[l + 1];
         const double rb = l == 0 ? sizeof(R0) : sizeof(RC);
@@ -1601,6 +1815,8 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
             ProfScope prof(ctx, EL_KC_OTHER, (double)n * 8);
             ctx->launches += march_enqueue_items(ctx);
         }
+        // the fused coarse cycle's barrier starts clear (a failed solve may have left arrivals)
+        if (ctx->coarse_bar) EL_CUDA_TRY(ctx, cudaMemsetAsync(ctx->coarse_bar, 0, 8, ctx->stream));
         rc = record_active(ctx, ctx->seg0, ctx->ni, &mg);
         if (rc != EL_OK) return rc;
         Scalars* s1 = ctx->dscal + 1;
@@ -1767,6 +1983,7 @@ static int enqueue_solve_device_t(el_ctx* ctx, const el_solve_params& prm, int k
     nk += 2 + enqueue_coarsen<float, ushort4, float4>(ctx, mg);
     const bool march = ctx->march.on && ctx->solver_tiles;
     if (march) nk += march_enqueue_items(ctx);
+    if (ctx->coarse_bar) EL_CUDA_TRY(ctx, cudaMemsetAsync(ctx->coarse_bar, 0, 8, ctx->stream));
     float *p = ctx->p32, *p_alt = ctx->p32b, *r = ctx->r32, *r_alt = ctx->r32b;
     mg[0].b = ctx->r32;
     cudaGraphConditionalHandle h_outer, h_inner;
@@ -1859,6 +2076,21 @@ int setup_solver_storage(el_ctx* ctx, int solver) {
     if (solver == EL_SOLVER_MIXED && !ctx->x32) {
         EL_CUDA_TRY(ctx, cudaFuncSetAttribute(mg_bottom_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               bottom_smem_bytes()));
+        // the fused coarse cycle: 1024-thread CTAs, all resident, where cooperative launches
+        // exist; otherwise the per-level launches stay in use
+        int coop = 0;
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
+        ctx->coarse_per_sm = 0;
+        if (coop) {
+            EL_CUDA_TRY(ctx, cudaFuncSetAttribute(mg_coarse_cycle_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  bottom_smem_bytes()));
+            int per_sm = 0;
+            EL_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mg_coarse_cycle_kernel,
+                                                                          kBottomThreads, bottom_smem_bytes()));
+            ctx->coarse_bar = (unsigned*)ctx_alloc(ctx, 64);
+            if (!ctx->coarse_bar) return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "coarse cycle barrier");
+            ctx->coarse_per_sm = per_sm;
+        }
         ctx->x32 = (float*)ctx_alloc(ctx, n * 4);
         ctx->r32 = (float*)ctx_alloc(ctx, n * 4);
         ctx->z32 = (float*)ctx_alloc(ctx, n * 4);

@@ -143,6 +143,9 @@ typedef struct el_tuning {
                                     tile kernels with TMA-staged planes, where the grid allows
                                     (ni a multiple of 8, at least 64 x 16 x 16 cells); 0: the
                                     row-segment kernels everywhere                              */
+    int coarse_fused;            /* 1 (default): the mixed solver's multigrid levels below the
+                                    finest, and the bottom pair, in one cooperative launch per
+                                    V-cycle (identical results); 0: one launch per level pass   */
 } el_tuning;
 int el_ctx_set_tuning(el_ctx* ctx, const el_tuning* t);
 int el_ctx_get_tuning(const el_ctx* ctx, el_tuning* t);
