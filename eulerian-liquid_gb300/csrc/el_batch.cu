@@ -222,6 +222,7 @@ EL_API int el_batch_create(el_ctx* const* scenes, int count, const el_step_param
     for (el_ctx* c : b->scenes) {
         rc = ensure_solver(c, EL_SOLVER_MIXED);
         if (rc == EL_OK) rc = prepare_device_solve(c);
+        if (rc == EL_OK) rc = ensure_extrapolation(c, 4);  // scratch of the captured step (allocates)
         if (rc == EL_OK && b->fork_steps) rc = prepare_device_step(c);
         if (rc != EL_OK) return fail(rc);
         if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(EL_ERR_CUDA);

@@ -25,7 +25,6 @@ int launch_flags_build(el_ctx* ctx, bool inner32, bool build = true);
 int launch_assign_indices(el_ctx* ctx, int* d_chunks, int* d_total);
 int launch_scatter_pressure(el_ctx* ctx);
 int launch_update_velocity(el_ctx* ctx, const Scalars* s, double dtv);
-int launch_extrapolate(el_ctx* ctx, int field, uint8_t* valid, int layers, bool write_back, int slot = 0);
 int launch_masks(el_ctx* ctx, bool gravity, double g, const Scalars* s, double dtv, bool zero);
 int launch_gravity(el_ctx* ctx, double g, const Scalars* s, double dtv);
 int launch_zero_invalid(el_ctx* ctx);
@@ -170,23 +169,20 @@ EL_API int el_ctx_create(int ni, int nj, int nk, double dx, int dtype, int devic
         ctx->tmp[q] = ctx_alloc(ctx, ctx->field_bytes[EL_FIELD_PHI + q]);
         ok = ok && ctx->tmp[q];
     }
-    size_t biggest_face = 0;
-    for (int f = EL_FIELD_VALID_U; f <= EL_FIELD_VALID_PHI; ++f)
-        biggest_face = std::max(biggest_face, ctx->field_bytes[f]);
-    ctx->ex_stamp_bytes = biggest_face;
-    ctx->valid_tmp = (uint8_t*)ctx_alloc(ctx, biggest_face);
-    // extrapolation tiles over the largest face grid (counted as 32 x 4 x 4: at least as many
-    // as the 32 x 8 x 4 tiles used)
-    const size_t tiles = (size_t)((ni + 1 + 31) / 32) * ((nj + 1 + 3) / 4) * ((nk + 1 + 3) / 4);
-    // per-tile bits (bytes, padded to 16), two flag words and two lists per tile, two counts
-    ctx->ex_tiles_bytes = ((tiles + 15) & ~size_t(15)) + 4 * tiles * 4 + 64;
-    ctx->ex_tiles = (uint8_t*)ctx_alloc(ctx, ctx->ex_tiles_bytes);
+    // extrapolation scratch sizes (allocated on first use): the largest face grid with rows
+    // padded to 16 bytes, and one index per cell of it
+    for (int f = EL_FIELD_U; f <= EL_FIELD_W; ++f) {
+        int n0, n1, n2;
+        field_dims(ctx, f, n0, n1, n2);
+        ctx->ex_dist_bytes = std::max(ctx->ex_dist_bytes, (size_t)((n0 + 15) & ~15) * n1 * n2);
+        ctx->ex_list_bytes = std::max(ctx->ex_list_bytes, (size_t)n0 * n1 * n2 * sizeof(int));
+    }
     ctx->dscal = (Scalars*)ctx_alloc(ctx, 4 * sizeof(Scalars));
     Geom g = stencil_geom(ni, nj, nk, ctx->num_sms);
     ctx->max_partials = std::max(g.blocks(), ctx->num_sms * 16) * 2 + 64;
     ctx->partials = (double*)ctx_alloc(ctx, ctx->max_partials * sizeof(double));
     ctx->counter = (unsigned*)ctx_alloc(ctx, 64);
-    ok = ok && ctx->valid_tmp && ctx->ex_tiles && ctx->dscal && ctx->partials && ctx->counter;
+    ok = ok && ctx->dscal && ctx->partials && ctx->counter;
     if (ok && cudaMallocHost(&ctx->hscal, 4 * sizeof(Scalars)) != cudaSuccess) ok = false;
     if (ok) {
         // create_grid (simulator.cpp:58-69): valid masks start at 1
@@ -485,21 +481,45 @@ EL_API int el_add_gravity(el_ctx* ctx, double dt, double gravity) {
     return finish(ctx, launch_gravity(ctx, gravity, nullptr, dt), "add_gravity");
 }
 
+// the velocity components (write_back: extrapolate) and the level set (extrapolate_const)
+static int extrapolate_fields(el_ctx* ctx, bool velocity, bool level_set, int layers) {
+    int fields[4];
+    uint8_t* valid[4];
+    bool wb[4];
+    int nf = 0;
+    if (velocity)
+        for (int c = 0; c < 3; ++c, ++nf) {
+            fields[nf] = EL_FIELD_U + c;
+            valid[nf] = (uint8_t*)ctx->field[EL_FIELD_VALID_U + c];
+            wb[nf] = true;
+        }
+    if (level_set) {
+        fields[nf] = EL_FIELD_PHI;
+        valid[nf] = (uint8_t*)ctx->field[EL_FIELD_VALID_PHI];
+        wb[nf] = false;
+        ++nf;
+    }
+    // each field's mask and values read once
+    double bytes = 0;
+    for (int q = 0; q < nf; ++q) bytes += (double)ctx->field_bytes[fields[q]] / ctx->esz * (1 + ctx->esz);
+    ProfScope prof(ctx, EL_KC_EXTRAPOLATE, bytes);
+    return launch_extrapolate_fields(ctx, nf, fields, valid, wb, layers);
+}
+
 EL_API int el_extrapolate_level_set(el_ctx* ctx, int layers) {
     CHECK_CTX(ctx);
     if (layers < 0) return EL_ERR_INVALID_ARGUMENT;
-    return finish(ctx,
-                  launch_extrapolate(ctx, EL_FIELD_PHI, (uint8_t*)ctx->field[EL_FIELD_VALID_PHI], layers, false),
-                  "extrapolate_level_set");
+    const int rc = ensure_extrapolation(ctx, 1);
+    if (rc != EL_OK) return rc;
+    return finish(ctx, extrapolate_fields(ctx, false, true, layers), "extrapolate_level_set");
 }
 
 EL_API int el_extrapolate_velocity(el_ctx* ctx, int layers) {
     CHECK_CTX(ctx);
     if (layers < 0) return EL_ERR_INVALID_ARGUMENT;
-    int n = 0;
-    for (int comp = 0; comp < 3; ++comp)
-        n += launch_extrapolate(ctx, EL_FIELD_U + comp, (uint8_t*)ctx->field[EL_FIELD_VALID_U + comp], layers, true);
-    return finish(ctx, n, "extrapolate_velocity");
+    const int rc = ensure_extrapolation(ctx, 3);
+    if (rc != EL_OK) return rc;
+    return finish(ctx, extrapolate_fields(ctx, true, false, layers), "extrapolate_velocity");
 }
 
 EL_API int el_find_valid_velocity(el_ctx* ctx) {
@@ -510,13 +530,6 @@ EL_API int el_find_valid_velocity(el_ctx* ctx) {
 EL_API int el_set_invalid_velocity_zero(el_ctx* ctx) {
     CHECK_CTX(ctx);
     return finish(ctx, launch_zero_invalid(ctx), "set_invalid_velocity_zero");
-}
-
-static int extrapolate_prof(el_ctx* ctx, int field, uint8_t* valid, int layers, bool write_back) {
-    // per layer: the stamp mask and the field, each read once (invalid cells also write)
-    const double per = (double)ctx->field_bytes[field] + ctx->field_bytes[field] / ctx->esz;
-    ProfScope prof(ctx, EL_KC_EXTRAPOLATE, per * layers);
-    return launch_extrapolate(ctx, field, valid, layers, write_back);
 }
 
 static int masks_prof(el_ctx* ctx, bool gravity, double g, const Scalars* s, double dtv, bool zero) {
@@ -604,11 +617,9 @@ EL_API int el_step(el_ctx* ctx, double dt, const el_step_params* p, el_step_stat
     int n = launch_set_dt(ctx, dt);
     const Scalars* dts = ctx->dscal;
     // update_second_order (apps/eulerian_liquid_3d.cpp:106-120), reinitialize() excluded
-    for (int comp = 0; comp < 3; ++comp)
-        n += extrapolate_prof(ctx, EL_FIELD_U + comp, (uint8_t*)ctx->field[EL_FIELD_VALID_U + comp],
-                              p->extrapolation_layers, true);
-    n += extrapolate_prof(ctx, EL_FIELD_PHI, (uint8_t*)ctx->field[EL_FIELD_VALID_PHI], p->extrapolation_layers,
-                          false);
+    rc = ensure_extrapolation(ctx, 4);
+    if (rc != EL_OK) return rc;
+    n += extrapolate_fields(ctx, true, true, p->extrapolation_layers);
     n += advect_level_set_impl(ctx, dts, dt, p->trace_phi, p->sample_phi);
     n += advect_velocity_impl(ctx, dts, dt, p->trace_vel, p->sample_vel);
     n += masks_prof(ctx, true, p->gravity, dts, dt, true);
@@ -623,19 +634,15 @@ EL_API int el_step(el_ctx* ctx, double dt, const el_step_params* p, el_step_stat
 // One sub-step of a scene with nothing decided on the host, for capture into a batch graph:
 // device dt (cut at the frame end), el_step's work, the solve with both loops on the device.
 // kernels[0]: kernels outside the solver loops; [1] per refinement sweep; [2] per PCG pass.
-// Streams, events and extrapolation scratch of the captured step's side branches (outside any
-// capture: they allocate).
+// Streams and events of the captured step's side branches, and the extrapolation scratch (outside
+// any capture: they allocate).
 int el::prepare_device_step(el_ctx* ctx) {
     for (int q = 0; q < 3; ++q) {
         if (!ctx->side[q]) EL_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->side[q], cudaStreamNonBlocking));
         if (!ctx->side_join[q]) EL_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->side_join[q], cudaEventDisableTiming));
-        if (!ctx->ex_stamp_extra[q]) {
-            ctx->ex_stamp_extra[q] = (uint8_t*)ctx_alloc(ctx, ctx->ex_stamp_bytes);
-            ctx->ex_tiles_extra[q] = (uint8_t*)ctx_alloc(ctx, ctx->ex_tiles_bytes);
-            if (!ctx->ex_stamp_extra[q] || !ctx->ex_tiles_extra[q])
-                return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "step branches");
-        }
     }
+    const int rc = ensure_extrapolation(ctx, 4);
+    if (rc != EL_OK) return rc;
     if (!ctx->side_fork) EL_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->side_fork, cudaEventDisableTiming));
     return EL_OK;
 }
@@ -668,14 +675,8 @@ int el::enqueue_step_device(el_ctx* ctx, const el_step_params& p, double cfl, do
                             const BatchRecord* rec, int kernels[3], bool fork) {
     int n = launch_substep(ctx, cfl, dt_frame, rec, (unsigned long long*)(ctx->dscal + 3));
     const Scalars* dts = ctx->dscal;
-    // the four extrapolations are independent: four branches, each with its own scratch
-    n += branches(ctx, fork ? 4 : 1, 4, [&](int q) {
-        if (q < 3)
-            return launch_extrapolate(ctx, EL_FIELD_U + q, (uint8_t*)ctx->field[EL_FIELD_VALID_U + q],
-                                      p.extrapolation_layers, true, fork ? q : 0);
-        return launch_extrapolate(ctx, EL_FIELD_PHI, (uint8_t*)ctx->field[EL_FIELD_VALID_PHI], p.extrapolation_layers,
-                                  false, fork ? 3 : 0);
-    });
+    // the four extrapolations go through each launch together
+    n += extrapolate_fields(ctx, true, true, p.extrapolation_layers);
     // the level set and the velocity advect independently (both read the old velocity); the
     // level set is enqueued first because enqueueing the velocity's advection swaps the
     // context's velocity buffers on the host

@@ -170,8 +170,13 @@ struct el_ctx {
 
     // advection / extrapolation ping-pong buffers (same shapes as phi, u, v, w)
     void* tmp[4] = {};
-    uint8_t* valid_tmp = nullptr;  // largest face mask
-    uint8_t* ex_tiles = nullptr;   // extrapolation tile activity (two maps)
+    // extrapolation scratch per field slot (el_extrap.cu): two distance buffers with rows padded
+    // to 16 bytes and the cells of each distance; counts / offsets / cursors per slot and distance
+    uint8_t* ex_da[4] = {};
+    uint8_t* ex_db[4] = {};
+    int* ex_list[4] = {};
+    int* ex_counts = nullptr;
+    size_t ex_dist_bytes = 0, ex_list_bytes = 0;
 
     // projection
     uint8_t* flags = nullptr;
@@ -206,13 +211,9 @@ struct el_ctx {
     // captured CUDA graphs of PCG iteration batches, one per solver (index EL_SOLVER_*)
     cudaGraphExec_t iter_graph[3] = {nullptr, nullptr, nullptr};
     cudaStream_t body_stream[2] = {nullptr, nullptr};  // capture of conditional-node bodies
-    // branches of a captured step (independent extrapolations and advections run side by side),
-    // each extra branch with its own extrapolation scratch
+    // branches of a captured step (the independent advections run side by side)
     cudaStream_t side[3] = {nullptr, nullptr, nullptr};
     cudaEvent_t side_fork = nullptr, side_join[3] = {nullptr, nullptr, nullptr};
-    uint8_t* ex_stamp_extra[3] = {nullptr, nullptr, nullptr};
-    uint8_t* ex_tiles_extra[3] = {nullptr, nullptr, nullptr};
-    size_t ex_stamp_bytes = 0, ex_tiles_bytes = 0;
     int iter_graph_len[3] = {0, 0, 0};
     int iter_graph_kernels[3] = {0, 0, 0};
     bool use_graphs = true;
@@ -274,6 +275,12 @@ int check_launch(el_ctx* ctx, const char* what);
 void* ctx_alloc(el_ctx* ctx, size_t bytes);  // zero-filled, owned by the context
 int ensure_projection(el_ctx* ctx);
 int ensure_solver(el_ctx* ctx, int solver);
+void field_dims(const el_ctx* ctx, int field, int& n0, int& n1, int& n2);
+// extrapolation (el_extrap.cu): scratch for `nfields` slots (outside capture), and up to four
+// fields extrapolated together; returns the kernels launched
+int ensure_extrapolation(el_ctx* ctx, int nfields);
+int launch_extrapolate_fields(el_ctx* ctx, int nf, const int* fields, uint8_t* const* valid, const bool* write_back,
+                              int layers);
 
 // finest-level tile kernels of the FP32 multigrid (el_march.cu); each returns its launches
 bool march_supported(const el_ctx* ctx);

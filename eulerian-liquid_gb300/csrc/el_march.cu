@@ -56,7 +56,8 @@ constexpr int kCX = 24;          // staged coarse row: i0/2 - 4 .. i0/2 + 19
 constexpr int kCY = kTJ / 2 + 2; // staged coarse rows: j0/2 - 1 .. j0/2 + 8
 constexpr int kComputeWarps = kTJ / 2;             // rows 2w and 2w + 1 each
 constexpr int kThreads = 32 * (kComputeWarps + 1);  // and one producer warp
-constexpr int kStages = 6;       // plane buffers in the ring: three in use, three in flight
+constexpr int kMaxStages = 6;    // plane buffers in the ring: three in use, the rest in flight
+constexpr int kMVW = kTI + 2;    // masked-value plane: columns i0 - 1 .. i0 + 32 of the staged rows
 constexpr unsigned kFull = 0xffffffffu;
 // a bounded wait: this many polls (each try_wait may itself suspend for a while) before the
 // kernel gives up, records the fault and stops
@@ -80,14 +81,22 @@ struct Layout {
     static constexpr int rec_box_bytes = rec_w * kHY * rec_bytes; // 9792 / 5184
     static constexpr int centre_bytes = kTI * kTJ * 4;           // 2048
     static constexpr int coarse_bytes = kCX * kCY * 4;           // 960
+    // ZERO2 and UPDZ read the first sweep's values x1 = w1 b / D (0 where D is not positive) at
+    // all seven stencil points: those of a plane are formed once, when it lands (the other modes
+    // mask their values by the points' diagonals directly, which costs less than a barrier)
+    static constexpr bool mv = M == UPDZ || M == ZERO2;
+    static constexpr int mv_bytes = kMVW * kHY * 4;              // 2448
     static constexpr int al(int b) { return (b + 127) / 128 * 128; }
     static constexpr int off_rec = 0;
     static constexpr int off_halo = al(rec_box_bytes);
     static constexpr int off_centre = off_halo + nhalo * al(halo_bytes);
     static constexpr int off_coarse = off_centre + ncentre * al(centre_bytes);
-    static constexpr int stage = al(off_coarse + (coarse ? coarse_bytes : 0));
-    static constexpr int smem = 128 + kStages * stage + 128;  // barriers first; alignment slack
-    static_assert(2 * kStages * 8 <= 128, "barriers fit in front of the ring");
+    static constexpr int off_mv = off_coarse + (coarse ? al(coarse_bytes) : 0);
+    static constexpr int stage = al(off_mv + (mv ? mv_bytes : 0));
+    // six slots, five for ZERO2 (so that four of its CTAs fit an SM)
+    static constexpr int stages = M == ZERO2 ? 5 : 6;
+    static constexpr int smem = 128 + stages * stage + 128;  // barriers first; alignment slack
+    static_assert(stages <= kMaxStages && 2 * kMaxStages * 8 <= 128, "barriers fit in front of the ring");
 };
 
 struct Maps {
@@ -158,6 +167,21 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
 
 __device__ __forceinline__ float mg_divf(float a, float b) { return __fdividef(a, b); }
 
+// named barrier 1 over the compute warps (the producer warp does not take part), returning the
+// OR of `pred` over them: the same value in every compute warp
+__device__ __forceinline__ bool compute_barrier_or(int pred) {
+    unsigned r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "barrier.cta.red.or.pred q, 1, %2, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"(pred), "r"(32 * kComputeWarps)
+        : "memory");
+    return r != 0;
+}
+
 // records of a staged plane: {diagonal, +x, +y, +z couplings}
 struct Rc {
     float d, x, y, z;
@@ -205,14 +229,15 @@ __device__ __forceinline__ bool dpos(const unsigned char* rec, int idx, int byte
 }
 
 template <int M>
-__global__ void __launch_bounds__(kThreads) march_kernel(const __grid_constant__ Maps maps, const Args a) {
+__global__ void __launch_bounds__(kThreads, 2) march_kernel(const __grid_constant__ Maps maps, const Args a) {
     using L = Layout<M>;
     Scalars* s = a.s;
     if (s->done) return;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char* smem = aligned_smem(smem_raw);
     uint64_t* full = reinterpret_cast<uint64_t*>(smem);   // a plane landed (transaction count)
-    uint64_t* empty = full + kStages;                     // every compute warp is done with it
+    constexpr int kStages = L::stages;
+    uint64_t* empty = full + kMaxStages;                  // every compute warp is done with it
     __shared__ volatile int abort_flag;
     const int tid = threadIdx.x;
     const int lane = tid & 31, w = tid >> 5;
@@ -294,16 +319,48 @@ __global__ void __launch_bounds__(kThreads) march_kernel(const __grid_constant__
             if (lane == 0) mbar_arrive(&empty[rslot]);
             if (++rslot == kStages) rslot = 0;
         };
-        for (int it = b; it < n && ok; it += G) {
+        // the masked values of a landed plane, by all compute warps, then a barrier of the
+        // compute warps.  A wait that ran out does not skip the barrier: every compute warp meets
+        // it, and the barrier ORs the warps' abort state, so that all of them stop together.
+        bool stop = false;
+        auto prepass = [&](int sl) {
+            if constexpr (L::mv) {
+                unsigned char* Pp = stage_ptr<M>(smem, sl);
+                const float* h0 = reinterpret_cast<const float*>(Pp + L::off_halo);
+                const float* h1 = reinterpret_cast<const float*>(Pp + L::off_halo + L::al(L::halo_bytes));
+                float* mvp = reinterpret_cast<float*>(Pp + L::off_mv);
+                for (int e = w * 32 + lane; e < kMVW * kHY; e += 32 * kComputeWarps) {
+                    const int hy = e / kMVW, hx = e - hy * kMVW + 3;    // in the staged value box
+                    const int ridx = hy * L::rec_w + (hx - 4) + L::rec_x0;  // the same cell's record
+                    float out = 0.f;
+                    if (dpos(Pp + L::off_rec, ridx, L::rec_bytes)) {
+                        float raw = h0[hy * kHX + hx];
+                        if (M == UPDZ) raw = raw - alpha * h1[hy * kHX + hx];
+                        out = mg_divf(w1 * raw, ld_rec(Pp + L::off_rec, ridx, L::rec_bytes).d);
+                    }
+                    mvp[e] = out;
+                }
+                stop = compute_barrier_or(!ok || abort_flag != 0);
+            }
+        };
+        auto aborted = [&]() -> bool { return L::mv ? stop : !ok; };
+        for (int it = b; it < n && !aborted(); it += G) {
             const int4 d = a.items[it];
             const int i0 = d.x, j0 = d.y, k0 = d.z, k1 = d.w;
             const int i = i0 + lane;
-            int sa = wait_next(), sb = wait_next();  // planes k0 - 1 and k0
+            int sa = wait_next();  // plane k0 - 1
+            prepass(sa);
+            int sb = wait_next();  // plane k0
+            prepass(sb);
             float racc0 = 0.f;                     // RESTRICT: this lane's 2x2 (j, k) sum
             for (int k = k0; k < k1; ++k) {
                 const int sc = wait_next();        // plane k + 1
-                if (!ok) break;
+                prepass(sc);
+                if (aborted()) break;
                 const unsigned char* P[3] = {stage_ptr<M>(smem, sa), stage_ptr<M>(smem, sb), stage_ptr<M>(smem, sc)};
+                auto MV = [&](int pl, int idx) -> float {
+                    return reinterpret_cast<const float*>(P[pl] + L::off_mv)[idx];
+                };
                 auto H = [&](int pl, int h, int idx) -> float {
                     return reinterpret_cast<const float*>(P[pl] + L::off_halo + h * L::al(L::halo_bytes))[idx];
                 };
@@ -362,51 +419,16 @@ __global__ void __launch_bounds__(kThreads) march_kernel(const __grid_constant__
                             part += pc * apc;
                         }
                     } else {
-                        // every other mode masks the stencil's values by the points' diagonals
-                        bool dp[7];
+                        // ZERO2 / UPDZ read the stencil's first-sweep values x1 = w1 b / D from
+                        // the planes' masked values, with b = r' = r - alpha Ap (UPDZ) or b (ZERO2);
+                        // RESTRICT / PROLONG / LAST mask the level's values by the points' diagonals
+                        float v[7];
+                        if constexpr (L::mv) {
+                            const int e0 = (row + 1) * kMVW + lane + 1;
+                            const int mo[7] = {0, -1, 1, -kMVW, kMVW, 0, 0};
 #pragma unroll
-                        for (int q = 0; q < 7; ++q) dp[q] = q == 0 ? (r0.d > 0.f) : D(pq[q], rc + ro[q]);
-                        if (M == UPDZ || M == ZERO2) {
-                            // b = r' = r - alpha Ap (UPDZ) or b (ZERO2) at every stencil point; the
-                            // first sweep from zero is pointwise, x1 = w1 b / D on cells with D > 0
-                            float x1[7];
-                            float bc = 0.f;
-#pragma unroll
-                            for (int q = 0; q < 7; ++q) {
-                                const int idx = hc + vo[q];
-                                const float bq =
-                                    M == UPDZ ? H(pq[q], 0, idx) - alpha * H(pq[q], 1, idx) : H(pq[q], 0, idx);
-                                if (q == 0) bc = bq;
-                                x1[q] = dp[q] ? mg_divf(w1 * bq, q == 0 ? r0.d : R(pq[q], rc + ro[q]).d) : 0.f;
-                            }
-                            st.v0 = x1[0];
-                            st.vxm = x1[1];
-                            st.vxp = x1[2];
-                            st.vym = x1[3];
-                            st.vyp = x1[4];
-                            st.vzm = x1[5];
-                            st.vzp = x1[6];
-                            float x2 = 0.f;
-                            if (dp[0]) x2 = st.v0 + mg_divf(w2 * (bc - apply7(st)), st.d);
-                            if (live) {
-                                if (M == UPDZ) {
-                                    // x += alpha p; r' out of place.  A tile also covers cells
-                                    // outside the system (diagonal 0), whose r may still hold an
-                                    // earlier solve's values: their r' is 0 and they stay out of
-                                    // |r'|^2, as in the segment kernels (where r is 0 on every
-                                    // such cell of an active segment).
-                                    const float rn = dp[0] ? bc : 0.f;
-                                    a.out0[c] = Cn(0, row) + alpha * Cn(1, row);
-                                    a.out1[c] = rn;
-                                    part += rn * rn;
-                                    a.out2[c] = x2;
-                                } else {
-                                    a.out0[c] = x2;
-                                }
-                            }
+                            for (int q = 0; q < 7; ++q) v[q] = MV(pq[q], e0 + mo[q]);
                         } else {
-                            // RESTRICT / PROLONG / LAST: the level's values at the stencil points
-                            float v[7];
 #pragma unroll
                             for (int q = 0; q < 7; ++q) {
                                 float raw = H(pq[q], 0, hc + vo[q]);
@@ -418,22 +440,46 @@ __global__ void __launch_bounds__(kThreads) march_kernel(const __grid_constant__
                                     const int cx = (fi >> 1) + 4, cy = (fj >> 1) + 1;
                                     raw += reinterpret_cast<const float*>(P[pq[q]] + L::off_coarse)[cy * kCX + cx];
                                 }
-                                v[q] = dp[q] ? raw : 0.f;
+                                const bool dq = q == 0 ? (r0.d > 0.f) : D(pq[q], rc + ro[q]);
+                                v[q] = dq ? raw : 0.f;
                             }
-                            st.v0 = v[0];
-                            st.vxm = v[1];
-                            st.vxp = v[2];
-                            st.vym = v[3];
-                            st.vyp = v[4];
-                            st.vzm = v[5];
-                            st.vzp = v[6];
+                        }
+                        st.v0 = v[0];
+                        st.vxm = v[1];
+                        st.vxp = v[2];
+                        st.vym = v[3];
+                        st.vyp = v[4];
+                        st.vzm = v[5];
+                        st.vzp = v[6];
+                        const bool dp0 = r0.d > 0.f;
+                        if (M == UPDZ || M == ZERO2) {
+                            const float bc = M == UPDZ ? H(1, 0, hc) - alpha * H(1, 1, hc) : H(1, 0, hc);
+                            float x2 = 0.f;
+                            if (dp0) x2 = st.v0 + mg_divf(w2 * (bc - apply7(st)), st.d);
+                            if (live) {
+                                if (M == UPDZ) {
+                                    // x += alpha p; r' out of place.  A tile also covers cells
+                                    // outside the system (diagonal 0), whose r may still hold an
+                                    // earlier solve's values: their r' is 0 and they stay out of
+                                    // |r'|^2, as in the segment kernels (where r is 0 on every
+                                    // such cell of an active segment).
+                                    const float rn = dp0 ? bc : 0.f;
+                                    a.out0[c] = Cn(0, row) + alpha * Cn(1, row);
+                                    a.out1[c] = rn;
+                                    part += rn * rn;
+                                    a.out2[c] = x2;
+                                } else {
+                                    a.out0[c] = x2;
+                                }
+                            }
+                        } else {
                             const float bc = Cn(0, row);
                             if (M == RESTRICT) {
-                                res[r] = dp[0] ? bc - apply7(st) : 0.f;
+                                res[r] = dp0 ? bc - apply7(st) : 0.f;
                             } else {
                                 const float omega = M == PROLONG ? w1 : w2;
                                 float xo = 0.f;
-                                if (dp[0]) xo = st.v0 + mg_divf(omega * (bc - apply7(st)), st.d);
+                                if (dp0) xo = st.v0 + mg_divf(omega * (bc - apply7(st)), st.d);
                                 if (live) {
                                     a.out0[c] = xo;
                                     if (M == LAST) part += bc * xo;
@@ -457,7 +503,7 @@ __global__ void __launch_bounds__(kThreads) march_kernel(const __grid_constant__
                 sa = sb;
                 sb = sc;
             }
-            if (!ok) break;
+            if (aborted()) break;
             // the item's last two planes are not needed any more
             release_next();
             release_next();

@@ -1141,7 +1141,7 @@ __global__ void __launch_bounds__(kBottomThreads) mg_bottom_kernel(LGeom gf, con
 // (fault, bad, done) and leaves; the other CTAs' waits then run out too.
 constexpr int kCoarseMaxLevels = 16;
 constexpr int kCoopQuads = kBottomThreads / 128;  // restriction quads per CTA
-constexpr long long kBarrierPolls = 1ll << 21;    // each poll sleeps ~100 ns: ~0.2 s per barrier
+constexpr long long kBarrierPolls = 1ll << 21;    // past the first 4096, each poll sleeps ~100 ns: ~0.2 s
 
 struct CoarseLevel {
     LGeom g;
@@ -1184,7 +1184,7 @@ __device__ __forceinline__ bool coarse_grid_barrier(unsigned* bar, unsigned nblo
                     ok = 0;
                     break;
                 }
-                __nanosleep(100);
+                if (n > 4096) __nanosleep(100);  // a tight poll first: the others are usually close
             }
         }
         __threadfence();

@@ -16,177 +16,6 @@ __device__ __forceinline__ float add_rn2(float a, float b) { return __fadd_rn(a,
 __device__ __forceinline__ double add_rn2(double a, double b) { return __dadd_rn(a, b); }
 
 // ---------------------------------------------------------------------------------------
-// Extrapolation.  Jacobi layers as extrapolate() does them, computed in place: a cell's
-// value changes only in the layer it becomes valid, and it reads only neighbours that were
-// valid before that layer began, whose values no longer change.  Validity is kept as a
-// stamp: 0 = valid from the start, l+1 = became valid in layer l, 255 = still invalid;
-// "valid before layer l" is stamp <= l.
-
-__global__ void valid_from_stamps_kernel(long long n, const uint8_t* __restrict__ stamp, uint8_t* __restrict__ valid) {
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
-        valid[c] = stamp[c] != 255 ? 1 : 0;
-}
-
-// One layer over the active tiles.  Tiles are 32 x 8 x 4 cells (i, j, k); a persistent grid
-// walks the layer's list of tiles (built by the layer before), skipping those with no invalid
-// cell left.  A cell
-// can only become valid in layer l+1 next to a cell that became valid in layer l (otherwise it
-// would have become valid in layer l already), so layer l+1 visits a tile only if a cell made
-// valid in layer l lies in it or on the face, edge or corner it shares with it; layer 0 visits
-// the tiles that hold an invalid cell and have a valid cell in their tile neighbourhood.  A
-// visited tile turns the stamps of its cells plus a one-cell halo into one 34-bit "valid before
-// this layer" mask per (y, z) row (warp ballots over coalesced byte loads) behind one barrier,
-// so a cell's 3x3x3 validity test is nine shared-memory words and a shift; only cells with a
-// valid neighbour read field values, and the sum walks the neighbours in z, y, x order like
-// the reference loop.  Stamps of cells updated in this layer become layer + 1, which reads as
-// "not yet valid" whether a block sees the old or new byte.
-constexpr int kExBX = 32, kExBY = 8, kExBZ = 4;
-
-struct TileGrid {
-    int tx, ty, tz;  // tiles per axis
-};
-
-// stamps from the valid mask, and per tile: any valid cell (bit 0), any invalid cell (bit 1)
-__global__ void __launch_bounds__(kExBX * kExBY) stamps_init_kernel(int n0, int n1, int n2,
-                                                                    const uint8_t* __restrict__ valid,
-                                                                    uint8_t* __restrict__ stamp, TileGrid tg,
-                                                                    uint8_t* __restrict__ tile_bits) {
-    const int t = blockIdx.x;
-    const int bx = t % tg.tx, by = (t / tg.tx) % tg.ty, bz = t / (tg.tx * tg.ty);
-    const int i = bx * kExBX + threadIdx.x, j = by * kExBY + threadIdx.y;
-    bool any_valid = false, any_invalid = false;
-    if (i < n0 && j < n1) {
-        for (int k = bz * kExBZ; k < min(n2, bz * kExBZ + kExBZ); ++k) {
-            const long long c = lin3(i, j, k, n0, n1);
-            const bool v = valid[c] != 0;
-            stamp[c] = v ? 0 : 255;
-            any_valid = any_valid || v;
-            any_invalid = any_invalid || !v;
-        }
-    }
-    const int bv = __syncthreads_or(any_valid), bi = __syncthreads_or(any_invalid);
-    if (threadIdx.x == 0 && threadIdx.y == 0) tile_bits[t] = (uint8_t)((bv ? 1 : 0) | (bi ? 2 : 0));
-}
-
-// layer 0's list: tiles with an invalid cell and a valid cell in their tile neighbourhood
-__global__ void tiles_layer0_kernel(TileGrid tg, const uint8_t* __restrict__ tile_bits, int* __restrict__ list,
-                                    int* __restrict__ count) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int ntiles = tg.tx * tg.ty * tg.tz;
-    if (t >= ntiles) return;
-    const int bx = t % tg.tx, by = (t / tg.tx) % tg.ty, bz = t / (tg.tx * tg.ty);
-    bool near_valid = false;
-    for (int dz = -1; dz <= 1; ++dz)
-        for (int dy = -1; dy <= 1; ++dy)
-            for (int dx = -1; dx <= 1; ++dx) {
-                const int x = bx + dx, y = by + dy, z = bz + dz;
-                if (x < 0 || y < 0 || z < 0 || x >= tg.tx || y >= tg.ty || z >= tg.tz) continue;
-                near_valid = near_valid || (tile_bits[x + tg.tx * (y + tg.ty * z)] & 1);
-            }
-    if ((tile_bits[t] & 2) && near_valid) list[atomicAdd(count, 1)] = t;
-}
-
-template <typename T>
-__global__ void __launch_bounds__(kExBX * kExBY) extrapolate_layer_kernel(int n0, int n1, int n2, T* __restrict__ g,
-                                                                          uint8_t* __restrict__ stamp, int layer,
-                                                                          TileGrid tg, const int* __restrict__ list_in,
-                                                                          const int* __restrict__ count_in,
-                                                                          uint8_t* __restrict__ flags_out,
-                                                                          int* __restrict__ list_out,
-                                                                          int* __restrict__ count_out,
-                                                                          uint8_t* __restrict__ tile_bits) {
-    // validity before this layer of the tile and its one-cell halo, one 34-bit row mask per
-    // (y, z) row: bit hx <-> cell i0 - 1 + hx
-    constexpr int kRows = (kExBZ + 2) * (kExBY + 2);
-    __shared__ unsigned long long rows[kExBZ + 2][kExBY + 2];
-    __shared__ unsigned int touched;  // bit (dz+1)*9 + (dy+1)*3 + (dx+1): that neighbour tile may change next
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int warp = ty, lane = tx;  // blocks are 32 x 8: one warp per y row of threads
-    const unsigned full = 0xffffffffu;
-    const int nlist = *count_in;
-    for (int q = blockIdx.x; q < nlist; q += gridDim.x) {
-        const int t = list_in[q];
-        if (!(tile_bits[t] & 2)) continue;  // block-uniform: no invalid cell left
-        const int bx = t % tg.tx, by = (t / tg.tx) % tg.ty, bz = t / (tg.tx * tg.ty);
-        const int i0 = bx * kExBX, j0 = by * kExBY, k0 = bz * kExBZ;
-        const int i = i0 + tx, j = j0 + ty;
-        if (tx == 0 && ty == 0) touched = 0u;
-        // each warp ballots whole rows: lanes read cells i0-1+lane, lanes 0 and 1 also the two
-        // beyond; out-of-grid cells count as invalid
-        for (int r = warp; r < kRows; r += kExBY) {
-            const int hz = r / (kExBY + 2), hy = r - hz * (kExBY + 2);
-            const int y = j0 + hy - 1, z = k0 + hz - 1;
-            const bool row_in = y >= 0 && y < n1 && z >= 0 && z < n2;
-            const long long base = row_in ? lin3(0, y, z, n0, n1) : 0;
-            const int xa = i0 - 1 + lane, xb = i0 + 31 + lane;
-            const bool va = row_in && xa >= 0 && xa < n0 && stamp[base + xa] <= layer;
-            const bool vb = row_in && lane < 2 && xb < n0 && stamp[base + xb] <= layer;
-            const unsigned lo = __ballot_sync(full, va), hi = __ballot_sync(full, vb);
-            if (lane == 0) rows[hz][hy] = (unsigned long long)lo | ((unsigned long long)(hi & 3u) << 32);
-        }
-        __syncthreads();
-        unsigned int dirs = 0u;
-        bool left = false;
-        if (i < n0 && j < n1) {
-            for (int kk = 0; kk < kExBZ; ++kk) {
-                const int k = k0 + kk;
-                if (k >= n2) break;
-                if ((rows[kk + 1][ty + 1] >> (tx + 1)) & 1ull) continue;  // valid already
-                unsigned long long near = 0;
-#pragma unroll
-                for (int dk = 0; dk < 3; ++dk)
-#pragma unroll
-                    for (int dj = 0; dj < 3; ++dj) near |= rows[kk + dk][ty + dj];
-                if (!((near >> tx) & 7ull)) {  // no valid neighbour yet
-                    left = true;
-                    continue;
-                }
-                T sum = T(0);
-                int count = 0;
-#pragma unroll
-                for (int dk = 0; dk < 3; ++dk)
-#pragma unroll
-                    for (int dj = 0; dj < 3; ++dj) {
-                        const unsigned long long m = rows[kk + dk][ty + dj] >> tx;
-#pragma unroll
-                        for (int di = 0; di < 3; ++di)
-                            if ((m >> di) & 1ull) {
-                                sum = add_rn2(sum, g[lin3(i + di - 1, j + dj - 1, k + dk - 1, n0, n1)]);
-                                ++count;
-                            }
-                    }
-                const long long c = lin3(i, j, k, n0, n1);
-                g[c] = sum / (T)count;
-                stamp[c] = (uint8_t)(layer + 1);
-                // next layer: this tile, and the neighbour tiles this cell touches
-                const int xl = tx == 0 ? -1 : 0, xh = tx == kExBX - 1 ? 1 : 0;
-                const int yl = ty == 0 ? -1 : 0, yh = ty == kExBY - 1 ? 1 : 0;
-                const int zl = kk == 0 ? -1 : 0, zh = kk == kExBZ - 1 ? 1 : 0;
-                for (int dz = zl; dz <= zh; ++dz)
-                    for (int dy = yl; dy <= yh; ++dy)
-                        for (int dx = xl; dx <= xh; ++dx) dirs |= 1u << ((dz + 1) * 9 + (dy + 1) * 3 + (dx + 1));
-            }
-        }
-        if (dirs) atomicOr(&touched, dirs);
-        // a tile whose cells are all valid now is never visited again; flag the tiles a cell
-        // made valid here touches for the next layer (the barriers also keep the row masks
-        // intact until every thread is done with them)
-        const int tid = tx + kExBX * ty;
-        if (!__syncthreads_or(left) && tid == 0) tile_bits[t] &= (uint8_t)~2u;
-        if (tid < 27 && ((touched >> tid) & 1u)) {
-            const int ox = bx + tid % 3 - 1, oy = by + (tid / 3) % 3 - 1, oz = bz + tid / 9 - 1;
-            if (ox >= 0 && ox < tg.tx && oy >= 0 && oy < tg.ty && oz >= 0 && oz < tg.tz) {
-                const int nt = ox + tg.tx * (oy + tg.ty * oz);
-                // the first to flag a tile lists it for the next layer
-                if (atomicExch(reinterpret_cast<unsigned int*>(flags_out) + nt, 1u) == 0u)
-                    list_out[atomicAdd(count_out, 1)] = nt;
-            }
-        }
-        __syncthreads();  // `touched` is read before the next tile resets it
-    }
-}
-
-// ---------------------------------------------------------------------------------------
 // add_gravity + find_valid_velocity + set_invalid_velocity_zero, fused per face component
 // (simulator.cpp:90-93, 125-158, 169-178).  The phi test applies on faces with index in
 // [1, n) along the normal and [1, n-1) along the tangential axes, as the reference's loops.
@@ -366,7 +195,7 @@ static int g1(el_ctx* ctx, long long n) {
     return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, (long long)ctx->num_sms * ctx->stencil_per_sm));
 }
 
-static void field_dims(el_ctx* ctx, int field, int& n0, int& n1, int& n2) {
+void field_dims(const el_ctx* ctx, int field, int& n0, int& n1, int& n2) {
     n0 = ctx->ni;
     n1 = ctx->nj;
     n2 = ctx->nk;
@@ -378,52 +207,6 @@ static void field_dims(el_ctx* ctx, int field, int& n0, int& n1, int& n2) {
         n1++;
         n2++;
     }
-}
-
-// extrapolate `field` over `layers` Jacobi layers using the mask `valid`; when write_back the
-// mask is updated like extrapolate() (velocity), else left alone like extrapolate_const().
-// slot 0 uses the context's extrapolation scratch, slots 1-3 the step branches' own
-int launch_extrapolate(el_ctx* ctx, int field, uint8_t* valid, int layers, bool write_back, int slot) {
-    int n0, n1, n2;
-    field_dims(ctx, field, n0, n1, n2);
-    const long long n = (long long)n0 * n1 * n2;
-    uint8_t* stamp = slot ? ctx->ex_stamp_extra[slot - 1] : ctx->valid_tmp;
-    uint8_t* tiles = slot ? ctx->ex_tiles_extra[slot - 1] : ctx->ex_tiles;
-    dim3 block(kExBX, kExBY, 1);
-    const TileGrid tg{(n0 + kExBX - 1) / kExBX, (n1 + kExBY - 1) / kExBY, (n2 + kExBZ - 1) / kExBZ};
-    const int ntiles = tg.tx * tg.ty * tg.tz;
-    // the context's tile buffer: per-tile bits, and per layer parity a flag word per tile and a
-    // list of the tiles to visit (with its length)
-    uint8_t* bits = tiles;
-    unsigned int* flags_base = reinterpret_cast<unsigned int*>(tiles + ((ntiles + 15) & ~15));
-    unsigned int* flag[2] = {flags_base, flags_base + ntiles};
-    int* list[2] = {reinterpret_cast<int*>(flags_base + 2 * ntiles), reinterpret_cast<int*>(flags_base + 3 * ntiles)};
-    int* count[2] = {reinterpret_cast<int*>(flags_base + 4 * ntiles), reinterpret_cast<int*>(flags_base + 4 * ntiles) + 1};
-    cudaMemsetAsync(count[0], 0, 2 * sizeof(int), ctx->stream);
-    stamps_init_kernel<<<ntiles, block, 0, ctx->stream>>>(n0, n1, n2, valid, stamp, tg, bits);
-    tiles_layer0_kernel<<<(ntiles + 255) / 256, 256, 0, ctx->stream>>>(tg, bits, list[0], count[0]);
-    int launched = 2;
-    const int grid = std::max(1, std::min(ntiles, ctx->num_sms * ctx->extrap_per_sm));
-    const int L = std::min(layers, 254);  // stamps are bytes: 255 marks "still invalid"
-    for (int l = 0; l < L; ++l) {
-        const int in = l & 1, out = (l + 1) & 1;
-        cudaMemsetAsync(flag[out], 0, ntiles * sizeof(unsigned int), ctx->stream);
-        cudaMemsetAsync(count[out], 0, sizeof(int), ctx->stream);
-        if (ctx->dtype == EL_F64)
-            extrapolate_layer_kernel<double><<<grid, block, 0, ctx->stream>>>(
-                n0, n1, n2, (double*)ctx->field[field], stamp, l, tg, list[in], count[in],
-                reinterpret_cast<uint8_t*>(flag[out]), list[out], count[out], bits);
-        else
-            extrapolate_layer_kernel<float><<<grid, block, 0, ctx->stream>>>(
-                n0, n1, n2, (float*)ctx->field[field], stamp, l, tg, list[in], count[in],
-                reinterpret_cast<uint8_t*>(flag[out]), list[out], count[out], bits);
-        ++launched;
-    }
-    if (write_back) {
-        valid_from_stamps_kernel<<<g1(ctx, n), 256, 0, ctx->stream>>>(n, stamp, valid);
-        ++launched;
-    }
-    return launched;
 }
 
 template <typename T>

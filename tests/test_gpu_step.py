@@ -117,3 +117,32 @@ def test_mixed_step_fp32_matches_oracle_to_solve_tolerance(el, orc):
     # the GPU pressure satisfies the oracle's system to the solve tolerance (FP32 grid rounding)
     assert residual_rel(orc, mats, sim.download("pressure")) <= 5e-5
     sim.close()
+
+
+@pytest.mark.parametrize("shape,density,layers", [((23, 17, 30), 0.02, 10), ((40, 9, 12), 0.3, 3),
+                                                  ((12, 33, 20), 0.0005, 40), ((16, 16, 16), 0.9, 1),
+                                                  ((18, 14, 11), 0.05, 0)])
+def test_extrapolation_random_masks_bitexact(el, orc, shape, density, layers):
+    """Extrapolation by distance order against the oracle's layer loop on random masks and
+    non-cubic grids: few valid cells (long reach), dense masks, more than 31 layers (the row
+    scan of the distance pass), no layers at all."""
+    ni, nj, nk = shape
+    rng = np.random.default_rng(ni * 1000 + layers)
+    for dtype in DTYPES:
+        sim = make_sim(el, shape, dtype)
+        vel = {}
+        for f in ("u", "v", "w", "phi"):
+            vel[f] = rng.standard_normal(sim.shape(f)).astype(dtype)
+            sim.upload(f, vel[f])
+            m = (rng.random(sim.shape(f)) < density).astype(np.uint8)
+            vel["valid_" + f] = m
+            sim.upload("valid_" + f, m)
+        sim.extrapolate_velocity(layers)
+        sim.extrapolate_level_set(layers)
+        for f in ("u", "v", "w", "phi"):
+            g, mm = orc.extrapolate(vel[f], vel["valid_" + f], layers)
+            np.testing.assert_array_equal(sim.download(f), g, err_msg=f)
+            # extrapolate_const leaves the level set's mask alone
+            want_mask = vel["valid_" + f] if f == "phi" else mm
+            np.testing.assert_array_equal(sim.download("valid_" + f), want_mask, err_msg=f)
+        sim.close()
