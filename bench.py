@@ -12,7 +12,8 @@ value      steps/s with the mixed solver (FP32 multigrid PCG inside FP64 refinem
            resident in HBM, CUDA events on the library's stream.
 plain_fp64 the same workload with plain FP64 PCG (Jacobi); mg_fp64: FP64 multigrid PCG.
 e2e        steps/s through the C ABI with host buffers: every step uploads phi, u, v, w from
-           pinned host memory and downloads phi, u, v, w and the pressure.
+           pinned host memory and downloads phi, u, v, w and the pressure (asynchronous copies
+           pipelined field by field on two streams).
 roofline   the dominant kernel class, algorithmic bytes / device time over the timed region.
 cpu_baseline  the CPU oracle (OpenMP restatement with MIC(0)-PCG) on one step of the workload.
 
@@ -253,27 +254,52 @@ def pressure_error(el, sim, params_mixed, n_steps):
 
 
 def e2e_batch_steps(el, torch, sims, batch, steps):
-    """Steps through the C ABI with host buffers: every scene's inputs up, one batch step, the
-    results down, every step."""
+    """Steps through the C ABI with pinned host buffers: every step uploads each scene's inputs
+    (phi, u, v, w) from host memory, runs one batch step and downloads its results (phi, u, v, w,
+    pressure).  The transfers are pipelined field by field with el_download_async /
+    el_upload_async on two streams: the downloads start when the step is done, and each field's
+    upload for the next step starts as soon as that field's download has landed, so downloads
+    and uploads of different fields share the full-duplex host link."""
+    ins = ("u", "v", "w", "phi")
+    outs = ins + ("pressure",)
     host = []
     for sim in sims:
         h = {}
-        for f in ("phi", "u", "v", "w", "pressure"):
+        for f in outs:
             h[f] = torch.empty(sim.shape(f), dtype=torch.float32, pin_memory=True).numpy()
             sim.download(f, out=h[f])
         host.append(h)
-    h2d = sum(h[f].nbytes for h in host for f in ("phi", "u", "v", "w"))
-    d2h = sum(h[f].nbytes for h in host for f in ("phi", "u", "v", "w", "pressure"))
+    h2d = sum(h[f].nbytes for h in host for f in ins)
+    d2h = sum(h[f].nbytes for h in host for f in outs)
+    s_down, s_up = torch.cuda.Stream(), torch.cuda.Stream()
+    scene_streams = [torch.cuda.ExternalStream(sim.stream_handle) for sim in sims]
+    ev_step = [torch.cuda.Event() for _ in sims]
+    ev_field = [{f: torch.cuda.Event() for f in outs} for _ in sims]
+    ev_up = torch.cuda.Event()
+
+    def uploads(wait_downloads):
+        for q, sim in enumerate(sims):
+            for f in ins:
+                if wait_downloads:
+                    s_up.wait_event(ev_field[q][f])
+                sim.upload_async(f, host[q][f], s_up.cuda_stream)
+        ev_up.record(s_up)
+        for st in scene_streams:
+            st.wait_event(ev_up)
+
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(steps):
-        for sim, h in zip(sims, host):
-            for f in ("phi", "u", "v", "w"):
-                sim.upload(f, h[f])
+    uploads(False)  # the first step's inputs
+    for step in range(steps):
         batch.step(1)
-        for sim, h in zip(sims, host):
-            for f in ("phi", "u", "v", "w", "pressure"):
-                sim.download(f, out=h[f])
+        for q, sim in enumerate(sims):
+            ev_step[q].record(scene_streams[q])
+            s_down.wait_event(ev_step[q])
+            for f in outs:
+                sim.download_async(f, host[q][f], s_down.cuda_stream)
+                ev_field[q][f].record(s_down)
+        if step + 1 < steps:
+            uploads(True)  # the next step's inputs, from the host buffers just filled
     torch.cuda.synchronize()
     return steps / (time.perf_counter() - t0), h2d, d2h
 
@@ -439,7 +465,8 @@ def run_ours(args, dist):
         e2e_value, h2d, d2h = e2e_batch_steps(el, torch, [sim], batch, max(3, K // 2))
         slowest_step_s = dist.max(1.0 / e2e_value)
         e2e = {"value": dist.world / slowest_step_s, "unit": "steps/s", "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "path": "el_upload, el_batch_step, el_download"}
+               "d2h_bytes_per_step": d2h,
+               "path": "el_upload_async, el_batch_step, el_download_async (pinned host buffers, two copy streams)"}
     batch.close()
     # roofline: the dominant class's launches over K eager steps, CUDA events around each launch
     _, stats, _, prof, _ = timed_steps(el, torch, sim, stream, params, K, dist,

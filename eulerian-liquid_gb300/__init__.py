@@ -162,6 +162,8 @@ def _declare(L):
     L.el_ctx_solver_tiles_active.argtypes = [ctxp, C.POINTER(C.c_int)]
     L.el_upload.argtypes = [ctxp, i, vp, sz]
     L.el_download.argtypes = [ctxp, i, vp, sz]
+    L.el_upload_async.argtypes = [ctxp, i, vp, sz, vp]
+    L.el_download_async.argtypes = [ctxp, i, vp, sz, vp]
     L.el_field_device_ptr.argtypes = [ctxp, i, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)]
     L.el_emit_clear.argtypes = [ctxp, i]
     L.el_emit_sphere.argtypes = [ctxp, i, d, d, d, d]
@@ -318,6 +320,30 @@ class Simulator:
             raise ValueError(f"{field}: output buffer must be a C-contiguous {self.field_dtype(field)} {self.shape(field)}")
         self._check(self.lib.el_download(self.h, FIELDS[field], a.ctypes.data, a.nbytes), f"download {field}")
         return a
+
+    def _host_buffer(self, field, a):
+        if a.shape != self.shape(field) or a.dtype != self.field_dtype(field) or not a.flags.c_contiguous:
+            raise ValueError(f"{field}: buffer must be a C-contiguous {self.field_dtype(field)} {self.shape(field)}")
+        return a
+
+    def upload_async(self, field, array, stream=None):
+        """Enqueue the copy of a (pinned, C-contiguous) host array into a field on `stream` (a
+        cudaStream_t handle; None = the context's stream) without waiting for it."""
+        a = self._host_buffer(field, array)
+        self._check(self.lib.el_upload_async(self.h, FIELDS[field], a.ctypes.data, a.nbytes, stream),
+                    f"upload_async {field}")
+
+    def download_async(self, field, out, stream=None):
+        """Enqueue the copy of a field into a (pinned) host array without waiting for it."""
+        a = self._host_buffer(field, out)
+        self._check(self.lib.el_download_async(self.h, FIELDS[field], a.ctypes.data, a.nbytes, stream),
+                    f"download_async {field}")
+        return a
+
+    @property
+    def stream_handle(self):
+        """The context's cudaStream_t (el_ctx_get_stream)."""
+        return self.lib.el_ctx_get_stream(self.h)
 
     def device_ptr(self, field):
         p = C.c_void_p()

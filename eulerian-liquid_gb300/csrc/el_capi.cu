@@ -341,6 +341,32 @@ EL_API int el_download(el_ctx* ctx, int field, void* host, size_t bytes) {
     return EL_OK;
 }
 
+static int check_transfer(el_ctx* ctx, int field, const void* host, size_t bytes) {
+    if (field < 0 || field >= EL_FIELD_COUNT || !host) return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "bad field");
+    if (bytes != ctx->field_bytes[field])
+        return set_error(ctx, EL_ERR_INVALID_ARGUMENT,
+                         "field size mismatch: expected " + std::to_string(ctx->field_bytes[field]) + " bytes");
+    return EL_OK;
+}
+
+EL_API int el_upload_async(el_ctx* ctx, int field, const void* host, size_t bytes, void* stream) {
+    CHECK_CTX(ctx);
+    const int rc = check_transfer(ctx, field, host, bytes);
+    if (rc != EL_OK) return rc;
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    EL_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->field[field], host, bytes, cudaMemcpyHostToDevice, s));
+    return EL_OK;
+}
+
+EL_API int el_download_async(el_ctx* ctx, int field, void* host, size_t bytes, void* stream) {
+    CHECK_CTX(ctx);
+    const int rc = check_transfer(ctx, field, host, bytes);
+    if (rc != EL_OK) return rc;
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    EL_CUDA_TRY(ctx, cudaMemcpyAsync(host, ctx->field[field], bytes, cudaMemcpyDeviceToHost, s));
+    return EL_OK;
+}
+
 EL_API int el_field_device_ptr(el_ctx* ctx, int field, void** dptr, size_t* bytes) {
     if (!ctx || field < 0 || field >= EL_FIELD_COUNT || !dptr) return EL_ERR_INVALID_ARGUMENT;
     *dptr = ctx->field[field];

@@ -158,7 +158,7 @@ struct el_ctx {
     int seg_per_sm = 6, stencil_per_sm = 8, extrap_per_sm = 12, advect_rows = 4;
     int advect_tiled = 1;  // advection through the staged-tile kernels
     int solver_tiles = 1;  // the mixed solver's finest level on the tile kernels (where supported)
-    int coarse_fused = 1;  // the FP32 V-cycle's coarse levels in one cooperative launch (where supported)
+    int coarse_fused = 0;  // the FP32 V-cycle's coarse levels in one cooperative launch (where supported)
     unsigned* coarse_bar = nullptr;  // its grid barrier words
     int coarse_per_sm = 0;           // its resident CTAs per SM (0: cannot run, per-level launches)
     cudaStream_t stream = nullptr;

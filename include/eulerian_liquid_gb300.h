@@ -143,9 +143,9 @@ typedef struct el_tuning {
                                     tile kernels with TMA-staged planes, where the grid allows
                                     (ni a multiple of 8, at least 64 x 16 x 16 cells); 0: the
                                     row-segment kernels everywhere                              */
-    int coarse_fused;            /* 1 (default): the mixed solver's multigrid levels below the
-                                    finest, and the bottom pair, in one cooperative launch per
-                                    V-cycle (identical results); 0: one launch per level pass   */
+    int coarse_fused;            /* 1: the mixed solver's multigrid levels below the finest, and
+                                    the bottom pair, in one cooperative launch per V-cycle
+                                    (identical results); 0 (default): one launch per level pass */
 } el_tuning;
 int el_ctx_set_tuning(el_ctx* ctx, const el_tuning* t);
 int el_ctx_get_tuning(const el_ctx* ctx, el_tuning* t);
@@ -188,6 +188,14 @@ int el_ctx_profile_end(el_ctx* ctx, el_profile_entry* out);
 /* Host <-> device copies of a whole field (bytes must equal the field's size). */
 int el_upload(el_ctx* ctx, int field, const void* host, size_t bytes);
 int el_download(el_ctx* ctx, int field, void* host, size_t bytes);
+/* The same copies enqueued on `stream` (a cudaStream_t; NULL = the context's stream) without
+ * waiting for them (no counterpart in the reference, whose grids live in host memory): the
+ * caller orders them against the context's work (e.g. with events on el_ctx_get_stream), keeps
+ * `host` alive until they complete, and gets overlapped transfers only from pinned memory.
+ * Downloads and uploads of different fields on two streams run at the same time (the host link
+ * is full duplex). */
+int el_upload_async(el_ctx* ctx, int field, const void* host, size_t bytes, void* stream);
+int el_download_async(el_ctx* ctx, int field, void* host, size_t bytes, void* stream);
 /* Device pointer of a field, for zero-copy use by a caller that owns device memory. */
 int el_field_device_ptr(el_ctx* ctx, int field, void** dptr, size_t* bytes);
 

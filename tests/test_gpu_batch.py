@@ -176,3 +176,30 @@ def test_tuning_rejects_out_of_range(el):
     sim.set_tuning(seg_blocks_per_sm=2, advect_rows=8)
     assert sim.get_tuning()["seg_blocks_per_sm"] == 2 and sim.get_tuning()["advect_rows"] == 8
     sim.close()
+
+
+def test_async_transfers_pipelined(el):
+    """el_download_async / el_upload_async on two streams ordered by events (the benchmark's
+    end-to-end pattern) move the same bytes as the synchronous copies."""
+    torch = pytest.importorskip("torch")
+    sim = el.Simulator(40, 24, 32, dtype=el.EL_F32)
+    rng = np.random.default_rng(5)
+    want = {f: rng.standard_normal(sim.shape(f)).astype(np.float32) for f in ("phi", "u", "v", "w")}
+    pinned = {f: torch.empty(sim.shape(f), dtype=torch.float32, pin_memory=True).numpy() for f in want}
+    back = {f: torch.empty(sim.shape(f), dtype=torch.float32, pin_memory=True).numpy() for f in want}
+    s_up, s_down = torch.cuda.Stream(), torch.cuda.Stream()
+    ev = {f: torch.cuda.Event() for f in want}
+    for f, a in want.items():
+        pinned[f][...] = a
+        sim.upload_async(f, pinned[f], s_up.cuda_stream)
+        ev[f].record(s_up)
+    for f in want:
+        s_down.wait_event(ev[f])
+        sim.download_async(f, back[f], s_down.cuda_stream)
+    torch.cuda.synchronize()
+    for f, a in want.items():
+        np.testing.assert_array_equal(back[f], a)
+        np.testing.assert_array_equal(sim.download(f), a)
+    with pytest.raises(ValueError):
+        sim.download_async("phi", np.empty((3, 3, 3), np.float32))
+    sim.close()
