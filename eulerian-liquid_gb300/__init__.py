@@ -95,7 +95,8 @@ class Grid(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("seg_blocks_per_sm", C.c_int), ("stencil_blocks_per_sm", C.c_int),
                 ("extrapolate_blocks_per_sm", C.c_int), ("advect_rows", C.c_int), ("advect_tiled", C.c_int),
-                ("solver_tiles", C.c_int), ("coarse_fused", C.c_int)]
+                ("solver_tiles", C.c_int), ("coarse_fused", C.c_int),
+                ("dependent_launch", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -118,18 +119,32 @@ class ProfileEntry(C.Structure):
 _lib = None
 
 
+def debug_check_take():
+    """(checked, word): whether the loaded library is the debug build, and the first failed
+    device-side index check since the last call as (site << 40) | index, or 0."""
+    w = C.c_uint64()
+    on = C.c_int()
+    st = load().el_debug_check_take(C.byref(w), C.byref(on))
+    if st != EL_OK:
+        raise ELError(st, "el_debug_check_take")
+    return bool(on.value), int(w.value)
+
+
 def library_path():
     return _build_mod.LIB
 
 
 def load(build_if_needed=True):
-    """Load the CUDA library (building it in-tree when sources are newer)."""
+    """Load the CUDA library (building it in-tree when sources are newer).  With the environment
+    variable EL_CHECKED=1 the process loads the debug build instead, whose kernels check their
+    indices (el_debug_check_take reports a failed check)."""
     global _lib
     if _lib is not None:
         return _lib
-    path = _build_mod.LIB
-    if build_if_needed and not _build_mod.up_to_date():
-        path = _build_mod.build()
+    checked = os.environ.get("EL_CHECKED", "0") == "1"
+    path = _build_mod.LIB_CHECKED if checked else _build_mod.LIB
+    if build_if_needed and not _build_mod.up_to_date(checked):
+        path = _build_mod.build(checked=checked)
     if not os.path.exists(path):
         raise ImportError(f"the CUDA hot-path library is not built: {path}")
     lib = C.CDLL(path)
@@ -162,6 +177,7 @@ def _declare(L):
     L.el_ctx_solver_tiles_active.argtypes = [ctxp, C.POINTER(C.c_int)]
     L.el_upload.argtypes = [ctxp, i, vp, sz]
     L.el_download.argtypes = [ctxp, i, vp, sz]
+    L.el_debug_check_take.argtypes = [C.POINTER(C.c_uint64), C.POINTER(C.c_int)]
     L.el_upload_async.argtypes = [ctxp, i, vp, sz, vp]
     L.el_download_async.argtypes = [ctxp, i, vp, sz, vp]
     L.el_field_device_ptr.argtypes = [ctxp, i, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)]

@@ -22,9 +22,9 @@ import time
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 # (seg_blocks_per_sm, stencil_blocks_per_sm, extrapolate_blocks_per_sm, advect_rows, advect_tiled,
-#  solver_tiles, coarse_fused)
-DEFAULT = (6, 8, 12, 4, 1, 1, 0)
-RANGES = ((1, 2, 3, 4, 6, 8), (2, 4, 8, 16), (4, 8, 12, 16), (2, 4, 8), (1, 0), (1, 0), (0, 1))
+#  solver_tiles, coarse_fused, dependent_launch)
+DEFAULT = (6, 8, 12, 4, 1, 1, 0, 1)
+RANGES = ((1, 2, 3, 4, 6, 8), (2, 4, 8, 16), (4, 8, 12, 16), (2, 4, 8), (1, 0), (1, 0), (0, 1), (1, 0))
 STATE_FIELDS = ("phi", "u", "v", "w", "valid_u", "valid_v", "valid_w")
 
 
@@ -35,7 +35,8 @@ def cache_path():
 def _as_tuning(c):
     c = tuple(c) + DEFAULT[len(c):]  # shorter (older) entries take the defaults for the rest
     return {"seg_blocks_per_sm": c[0], "stencil_blocks_per_sm": c[1], "extrapolate_blocks_per_sm": c[2],
-            "advect_rows": c[3], "advect_tiled": c[4], "solver_tiles": c[5], "coarse_fused": c[6]}
+            "advect_rows": c[3], "advect_tiled": c[4], "solver_tiles": c[5], "coarse_fused": c[6],
+            "dependent_launch": c[7]}
 
 
 def batch_key(device_name, sims, params, cfl, dt_frame):

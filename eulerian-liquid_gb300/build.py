@@ -22,6 +22,8 @@ CSRC = os.path.join(HERE, "csrc")
 HOST = os.path.join(HERE, "host")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libeulerian_liquid_gb300.so")
+# the debug build: every kernel index check on (-DEL_CHECKED); objects in _build/checked/
+LIB_CHECKED = os.path.join(OUT_DIR, "libeulerian_liquid_gb300_checked.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
@@ -49,10 +51,11 @@ def headers():
     return hs
 
 
-def _compile(src):
-    obj = os.path.join(OUT_DIR, os.path.basename(src) + ".o")
+def _compile(src, checked=False):
+    obj_dir = os.path.join(OUT_DIR, "checked") if checked else OUT_DIR
+    obj = os.path.join(obj_dir, os.path.basename(src) + ".o")
     if src.endswith(".cu"):
-        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
+        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *(["-DEL_CHECKED"] if checked else []), "-c", src, "-o", obj]
     else:
         cmd = [nvcc(), "-x", "c++", "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
                "-fvisibility=hidden", "-I", os.path.join(ROOT, "include"), "-I", HOST, "-c", src, "-o", obj]
@@ -62,30 +65,33 @@ def _compile(src):
     return obj
 
 
-def up_to_date():
-    if not os.path.exists(LIB):
+def up_to_date(checked=False):
+    lib = LIB_CHECKED if checked else LIB
+    if not os.path.exists(lib):
         return False
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     cu, cpp = sources()
     return all(os.path.getmtime(f) <= t for f in cu + cpp + headers() + [__file__])
 
 
-def build(force=False, verbose=False):
-    if not force and up_to_date():
-        return LIB
-    os.makedirs(OUT_DIR, exist_ok=True)
+def build(force=False, verbose=False, checked=False):
+    """The product library, or with checked=True the debug build with the kernels' index checks."""
+    lib = LIB_CHECKED if checked else LIB
+    if not force and up_to_date(checked):
+        return lib
+    os.makedirs(os.path.join(OUT_DIR, "checked") if checked else OUT_DIR, exist_ok=True)
     cu, cpp = sources()
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(_compile, cu + cpp))
-    tmp = LIB + ".tmp"
+        objs = list(ex.map(lambda f: _compile(f, checked), cu + cpp))
+    tmp = lib + ".tmp"
     cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart_static", "-lrt", "-lpthread", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     if verbose:
-        print(LIB)
-    return LIB
+        print(lib)
+    return lib
 
 
 def build_cpp_program(main_src, out_name, force=False):
@@ -111,4 +117,4 @@ def build_cpp_program(main_src, out_name, force=False):
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose=True)
+    build(force="--force" in sys.argv, verbose=True, checked="--checked" in sys.argv)

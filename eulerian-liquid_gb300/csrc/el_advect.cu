@@ -76,7 +76,8 @@ __global__ void __launch_bounds__(256) advect_kernel(GridView<T> src, T* __restr
         r = sample_weno6(src, x, y, z, dx, inv_dx);
     else
         r = sample_trilinear(src, x, y, z, dx, inv_dx);
-    out[lin3(i, j, k, src.n0, src.n1)] = r;
+    const long long oc = lin3(i, j, k, src.n0, src.n1);
+    if (EL_IN(oc, (long long)src.n0 * src.n1 * src.n2, 1)) out[oc] = r;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -277,7 +278,9 @@ __global__ void __launch_bounds__(kTileX * kTileY) advect_velocity_tiled_kernel(
             T y = (j + T(0.5)) * dx + g.oy;
             T z = (k + T(0.5)) * dx + g.oz;
             backtrace_staged<T, TRACE>(mac, sm, x, y, z, h, dx, inv_dx);
-            o[lin3(i, j, k, g.n0, g.n1)] = sample_staged(g, b, x, y, z, dx, inv_dx);
+            const long long oc = lin3(i, j, k, g.n0, g.n1);
+            const T r = sample_staged(g, b, x, y, z, dx, inv_dx);
+            if (EL_IN(oc, (long long)g.n0 * g.n1 * g.n2, 2)) o[oc] = r;
         }
     }
 }
@@ -307,7 +310,8 @@ __global__ void __launch_bounds__(kTileX * kTileY) advect_phi_tiled_kernel(GridV
             r = sample_weno6(src, x, y, z, dx, inv_dx);
         else
             r = sample_trilinear(src, x, y, z, dx, inv_dx);
-        out[lin3(i, j, k, src.n0, src.n1)] = r;
+        const long long oc = lin3(i, j, k, src.n0, src.n1);
+        if (EL_IN(oc, (long long)src.n0 * src.n1 * src.n2, 3)) out[oc] = r;
     }
 }
 
@@ -402,7 +406,8 @@ __global__ void __launch_bounds__(kWX * kWY, sizeof(T) == 4 ? 2 : 1) advect_phi_
         } else {
             r = sample_weno6(src, x, y, z, dx, inv_dx);
         }
-        out[lin3(i, j, k, src.n0, src.n1)] = r;
+        const long long oc = lin3(i, j, k, src.n0, src.n1);
+        if (EL_IN(oc, (long long)src.n0 * src.n1 * src.n2, 3)) out[oc] = r;
     }
 }
 
@@ -542,5 +547,7 @@ int advect_any(int dtype, int ni, int nj, int nk, double dx, int comp, void* out
         return advect_launch<double>(ni, nj, nk, dx, comp, out, in, vu, vv, vw, dt, trace, sample, rows, s);
     return advect_launch<float>(ni, nj, nk, dx, comp, out, in, vu, vv, vw, dt, trace, sample, rows, s);
 }
+
+EL_CHECK_EXPORT(advect)
 
 }  // namespace el

@@ -276,6 +276,7 @@ EL_API int el_batch_step(el_batch* b, int steps) {
     if (parity < 0) return batch_error(b, EL_ERR_INVALID_ARGUMENT, "a scene was stepped outside the batch");
     int rc = order_with_scenes(b, true);
     if (rc != EL_OK) return rc;
+    NvtxRange range("el_batch_step");
     for (int s = 0; s < steps; ++s) {
         const cudaError_t e = cudaGraphLaunch(b->exec[parity], b->stream);
         if (e != cudaSuccess) return batch_error(b, EL_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));

@@ -38,6 +38,12 @@ int enqueue_solve_device(el_ctx* ctx, const el_solve_params& prm, int kernels[3]
 int enqueue_step_device(el_ctx* ctx, const el_step_params& p, double cfl, double dt_frame, const BatchRecord* rec,
                         int kernels[3], bool fork);
 int prepare_device_step(el_ctx* ctx);
+// debug-build check words of the kernel translation units (0 in the product build)
+unsigned long long check_take_advect();
+unsigned long long check_take_march();
+unsigned long long check_take_extrap();
+unsigned long long check_take_solve();
+unsigned long long check_take_project();
 
 int set_error(el_ctx* ctx, int code, const std::string& msg) {
     if (ctx) ctx->last_error = msg;
@@ -130,6 +136,21 @@ EL_API const char* el_status_string(int status) {
         case EL_ERR_TOO_LARGE: return "grid exceeds the no-allocation scratch limit (EL_NOALLOC_MAX_CELLS)";
         default: return "unknown status";
     }
+}
+
+EL_API int el_debug_check_take(uint64_t* word, int* checked) {
+    if (!word || !checked) return EL_ERR_INVALID_ARGUMENT;
+#ifdef EL_CHECKED
+    *checked = 1;
+#else
+    *checked = 0;
+#endif
+    const unsigned long long w[5] = {check_take_advect(), check_take_march(), check_take_extrap(), check_take_solve(),
+                                     check_take_project()};
+    *word = 0;
+    for (unsigned long long v : w)
+        if (v && !*word) *word = v;
+    return EL_OK;
 }
 
 EL_API const char* el_ctx_last_error(const el_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
@@ -249,7 +270,7 @@ EL_API int el_ctx_set_tuning(el_ctx* ctx, const el_tuning* t) {
         t->stencil_blocks_per_sm > 16 || t->extrapolate_blocks_per_sm < 1 || t->extrapolate_blocks_per_sm > 16 ||
         (t->advect_rows != 1 && t->advect_rows != 2 && t->advect_rows != 4 && t->advect_rows != 8) ||
         (t->advect_tiled != 0 && t->advect_tiled != 1) || (t->solver_tiles != 0 && t->solver_tiles != 1) ||
-        (t->coarse_fused != 0 && t->coarse_fused != 1))
+        (t->coarse_fused != 0 && t->coarse_fused != 1) || (t->dependent_launch != 0 && t->dependent_launch != 1))
         return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "tuning out of range");
     // the reduction partials are sized for 16 stencil blocks per SM (el_ctx_create)
     ctx->seg_per_sm = t->seg_blocks_per_sm;
@@ -259,6 +280,7 @@ EL_API int el_ctx_set_tuning(el_ctx* ctx, const el_tuning* t) {
     ctx->advect_tiled = t->advect_tiled;
     ctx->solver_tiles = t->solver_tiles;
     ctx->coarse_fused = t->coarse_fused;
+    ctx->dependent_launch = t->dependent_launch;
     // cached PCG iteration graphs hold the old launch shapes
     cudaStreamSynchronize(ctx->stream);
     for (auto& g : ctx->iter_graph)
@@ -278,6 +300,7 @@ EL_API int el_ctx_get_tuning(const el_ctx* ctx, el_tuning* t) {
     t->advect_tiled = ctx->advect_tiled;
     t->solver_tiles = ctx->solver_tiles;
     t->coarse_fused = ctx->coarse_fused;
+    t->dependent_launch = ctx->dependent_launch;
     return EL_OK;
 }
 
@@ -645,14 +668,26 @@ EL_API int el_step(el_ctx* ctx, double dt, const el_step_params* p, el_step_stat
     // update_second_order (apps/eulerian_liquid_3d.cpp:106-120), reinitialize() excluded
     rc = ensure_extrapolation(ctx, 4);
     if (rc != EL_OK) return rc;
-    n += extrapolate_fields(ctx, true, true, p->extrapolation_layers);
-    n += advect_level_set_impl(ctx, dts, dt, p->trace_phi, p->sample_phi);
-    n += advect_velocity_impl(ctx, dts, dt, p->trace_vel, p->sample_vel);
-    n += masks_prof(ctx, true, p->gravity, dts, dt, true);
+    {
+        NvtxRange r("el_step extrapolate");
+        n += extrapolate_fields(ctx, true, true, p->extrapolation_layers);
+    }
+    {
+        NvtxRange r("el_step advect");
+        n += advect_level_set_impl(ctx, dts, dt, p->trace_phi, p->sample_phi);
+        n += advect_velocity_impl(ctx, dts, dt, p->trace_vel, p->sample_vel);
+    }
+    {
+        NvtxRange r("el_step gravity and masks");
+        n += masks_prof(ctx, true, p->gravity, dts, dt, true);
+    }
     ctx->launches += n;
     rc = check_launch(ctx, "step");
     if (rc != EL_OK) return rc;
-    rc = solve_pressure_impl(ctx, p->solve, &st->solve);
+    {
+        NvtxRange r("el_step solve_pressure");
+        rc = solve_pressure_impl(ctx, p->solve, &st->solve);
+    }
     if (rc != EL_OK) return rc;
     return st->solve.status == EL_OK ? EL_OK : set_error(ctx, st->solve.status, "pressure solve did not converge");
 }

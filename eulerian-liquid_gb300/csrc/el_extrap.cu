@@ -300,7 +300,9 @@ __global__ void __launch_bounds__(kDistThreads) ex_scatter_kernel(const ExArgs a
 #pragma unroll
             for (int b = 0; b < 4; ++b) {
                 const int d = (int)((wv[u] >> (8 * b)) & 0xffu);
-                if (i0 + b < F.n0 && d >= 1 && d <= L) F.list[bbase[d] + rank[u][b]] = (int)(cell0 + b);
+                if (i0 + b < F.n0 && d >= 1 && d <= L &&
+                    EL_IN(bbase[d] + rank[u][b], (long long)F.n0 * F.n1 * F.n2, 20))
+                    F.list[bbase[d] + rank[u][b]] = (int)(cell0 + b);
             }
         }
         __syncthreads();
@@ -325,7 +327,10 @@ __global__ void __launch_bounds__(kDistThreads) ex_layer_kernel(const ExArgs a, 
         int f = 0;
         while (f + 1 < a.nf && q >= start[f + 1]) ++f;
         const ExField& F = a.f[f];
-        const int c = F.list[a.offsets[f * 256 + dist] + (q - start[f])];
+        const int li = a.offsets[f * 256 + dist] + (q - start[f]);
+        if (!EL_IN(li, (long long)F.n0 * F.n1 * F.n2, 21)) continue;
+        const int c = F.list[li];
+        if (!EL_IN(c, (long long)F.n0 * F.n1 * F.n2, 22)) continue;
         const int i = c % F.n0, r = c / F.n0;
         const int j = r % F.n1, k = r / F.n1;
         T* g = static_cast<T*>(F.g);
@@ -456,5 +461,7 @@ int launch_extrapolate_fields(el_ctx* ctx, int nf, const int* fields, uint8_t* c
     }
     return n;
 }
+
+EL_CHECK_EXPORT(extrap)
 
 }  // namespace el

@@ -8,10 +8,12 @@
 
 #include <cuda.h>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/eulerian_liquid_gb300.h"
@@ -138,6 +140,49 @@ struct DeviceGuard {
     DeviceGuard& operator=(const DeviceGuard&) = delete;
 };
 
+// Debug build (compiled with -DEL_CHECKED, the library libeulerian_liquid_gb300_checked.so):
+// the main kernels check the index of each global store (and of the indirect loads) against
+// its array before the access.  A failed check skips the access and records the first failure
+// -- a site number and the index -- in its translation unit's check word; it never traps.
+// el_checked_take() reads and clears every unit's word.  In the product build the checks are
+// `true` and cost nothing.
+#ifdef EL_CHECKED
+static __device__ unsigned long long el_check_word;  // one per translation unit
+__device__ __forceinline__ bool el_in_bounds(long long idx, long long n, unsigned site) {
+    if (idx >= 0 && idx < n) return true;
+    atomicCAS(&el_check_word, 0ull, ((unsigned long long)site << 40) | ((unsigned long long)idx & 0xffffffffffull));
+    return false;
+}
+#define EL_IN(idx, n, site) el::el_in_bounds((long long)(idx), (long long)(n), (site))
+#define EL_CHECK_EXPORT(unit)                                                  \
+    unsigned long long check_take_##unit() {                                   \
+        unsigned long long v = 0, z = 0;                                       \
+        cudaMemcpyFromSymbol(&v, el_check_word, sizeof(v));                    \
+        cudaMemcpyToSymbol(el_check_word, &z, sizeof(z));                      \
+        return v;                                                              \
+    }
+#else
+#define EL_IN(idx, n, site) true
+#define EL_CHECK_EXPORT(unit) \
+    unsigned long long check_take_##unit() { return 0ull; }
+#endif
+
+// Programmatic dependent launch: a kernel launched with launch_dependent() may be scheduled
+// while the kernel before it on the stream is still running; its first act is pdl_wait(), which
+// returns once that kernel has completed and its memory operations are visible (at once for a
+// kernel launched the ordinary way).  pdl_trigger() lets the next such kernel be scheduled.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// An NVTX range around one phase of a step on the host timeline (no cost unless a profiler
+// that collects NVTX is attached).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
 struct DeviceBuffer {
     void* ptr = nullptr;
     size_t bytes = 0;
@@ -159,6 +204,7 @@ struct el_ctx {
     int advect_tiled = 1;  // advection through the staged-tile kernels
     int solver_tiles = 1;  // the mixed solver's finest level on the tile kernels (where supported)
     int coarse_fused = 0;  // the FP32 V-cycle's coarse levels in one cooperative launch (where supported)
+    int dependent_launch = 1;  // the solver's chained kernels as programmatic dependent launches
     unsigned* coarse_bar = nullptr;  // its grid barrier words
     int coarse_per_sm = 0;           // its resident CTAs per SM (0: cannot run, per-level launches)
     cudaStream_t stream = nullptr;
@@ -232,6 +278,26 @@ struct el_ctx {
     // current solve (read back once per solve), for the byte counts of the segment kernels
     std::vector<double> prof_active;
 };
+
+namespace el {
+// launch `kernel` on the context's stream; with the context's `dependent_launch` set, as a
+// programmatic dependent launch (the kernel must begin with pdl_wait())
+template <typename... KArgs, typename... Args>
+cudaError_t launch_dependent(const el_ctx* ctx, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                             Args&&... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = ctx->dependent_launch ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+}  // namespace el
 
 namespace el {
 

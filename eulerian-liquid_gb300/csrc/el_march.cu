@@ -232,6 +232,8 @@ template <int M>
 __global__ void __launch_bounds__(kThreads, 2) march_kernel(const __grid_constant__ Maps maps, const Args a) {
     using L = Layout<M>;
     Scalars* s = a.s;
+    pdl_wait();
+    pdl_trigger();
     if (s->done) return;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char* smem = aligned_smem(smem_raw);
@@ -413,7 +415,7 @@ __global__ void __launch_bounds__(kThreads, 2) march_kernel(const __grid_constan
                             pc = st.v0;
                             apc = apply7(st);
                         }
-                        if (live) {
+                        if (live && EL_IN(c, (long long)a.n0 * a.n1 * a.n2, 10)) {
                             a.out0[c] = pc;
                             a.out1[c] = apc;
                             part += pc * apc;
@@ -456,7 +458,7 @@ __global__ void __launch_bounds__(kThreads, 2) march_kernel(const __grid_constan
                             const float bc = M == UPDZ ? H(1, 0, hc) - alpha * H(1, 1, hc) : H(1, 0, hc);
                             float x2 = 0.f;
                             if (dp0) x2 = st.v0 + mg_divf(w2 * (bc - apply7(st)), st.d);
-                            if (live) {
+                            if (live && EL_IN(c, (long long)a.n0 * a.n1 * a.n2, 11)) {
                                 if (M == UPDZ) {
                                     // x += alpha p; r' out of place.  A tile also covers cells
                                     // outside the system (diagonal 0), whose r may still hold an
@@ -480,7 +482,7 @@ __global__ void __launch_bounds__(kThreads, 2) march_kernel(const __grid_constan
                                 const float omega = M == PROLONG ? w1 : w2;
                                 float xo = 0.f;
                                 if (dp0) xo = st.v0 + mg_divf(omega * (bc - apply7(st)), st.d);
-                                if (live) {
+                                if (live && EL_IN(c, (long long)a.n0 * a.n1 * a.n2, 12)) {
                                     a.out0[c] = xo;
                                     if (M == LAST) part += bc * xo;
                                 }
@@ -495,7 +497,9 @@ __global__ void __launch_bounds__(kThreads, 2) march_kernel(const __grid_constan
                     if ((k & 1) || k + 1 == a.n2) {
                         const float pr = racc0 + __shfl_down_sync(kFull, racc0, 1);
                         const int I = i0 / 2 + (lane >> 1), J = j0 / 2 + w, K = k >> 1;
-                        if (!(lane & 1) && I < a.c0 && J < a.c1) a.out0[I + a.c0 * (J + a.c1 * K)] = pr;
+                        if (!(lane & 1) && I < a.c0 && J < a.c1 &&
+                            EL_IN(I + a.c0 * (J + a.c1 * K), (long long)a.c0 * a.c1 * a.c2, 13))
+                            a.out0[I + a.c0 * (J + a.c1 * K)] = pr;
                         racc0 = 0.f;
                     }
                 }
@@ -652,7 +656,7 @@ int march_grid(el_ctx* ctx) {
 
 template <int M>
 void launch(el_ctx* ctx, const Maps& maps, const Args& a) {
-    march_kernel<M><<<march_grid<M>(ctx), kThreads, smem_bytes<M>(), ctx->stream>>>(maps, a);
+    launch_dependent(ctx, march_kernel<M>, dim3(march_grid<M>(ctx)), dim3(kThreads), (size_t)smem_bytes<M>(), maps, a);
 }
 
 Args base_args(el_ctx* ctx, Scalars* s) {
@@ -842,5 +846,7 @@ int march_last(el_ctx* ctx, const float* t, const float* b, float* x, Scalars* s
     launch<LAST>(ctx, maps, a);
     return 1;
 }
+
+EL_CHECK_EXPORT(march)
 
 }  // namespace el

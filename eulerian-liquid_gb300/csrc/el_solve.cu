@@ -760,7 +760,7 @@ __device__ __forceinline__ DotAcc<V> smooth_segments(const LGeom& g, const SegAr
         const V bc = ldv<COH>(b, c);
         V xo = V(0);
         if (st.d > V(0)) xo = st.v0 + mg_div(omega * (bc - apply7(st)), st.d);
-        x_out[c] = xo;
+        if (EL_IN(c, (long long)g.s2 * g.n2, 30)) x_out[c] = xo;
         if (DOT != DOT_NONE) part += (DotAcc<V>)bc * (DotAcc<V>)xo;
     }
     SEG_LOOP_END
@@ -773,6 +773,8 @@ __global__ void __launch_bounds__(kSegThreads) smooth_kernel(LGeom g, SegArg seg
                                                              LGeom gc, const V* __restrict__ e,
                                                              V* __restrict__ x_out, Scalars* s, double* partials,
                                                              unsigned* counter) {
+    pdl_wait();
+    pdl_trigger();
     if (s->done) return;
     const DotAcc<V> part = smooth_segments<V, R, MODE, DOT>(g, seg, A, b, x_in, gc, e, x_out,
                                                             (blockIdx.x * blockDim.x + threadIdx.x) >> 5,
@@ -831,7 +833,8 @@ __global__ void __launch_bounds__(kSegThreads, sizeof(V) == 4 ? 5 : 4) restrict_
         for (int h = 0; h < 2; ++h) {
             const V pair = sum[h] + __shfl_down_sync(kFull, sum[h], 1);
             const int I = I0 + 16 * h + (lane >> 1);
-            if ((lane & 1) == 0 && I < gc.n0) bc[I + gc.s1 * J + gc.s2 * K] = pair;
+            if ((lane & 1) == 0 && I < gc.n0 && EL_IN(I + gc.s1 * J + gc.s2 * K, (long long)gc.s2 * gc.n2, 31))
+                bc[I + gc.s1 * J + gc.s2 * K] = pair;
         }
     }
 }
@@ -886,7 +889,8 @@ __device__ __forceinline__ void restrict_quad_segments(const LGeom& g, const R* 
             const V tot = ((part[quad_b][0][h][q] + part[quad_b][1][h][q]) + part[quad_b][2][h][q]) +
                           part[quad_b][3][h][q];
             const int I = I0 + 16 * h + q;
-            if (I < gc.n0) bc[I + gc.s1 * J + gc.s2 * K] = tot;
+            if (I < gc.n0 && EL_IN(I + gc.s1 * J + gc.s2 * K, (long long)gc.s2 * gc.n2, 32))
+                bc[I + gc.s1 * J + gc.s2 * K] = tot;
         }
         asm volatile("bar.sync %0, %1;" ::"r"(1 + quad_b), "r"(128) : "memory");
     }
@@ -897,6 +901,8 @@ __global__ void __launch_bounds__(kSegThreads, 4) restrict_quad_kernel(LGeom g, 
                                                                     const V* __restrict__ b, const V* __restrict__ x,
                                                                     LGeom gc, SegArg cseg, V* __restrict__ bc,
                                                                     const Scalars* s) {
+    pdl_wait();
+    pdl_trigger();
     if (s->done) return;
     __shared__ V part[kQuadsPerBlock][4][2][16];
     const int wb = threadIdx.x >> 5;                  // warp in the block
@@ -1122,6 +1128,8 @@ __global__ void __launch_bounds__(kBottomThreads) mg_bottom_kernel(LGeom gf, con
                                                                    float* __restrict__ xf, LGeom gc,
                                                                    const float4* __restrict__ recc, int sweeps,
                                                                    const Scalars* s) {
+    pdl_wait();
+    pdl_trigger();
     if (s->done) return;
     extern __shared__ __align__(16) unsigned char bottom_smem[];
     bottom_cycle(gf, recf, bf, xf, gc, recc, sweeps, bottom_smem);
@@ -1374,8 +1382,9 @@ static void launch_smooth(el_ctx* ctx, const MGLevel<V>& F, const SegList& seg, 
                           V* x_out, Scalars* s) {
     const LGeom g = make_geom(F.n0, F.n1, F.n2);
     const LGeom gc = C ? make_geom(C->n0, C->n1, C->n2) : g;
-    smooth_kernel<V, R, MODE, DOT><<<seg_blocks(ctx, seg.total), kSegThreads, 0, ctx->stream>>>(
-        g, seg_arg(seg), (const R*)F.rec, F.b, x_in, gc, C ? C->x : nullptr, x_out, s, ctx->partials, ctx->counter);
+    launch_dependent(ctx, smooth_kernel<V, R, MODE, DOT>, dim3(seg_blocks(ctx, seg.total)), dim3(kSegThreads), 0, g,
+                     seg_arg(seg), (const R*)F.rec, (const V*)F.b, x_in, gc, C ? (const V*)C->x : (const V*)nullptr,
+                     x_out, s, ctx->partials, ctx->counter);
 }
 
 // The coarse part of an FP32 V-cycle, levels [from, pre_end) and the bottom pair, as one
@@ -1468,8 +1477,9 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
                 restrict_kernel<V, R0><<<restrict_blocks(ctx, C.seg.total), kSegThreads, 0, ctx->stream>>>(
                     gf, (const R0*)F.rec, F.b, F.x, gc, seg_arg(C.seg), C.b, s);
             else
-                restrict_quad_kernel<V, RC><<<seg_blocks(ctx, 4 * C.seg.total), kSegThreads, 0, ctx->stream>>>(
-                    gf, (const RC*)F.rec, F.b, F.x, gc, seg_arg(C.seg), C.b, s);
+                launch_dependent(ctx, restrict_quad_kernel<V, RC>, dim3(seg_blocks(ctx, 4 * C.seg.total)),
+                                 dim3(kSegThreads), 0, gf, (const RC*)F.rec, (const V*)F.b, (const V*)F.x, gc,
+                                 seg_arg(C.seg), C.b, (const Scalars*)s);
         }
         launched += 2;
     }
@@ -1489,9 +1499,10 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
             MGLevel<V>& C = mg[L - 1];
             // reads the level's records and b and the coarsest records; writes the level's x
             ProfScope prof(ctx, EL_KC_MG_COARSE, cells(F) * (sizeof(RC) + 2 * vs) + cells(C) * sizeof(RC));
-            mg_bottom_kernel<<<1, kBottomThreads, bottom_smem_bytes(), ctx->stream>>>(
-                make_geom(F.n0, F.n1, F.n2), (const float4*)F.rec, F.b, F.x, make_geom(C.n0, C.n1, C.n2),
-                (const float4*)C.rec, kCoarsestSweeps, s);
+            launch_dependent(ctx, mg_bottom_kernel, dim3(1), dim3(kBottomThreads), bottom_smem_bytes(),
+                             make_geom(F.n0, F.n1, F.n2), (const float4*)F.rec, (const float*)F.b, F.x,
+                             make_geom(C.n0, C.n1, C.n2), (const float4*)C.rec, (int)kCoarsestSweeps,
+                             (const Scalars*)s);
             ++launched;
         }
     } else {
@@ -2113,5 +2124,7 @@ int setup_solver_storage(el_ctx* ctx, int solver) {
     }
     return EL_OK;
 }
+
+EL_CHECK_EXPORT(solve)
 
 }  // namespace el

@@ -146,6 +146,10 @@ typedef struct el_tuning {
     int coarse_fused;            /* 1: the mixed solver's multigrid levels below the finest, and
                                     the bottom pair, in one cooperative launch per V-cycle
                                     (identical results); 0 (default): one launch per level pass */
+    int dependent_launch;        /* 1 (default): the mixed solver's chained kernels (finest-level
+                                    tile kernels, coarse-level passes, the bottom) are launched as
+                                    programmatic dependent launches, so that each is scheduled
+                                    while the one before it drains (identical results); 0: not  */
 } el_tuning;
 int el_ctx_set_tuning(el_ctx* ctx, const el_tuning* t);
 int el_ctx_get_tuning(const el_ctx* ctx, el_tuning* t);
@@ -184,6 +188,14 @@ typedef struct el_profile_entry {
 int el_ctx_profile_begin(el_ctx* ctx, uint32_t class_mask);
 /* out must hold EL_KC_COUNT entries */
 int el_ctx_profile_end(el_ctx* ctx, el_profile_entry* out);
+
+/* Debug build (libeulerian_liquid_gb300_checked.so, compiled with -DEL_CHECKED; no counterpart
+ * in the reference): the kernels check each global store index (and their indirect loads)
+ * against the array before the access, skip a failed access and record it.  *checked = 1 in
+ * that build, 0 in the product build (where *word is always 0); *word = the first failed check
+ * since the last call, (site << 40) | index, or 0.  Reading clears it.  Call it between steps,
+ * with no work of the library in flight. */
+int el_debug_check_take(uint64_t* word, int* checked);
 
 /* Host <-> device copies of a whole field (bytes must equal the field's size). */
 int el_upload(el_ctx* ctx, int field, const void* host, size_t bytes);

@@ -69,3 +69,28 @@ def test_fused_coarse_cycle_in_batch_graph(el):
     for a, b in zip(f1, f0):
         for f in a:
             np.testing.assert_array_equal(a[f], b[f], err_msg=f)
+
+
+@pytest.mark.parametrize("tiles", [1, 0])
+def test_dependent_launch_is_bit_identical(el, tiles):
+    """The solver's chained kernels as programmatic dependent launches (each scheduled while the
+    one before it drains) give the same bits as ordinary launches, host-driven and in a batch."""
+    shape = (96, 72, 80)
+    out = []
+    for pdl in (1, 0):
+        sim = _scene(el, shape, 11)
+        sim.set_tuning(solver_tiles=tiles, dependent_launch=pdl)
+        st = sim.solve_pressure(0.01, solver=el.SOLVER_MIXED, tol=1e-8, max_iter=400)
+        assert st["status"] == 0, st
+        params = el.step_params(sample_phi=el.SAMPLE_WENO6, trace_vel=el.TRACE_RK3, gravity=9.8,
+                                solver=el.SOLVER_MIXED, tol=1e-6, max_iter=400, check_every=4, max_outer=8)
+        batch = el.Batch([sim], params=params, cfl=1.0, dt_frame=1.0 / 60.0)
+        batch.step(2)
+        batch.sync()
+        bst = batch.stats()[0]
+        batch.close()
+        out.append((st["iterations"], bst["iterations"], {f: sim.download(f) for f in ("pressure", "u", "phi")}))
+        sim.close()
+    assert out[0][0] == out[1][0] and out[0][1] == out[1][1]
+    for f in out[0][2]:
+        np.testing.assert_array_equal(out[0][2][f], out[1][2][f], err_msg=f)
