@@ -152,12 +152,12 @@ __device__ __forceinline__ T lerp_combine(T fx, T fy, T fz, T c000, T c100, T c0
 }
 
 // trilinear sample from a staged box at box-relative (x, y, z); false when the 8 points are not
-// all inside the box
-template <typename T>
+// all inside the box.  CHECK = false: the caller knows they are (see advect_velocity_tiled_kernel)
+template <typename T, bool CHECK = true>
 __device__ __forceinline__ bool staged_lerp(const T* box, const AxisPos<T>& x, const AxisPos<T>& y,
                                             const AxisPos<T>& z, T& out) {
-    if ((unsigned)x.a >= (unsigned)(kBoxX - 1) || (unsigned)y.a >= (unsigned)(kBoxY - 1) ||
-        (unsigned)z.a >= (unsigned)(kBoxZ - 1))
+    if (CHECK && ((unsigned)x.a >= (unsigned)(kBoxX - 1) || (unsigned)y.a >= (unsigned)(kBoxY - 1) ||
+                  (unsigned)z.a >= (unsigned)(kBoxZ - 1)))
         return false;
     const T* p = box + (z.a * kBoxY + y.a) * kBoxX + x.a;
     constexpr int SY = kBoxX, SZ = kBoxX * kBoxY;
@@ -171,11 +171,12 @@ struct Staged {
     int bx0, by0, bz0;    // grid index of the box's first entry
 };
 
-template <typename T>
+template <typename T, bool CHECK = true>
 __device__ __forceinline__ T sample_staged(const GridView<T>& g, const Staged<T>& b, T x, T y, T z, T dx, T inv) {
     T r;
-    if (staged_lerp(b.box, axis_pos(x, g.ox, b.bx0, dx, inv), axis_pos(y, g.oy, b.by0, dx, inv),
-                    axis_pos(z, g.oz, b.bz0, dx, inv), r))
+    if (staged_lerp<T, CHECK>(b.box, axis_pos(x, g.ox, b.bx0, dx, inv), axis_pos(y, g.oy, b.by0, dx, inv),
+                              axis_pos(z, g.oz, b.bz0, dx, inv), r) ||
+        !CHECK)
         return r;
     return sample_trilinear(g, x, y, z, dx, inv);
 }
@@ -187,26 +188,26 @@ struct StagedMac {
 
 // u at (face x, cell y, cell z), v at (cell, face, cell), w at (cell, cell, face): six axis
 // positions serve all three (the cell origins are those of the other components' grids)
-template <typename T>
+template <typename T, bool CHECK = true>
 __device__ __forceinline__ void velocity_at_staged(const Mac<T>& m, const StagedMac<T>& s, T x, T y, T z, T dx, T inv,
                                                    T& vx, T& vy, T& vz) {
     const AxisPos<T> xf = axis_pos(x, m.u.ox, s.u.bx0, dx, inv), xc = axis_pos(x, m.v.ox, s.u.bx0, dx, inv);
     const AxisPos<T> yf = axis_pos(y, m.v.oy, s.u.by0, dx, inv), yc = axis_pos(y, m.u.oy, s.u.by0, dx, inv);
     const AxisPos<T> zf = axis_pos(z, m.w.oz, s.u.bz0, dx, inv), zc = axis_pos(z, m.u.oz, s.u.bz0, dx, inv);
-    if (!staged_lerp(s.u.box, xf, yc, zc, vx)) vx = sample_trilinear(m.u, x, y, z, dx, inv);
-    if (!staged_lerp(s.v.box, xc, yf, zc, vy)) vy = sample_trilinear(m.v, x, y, z, dx, inv);
-    if (!staged_lerp(s.w.box, xc, yc, zf, vz)) vz = sample_trilinear(m.w, x, y, z, dx, inv);
+    if (!staged_lerp<T, CHECK>(s.u.box, xf, yc, zc, vx) && CHECK) vx = sample_trilinear(m.u, x, y, z, dx, inv);
+    if (!staged_lerp<T, CHECK>(s.v.box, xc, yf, zc, vy) && CHECK) vy = sample_trilinear(m.v, x, y, z, dx, inv);
+    if (!staged_lerp<T, CHECK>(s.w.box, xc, yc, zf, vz) && CHECK) vz = sample_trilinear(m.w, x, y, z, dx, inv);
 }
 
 // backtrace with the staged velocity: the same stages and arithmetic as backtrace()
-template <typename T, int TRACE>
+template <typename T, int TRACE, bool CHECK = true>
 __device__ __forceinline__ void backtrace_staged(const Mac<T>& m, const StagedMac<T>& sm, T& x, T& y, T& z, T h, T dx,
                                                  T inv) {
     T ax, ay, az;
-    velocity_at_staged(m, sm, x, y, z, dx, inv, ax, ay, az);
+    velocity_at_staged<T, CHECK>(m, sm, x, y, z, dx, inv, ax, ay, az);
     const T h2 = T(0.5) * h;
     T bx, by, bz;
-    velocity_at_staged(m, sm, x + h2 * ax, y + h2 * ay, z + h2 * az, dx, inv, bx, by, bz);
+    velocity_at_staged<T, CHECK>(m, sm, x + h2 * ax, y + h2 * ay, z + h2 * az, dx, inv, bx, by, bz);
     if constexpr (TRACE == EL_TRACE_RK2) {
         x = x + h * bx;
         y = y + h * by;
@@ -214,7 +215,7 @@ __device__ __forceinline__ void backtrace_staged(const Mac<T>& m, const StagedMa
     } else {
         const T h3 = T(0.75) * h;
         T cx, cy, cz;
-        velocity_at_staged(m, sm, x + h3 * bx, y + h3 * by, z + h3 * bz, dx, inv, cx, cy, cz);
+        velocity_at_staged<T, CHECK>(m, sm, x + h3 * bx, y + h3 * by, z + h3 * bz, dx, inv, cx, cy, cz);
         const T w1 = h * (T(2) / T(9)), w2 = h * (T(1) / T(3)), w3 = h * (T(4) / T(9));
         x = x + w1 * ax + w2 * bx + w3 * cx;
         y = y + w1 * ay + w2 * by + w3 * cy;
@@ -222,10 +223,17 @@ __device__ __forceinline__ void backtrace_staged(const Mac<T>& m, const StagedMa
     }
 }
 
-// stages the clamped boxes of u, v, w around tile (x0, y0, z0): rows of kBoxX along x, one warp
-// per row
+// max(|a|, |b|) that is NaN when either is (fmax would drop a NaN)
 template <typename T>
-__device__ __forceinline__ StagedMac<T> stage_mac(const Mac<T>& m, T* smem, int x0, int y0, int z0) {
+__device__ __forceinline__ T fmax_nan(T m, T v) {
+    const T a = v < T(0) ? -v : v;
+    return (a > m || a != a) ? a : m;
+}
+
+// stages the clamped boxes of u, v, w around tile (x0, y0, z0): rows of kBoxX along x, one warp
+// per row; vmax gathers the largest |value| this thread staged (NaN if it staged one)
+template <typename T>
+__device__ __forceinline__ StagedMac<T> stage_mac(const Mac<T>& m, T* smem, int x0, int y0, int z0, T& vmax) {
     const int bx0 = x0 - kHalo, by0 = y0 - kHalo, bz0 = z0 - kHalo;
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     const int lane = tid & 31, warp = tid >> 5, nwarps = (blockDim.x * blockDim.y) >> 5;
@@ -236,24 +244,49 @@ __device__ __forceinline__ StagedMac<T> stage_mac(const Mac<T>& m, T* smem, int 
         T* dst = smem + comp * kBoxN + (bz * kBoxY + by) * kBoxX;
         const int gy = clampi(by0 + by, 0, g.n1 - 1), gz = clampi(bz0 + bz, 0, g.n2 - 1);
         const T* src = g.d + (long long)g.n0 * (gy + (long long)g.n1 * gz);
-        dst[lane] = __ldg(src + clampi(bx0 + lane, 0, g.n0 - 1));
-        if (lane < kBoxX - 32) dst[32 + lane] = __ldg(src + clampi(bx0 + 32 + lane, 0, g.n0 - 1));
+        const T va = __ldg(src + clampi(bx0 + lane, 0, g.n0 - 1));
+        dst[lane] = va;
+        vmax = fmax_nan(vmax, va);
+        if (lane < kBoxX - 32) {
+            const T vb = __ldg(src + clampi(bx0 + 32 + lane, 0, g.n0 - 1));
+            dst[32 + lane] = vb;
+            vmax = fmax_nan(vmax, vb);
+        }
     }
     return StagedMac<T>{{smem, bx0, by0, bz0}, {smem + kBoxN, bx0, by0, bz0}, {smem + 2 * kBoxN, bx0, by0, bz0}};
 }
 
-// u, v, w of a tile, each advected through the (old) velocity itself
-template <typename T, int TRACE>
-__global__ void __launch_bounds__(kTileX * kTileY) advect_velocity_tiled_kernel(Mac<T> mac, T* __restrict__ ou,
-                                                                                T* __restrict__ ov,
-                                                                                T* __restrict__ ow, DtArg dt, T dx,
-                                                                                T inv_dx) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* smem = reinterpret_cast<T*>(smem_raw);
-    const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * kTileY, z0 = blockIdx.z * kTileZ;
-    const StagedMac<T> sm = stage_mac(mac, smem, x0, y0, z0);
+// The largest |velocity| the CTA staged (NaN if it staged a NaN), as the same value in every
+// thread.  Call after the staging, in place of the __syncthreads that ends it.
+template <typename T>
+__device__ __forceinline__ T box_max(T vmax) {
+    __shared__ T wmax[kTileX * kTileY / 32];
+    for (int o = 16; o > 0; o >>= 1) vmax = fmax_nan(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    if ((tid & 31) == 0) wmax[tid >> 5] = vmax;
     __syncthreads();
-    const T h = -(T)dt_value(dt);
+    T m = T(0);
+#pragma unroll
+    for (int q = 0; q < kTileX * kTileY / 32; ++q) m = fmax_nan(m, wmax[q]);
+    return m;
+}
+
+// A step moves no sample more than one cell when |v| |dt| / dx < 1 over the staged boxes (every
+// RK stage and the foot point are convex combinations of velocities read inside the boxes, by
+// induction): then all of a tile's staged reads fall inside its boxes (the halo is two cells)
+// and the reads need no check.  False for a NaN or infinite velocity or dt.
+template <typename T>
+__device__ __forceinline__ bool within_one_cell(T vmax, T h, T inv_dx) {
+    const T reach = vmax * (h < T(0) ? -h : h) * inv_dx;
+    return reach <= T(0.999);
+}
+
+// the u, v, w samples of a tile (CHECK: each staged read is checked and falls back to the
+// global read outside the box)
+template <typename T, int TRACE, bool CHECK>
+__device__ __forceinline__ void velocity_tile(const Mac<T>& mac, const StagedMac<T>& sm, T* __restrict__ ou,
+                                              T* __restrict__ ov, T* __restrict__ ow, T h, T dx, T inv_dx, int x0,
+                                              int y0, int z0) {
     const int i = x0 + threadIdx.x, j = y0 + threadIdx.y;
 #pragma unroll 1
     for (int kk = 0; kk < kTileZ; ++kk) {
@@ -277,12 +310,31 @@ __global__ void __launch_bounds__(kTileX * kTileY) advect_velocity_tiled_kernel(
             T x = (i + T(0.5)) * dx + g.ox;
             T y = (j + T(0.5)) * dx + g.oy;
             T z = (k + T(0.5)) * dx + g.oz;
-            backtrace_staged<T, TRACE>(mac, sm, x, y, z, h, dx, inv_dx);
+            backtrace_staged<T, TRACE, CHECK>(mac, sm, x, y, z, h, dx, inv_dx);
             const long long oc = lin3(i, j, k, g.n0, g.n1);
-            const T r = sample_staged(g, b, x, y, z, dx, inv_dx);
+            const T r = sample_staged<T, CHECK>(g, b, x, y, z, dx, inv_dx);
             if (EL_IN(oc, (long long)g.n0 * g.n1 * g.n2, 2)) o[oc] = r;
         }
     }
+}
+
+// u, v, w of a tile, each advected through the (old) velocity itself
+template <typename T, int TRACE>
+__global__ void __launch_bounds__(kTileX * kTileY, 3) advect_velocity_tiled_kernel(Mac<T> mac, T* __restrict__ ou,
+                                                                                T* __restrict__ ov,
+                                                                                T* __restrict__ ow, DtArg dt, T dx,
+                                                                                T inv_dx) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* smem = reinterpret_cast<T*>(smem_raw);
+    const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * kTileY, z0 = blockIdx.z * kTileZ;
+    T vmax = T(0);
+    const StagedMac<T> sm = stage_mac(mac, smem, x0, y0, z0, vmax);
+    const T bm = box_max(vmax);  // ends the staging (a barrier)
+    const T h = -(T)dt_value(dt);
+    if (within_one_cell(bm, h, inv_dx))
+        velocity_tile<T, TRACE, false>(mac, sm, ou, ov, ow, h, dx, inv_dx, x0, y0, z0);
+    else
+        velocity_tile<T, TRACE, true>(mac, sm, ou, ov, ow, h, dx, inv_dx, x0, y0, z0);
 }
 
 // the level set (cells) through the staged velocity; phi itself from global memory
@@ -292,8 +344,9 @@ __global__ void __launch_bounds__(kTileX * kTileY) advect_phi_tiled_kernel(GridV
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* smem = reinterpret_cast<T*>(smem_raw);
     const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * kTileY, z0 = blockIdx.z * kTileZ;
-    const StagedMac<T> sm = stage_mac(mac, smem, x0, y0, z0);
-    __syncthreads();
+    T vmax = T(0);
+    const StagedMac<T> sm = stage_mac(mac, smem, x0, y0, z0, vmax);
+    const bool inside = within_one_cell(box_max(vmax), -(T)dt_value(dt), inv_dx);  // ends the staging
     const T h = -(T)dt_value(dt);
     const int i = x0 + threadIdx.x, j = y0 + threadIdx.y;
     if (i >= src.n0 || j >= src.n1) return;
@@ -304,7 +357,10 @@ __global__ void __launch_bounds__(kTileX * kTileY) advect_phi_tiled_kernel(GridV
         T x = (i + T(0.5)) * dx + src.ox;
         T y = (j + T(0.5)) * dx + src.oy;
         T z = (k + T(0.5)) * dx + src.oz;
-        backtrace_staged<T, TRACE>(mac, sm, x, y, z, h, dx, inv_dx);
+        if (inside)
+            backtrace_staged<T, TRACE, false>(mac, sm, x, y, z, h, dx, inv_dx);
+        else
+            backtrace_staged<T, TRACE, true>(mac, sm, x, y, z, h, dx, inv_dx);
         T r;
         if constexpr (SAMPLE == EL_SAMPLE_WENO6)
             r = sample_weno6(src, x, y, z, dx, inv_dx);
