@@ -25,12 +25,72 @@ struct DtArg {
 
 __device__ __forceinline__ double dt_value(const DtArg& a) { return a.s ? a.s->dt : a.v; }
 
+// floor(t) and t - floor(t), the same values as index_fraction.  FP32: t + 1.5 * 2^23 rounded
+// toward -inf holds floor(t) in its low mantissa bits (exact for |t| < 2^22); outside that range
+// (and for NaN) the index lands millions of cells away, i.e. outside every staged box, and the
+// sample takes the exact global path.
+template <typename T>
+__device__ __forceinline__ void floor_index(T t, int& idx, T& frac) {
+    if constexpr (sizeof(T) == 4) {
+        const float big = 12582912.0f;  // 1.5 * 2^23, bit pattern 0x4B400000
+        const float r = __fadd_rd(t, big);
+        idx = (int)((unsigned)__float_as_int(r) - 0x4B400000u);
+        frac = t - (r - big);
+    } else {
+        const T fl = floor(t);
+        idx = (int)fl;
+        frac = t - fl;
+    }
+}
+
+// one axis of a trilinear read: index_fraction's floor index and fraction (floor_index: the
+// same values)
+template <typename T>
+__device__ __forceinline__ void axis_index(T pos, T origin, T dx, T inv_dx, int& idx, T& frac) {
+    T t;
+    if constexpr (sizeof(T) == 8)
+        t = (pos - origin - T(0.5) * dx) / dx;
+    else
+        t = (pos - origin - T(0.5) * dx) * inv_dx;
+    floor_index(t, idx, frac);
+}
+
+// trilinear read of a grid at floor indices (i, j, k) and fractions when all 8 points are inside
+// the grid (then clamping changes none of them): one base address and fixed strides, the same
+// values and arithmetic as the clamped gather; false, with nothing read, otherwise
+template <typename T>
+__device__ __forceinline__ bool tri_interior(const GridView<T>& g, int i, int j, int k, T fx, T fy, T fz, T& out) {
+    if ((unsigned)i >= (unsigned)(g.n0 - 1) || (unsigned)j >= (unsigned)(g.n1 - 1) ||
+        (unsigned)k >= (unsigned)(g.n2 - 1))
+        return false;
+    const long long sy = g.n0, sz = (long long)g.n0 * g.n1;
+    const T* p = g.d + (i + sy * j + sz * k);
+    TriIdx<T> t;
+    t.fx = fx;
+    t.fy = fy;
+    t.fz = fz;
+    out = tri_combine(t, __ldg(p), __ldg(p + 1), __ldg(p + sy), __ldg(p + sy + 1), __ldg(p + sz), __ldg(p + sz + 1),
+                      __ldg(p + sz + sy), __ldg(p + sz + sy + 1));
+    return true;
+}
+
+// u, v, w at one position from global memory: the three components share six axis coordinates
+// (u at a face in x, cells in y and z; v and w likewise), interior reads take tri_interior and
+// the rest the clamped gather -- the values of three sample_trilinear calls
 template <typename T>
 __device__ __forceinline__ void velocity_at(const Mac<T>& m, T x, T y, T z, T dx, T inv, T& vx, T& vy,
                                             T& vz) {
-    vx = sample_trilinear(m.u, x, y, z, dx, inv);
-    vy = sample_trilinear(m.v, x, y, z, dx, inv);
-    vz = sample_trilinear(m.w, x, y, z, dx, inv);
+    int ixf, ixc, jyf, jyc, kzf, kzc;
+    T fxf, fxc, fyf, fyc, fzf, fzc;
+    axis_index(x, m.u.ox, dx, inv, ixf, fxf);
+    axis_index(x, m.v.ox, dx, inv, ixc, fxc);
+    axis_index(y, m.v.oy, dx, inv, jyf, fyf);
+    axis_index(y, m.u.oy, dx, inv, jyc, fyc);
+    axis_index(z, m.w.oz, dx, inv, kzf, fzf);
+    axis_index(z, m.u.oz, dx, inv, kzc, fzc);
+    if (!tri_interior(m.u, ixf, jyc, kzc, fxf, fyc, fzc, vx)) vx = sample_trilinear(m.u, x, y, z, dx, inv);
+    if (!tri_interior(m.v, ixc, jyf, kzc, fxc, fyf, fzc, vy)) vy = sample_trilinear(m.v, x, y, z, dx, inv);
+    if (!tri_interior(m.w, ixc, jyc, kzf, fxc, fyc, fzf, vz)) vz = sample_trilinear(m.w, x, y, z, dx, inv);
 }
 
 // trace_rk2 (ode.h:30-35) or Ralston RK3 (c = 0, 1/2, 3/4; b = 2/9, 1/3, 4/9); h is the
@@ -99,24 +159,6 @@ __global__ void __launch_bounds__(256) advect_kernel(GridView<T> src, T* __restr
 constexpr int kTileX = 32, kTileY = 8, kTileZ = 8, kHalo = 2;
 constexpr int kBoxX = kTileX + 2 * kHalo, kBoxY = kTileY + 2 * kHalo, kBoxZ = kTileZ + 2 * kHalo;
 constexpr int kBoxN = kBoxX * kBoxY * kBoxZ;
-
-// floor(t) and t - floor(t), the same values as index_fraction.  FP32: t + 1.5 * 2^23 rounded
-// toward -inf holds floor(t) in its low mantissa bits (exact for |t| < 2^22); outside that range
-// (and for NaN) the index lands millions of cells away, i.e. outside every staged box, and the
-// sample takes the exact global path.
-template <typename T>
-__device__ __forceinline__ void floor_index(T t, int& idx, T& frac) {
-    if constexpr (sizeof(T) == 4) {
-        const float big = 12582912.0f;  // 1.5 * 2^23, bit pattern 0x4B400000
-        const float r = __fadd_rd(t, big);
-        idx = (int)((unsigned)__float_as_int(r) - 0x4B400000u);
-        frac = t - (r - big);
-    } else {
-        const T fl = floor(t);
-        idx = (int)fl;
-        frac = t - fl;
-    }
-}
 
 // the cell coordinate of index_fraction: (pos - origin - dx / 2) / dx
 template <typename T>

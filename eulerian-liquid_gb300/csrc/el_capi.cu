@@ -597,6 +597,7 @@ static int build_prof(el_ctx* ctx, bool inner32) {
     for (int c = 0; c < 3; ++c) faces += nbytes(ctx, EL_FIELD_U + c);
     double b = faces + nbytes(ctx, EL_FIELD_PHI) + N;
     b += 2 * faces + nbytes(ctx, EL_FIELD_PHI) + N + 16 * N + 3 * N * ctx->esz;
+    if (inner32 && ctx->A32) b += 24 * N;  // the mixed solver's float4 and half4 records
     ProfScope prof(ctx, EL_KC_BUILD, b);
     return launch_flags_build(ctx, inner32);
 }

@@ -236,6 +236,7 @@ struct el_ctx {
     // multigrid operator as half4 records
     float4* A32 = nullptr;
     ushort4* A16 = nullptr;
+    bool records_fresh = false;  // the last matrix build also wrote A32 / A16 (no packing pass needed)
     float *x32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *ap32 = nullptr;
     float* p32b = nullptr;
     float* r32b = nullptr;  // second residual buffer (the fused update writes r out of place)

@@ -9,6 +9,8 @@
 // neighbour order -x,+x,-y,+y,-z,+z), off[a][c] = A(c, c+e_a) = -weight (field type, exact),
 // rhs64[c] = b(c) (double).  Products are rounded with __*_rn intrinsics where the reference
 // rounds them, so the coefficients match the CPU restatement bit for bit.
+#include <cuda_fp16.h>
+
 #include "el_internal.cuh"
 
 namespace el {
@@ -139,13 +141,15 @@ struct FaceView {
 // fluid-cell count.
 template <typename T>
 __global__ void flags_kernel(FaceView<T> wt, const T* __restrict__ phi, uint8_t* __restrict__ flags,
-                             Scalars* s, double* partials, unsigned* counter) {
+                             Scalars* s, double* partials, unsigned* counter, int kz) {
     const int ni = wt.ni, nj = wt.nj, nk = wt.nk;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     double cnt[1] = {0.0};
     if (i < ni && j < nj) {
-        for (int k = blockIdx.z; k < nk; k += gridDim.z) {
+        // a contiguous chunk of planes per block: the neighbour planes come from L1
+        const int k_end = min(nk, (int)(blockIdx.z + 1) * kz);
+        for (int k = blockIdx.z * kz; k < k_end; ++k) {
             const bool pv = wt.U(i, j, k) > T(0) || wt.U(i + 1, j, k) > T(0) || wt.V(i, j, k) > T(0)
                             || wt.V(i, j + 1, k) > T(0) || wt.W(i, j, k) > T(0) || wt.W(i, j, k + 1) > T(0);
             const long long c = lin3(i, j, k, ni, nj);
@@ -163,13 +167,17 @@ struct CoeffOut {
     double* diag64;
     T* off[3];
     double* rhs64;
+    // when set, also the mixed solver's FP32 records of the same row: {d, cx, cy, cz} as float4,
+    // and as half4 with the diagonal rounded up and the couplings rounded toward zero
+    float4* a32;
+    ushort4* a16;
 };
 
 // build_matrix (projection.cpp:30-83), grid-shaped, plus |b|^2.
 template <typename T>
 __global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restrict__ phi,
                              const uint8_t* __restrict__ flags, CoeffOut<T> o, T dx, Scalars* s,
-                             double* partials, unsigned* counter) {
+                             double* partials, unsigned* counter, int kz) {
     const int ni = wt.ni, nj = wt.nj, nk = wt.nk;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -177,7 +185,9 @@ __global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restric
     const T scale = dx / dt;
     double bb[1] = {0.0};
     if (i < ni && j < nj) {
-        for (int k = blockIdx.z; k < nk; k += gridDim.z) {
+        // a contiguous chunk of planes per block: the neighbour planes come from L1
+        const int k_end = min(nk, (int)(blockIdx.z + 1) * kz);
+        for (int k = blockIdx.z * kz; k < k_end; ++k) {
             const long long c = lin3(i, j, k, ni, nj);
             double d = 0.0, b = 0.0;
             double offv[3] = {0.0, 0.0, 0.0};
@@ -213,6 +223,12 @@ __global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restric
             o.rhs64[c] = b;
 #pragma unroll
             for (int a = 0; a < 3; ++a) o.off[a][c] = (T)offv[a];
+            if (o.a32) {
+                const float4 r = make_float4((float)d, (float)(T)offv[0], (float)(T)offv[1], (float)(T)offv[2]);
+                o.a32[c] = r;
+                o.a16[c] = make_ushort4(__half_as_ushort(__float2half_ru(r.x)), __half_as_ushort(__float2half_rz(r.y)),
+                                        __half_as_ushort(__float2half_rz(r.z)), __half_as_ushort(__float2half_rz(r.w)));
+            }
             bb[0] += b * b;
         }
     }
@@ -378,15 +394,19 @@ static int launch_flags_build_t(el_ctx* ctx, bool inner32, bool build) {
                     (const T*)ctx->field[EL_FIELD_W], ctx->ni, ctx->nj, ctx->nk};
     const T* phi = (const T*)ctx->field[EL_FIELD_PHI];
     flags_kernel<T><<<g.grid, g.block, 0, ctx->stream>>>(wt, phi, ctx->flags, ctx->dscal, ctx->partials,
-                                                         ctx->counter);
+                                                         ctx->counter, g.kz);
     if (!build) return 1;
     CoeffOut<T> o;
     o.diag64 = ctx->diag64;
     o.rhs64 = ctx->rhs64;
     for (int a = 0; a < 3; ++a) o.off[a] = (T*)ctx->off[a];
-    (void)inner32;
+    // the mixed solver's records written by the build itself (no separate packing pass)
+    const bool records = inner32 && ctx->A32 && ctx->A16;
+    o.a32 = records ? ctx->A32 : nullptr;
+    o.a16 = records ? ctx->A16 : nullptr;
+    ctx->records_fresh = records;
     build_kernel<T><<<g.grid, g.block, 0, ctx->stream>>>(vel, wt, phi, ctx->flags, o, (T)ctx->dx, ctx->dscal,
-                                                         ctx->partials, ctx->counter);
+                                                         ctx->partials, ctx->counter, g.kz);
     return 2;
 }
 

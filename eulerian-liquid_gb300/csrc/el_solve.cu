@@ -1815,12 +1815,13 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
         mg[0].rec = ctx->A16;
         mg[0].b = ctx->r32;
         mg[0].x = ctx->z32;
-        {
+        if (!ctx->records_fresh) {
             ProfScope prof(ctx, EL_KC_OTHER, (double)n * (8 + 3 * sizeof(T) + 24));
             pack32_kernel<T><<<grid1d(ctx, n), 256, 0, ctx->stream>>>(n, ctx->diag64, A64.x, A64.y, A64.z, ctx->A32,
                                                                       ctx->A16);
+            ctx->launches += 1;
         }
-        ctx->launches += 1 + enqueue_coarsen<float, ushort4, float4>(ctx, mg);
+        ctx->launches += enqueue_coarsen<float, ushort4, float4>(ctx, mg);
         const bool march = ctx->march.on && ctx->solver_tiles;
         if (march) {
             ProfScope prof(ctx, EL_KC_OTHER, (double)n * 8);
@@ -1990,8 +1991,12 @@ static int enqueue_solve_device_t(el_ctx* ctx, const el_solve_params& prm, int k
     nk += 1 + enqueue_compact(ctx, ctx->seg0, g);
     solve_init_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
         g, seg_arg(ctx->seg0), ctx->rhs64, ctx->x64, ctx->r64, s0, prm.tol);
-    pack32_kernel<T><<<grid1d(ctx, n), 256, 0, ctx->stream>>>(n, ctx->diag64, A64.x, A64.y, A64.z, ctx->A32, ctx->A16);
-    nk += 2 + enqueue_coarsen<float, ushort4, float4>(ctx, mg);
+    if (!ctx->records_fresh) {
+        pack32_kernel<T><<<grid1d(ctx, n), 256, 0, ctx->stream>>>(n, ctx->diag64, A64.x, A64.y, A64.z, ctx->A32,
+                                                                  ctx->A16);
+        ++nk;
+    }
+    nk += 1 + enqueue_coarsen<float, ushort4, float4>(ctx, mg);
     const bool march = ctx->march.on && ctx->solver_tiles;
     if (march) nk += march_enqueue_items(ctx);
     if (ctx->coarse_bar) EL_CUDA_TRY(ctx, cudaMemsetAsync(ctx->coarse_bar, 0, 8, ctx->stream));
