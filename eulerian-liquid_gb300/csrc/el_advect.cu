@@ -55,28 +55,38 @@ __device__ __forceinline__ void axis_index(T pos, T origin, T dx, T inv_dx, int&
     floor_index(t, idx, frac);
 }
 
-// trilinear read of a grid at floor indices (i, j, k) and fractions when all 8 points are inside
-// the grid (then clamping changes none of them): one base address and fixed strides, the same
-// values and arithmetic as the clamped gather; false, with nothing read, otherwise
+// the 8 points of a trilinear read at floor indices (i, j, k) are inside the grid (then clamping
+// changes none of them)
 template <typename T>
-__device__ __forceinline__ bool tri_interior(const GridView<T>& g, int i, int j, int k, T fx, T fy, T fz, T& out) {
-    if ((unsigned)i >= (unsigned)(g.n0 - 1) || (unsigned)j >= (unsigned)(g.n1 - 1) ||
-        (unsigned)k >= (unsigned)(g.n2 - 1))
-        return false;
+__device__ __forceinline__ bool tri_inside(const GridView<T>& g, int i, int j, int k) {
+    return (unsigned)i < (unsigned)(g.n0 - 1) && (unsigned)j < (unsigned)(g.n1 - 1) && (unsigned)k < (unsigned)(g.n2 - 1);
+}
+
+// the 8 values of an inside read: one base address and fixed strides
+template <typename T>
+struct Tri8 {
+    T c[8];
+};
+template <typename T>
+__device__ __forceinline__ Tri8<T> tri_load(const GridView<T>& g, int i, int j, int k) {
     const long long sy = g.n0, sz = (long long)g.n0 * g.n1;
     const T* p = g.d + (i + sy * j + sz * k);
+    return Tri8<T>{{__ldg(p), __ldg(p + 1), __ldg(p + sy), __ldg(p + sy + 1), __ldg(p + sz), __ldg(p + sz + 1),
+                    __ldg(p + sz + sy), __ldg(p + sz + sy + 1)}};
+}
+template <typename T>
+__device__ __forceinline__ T tri_mix(const Tri8<T>& v, T fx, T fy, T fz) {
     TriIdx<T> t;
     t.fx = fx;
     t.fy = fy;
     t.fz = fz;
-    out = tri_combine(t, __ldg(p), __ldg(p + 1), __ldg(p + sy), __ldg(p + sy + 1), __ldg(p + sz), __ldg(p + sz + 1),
-                      __ldg(p + sz + sy), __ldg(p + sz + sy + 1));
-    return true;
+    return tri_combine(t, v.c[0], v.c[1], v.c[2], v.c[3], v.c[4], v.c[5], v.c[6], v.c[7]);
 }
 
 // u, v, w at one position from global memory: the three components share six axis coordinates
-// (u at a face in x, cells in y and z; v and w likewise), interior reads take tri_interior and
-// the rest the clamped gather -- the values of three sample_trilinear calls
+// (u at a face in x, cells in y and z; v and w likewise).  When all three reads are inside the
+// grid (the common case) their 24 loads go out together from fixed offsets; otherwise each
+// takes the clamped gather -- the values of three sample_trilinear calls either way
 template <typename T>
 __device__ __forceinline__ void velocity_at(const Mac<T>& m, T x, T y, T z, T dx, T inv, T& vx, T& vy,
                                             T& vz) {
@@ -88,9 +98,17 @@ __device__ __forceinline__ void velocity_at(const Mac<T>& m, T x, T y, T z, T dx
     axis_index(y, m.u.oy, dx, inv, jyc, fyc);
     axis_index(z, m.w.oz, dx, inv, kzf, fzf);
     axis_index(z, m.u.oz, dx, inv, kzc, fzc);
-    if (!tri_interior(m.u, ixf, jyc, kzc, fxf, fyc, fzc, vx)) vx = sample_trilinear(m.u, x, y, z, dx, inv);
-    if (!tri_interior(m.v, ixc, jyf, kzc, fxc, fyf, fzc, vy)) vy = sample_trilinear(m.v, x, y, z, dx, inv);
-    if (!tri_interior(m.w, ixc, jyc, kzf, fxc, fyc, fzf, vz)) vz = sample_trilinear(m.w, x, y, z, dx, inv);
+    if (tri_inside(m.u, ixf, jyc, kzc) && tri_inside(m.v, ixc, jyf, kzc) && tri_inside(m.w, ixc, jyc, kzf)) {
+        const Tri8<T> a = tri_load(m.u, ixf, jyc, kzc), b = tri_load(m.v, ixc, jyf, kzc),
+                      c = tri_load(m.w, ixc, jyc, kzf);
+        vx = tri_mix(a, fxf, fyc, fzc);
+        vy = tri_mix(b, fxc, fyf, fzc);
+        vz = tri_mix(c, fxc, fyc, fzf);
+    } else {
+        vx = sample_trilinear(m.u, x, y, z, dx, inv);
+        vy = sample_trilinear(m.v, x, y, z, dx, inv);
+        vz = sample_trilinear(m.w, x, y, z, dx, inv);
+    }
 }
 
 // trace_rk2 (ode.h:30-35) or Ralston RK3 (c = 0, 1/2, 3/4; b = 2/9, 1/3, 4/9); h is the

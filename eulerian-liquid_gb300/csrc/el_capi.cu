@@ -939,6 +939,7 @@ EL_API int el_solve_pressure_noalloc(const el_grid* g, const float* phi, float* 
     ctx.stream = static_cast<cudaStream_t>(stream);
     ctx.own_stream = false;
     ctx.use_graphs = false;  // instantiating a graph would allocate
+    ctx.build_skip_zero = false;  // the scratch keeps an earlier call's matrix: every row is written
     ctx.field[EL_FIELD_PHI] = const_cast<float*>(phi);
     ctx.field[EL_FIELD_U] = u;
     ctx.field[EL_FIELD_V] = v;

@@ -154,7 +154,8 @@ __global__ void flags_kernel(FaceView<T> wt, const T* __restrict__ phi, uint8_t*
                             || wt.V(i, j + 1, k) > T(0) || wt.W(i, j, k) > T(0) || wt.W(i, j, k + 1) > T(0);
             const long long c = lin3(i, j, k, ni, nj);
             const bool fl = pv && phi[c] < T(0);
-            flags[c] = (pv ? kFlagPressureValid : 0) | (fl ? kFlagFluid : 0);
+            // the build's marker survives: it says what the build last wrote at the cell
+            flags[c] = (pv ? kFlagPressureValid : 0) | (fl ? kFlagFluid : 0) | (flags[c] & kFlagBuilt);
             cnt[0] += fl ? 1.0 : 0.0;
         }
     }
@@ -175,9 +176,9 @@ struct CoeffOut {
 
 // build_matrix (projection.cpp:30-83), grid-shaped, plus |b|^2.
 template <typename T>
-__global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restrict__ phi,
-                             const uint8_t* __restrict__ flags, CoeffOut<T> o, T dx, Scalars* s,
-                             double* partials, unsigned* counter, int kz) {
+__global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restrict__ phi, uint8_t* flags,
+                             CoeffOut<T> o, T dx, Scalars* s, double* partials, unsigned* counter, int kz,
+                             int skip_zero) {
     const int ni = wt.ni, nj = wt.nj, nk = wt.nk;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -189,9 +190,13 @@ __global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restric
         const int k_end = min(nk, (int)(blockIdx.z + 1) * kz);
         for (int k = blockIdx.z * kz; k < k_end; ++k) {
             const long long c = lin3(i, j, k, ni, nj);
+            const uint8_t fc = flags[c];
+            const bool fluid = (fc & kFlagFluid) != 0;
+            // a row that is zero now and was zero after the previous build is left as it is
+            if (skip_zero && !fluid && !(fc & kFlagBuilt)) continue;
             double d = 0.0, b = 0.0;
             double offv[3] = {0.0, 0.0, 0.0};
-            if (flags[c] & kFlagFluid) {
+            if (fluid) {
                 const T pc = phi[c];
                 auto visit = [&](int x, int y, int z, T face_vel, T weight, bool forward, int axis) {
                     const bool inside = x >= 0 && y >= 0 && z >= 0 && x < ni && y < nj && z < nk;
@@ -229,6 +234,9 @@ __global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restric
                 o.a16[c] = make_ushort4(__half_as_ushort(__float2half_ru(r.x)), __half_as_ushort(__float2half_rz(r.y)),
                                         __half_as_ushort(__float2half_rz(r.z)), __half_as_ushort(__float2half_rz(r.w)));
             }
+            // only this thread writes the byte; others read its low bits, which do not change
+            const uint8_t fn = fluid ? (uint8_t)(fc | kFlagBuilt) : (uint8_t)(fc & ~kFlagBuilt);
+            if (fn != fc) flags[c] = fn;
             bb[0] += b * b;
         }
     }
@@ -406,7 +414,8 @@ static int launch_flags_build_t(el_ctx* ctx, bool inner32, bool build) {
     o.a16 = records ? ctx->A16 : nullptr;
     ctx->records_fresh = records;
     build_kernel<T><<<g.grid, g.block, 0, ctx->stream>>>(vel, wt, phi, ctx->flags, o, (T)ctx->dx, ctx->dscal,
-                                                         ctx->partials, ctx->counter, g.kz);
+                                                         ctx->partials, ctx->counter, g.kz,
+                                                         ctx->build_skip_zero ? 1 : 0);
     return 2;
 }
 
