@@ -8,8 +8,15 @@
 // operators; any dt), and the tiled kernels below, which stage what a tile of samples reads
 // (the velocity boxes; for WENO6 the level-set box and its x-pass smoothness terms) in shared
 // memory once -- under the CFL limit the foot point moves at most about one cell -- and fall
-// back to the global reads for a sample whose stencil leaves the box.
+// back to the global reads for a sample whose stencil leaves the box.  The boxes arrive by TMA
+// box copies (cp.async.bulk.tensor) wherever the array's row pitch is a multiple of 16 bytes;
+// the parts of a box outside the grid are then filled in from the clamped entries in shared
+// memory, so that a box holds the clamped grid either way.
+#include <cstring>
+#include <limits>
+
 #include "el_internal.cuh"
+#include "el_tma.cuh"
 
 namespace el {
 
@@ -24,6 +31,19 @@ struct DtArg {
 };
 
 __device__ __forceinline__ double dt_value(const DtArg& a) { return a.s ? a.s->dt : a.v; }
+
+// Set when a tile's wait for its box copies gave up (the tile's outputs are then NaN, so that
+// the step's solve fails on them); read and cleared by advect_fault_take().
+__device__ unsigned advect_wait_fault;
+
+// a box copy of one array (on = 0: the array is staged by plain loads)
+struct BoxMap {
+    CUtensorMap m;
+    int on;
+};
+struct MacMaps {
+    BoxMap c[3];
+};
 
 // floor(t) and t - floor(t), the same values as index_fraction.  FP32: t + 1.5 * 2^23 rounded
 // toward -inf holds floor(t) in its low mantissa bits (exact for |t| < 2^22); outside that range
@@ -162,7 +182,7 @@ __global__ void __launch_bounds__(256) advect_kernel(GridView<T> src, T* __restr
 // Tiled variants.  Under the CFL limit (cfl <= 1) the foot point and every RK stage lie within
 // one cell of the sample, so every trilinear velocity sample of a 32 x 8 x 8 tile of outputs
 // reads indices within [tile - 2, tile + 1] of each MAC grid: a CTA stages those boxes of u, v
-// and w (36 x 12 x 12 values each) in shared memory once and samples them there.  A sample
+// and w (40 x 12 x 12 values each) in shared memory once and samples them there.  A sample
 // whose 8 points are not all in the box (a larger dt) reads global memory instead, with the
 // same arithmetic, so the results do not depend on which path a sample took.  The velocity
 // advection computes u, v and w of a tile in one CTA (when the advected field is the advecting
@@ -173,9 +193,11 @@ __global__ void __launch_bounds__(256) advect_kernel(GridView<T> src, T* __restr
 // its 8 points at the unclamped indices i, i+1 (j, k likewise) with no clamping and gets exactly
 // the values of the clamped gather lerp() makes; the 8 reads sit at fixed offsets from one
 // address.  The floor of the cell coordinate is taken without conversions (floor_index), and
-// the three components at one position share their cell-centred and face coordinates.
-constexpr int kTileX = 32, kTileY = 8, kTileZ = 8, kHalo = 2;
-constexpr int kBoxX = kTileX + 2 * kHalo, kBoxY = kTileY + 2 * kHalo, kBoxZ = kTileZ + 2 * kHalo;
+// the three components at one position share their cell-centred and face coordinates.  Along
+// x a box starts four entries left of the tile (a box copy starts on a 16-byte boundary) and
+// holds 40 entries; along y and z the halo is two.
+constexpr int kTileX = 32, kTileY = 8, kTileZ = 8, kHalo = 2, kHaloX = 4;
+constexpr int kBoxX = kTileX + 2 * kHaloX, kBoxY = kTileY + 2 * kHalo, kBoxZ = kTileZ + 2 * kHalo;
 constexpr int kBoxN = kBoxX * kBoxY * kBoxZ;
 
 // the cell coordinate of index_fraction: (pos - origin - dx / 2) / dx
@@ -290,15 +312,102 @@ __device__ __forceinline__ T fmax_nan(T m, T v) {
     return (a > m || a != a) ? a : m;
 }
 
-// stages the clamped boxes of u, v, w around tile (x0, y0, z0): rows of kBoxX along x, one warp
-// per row; vmax gathers the largest |value| this thread staged (NaN if it staged one)
+// A box that arrived by a box copy, made the clamped box: an entry outside the grid takes the
+// value of its clamped entry (inside the grid, so the copy filled it), one warp per row; with
+// MAX, vmax gathers the largest |value| of the entries inside the grid (the values the clamped
+// box holds).  A box that lies inside the grid is only scanned for vmax, in 16-byte reads.
+template <typename T, int BX, int BY, int BZ, bool MAX>
+__device__ __forceinline__ void finish_box(T* box, const GridView<T>& g, int bx0, int by0, int bz0, T& vmax) {
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y, nthr = blockDim.x * blockDim.y;
+    const bool edge = bx0 < 0 || by0 < 0 || bz0 < 0 || bx0 + BX > g.n0 || by0 + BY > g.n1 || bz0 + BZ > g.n2;
+    if (!edge) {
+        if constexpr (MAX) {
+            static_assert((BX * BY * BZ * sizeof(T)) % 16 == 0, "whole 16-byte reads");
+            constexpr int nv = BX * BY * BZ * (int)sizeof(T) / 16;
+            for (int e = tid; e < nv; e += nthr) {
+                if constexpr (sizeof(T) == 4) {
+                    const float4 q = reinterpret_cast<const float4*>(box)[e];
+                    vmax = fmax_nan(fmax_nan(fmax_nan(fmax_nan(vmax, q.x), q.y), q.z), q.w);
+                } else {
+                    const double2 q = reinterpret_cast<const double2*>(box)[e];
+                    vmax = fmax_nan(fmax_nan(vmax, q.x), q.y);
+                }
+            }
+        }
+        return;
+    }
+    const int lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
+    for (int row = warp; row < BY * BZ; row += nwarps) {
+        const int bz = row / BY, by = row - bz * BY;
+        const int cy = clampi(by0 + by, 0, g.n1 - 1) - by0, cz = clampi(bz0 + bz, 0, g.n2 - 1) - bz0;
+        const bool row_in = cy == by && cz == bz;
+        const T* src = box + (cz * BY + cy) * BX;
+        T* dst = box + row * BX;
+        for (int x = lane; x < BX; x += 32) {
+            const int cx = clampi(bx0 + x, 0, g.n0 - 1) - bx0;
+            if (row_in && cx == x) {
+                if (MAX) vmax = fmax_nan(vmax, dst[x]);
+            } else {
+                dst[x] = src[cx];
+            }
+        }
+    }
+}
+
+// Issues the box copies of a tile (one thread; the mbarrier is the CTA's own), `bytes` in all.
+__device__ __forceinline__ void copy_boxes_begin(uint64_t* bar, unsigned bytes) {
+    mbar_init(bar, 1);
+    mbar_init_fence();
+    mbar_expect_tx(bar, bytes);
+}
+
+// Every thread waits (bounded) for the CTA's box copies; true, the same in every thread, when a
+// wait gave up.  Then the fault is recorded and one thread waits once more (bounded) so that no
+// copy is still landing when the CTA ends.  Call after a barrier that follows the mbarrier's
+// initialisation.
+__device__ __forceinline__ bool copy_boxes_failed(uint64_t* bar) {
+    const bool ok = mbar_wait(bar, 0);
+    if (!__syncthreads_or(!ok)) return false;
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        atomicOr(&advect_wait_fault, 1u);
+        mbar_wait(bar, 0);
+    }
+    __syncthreads();
+    return true;
+}
+
+// NaN into a thread's outputs of a tile whose boxes did not arrive (rows j, planes z0 .. z0+nz-1)
 template <typename T>
-__device__ __forceinline__ StagedMac<T> stage_mac(const Mac<T>& m, T* smem, int x0, int y0, int z0, T& vmax) {
-    const int bx0 = x0 - kHalo, by0 = y0 - kHalo, bz0 = z0 - kHalo;
+__device__ __forceinline__ void nan_column(const GridView<T>& g, T* __restrict__ o, int i, int j, int z0, int nz) {
+    if (i >= g.n0 || j >= g.n1) return;
+    for (int kk = 0; kk < nz && z0 + kk < g.n2; ++kk) {
+        const long long oc = lin3(i, j, z0 + kk, g.n0, g.n1);
+        if (EL_IN(oc, (long long)g.n0 * g.n1 * g.n2, 4)) o[oc] = std::numeric_limits<T>::quiet_NaN();
+    }
+}
+
+// Stages the clamped boxes of u, v, w around tile (x0, y0, z0): a component with a box map by a
+// box copy (then finish_box), the others by plain loads, rows of kBoxX along x, one warp per row.
+// vmax gathers the largest |value| this thread staged or scanned (NaN if it met one).  `failed`:
+// the box copies did not arrive (the same in every thread).
+template <typename T>
+__device__ __forceinline__ StagedMac<T> stage_mac(const Mac<T>& m, const MacMaps& maps, T* smem, uint64_t* bar,
+                                                  int x0, int y0, int z0, T& vmax, bool& failed) {
+    const int bx0 = x0 - kHaloX, by0 = y0 - kHalo, bz0 = z0 - kHalo;
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     const int lane = tid & 31, warp = tid >> 5, nwarps = (blockDim.x * blockDim.y) >> 5;
+    // the flags in registers (a parameter indexed at run time would be copied to local memory)
+    const bool on0 = maps.c[0].on != 0, on1 = maps.c[1].on != 0, on2 = maps.c[2].on != 0;
+    const int ncopy = (int)on0 + (int)on1 + (int)on2;
+    if (ncopy && tid == 0) {
+        copy_boxes_begin(bar, (unsigned)(ncopy * kBoxN * sizeof(T)));
+        if (on0) tma_load_3d(smem, &maps.c[0].m, bar, bx0, by0, bz0);
+        if (on1) tma_load_3d(smem + kBoxN, &maps.c[1].m, bar, bx0, by0, bz0);
+        if (on2) tma_load_3d(smem + 2 * kBoxN, &maps.c[2].m, bar, bx0, by0, bz0);
+    }
     for (int row = warp; row < 3 * kBoxY * kBoxZ; row += nwarps) {
         const int comp = row / (kBoxY * kBoxZ), r = row - comp * (kBoxY * kBoxZ);
+        if (comp == 0 ? on0 : (comp == 1 ? on1 : on2)) continue;
         const int bz = r / kBoxY, by = r - bz * kBoxY;
         const GridView<T>& g = comp == 0 ? m.u : (comp == 1 ? m.v : m.w);
         T* dst = smem + comp * kBoxN + (bz * kBoxY + by) * kBoxX;
@@ -311,6 +420,16 @@ __device__ __forceinline__ StagedMac<T> stage_mac(const Mac<T>& m, T* smem, int 
             const T vb = __ldg(src + clampi(bx0 + 32 + lane, 0, g.n0 - 1));
             dst[32 + lane] = vb;
             vmax = fmax_nan(vmax, vb);
+        }
+    }
+    failed = false;
+    if (ncopy) {
+        __syncthreads();  // the mbarrier's initialisation is seen by every thread
+        failed = copy_boxes_failed(bar);
+        if (!failed) {
+            if (on0) finish_box<T, kBoxX, kBoxY, kBoxZ, true>(smem, m.u, bx0, by0, bz0, vmax);
+            if (on1) finish_box<T, kBoxX, kBoxY, kBoxZ, true>(smem + kBoxN, m.v, bx0, by0, bz0, vmax);
+            if (on2) finish_box<T, kBoxX, kBoxY, kBoxZ, true>(smem + 2 * kBoxN, m.w, bx0, by0, bz0, vmax);
         }
     }
     return StagedMac<T>{{smem, bx0, by0, bz0}, {smem + kBoxN, bx0, by0, bz0}, {smem + 2 * kBoxN, bx0, by0, bz0}};
@@ -380,15 +499,23 @@ __device__ __forceinline__ void velocity_tile(const Mac<T>& mac, const StagedMac
 
 // u, v, w of a tile, each advected through the (old) velocity itself
 template <typename T, int TRACE>
-__global__ void __launch_bounds__(kTileX * kTileY, 3) advect_velocity_tiled_kernel(Mac<T> mac, T* __restrict__ ou,
-                                                                                T* __restrict__ ov,
-                                                                                T* __restrict__ ow, DtArg dt, T dx,
-                                                                                T inv_dx) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* smem = reinterpret_cast<T*>(smem_raw);
+__global__ void __launch_bounds__(kTileX * kTileY, 3) advect_velocity_tiled_kernel(
+    Mac<T> mac, T* __restrict__ ou, T* __restrict__ ov, T* __restrict__ ow, DtArg dt, T dx, T inv_dx,
+    const __grid_constant__ MacMaps maps) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T* smem = reinterpret_cast<T*>(align128(smem_raw));
+    __shared__ uint64_t bar;
     const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * kTileY, z0 = blockIdx.z * kTileZ;
     T vmax = T(0);
-    const StagedMac<T> sm = stage_mac(mac, smem, x0, y0, z0, vmax);
+    bool failed;
+    const StagedMac<T> sm = stage_mac(mac, maps, smem, &bar, x0, y0, z0, vmax, failed);
+    if (failed) {
+        const int i = x0 + threadIdx.x, j = y0 + threadIdx.y;
+        nan_column(mac.u, ou, i, j, z0, kTileZ);
+        nan_column(mac.v, ov, i, j, z0, kTileZ);
+        nan_column(mac.w, ow, i, j, z0, kTileZ);
+        return;
+    }
     const T bm = box_max(vmax);  // ends the staging (a barrier)
     const T h = -(T)dt_value(dt);
     if (within_one_cell(bm, h, inv_dx))
@@ -400,12 +527,19 @@ __global__ void __launch_bounds__(kTileX * kTileY, 3) advect_velocity_tiled_kern
 // the level set (cells) through the staged velocity; phi itself from global memory
 template <typename T, int TRACE, int SAMPLE>
 __global__ void __launch_bounds__(kTileX * kTileY) advect_phi_tiled_kernel(GridView<T> src, T* __restrict__ out,
-                                                                           Mac<T> mac, DtArg dt, T dx, T inv_dx) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* smem = reinterpret_cast<T*>(smem_raw);
+                                                                           Mac<T> mac, DtArg dt, T dx, T inv_dx,
+                                                                           const __grid_constant__ MacMaps maps) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T* smem = reinterpret_cast<T*>(align128(smem_raw));
+    __shared__ uint64_t bar;
     const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * kTileY, z0 = blockIdx.z * kTileZ;
     T vmax = T(0);
-    const StagedMac<T> sm = stage_mac(mac, smem, x0, y0, z0, vmax);
+    bool failed;
+    const StagedMac<T> sm = stage_mac(mac, maps, smem, &bar, x0, y0, z0, vmax, failed);
+    if (failed) {
+        nan_column(src, out, x0 + threadIdx.x, y0 + threadIdx.y, z0, kTileZ);
+        return;
+    }
     const bool inside = within_one_cell(box_max(vmax), -(T)dt_value(dt), inv_dx);  // ends the staging
     const T h = -(T)dt_value(dt);
     const int i = x0 + threadIdx.x, j = y0 + threadIdx.y;
@@ -434,43 +568,62 @@ __global__ void __launch_bounds__(kTileX * kTileY) advect_phi_tiled_kernel(GridV
 // ---------------------------------------------------------------------------------------
 // WENO6 level set, tiled.  Under the CFL limit the foot point of a cell lies within one cell
 // of it, so the 6^3 stencils of a 32 x 8 x 4 tile of cells read phi within [tile - 3, tile + 4]:
-// the CTA stages that clamped box (39 x 15 x 11) once.  The smoothness indicators of an x-pass
+// the CTA stages that clamped box (39 x 15 x 11 nodes) once.  The smoothness indicators of an x-pass
 // depend only on the six values it reads, not on the sample's fraction, so they are formed once
 // per (row, floor index) of the box -- (eps + IS_s)^2, in FP32 its reciprocal, for the 34 floor
 // indices of each of the 165 rows -- and shared by every sample whose stencil uses that row
 // segment, instead of being recomputed by all 36 x-passes of every sample.  The y- and z-passes
-// combine per-sample values and are evaluated in full.  The backtrace reads the velocity from global memory (L1-served).
-// A foot point outside the box (a larger dt) takes the global sample_weno6 path, with the same
-// arithmetic.
+// combine per-sample values and are evaluated in full.  The backtrace reads the velocity from
+// global memory (L1-served).  A foot point outside the box (a larger dt) takes the global
+// sample_weno6 path, with the same arithmetic.  The box arrives by one box copy where the cell
+// grid's row pitch allows it; along x it then starts four cells left of the tile (a 16-byte
+// boundary) and holds 40 entries, of which the first is never read.
 constexpr int kWX = 32, kWY = 8, kWZ = 4;
-constexpr int kWBX = kWX + 7, kWBY = kWY + 7, kWBZ = kWZ + 7;  // nodes [tile - 3, tile + 4]
+constexpr int kWBX = kWX + 8, kWBY = kWY + 7, kWBZ = kWZ + 7;  // nodes [tile - 4, tile + 4] x [tile - 3, tile + 4]^2
 constexpr int kWRows = kWBY * kWBZ;
 constexpr int kWBases = kWX + 2;                 // floor indices [tile - 1, tile + 32]
-constexpr int kWBoxN = (kWBX * kWRows + 3) & ~3;  // phi box, padded to 16 bytes (float)
+constexpr int kWBoxN = kWBX * kWRows;            // phi box (a multiple of 16 bytes)
 constexpr int kWQ = kWRows * kWBases;            // one indicator plane
 
 template <typename T, int TRACE>
-__global__ void __launch_bounds__(kWX * kWY, sizeof(T) == 4 ? 2 : 1) advect_phi_weno_tiled_kernel(GridView<T> src, T* __restrict__ out,
-                                                                           Mac<T> mac, DtArg dt, T dx, T inv_dx) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* pbox = reinterpret_cast<T*>(smem_raw);  // [z][y][x]
-    T* qbox = pbox + kWBoxN;                    // [s][row][floor index]
+__global__ void __launch_bounds__(kWX * kWY, sizeof(T) == 4 ? 2 : 1)
+    advect_phi_weno_tiled_kernel(GridView<T> src, T* __restrict__ out, Mac<T> mac, DtArg dt, T dx, T inv_dx,
+                                 const __grid_constant__ BoxMap pmap) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T* pbox = reinterpret_cast<T*>(align128(smem_raw));  // [z][y][x]
+    T* qbox = pbox + kWBoxN;                              // [s][row][floor index]
+    const T* pb = pbox + 1;  // the box from node tile - 3 along x
+    __shared__ uint64_t bar;
     const int x0 = blockIdx.x * kWX, y0 = blockIdx.y * kWY, z0 = blockIdx.z * kWZ;
-    const int bx0 = x0 - 3, by0 = y0 - 3, bz0 = z0 - 3;
+    const int bx0 = x0 - 4, by0 = y0 - 3, bz0 = z0 - 3;
     const int tid = threadIdx.x + kWX * threadIdx.y;
     const int lane = tid & 31, warp = tid >> 5;
-    for (int row = warp; row < kWRows; row += (kWX * kWY) / 32) {
-        const int bz = row / kWBY, by = row - bz * kWBY;
-        const int gy = clampi(by0 + by, 0, src.n1 - 1), gz = clampi(bz0 + bz, 0, src.n2 - 1);
-        const T* s = src.d + (long long)src.n0 * (gy + (long long)src.n1 * gz);
-        T* d = pbox + row * kWBX;
-        d[lane] = __ldg(s + clampi(bx0 + lane, 0, src.n0 - 1));
-        if (lane < kWBX - 32) d[32 + lane] = __ldg(s + clampi(bx0 + 32 + lane, 0, src.n0 - 1));
+    if (pmap.on) {
+        if (tid == 0) {
+            copy_boxes_begin(&bar, (unsigned)(kWBoxN * sizeof(T)));
+            tma_load_3d(pbox, &pmap.m, &bar, bx0, by0, bz0);
+        }
+        __syncthreads();  // the mbarrier's initialisation is seen by every thread
+        if (copy_boxes_failed(&bar)) {
+            nan_column(src, out, x0 + threadIdx.x, y0 + threadIdx.y, z0, kWZ);
+            return;
+        }
+        T unused = T(0);
+        finish_box<T, kWBX, kWBY, kWBZ, false>(pbox, src, bx0, by0, bz0, unused);
+    } else {
+        for (int row = warp; row < kWRows; row += (kWX * kWY) / 32) {
+            const int bz = row / kWBY, by = row - bz * kWBY;
+            const int gy = clampi(by0 + by, 0, src.n1 - 1), gz = clampi(bz0 + bz, 0, src.n2 - 1);
+            const T* s = src.d + (long long)src.n0 * (gy + (long long)src.n1 * gz);
+            T* d = pbox + row * kWBX;
+            d[lane] = __ldg(s + clampi(bx0 + lane, 0, src.n0 - 1));
+            if (lane < kWBX - 32) d[32 + lane] = __ldg(s + clampi(bx0 + 32 + lane, 0, src.n0 - 1));
+        }
     }
     __syncthreads();
     for (int e = tid; e < kWQ; e += kWX * kWY) {
         const int row = e / kWBases, b = e - row * kWBases;
-        const T* v = pbox + row * kWBX + b;
+        const T* v = pb + row * kWBX + b;
         T qa, qb, qc;
         weno6_sq(v[0], v[1], v[2], v[3], v[4], v[5], qa, qb, qc);
         qbox[e] = qa;
@@ -506,7 +659,7 @@ __global__ void __launch_bounds__(kWX * kWY, sizeof(T) == 4 ? 2 : 1) advect_phi_
 #pragma unroll
                 for (int dj = 0; dj < 6; ++dj) {
                     const int row = row0 + dj;
-                    const T* v = pbox + row * kWBX + px.a;
+                    const T* v = pb + row * kWBX + px.a;
                     const T* q = qbox + row * kWBases + px.a;
                     yl[dj] = weno6_combine(wx, v[0], v[1], v[2], v[3], v[4], v[5], q[0], q[kWQ], q[2 * kWQ]);
                 }
@@ -574,34 +727,58 @@ static int advect_launch(int ni, int nj, int nk, double dx_d, int comp, void* ou
     return 1;
 }
 
-// the tiled kernels: the level set (any scheme), and the velocity advecting itself (trilinear)
+// The box map of one array for boxes of bx x by x bz (on = 0 when copies are off or the
+// array's pitch or address does not allow them: the kernel then stages it by plain loads).
+template <typename T>
+static BoxMap box_map(const GridView<T>& g, bool copy, unsigned bx, unsigned by, unsigned bz) {
+    BoxMap b;
+    std::memset(&b, 0, sizeof(b));
+    b.on = copy && tma_encode_3d(&b.m, sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+                                 (int)sizeof(T), g.d, g.n0, g.n1, g.n2, g.n0, bx, by, bz);
+    return b;
+}
+
+template <typename T>
+static MacMaps mac_maps(const Mac<T>& mac, bool copy) {
+    MacMaps m;
+    m.c[0] = box_map(mac.u, copy, kBoxX, kBoxY, kBoxZ);
+    m.c[1] = box_map(mac.v, copy, kBoxX, kBoxY, kBoxZ);
+    m.c[2] = box_map(mac.w, copy, kBoxX, kBoxY, kBoxZ);
+    return m;
+}
+
+// the tiled kernels: the level set (any scheme), and the velocity advecting itself (trilinear);
+// dynamic shared memory holds the boxes plus 128 bytes to align them
 template <typename T, int TRACE, int SAMPLE>
-static int launch_phi_tiled(const GridView<T>& src, void* out, const Mac<T>& mac, DtArg dt, T dx, cudaStream_t s) {
-    const int smem = 3 * kBoxN * (int)sizeof(T);
+static int launch_phi_tiled(const GridView<T>& src, void* out, const Mac<T>& mac, DtArg dt, T dx, bool copy,
+                            cudaStream_t s) {
+    const int smem = 3 * kBoxN * (int)sizeof(T) + 128;
     if (cudaFuncSetAttribute(advect_phi_tiled_kernel<T, TRACE, SAMPLE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              smem) != cudaSuccess)
         return -1;
     const dim3 grid((src.n0 + kTileX - 1) / kTileX, (src.n1 + kTileY - 1) / kTileY, (src.n2 + kTileZ - 1) / kTileZ);
     advect_phi_tiled_kernel<T, TRACE, SAMPLE><<<grid, dim3(kTileX, kTileY, 1), smem, s>>>(
-        src, static_cast<T*>(out), mac, dt, dx, T(1) / dx);
+        src, static_cast<T*>(out), mac, dt, dx, T(1) / dx, mac_maps(mac, copy));
     return 1;
 }
 
 template <typename T, int TRACE>
-static int launch_phi_weno_tiled(const GridView<T>& src, void* out, const Mac<T>& mac, DtArg dt, T dx, cudaStream_t s) {
-    const int smem = (kWBoxN + 3 * kWQ) * (int)sizeof(T);
+static int launch_phi_weno_tiled(const GridView<T>& src, void* out, const Mac<T>& mac, DtArg dt, T dx, bool copy,
+                                 cudaStream_t s) {
+    const int smem = (kWBoxN + 3 * kWQ) * (int)sizeof(T) + 128;
     if (cudaFuncSetAttribute(advect_phi_weno_tiled_kernel<T, TRACE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              smem) != cudaSuccess)
         return -1;
     const dim3 grid((src.n0 + kWX - 1) / kWX, (src.n1 + kWY - 1) / kWY, (src.n2 + kWZ - 1) / kWZ);
-    advect_phi_weno_tiled_kernel<T, TRACE><<<grid, dim3(kWX, kWY, 1), smem, s>>>(src, static_cast<T*>(out), mac, dt,
-                                                                                  dx, T(1) / dx);
+    advect_phi_weno_tiled_kernel<T, TRACE><<<grid, dim3(kWX, kWY, 1), smem, s>>>(
+        src, static_cast<T*>(out), mac, dt, dx, T(1) / dx, box_map(src, copy, kWBX, kWBY, kWBZ));
     return 1;
 }
 
 template <typename T, int TRACE>
-static int launch_velocity_tiled(const Mac<T>& mac, void* ou, void* ov, void* ow, DtArg dt, T dx, cudaStream_t s) {
-    const int smem = 3 * kBoxN * (int)sizeof(T);
+static int launch_velocity_tiled(const Mac<T>& mac, void* ou, void* ov, void* ow, DtArg dt, T dx, bool copy,
+                                 cudaStream_t s) {
+    const int smem = 3 * kBoxN * (int)sizeof(T) + 128;
     if (cudaFuncSetAttribute(advect_velocity_tiled_kernel<T, TRACE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              smem) != cudaSuccess)
         return -1;
@@ -609,49 +786,63 @@ static int launch_velocity_tiled(const Mac<T>& mac, void* ou, void* ov, void* ow
     const dim3 grid((mac.u.n0 + kTileX - 1) / kTileX, (mac.v.n1 + kTileY - 1) / kTileY,
                     (mac.w.n2 + kTileZ - 1) / kTileZ);
     advect_velocity_tiled_kernel<T, TRACE><<<grid, dim3(kTileX, kTileY, 1), smem, s>>>(
-        mac, static_cast<T*>(ou), static_cast<T*>(ov), static_cast<T*>(ow), dt, dx, T(1) / dx);
+        mac, static_cast<T*>(ou), static_cast<T*>(ov), static_cast<T*>(ow), dt, dx, T(1) / dx, mac_maps(mac, copy));
     return 1;
 }
 
 template <typename T>
 static int advect_phi_tiled_t(int ni, int nj, int nk, double dx_d, void* out, const void* in, const void* vu,
-                              const void* vv, const void* vw, DtArg dt, int trace, int sample, cudaStream_t s) {
+                              const void* vv, const void* vw, DtArg dt, int trace, int sample, bool copy,
+                              cudaStream_t s) {
     const T dx = (T)dx_d;
     Mac<T> mac{make_view<T>(vu, ni, nj, nk, dx, 1), make_view<T>(vv, ni, nj, nk, dx, 2),
                make_view<T>(vw, ni, nj, nk, dx, 3)};
     GridView<T> src = make_view<T>(in, ni, nj, nk, dx, 0);
     if (sample == EL_SAMPLE_WENO6)
-        return trace == EL_TRACE_RK2 ? launch_phi_weno_tiled<T, EL_TRACE_RK2>(src, out, mac, dt, dx, s)
-                                     : launch_phi_weno_tiled<T, EL_TRACE_RK3>(src, out, mac, dt, dx, s);
-    if (trace == EL_TRACE_RK2) return launch_phi_tiled<T, EL_TRACE_RK2, EL_SAMPLE_TRILINEAR>(src, out, mac, dt, dx, s);
-    return launch_phi_tiled<T, EL_TRACE_RK3, EL_SAMPLE_TRILINEAR>(src, out, mac, dt, dx, s);
+        return trace == EL_TRACE_RK2 ? launch_phi_weno_tiled<T, EL_TRACE_RK2>(src, out, mac, dt, dx, copy, s)
+                                     : launch_phi_weno_tiled<T, EL_TRACE_RK3>(src, out, mac, dt, dx, copy, s);
+    if (trace == EL_TRACE_RK2)
+        return launch_phi_tiled<T, EL_TRACE_RK2, EL_SAMPLE_TRILINEAR>(src, out, mac, dt, dx, copy, s);
+    return launch_phi_tiled<T, EL_TRACE_RK3, EL_SAMPLE_TRILINEAR>(src, out, mac, dt, dx, copy, s);
 }
 
 template <typename T>
 static int advect_velocity_tiled_t(int ni, int nj, int nk, double dx_d, void* ou, void* ov, void* ow, const void* vu,
-                                   const void* vv, const void* vw, DtArg dt, int trace, cudaStream_t s) {
+                                   const void* vv, const void* vw, DtArg dt, int trace, bool copy, cudaStream_t s) {
     const T dx = (T)dx_d;
     Mac<T> mac{make_view<T>(vu, ni, nj, nk, dx, 1), make_view<T>(vv, ni, nj, nk, dx, 2),
                make_view<T>(vw, ni, nj, nk, dx, 3)};
-    if (trace == EL_TRACE_RK2) return launch_velocity_tiled<T, EL_TRACE_RK2>(mac, ou, ov, ow, dt, dx, s);
-    return launch_velocity_tiled<T, EL_TRACE_RK3>(mac, ou, ov, ow, dt, dx, s);
+    if (trace == EL_TRACE_RK2) return launch_velocity_tiled<T, EL_TRACE_RK2>(mac, ou, ov, ow, dt, dx, copy, s);
+    return launch_velocity_tiled<T, EL_TRACE_RK3>(mac, ou, ov, ow, dt, dx, copy, s);
 }
 
 // Level set through the tiled kernel; returns kernels launched, -1 on a launch set-up failure.
+// copy: stage the boxes by box copies where the arrays allow it (else plain loads throughout).
 int advect_phi_tiled(int dtype, int ni, int nj, int nk, double dx, void* out, const void* in, const void* vu,
-                     const void* vv, const void* vw, const Scalars* dts, double dtv, int trace, int sample,
+                     const void* vv, const void* vw, const Scalars* dts, double dtv, int trace, int sample, bool copy,
                      cudaStream_t s) {
     DtArg dt{dts, dtv};
-    if (dtype == EL_F64) return advect_phi_tiled_t<double>(ni, nj, nk, dx, out, in, vu, vv, vw, dt, trace, sample, s);
-    return advect_phi_tiled_t<float>(ni, nj, nk, dx, out, in, vu, vv, vw, dt, trace, sample, s);
+    if (dtype == EL_F64)
+        return advect_phi_tiled_t<double>(ni, nj, nk, dx, out, in, vu, vv, vw, dt, trace, sample, copy, s);
+    return advect_phi_tiled_t<float>(ni, nj, nk, dx, out, in, vu, vv, vw, dt, trace, sample, copy, s);
 }
 
 // u, v, w advected through themselves with trilinear sampling, one tiled launch
 int advect_velocity_tiled(int dtype, int ni, int nj, int nk, double dx, void* ou, void* ov, void* ow, const void* vu,
-                          const void* vv, const void* vw, const Scalars* dts, double dtv, int trace, cudaStream_t s) {
+                          const void* vv, const void* vw, const Scalars* dts, double dtv, int trace, bool copy,
+                          cudaStream_t s) {
     DtArg dt{dts, dtv};
-    if (dtype == EL_F64) return advect_velocity_tiled_t<double>(ni, nj, nk, dx, ou, ov, ow, vu, vv, vw, dt, trace, s);
-    return advect_velocity_tiled_t<float>(ni, nj, nk, dx, ou, ov, ow, vu, vv, vw, dt, trace, s);
+    if (dtype == EL_F64)
+        return advect_velocity_tiled_t<double>(ni, nj, nk, dx, ou, ov, ow, vu, vv, vw, dt, trace, copy, s);
+    return advect_velocity_tiled_t<float>(ni, nj, nk, dx, ou, ov, ow, vu, vv, vw, dt, trace, copy, s);
+}
+
+// the box-copy wait fault word, read and cleared (synchronises the device)
+bool advect_fault_take() {
+    unsigned v = 0, z = 0;
+    if (cudaMemcpyFromSymbol(&v, advect_wait_fault, sizeof(v)) != cudaSuccess) return false;
+    if (v) cudaMemcpyToSymbol(advect_wait_fault, &z, sizeof(z));
+    return v != 0;
 }
 
 int advect_any(int dtype, int ni, int nj, int nk, double dx, int comp, void* out, const void* in,

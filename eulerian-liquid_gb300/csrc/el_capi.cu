@@ -14,10 +14,12 @@ int advect_any(int dtype, int ni, int nj, int nk, double dx, int comp, void* out
                const void* vv, const void* vw, const Scalars* dts, double dtv, int trace, int sample,
                cudaStream_t s, int rows = 4);
 int advect_phi_tiled(int dtype, int ni, int nj, int nk, double dx, void* out, const void* in, const void* vu,
-                     const void* vv, const void* vw, const Scalars* dts, double dtv, int trace, int sample,
+                     const void* vv, const void* vw, const Scalars* dts, double dtv, int trace, int sample, bool copy,
                      cudaStream_t s);
 int advect_velocity_tiled(int dtype, int ni, int nj, int nk, double dx, void* ou, void* ov, void* ow, const void* vu,
-                          const void* vv, const void* vw, const Scalars* dts, double dtv, int trace, cudaStream_t s);
+                          const void* vv, const void* vw, const Scalars* dts, double dtv, int trace, bool copy,
+                          cudaStream_t s);
+bool advect_fault_take();
 int launch_weights(int dtype, int ni, int nj, int nk, const void* solid, void* wu, void* wv, void* ww,
                    cudaStream_t s);
 int launch_cell_solid(el_ctx* ctx);
@@ -269,7 +271,7 @@ EL_API int el_ctx_set_tuning(el_ctx* ctx, const el_tuning* t) {
     if (!t || t->seg_blocks_per_sm < 1 || t->seg_blocks_per_sm > 8 || t->stencil_blocks_per_sm < 1 ||
         t->stencil_blocks_per_sm > 16 || t->extrapolate_blocks_per_sm < 1 || t->extrapolate_blocks_per_sm > 16 ||
         (t->advect_rows != 1 && t->advect_rows != 2 && t->advect_rows != 4 && t->advect_rows != 8) ||
-        (t->advect_tiled != 0 && t->advect_tiled != 1) || (t->solver_tiles != 0 && t->solver_tiles != 1) ||
+        t->advect_tiled < 0 || t->advect_tiled > 2 || (t->solver_tiles != 0 && t->solver_tiles != 1) ||
         (t->coarse_fused != 0 && t->coarse_fused != 1) || (t->dependent_launch != 0 && t->dependent_launch != 1))
         return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "tuning out of range");
     // the reduction partials are sized for 16 stencil blocks per SM (el_ctx_create)
@@ -478,7 +480,7 @@ static int advect_level_set_impl(el_ctx* ctx, const Scalars* dts, double dt, int
     int n = ctx->advect_tiled ? advect_phi_tiled(ctx->dtype, ctx->ni, ctx->nj, ctx->nk, ctx->dx, ctx->tmp[0],
                                                  ctx->field[EL_FIELD_PHI], ctx->field[EL_FIELD_U],
                                                  ctx->field[EL_FIELD_V], ctx->field[EL_FIELD_W], dts, dt, trace,
-                                                 sample, ctx->stream)
+                                                 sample, ctx->advect_tiled == 1, ctx->stream)
                               : -1;
     if (n < 0)
         n = advect_any(ctx->dtype, ctx->ni, ctx->nj, ctx->nk, ctx->dx, 0, ctx->tmp[0], ctx->field[EL_FIELD_PHI],
@@ -497,7 +499,7 @@ static int advect_velocity_impl(el_ctx* ctx, const Scalars* dts, double dt, int 
         ProfScope prof(ctx, EL_KC_ADVECT_VEL, 2 * vel_bytes);
         n = advect_velocity_tiled(ctx->dtype, ctx->ni, ctx->nj, ctx->nk, ctx->dx, ctx->tmp[1], ctx->tmp[2],
                                   ctx->tmp[3], ctx->field[EL_FIELD_U], ctx->field[EL_FIELD_V],
-                                  ctx->field[EL_FIELD_W], dts, dt, trace, ctx->stream);
+                                  ctx->field[EL_FIELD_W], dts, dt, trace, ctx->advect_tiled == 1, ctx->stream);
     }
     if (n <= 0) {  // one launch per component
         n = 0;
@@ -689,7 +691,12 @@ EL_API int el_step(el_ctx* ctx, double dt, const el_step_params* p, el_step_stat
         NvtxRange r("el_step solve_pressure");
         rc = solve_pressure_impl(ctx, p->solve, &st->solve);
     }
-    if (rc != EL_OK) return rc;
+    if (rc != EL_OK) {
+        // a tile whose box copies never arrived wrote NaN, which the solve met
+        if (rc == EL_ERR_NAN && advect_fault_take())
+            return set_error(ctx, EL_ERR_TIMEOUT, "a wait for the advection's box copies gave up");
+        return rc;
+    }
     return st->solve.status == EL_OK ? EL_OK : set_error(ctx, st->solve.status, "pressure solve did not converge");
 }
 

@@ -16,7 +16,9 @@
 // the copies: full / empty mbarrier pairs per ring slot, no CTA-wide barrier per plane.  CTAs
 // take the work items round robin, so the CTAs running at any moment hold neighbouring tiles of
 // the same planes and read each other's halo rows from L2 rather than from DRAM; a CTA's planes
-// stream in one sequence across its items.
+// stream in one sequence across its items.  The items left over after the last full round are
+// split into plane runs of equal length over all CTAs (SegWalk), so that the launch has no tail
+// in which a fraction of the CTAs march one more whole item.
 //
 // Kernels (one launch each, over the work items of el::MarchPlan):
 //   DIRSPMV   p' = z + beta p ; Ap' ; p'.Ap'                            (K1 of a PCG iteration)
@@ -43,6 +45,7 @@
 #include <cstring>
 
 #include "el_internal.cuh"
+#include "el_tma.cuh"
 
 namespace el {
 
@@ -59,9 +62,6 @@ constexpr int kThreads = 32 * (kComputeWarps + 1);  // and one producer warp
 constexpr int kMaxStages = 6;    // plane buffers in the ring: three in use, the rest in flight
 constexpr int kMVW = kTI + 2;    // masked-value plane: columns i0 - 1 .. i0 + 32 of the staged rows
 constexpr unsigned kFull = 0xffffffffu;
-// a bounded wait: this many polls (each try_wait may itself suspend for a while) before the
-// kernel gives up, records the fault and stops
-constexpr long long kWaitPolls = 1ll << 24;
 
 enum Mode { DIRSPMV = 0, UPDZ = 1, ZERO2 = 2, RESTRICT = 3, PROLONG = 4, LAST = 5 };
 
@@ -96,6 +96,8 @@ struct Layout {
     // six slots, five for ZERO2 (so that four of its CTAs fit an SM)
     static constexpr int stages = M == ZERO2 ? 5 : 6;
     static constexpr int smem = 128 + stages * stage + 128;  // barriers first; alignment slack
+    // the CTAs an SM holds by shared memory, which the register budget must not lower
+    static constexpr int min_blocks = M == ZERO2 ? 4 : (M == DIRSPMV || M == UPDZ ? 2 : 3);
     static_assert(stages <= kMaxStages && 2 * kMaxStages * 8 <= 128, "barriers fit in front of the ring");
 };
 
@@ -120,50 +122,6 @@ struct Args {
     int first;                  // DIRSPMV: first iteration (p' = z)
     int dot;                    // LAST: DOT_INIT (1) or DOT_BETA (2)
 };
-
-__device__ __forceinline__ unsigned smem_u32(const void* p) {
-    return static_cast<unsigned>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
-    unsigned ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// bounded wait for the completion of the phase with the given parity
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
-    for (long long n = 0; n < kWaitPolls; ++n)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-        "[%5];" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-        : "memory");
-}
 
 __device__ __forceinline__ float mg_divf(float a, float b) { return __fdividef(a, b); }
 
@@ -212,10 +170,47 @@ __device__ __forceinline__ unsigned char* stage_ptr(unsigned char* smem, int slo
     return smem + 128 + slot * Layout<M>::stage;
 }
 
-// the dynamic shared memory, rounded up to a 128-byte boundary (the launch reserves the slack)
-__device__ __forceinline__ unsigned char* aligned_smem(unsigned char* raw) {
-    const unsigned a = smem_u32(raw);
-    return raw + ((128u - (a & 127u)) & 127u);
+// The plane runs {i0, j0, ka, kb} a CTA marches.  Whole items go round robin while every CTA
+// still gets one; the planes of the items left over are then split evenly over all CTAs, in
+// plane pairs (so that a run starts on an even plane, as the 2 x 2 x 2 restriction needs), so
+// that no CTA marches a whole extra item while the others wait.  A run that starts inside an
+// item stages its own plane ka - 1, like an item's first run.  The producer warp and the
+// compute warps walk the same sequence.
+struct SegWalk {
+    int it, whole_end;
+    int q, qend;  // the CTA's share of the leftover items' planes, [q, qend)
+};
+
+__device__ __forceinline__ SegWalk seg_begin(int n, int G, int b) {
+    SegWalk s;
+    s.whole_end = (n / G) * G;
+    s.it = b;
+    // fewer than G leftover items of kMarchPlanes / 2 pairs each: the products fit 32 bits
+    const int pairs = (n - s.whole_end) * (kMarchPlanes / 2);
+    s.q = 2 * (b * pairs / G);
+    s.qend = 2 * ((b + 1) * pairs / G);
+    return s;
+}
+
+__device__ __forceinline__ bool seg_next(SegWalk& s, const int4* items, int4& run) {
+    if (s.it < s.whole_end) {
+        run = items[s.it];
+        s.it += gridDim.x;
+        return true;
+    }
+    while (s.q < s.qend) {
+        const int item = s.whole_end + s.q / kMarchPlanes;
+        const int off = s.q % kMarchPlanes;
+        const int len = min(s.qend - s.q, kMarchPlanes - off);
+        s.q += len;
+        const int4 d = items[item];
+        const int ka = d.z + off, kb = min(d.w, ka + len);
+        if (ka < kb) {
+            run = make_int4(d.x, d.y, ka, kb);
+            return true;
+        }
+    }
+    return false;
 }
 
 }  // namespace
@@ -229,14 +224,14 @@ __device__ __forceinline__ bool dpos(const unsigned char* rec, int idx, int byte
 }
 
 template <int M>
-__global__ void __launch_bounds__(kThreads, 2) march_kernel(const __grid_constant__ Maps maps, const Args a) {
+__global__ void __launch_bounds__(kThreads, Layout<M>::min_blocks) march_kernel(const __grid_constant__ Maps maps, const Args a) {
     using L = Layout<M>;
     Scalars* s = a.s;
     pdl_wait();
     pdl_trigger();
     if (s->done) return;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    unsigned char* smem = aligned_smem(smem_raw);
+    unsigned char* smem = align128(smem_raw);
     uint64_t* full = reinterpret_cast<uint64_t*>(smem);   // a plane landed (transaction count)
     constexpr int kStages = L::stages;
     uint64_t* empty = full + kMaxStages;                  // every compute warp is done with it
@@ -251,8 +246,7 @@ __global__ void __launch_bounds__(kThreads, 2) march_kernel(const __grid_constan
             mbar_init(&full[q], 1);
             mbar_init(&empty[q], kComputeWarps);
         }
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_init_fence();
     }
     __syncthreads();
     float part = 0.f;  // this thread's share of the mode's dot product
@@ -264,8 +258,9 @@ __global__ void __launch_bounds__(kThreads, 2) march_kernel(const __grid_constan
             const unsigned tx = (unsigned)(L::rec_box_bytes + nhalo * L::halo_bytes + L::ncentre * L::centre_bytes +
                                            (L::coarse ? L::coarse_bytes : 0));
             int slot = 0, round = 0, issued = 0;
-            for (int it = b; it < n && !abort_flag; it += G) {
-                const int4 d = a.items[it];
+            SegWalk walk = seg_begin(n, G, b);
+            int4 d;
+            while (!abort_flag && seg_next(walk, a.items, d)) {
                 const int i0 = d.x, j0 = d.y;
                 for (int k = d.z - 1; k <= d.w; ++k) {
                     // the slot's previous plane must have been released by every compute warp
@@ -346,8 +341,9 @@ __global__ void __launch_bounds__(kThreads, 2) march_kernel(const __grid_constan
             }
         };
         auto aborted = [&]() -> bool { return L::mv ? stop : !ok; };
-        for (int it = b; it < n && !aborted(); it += G) {
-            const int4 d = a.items[it];
+        SegWalk walk = seg_begin(n, G, b);
+        int4 d;
+        while (!aborted() && seg_next(walk, a.items, d)) {
             const int i0 = d.x, j0 = d.y, k0 = d.z, k1 = d.w;
             const int i = i0 + lane;
             int sa = wait_next();  // plane k0 - 1
@@ -601,35 +597,6 @@ __global__ void march_compact_kernel(int total, int nib, int njb, int n2, const 
 
 namespace {
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }
-    return fn;
-}
-
-// a 3-D tensor map over an i-fastest array of (d0 elements of `type`) x n1 x n2
-bool encode(CUtensorMap* map, CUtensorMapDataType type, int esize, const void* base, long long d0, int n1, int n2,
-            long long row_elems, unsigned bx, unsigned by) {
-    auto fn = encode_fn();
-    if (!fn) return false;
-    const cuuint64_t dims[3] = {(cuuint64_t)d0, (cuuint64_t)n1, (cuuint64_t)n2};
-    const cuuint64_t strides[2] = {(cuuint64_t)(row_elems * esize), (cuuint64_t)(row_elems * esize * n1)};
-    const cuuint32_t box[3] = {bx, by, 1};
-    const cuuint32_t estr[3] = {1, 1, 1};
-    return fn(map, type, 3, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
 template <int M>
 int smem_bytes() {
     return Layout<M>::smem;
@@ -702,7 +669,7 @@ int centre_index(el_ctx* ctx, const float* v) {
 
 bool march_supported(const el_ctx* ctx) {
     return ctx->dtype == EL_F32 && ctx->ni % 8 == 0 && ctx->ni >= 64 && ctx->nj >= 16 && ctx->nk >= 16 &&
-           ctx->mg32.size() >= 3 && encode_fn() != nullptr;
+           ctx->mg32.size() >= 3 && tma_encode_fn() != nullptr;
 }
 
 // Tensor maps and the work-item storage, once per context (the arrays never move).
@@ -723,17 +690,17 @@ int march_setup(el_ctx* ctx) {
                                                ctx->r32,   ctx->r32b, ctx->mg32[0].t};
     bool ok = true;
     for (int h = 0; h < MarchPlan::NHALO; ++h)
-        ok = ok && encode(&mp.halo[h], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, halo_src[h], ni, nj, nk, ni, kHX, kHY);
+        ok = ok && tma_encode_3d(&mp.halo[h], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, halo_src[h], ni, nj, nk, ni, kHX, kHY);
     const float* centre_src[MarchPlan::NCENTRE] = {ctx->x32, ctx->p32, ctx->p32b, ctx->r32, ctx->r32b};
     for (int c = 0; c < MarchPlan::NCENTRE; ++c)
-        ok = ok && encode(&mp.centre[c], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, centre_src[c], ni, nj, nk, ni, kTI, kTJ);
+        ok = ok && tma_encode_3d(&mp.centre[c], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, centre_src[c], ni, nj, nk, ni, kTI, kTJ);
     // records: four components per cell as the innermost dimension
-    ok = ok && encode(&mp.rec32, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, ctx->A32, 4ll * ni, nj, nk, 4ll * ni,
+    ok = ok && tma_encode_3d(&mp.rec32, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, ctx->A32, 4ll * ni, nj, nk, 4ll * ni,
                       4 * Layout<DIRSPMV>::rec_w, kHY);
-    ok = ok && encode(&mp.rec16, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, ctx->A16, 4ll * ni, nj, nk, 4ll * ni,
+    ok = ok && tma_encode_3d(&mp.rec16, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, ctx->A16, 4ll * ni, nj, nk, 4ll * ni,
                       4 * Layout<LAST>::rec_w, kHY);
     const auto& C = ctx->mg32[1];
-    ok = ok && encode(&mp.coarse_x, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, C.x, C.n0, C.n1, C.n2, C.n0, kCX, kCY);
+    ok = ok && tma_encode_3d(&mp.coarse_x, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, C.x, C.n0, C.n1, C.n2, C.n0, kCX, kCY);
     if (!ok) return EL_OK;  // the segment kernels stay in use
     int rc;
     if ((rc = set_smem<DIRSPMV>(ctx)) != EL_OK || (rc = set_smem<UPDZ>(ctx)) != EL_OK ||

@@ -138,7 +138,10 @@ typedef struct el_tuning {
     int extrapolate_blocks_per_sm; /* extrapolation tiles in flight per SM, 1..16 (default 12)  */
     int advect_rows;             /* per-sample advection: 32 x rows cells per block, 1, 2, 4 or 8 */
     int advect_tiled;            /* 1 (default): advection kernels that stage the velocity of a
-                                    32x8x8 tile in shared memory; 0: one thread per sample      */
+                                    32x8x8 tile in shared memory, its boxes by TMA box copies
+                                    where an array's row pitch is a multiple of 16 bytes; 2: the
+                                    same kernels with every box staged by plain loads (identical
+                                    results); 0: one thread per sample                          */
     int solver_tiles;            /* 1 (default): the mixed solver's finest level on the z-marching
                                     tile kernels with TMA-staged planes, where the grid allows
                                     (ni a multiple of 8, at least 64 x 16 x 16 cells); 0: the
