@@ -973,9 +973,22 @@ __global__ void __launch_bounds__(kCoarsestMaxCells) coarsest_kernel(LGeom g, co
 // prolongation reads it).
 constexpr int kBottomMaxCells = 4096;
 constexpr int kBottomThreads = 1024;
+// Each thread owns fixed cells: on the level, (i, j) = (t mod 16, t / 16 mod 16) and the planes
+// k = t / 256 + 4 m, m = 0..3 (the level is at most 16 cells a side: its coarse level is at
+// most 8); on the coarsest, thread t < 512 owns (t mod 8, t / 8 mod 8, t / 64).  No index is
+// divided at run time, and the coarsest cell's record stays in registers across its sweeps.
+constexpr int kBottomDim = 16, kBottomPlanes = kBottomThreads / (kBottomDim * kBottomDim);
+constexpr int kBottomCells = kBottomDim / kBottomPlanes;  // cells per thread on the level
 
-// the 7-point stencil of cell c of a dense level held in shared memory (float4 records)
-__device__ __forceinline__ St7<float> dense_st7(const float4* rec, const float* v, int c, int i, int j, int k,
+// neighbour bits of a cell: 1 -x, 2 +x, 4 -y, 8 +y, 16 -z, 32 +z inside the level
+__device__ __forceinline__ unsigned inside_bits(int i, int j, int k, const LGeom& g) {
+    return (i > 0 ? 1u : 0u) | (i < g.n0 - 1 ? 2u : 0u) | (j > 0 ? 4u : 0u) | (j < g.n1 - 1 ? 8u : 0u) |
+           (k > 0 ? 16u : 0u) | (k < g.n2 - 1 ? 32u : 0u);
+}
+
+// the 7-point stencil of cell c of a dense level held in shared memory (float4 records); a
+// neighbour outside the level gives coupling and value 0
+__device__ __forceinline__ St7<float> dense_st7(const float4* rec, const float* v, int c, unsigned in,
                                                 const LGeom& g) {
     St7<float> st;
     const float4 r0 = rec[c];
@@ -983,16 +996,16 @@ __device__ __forceinline__ St7<float> dense_st7(const float4* rec, const float* 
     st.cxp = r0.y;
     st.cyp = r0.z;
     st.czp = r0.w;
-    st.cxm = i > 0 ? rec[c - 1].y : 0.f;
-    st.cym = j > 0 ? rec[c - g.s1].z : 0.f;
-    st.czm = k > 0 ? rec[c - g.s2].w : 0.f;
+    st.cxm = (in & 1u) ? rec[c - 1].y : 0.f;
+    st.cym = (in & 4u) ? rec[c - g.s1].z : 0.f;
+    st.czm = (in & 16u) ? rec[c - g.s2].w : 0.f;
     st.v0 = v[c];
-    st.vxm = i > 0 ? v[c - 1] : 0.f;
-    st.vxp = i < g.n0 - 1 ? v[c + 1] : 0.f;
-    st.vym = j > 0 ? v[c - g.s1] : 0.f;
-    st.vyp = j < g.n1 - 1 ? v[c + g.s1] : 0.f;
-    st.vzm = k > 0 ? v[c - g.s2] : 0.f;
-    st.vzp = k < g.n2 - 1 ? v[c + g.s2] : 0.f;
+    st.vxm = (in & 1u) ? v[c - 1] : 0.f;
+    st.vxp = (in & 2u) ? v[c + 1] : 0.f;
+    st.vym = (in & 4u) ? v[c - g.s1] : 0.f;
+    st.vyp = (in & 8u) ? v[c + g.s1] : 0.f;
+    st.vzm = (in & 16u) ? v[c - g.s2] : 0.f;
+    st.vzp = (in & 32u) ? v[c + g.s2] : 0.f;
     return st;
 }
 
@@ -1011,18 +1024,28 @@ __device__ __forceinline__ void bottom_cycle(const LGeom& gf, const float4* __re
     float* s1 = sb + kBottomMaxCells;
     float* s2 = s1 + kBottomMaxCells;
     float4* cr = reinterpret_cast<float4*>(s2 + kBottomMaxCells);
-    float* cb = reinterpret_cast<float*>(cr + kCoarsestMaxCells);
-    float* c1 = cb + kCoarsestMaxCells;
+    float* c1 = reinterpret_cast<float*>(cr + kCoarsestMaxCells);
     float* c2 = c1 + kCoarsestMaxCells;
     const float omega = (float)kOmega;  // the coarsest level's sweeps
     const float w1 = (float)kSweep1, w2 = (float)kSweep2;
     const int nf = gf.n0 * gf.n1 * gf.n2, nc = gc.n0 * gc.n1 * gc.n2;
     const int tid = threadIdx.x;
-    auto fine_ijk = [&](int c, int& i, int& j, int& k) {
-        i = c % gf.n0;
-        j = (c / gf.n0) % gf.n1;
-        k = c / (gf.n0 * gf.n1);
-    };
+    // this thread's cells of the level: index (-1: none) and neighbour bits
+    const int fi = tid & (kBottomDim - 1), fj = (tid / kBottomDim) & (kBottomDim - 1);
+    const int fk0 = tid / (kBottomDim * kBottomDim);
+    int fc[kBottomCells];
+    unsigned fin[kBottomCells];
+#pragma unroll
+    for (int m = 0; m < kBottomCells; ++m) {
+        const int k = fk0 + kBottomPlanes * m;
+        const bool live = fi < gf.n0 && fj < gf.n1 && k < gf.n2;
+        fc[m] = live ? fi + gf.s1 * fj + gf.s2 * k : -1;
+        fin[m] = live ? inside_bits(fi, fj, k, gf) : 0u;
+    }
+    // this thread's cell of the coarsest level
+    const int ci = tid & 7, cj = (tid >> 3) & 7, ck = tid >> 6;
+    const bool clive = tid < kCoarsestMaxCells && ci < gc.n0 && cj < gc.n1 && ck < gc.n2;
+    const int cq = clive ? ci + gc.s1 * cj + gc.s2 * ck : 0;
     for (int c = tid; c < nf; c += kBottomThreads) {
         sr[c] = recf[c];
         sb[c] = __ldcg(bf + c);  // written by other CTAs of the fused coarse cycle
@@ -1030,15 +1053,19 @@ __device__ __forceinline__ void bottom_cycle(const LGeom& gf, const float4* __re
     for (int c = tid; c < nc; c += kBottomThreads) cr[c] = recc[c];
     __syncthreads();
     // two sweeps from zero: the first is pointwise
-    for (int c = tid; c < nf; c += kBottomThreads) {
+#pragma unroll
+    for (int m = 0; m < kBottomCells; ++m) {
+        const int c = fc[m];
+        if (c < 0) continue;
         const float d = sr[c].x;
         s1[c] = d > 0.f ? mg_div(w1 * sb[c], d) : 0.f;
     }
     __syncthreads();
-    for (int c = tid; c < nf; c += kBottomThreads) {
-        int i, j, k;
-        fine_ijk(c, i, j, k);
-        const St7<float> st = dense_st7(sr, s1, c, i, j, k, gf);
+#pragma unroll
+    for (int m = 0; m < kBottomCells; ++m) {
+        const int c = fc[m];
+        if (c < 0) continue;
+        const St7<float> st = dense_st7(sr, s1, c, fin[m], gf);
         float xo = 0.f;
         if (st.d > 0.f) xo = st.v0 + mg_div(w2 * (sb[c] - apply7(st)), st.d);
         s2[c] = xo;
@@ -1046,15 +1073,18 @@ __device__ __forceinline__ void bottom_cycle(const LGeom& gf, const float4* __re
     __syncthreads();
     // residual, then its 2 x 2 x 2 sums onto the coarsest level (order of the segment kernels:
     // i-pairs of the rows (jj, kk) = (0,0), (1,0), (0,1), (1,1), summed in that order)
-    for (int c = tid; c < nf; c += kBottomThreads) {
-        int i, j, k;
-        fine_ijk(c, i, j, k);
-        const St7<float> st = dense_st7(sr, s2, c, i, j, k, gf);
+#pragma unroll
+    for (int m = 0; m < kBottomCells; ++m) {
+        const int c = fc[m];
+        if (c < 0) continue;
+        const St7<float> st = dense_st7(sr, s2, c, fin[m], gf);
         s1[c] = st.d > 0.f ? sb[c] - apply7(st) : 0.f;
     }
     __syncthreads();
-    for (int q = tid; q < nc; q += kBottomThreads) {
-        const int I = q % gc.n0, J = (q / gc.n0) % gc.n1, K = q / (gc.n0 * gc.n1);
+    // the coarsest cell's record, rhs and neighbour bits in registers for all its sweeps
+    float cbq = 0.f, cd = 0.f, cxm = 0.f, cxp = 0.f, cym = 0.f, cyp = 0.f, czm = 0.f, czp = 0.f;
+    unsigned cin = 0u;
+    if (clive) {
         auto res = [&](int i, int j, int k) -> float {
             return (i < gf.n0 && j < gf.n1 && k < gf.n2) ? s1[i + gf.s1 * j + gf.s2 * k] : 0.f;
         };
@@ -1062,35 +1092,39 @@ __device__ __forceinline__ void bottom_cycle(const LGeom& gf, const float4* __re
 #pragma unroll
         for (int sub = 0; sub < 4; ++sub) {
             const int jj = sub & 1, kk = sub >> 1;
-            part[sub] = res(2 * I, 2 * J + jj, 2 * K + kk) + res(2 * I + 1, 2 * J + jj, 2 * K + kk);
+            part[sub] = res(2 * ci, 2 * cj + jj, 2 * ck + kk) + res(2 * ci + 1, 2 * cj + jj, 2 * ck + kk);
         }
-        cb[q] = ((part[0] + part[1]) + part[2]) + part[3];
-    }
-    __syncthreads();
-    // the coarsest level: damped Jacobi from zero, as coarsest_kernel
-    for (int q = tid; q < nc; q += kBottomThreads) {
-        const float d = cr[q].x;
-        c1[q] = d > 0.f ? mg_div(omega * cb[q], d) : 0.f;
+        cbq = ((part[0] + part[1]) + part[2]) + part[3];
+        cin = inside_bits(ci, cj, ck, gc);
+        const float4 r = cr[cq];
+        cd = r.x;
+        cxp = r.y;
+        cyp = r.z;
+        czp = r.w;
+        if (cin & 1u) cxm = cr[cq - 1].y;
+        if (cin & 4u) cym = cr[cq - gc.s1].z;
+        if (cin & 16u) czm = cr[cq - gc.s2].w;
+        // the coarsest level: damped Jacobi from zero, as coarsest_kernel
+        c1[cq] = cd > 0.f ? mg_div(omega * cbq, cd) : 0.f;
     }
     __syncthreads();
     float* cur = c1;
     float* nxt = c2;
     for (int it = 1; it < sweeps; ++it) {
-        for (int q = tid; q < nc; q += kBottomThreads) {
-            const int i = q % gc.n0, j = (q / gc.n0) % gc.n1, k = q / (gc.n0 * gc.n1);
+        if (clive) {
             float xo = 0.f;
-            const float d = cr[q].x;
-            if (d > 0.f) {
-                float a = d * cur[q];
-                if (i > 0) a += cr[q - 1].y * cur[q - 1];
-                if (i < gc.n0 - 1) a += cr[q].y * cur[q + 1];
-                if (j > 0) a += cr[q - gc.s1].z * cur[q - gc.s1];
-                if (j < gc.n1 - 1) a += cr[q].z * cur[q + gc.s1];
-                if (k > 0) a += cr[q - gc.s2].w * cur[q - gc.s2];
-                if (k < gc.n2 - 1) a += cr[q].w * cur[q + gc.s2];
-                xo = cur[q] + mg_div(omega * (cb[q] - a), d);
+            if (cd > 0.f) {
+                const float x0 = cur[cq];
+                float a = cd * x0;
+                if (cin & 1u) a += cxm * cur[cq - 1];
+                if (cin & 2u) a += cxp * cur[cq + 1];
+                if (cin & 4u) a += cym * cur[cq - gc.s1];
+                if (cin & 8u) a += cyp * cur[cq + gc.s1];
+                if (cin & 16u) a += czm * cur[cq - gc.s2];
+                if (cin & 32u) a += czp * cur[cq + gc.s2];
+                xo = x0 + mg_div(omega * (cbq - a), cd);
             }
-            nxt[q] = xo;
+            nxt[cq] = xo;
         }
         __syncthreads();
         float* t = cur;
@@ -1098,25 +1132,29 @@ __device__ __forceinline__ void bottom_cycle(const LGeom& gf, const float4* __re
         nxt = t;
     }
     // prolongation (x + P e) and a sweep, then the last sweep into global memory
-    for (int c = tid; c < nf; c += kBottomThreads) {
-        int i, j, k;
-        fine_ijk(c, i, j, k);
-        s1[c] = s2[c] + cur[(i >> 1) + gc.s1 * (j >> 1) + gc.s2 * (k >> 1)];
+#pragma unroll
+    for (int m = 0; m < kBottomCells; ++m) {
+        const int c = fc[m];
+        if (c < 0) continue;
+        const int k = fk0 + kBottomPlanes * m;
+        s1[c] = s2[c] + cur[(fi >> 1) + gc.s1 * (fj >> 1) + gc.s2 * (k >> 1)];
     }
     __syncthreads();
-    for (int c = tid; c < nf; c += kBottomThreads) {
-        int i, j, k;
-        fine_ijk(c, i, j, k);
-        const St7<float> st = dense_st7(sr, s1, c, i, j, k, gf);
+#pragma unroll
+    for (int m = 0; m < kBottomCells; ++m) {
+        const int c = fc[m];
+        if (c < 0) continue;
+        const St7<float> st = dense_st7(sr, s1, c, fin[m], gf);
         float xo = 0.f;
         if (st.d > 0.f) xo = st.v0 + mg_div(w1 * (sb[c] - apply7(st)), st.d);
         s2[c] = xo;
     }
     __syncthreads();
-    for (int c = tid; c < nf; c += kBottomThreads) {
-        int i, j, k;
-        fine_ijk(c, i, j, k);
-        const St7<float> st = dense_st7(sr, s2, c, i, j, k, gf);
+#pragma unroll
+    for (int m = 0; m < kBottomCells; ++m) {
+        const int c = fc[m];
+        if (c < 0) continue;
+        const St7<float> st = dense_st7(sr, s2, c, fin[m], gf);
         float xo = 0.f;
         if (st.d > 0.f) xo = st.v0 + mg_div(w2 * (sb[c] - apply7(st)), st.d);
         xf[c] = xo;
@@ -1449,8 +1487,9 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
     }
     // the FP32 hierarchy's last two levels in one CTA (mg_bottom_kernel)
     constexpr bool kBottomType = std::is_same<V, float>::value && std::is_same<RC, float4>::value;
-    const bool fused_bottom = kBottomType && L >= 3 && cells(mg[L - 2]) <= kBottomMaxCells &&
-                              cells(mg[L - 1]) <= kCoarsestMaxCells;
+    const bool fused_bottom = kBottomType && L >= 3 && mg[L - 2].n0 <= kBottomDim && mg[L - 2].n1 <= kBottomDim &&
+                              mg[L - 2].n2 <= kBottomDim && mg[L - 1].n0 <= 8 && mg[L - 1].n1 <= 8 &&
+                              mg[L - 1].n2 <= 8;
     const int pre_end = fused_bottom ? L - 2 : L - 1;  // levels smoothed and restricted by the loops
     // levels [coop_from, pre_end) and the bottom in one cooperative launch (the FP32 hierarchy)
     int coop_from = -1;
