@@ -192,12 +192,12 @@ EL_API int el_ctx_create(int ni, int nj, int nk, double dx, int dtype, int devic
         ctx->tmp[q] = ctx_alloc(ctx, ctx->field_bytes[EL_FIELD_PHI + q]);
         ok = ok && ctx->tmp[q];
     }
-    // extrapolation scratch sizes (allocated on first use): the largest face grid with rows
-    // padded to 16 bytes, and one index per cell of it
+    // extrapolation scratch sizes (allocated on first use): the padded bitmask of the largest
+    // face grid, and one index per cell of it
     for (int f = EL_FIELD_U; f <= EL_FIELD_W; ++f) {
         int n0, n1, n2;
         field_dims(ctx, f, n0, n1, n2);
-        ctx->ex_dist_bytes = std::max(ctx->ex_dist_bytes, (size_t)((n0 + 15) & ~15) * n1 * n2);
+        ctx->ex_bits_bytes = std::max(ctx->ex_bits_bytes, extrapolation_bits_bytes(n0, n1, n2));
         ctx->ex_list_bytes = std::max(ctx->ex_list_bytes, (size_t)n0 * n1 * n2 * sizeof(int));
     }
     ctx->dscal = (Scalars*)ctx_alloc(ctx, 4 * sizeof(Scalars));

@@ -1,25 +1,23 @@
-// el_extrap.cu -- extrapolation (src/project/3d/fluid/extrapolation.cpp:5-51) ordered by
-// distance instead of by sweeps.
+// el_extrap.cu -- extrapolation (src/project/3d/fluid/extrapolation.cpp:5-51): the reference's
+// layer loop over a bitmask of the valid cells.
 //
 // extrapolate() runs `layers` Jacobi layers: in layer l every cell that is not valid yet and
 // has a valid cell among its 26 neighbours (valid when the layer began) takes the mean of those
-// neighbours (summed in z, y, x order) and becomes valid.  By induction a cell becomes valid in
-// layer l exactly when its Chebyshev (L-infinity) distance d to the initially valid cells is
-// l + 1 (the grid is a box, so king-move paths stay inside it), and the neighbours it averages
-// are exactly those with a smaller d.  So the result is fixed by d alone:
-//
-//   1. d of every cell, capped at layers + 1, by three separable passes (a cube is separable):
-//      along x from the valid mask (warp ballots, bit scans), then along y and z,
-//      d_xy(c) = min_t max(|t|, d_x(c + t e_y)) with |t| <= layers (four cells per 32-bit word:
-//      vmaxu4 / vminu4), the z pass counting the cells of each distance;
-//   2. the cells of each distance 1..layers listed (a scan of the counts, block-aggregated
-//      scatter);
-//   3. one launch per layer over that layer's list: the mean of the neighbours with a smaller d,
-//      in the reference's z, y, x order, written in place (no cell of the layer reads another).
-//
-// The results are those of the reference loop bit for bit (same sums in the same order, same
-// division); only cells the layers reach are touched.  Up to four fields go through each
-// launch (velocity u, v, w and the level set of a step), each with its own scratch slot.
+// neighbours (summed in z, y, x order) and becomes valid.  Here the valid set S of a field is a
+// bitmask, one bit per cell and 32 cells of a row per word, with a zero word before and after
+// every row and zero rows and planes around the grid, so that a neighbour outside the grid is a
+// zero bit and needs no bounds test.  Per layer:
+//   1. ex_dilate_kernel: S' = S dilated by the 3 x 3 x 3 cube -- an OR over z, then over y,
+//      through shared memory, then along x by shifts that take the neighbouring words' edge
+//      bits -- is written to the other buffer, and the cells of S' \ S (this layer's) are listed
+//      per field (block-aggregated).  A tile with no set bit around it, or with every cell set,
+//      has none and is copied.
+//   2. ex_average_kernel: every listed cell takes the mean of its neighbours in S (the bits of
+//      the layer before), summed in z, y, x order, and is marked valid (extrapolate) or not
+//      (extrapolate_const).  No listed cell reads another.
+// The results are those of the reference loop bit for bit: the same cells, the same sums in the
+// same order and the same division.  Up to four fields go through each launch (velocity u, v,
+// w and the level set of a step), each with its own scratch slot.
 #include "el_internal.cuh"
 
 namespace el {
@@ -27,350 +25,303 @@ namespace el {
 namespace {
 
 constexpr int kExMaxFields = 4;
-constexpr int kDistThreads = 256;
+constexpr int kExThreads = 256;
+// the dilation tile: 8 words (256 cells) of a row x 32 rows x 8 planes, and its one-word /
+// one-row / one-plane halo
+constexpr int kTW = 8, kTY = 32, kTZ = 8;
+constexpr int kHW = kTW + 2, kHY = kTY + 2, kHZ = kTZ + 2;
+constexpr int kTileWords = kTW * kTY * kTZ;
+constexpr int kPerThread = kTileWords / kExThreads;
+constexpr int kHaloWords = kHW * kHY * kHZ;
+constexpr int kHaloLoads = (kHaloWords + kExThreads - 1) / kExThreads;
+static_assert(kTileWords % kExThreads == 0, "whole outputs per thread");
 
 struct ExField {
-    void* g;              // the field (float or double), i-fastest n0 x n1 x n2
-    uint8_t* valid;       // its valid mask (written back when write_back)
-    uint8_t* da;          // distance scratch, rows padded to `pitch` bytes
-    uint8_t* db;
-    int* list;            // the cells of distance 1..layers, grouped by distance
-    int n0, n1, n2, pitch;
+    void* g;          // the field (float or double), i-fastest n0 x n1 x n2
+    uint8_t* valid;   // its valid mask (written for the layers' cells when write_back)
+    unsigned* s;      // the valid set before the layer: padded bitmask
+    unsigned* s_next; // and after it
+    int* list;        // the layer's cells (linear indices)
+    int n0, n1, n2;
+    int rw;           // words per row, ceil(n0 / 32); a padded row holds rw + 2
     int write_back;
 };
 
 struct ExArgs {
     ExField f[kExMaxFields];
     int nf;
-    int layers;
-    int* counts;   // [kExMaxFields][256] cells per distance
-    int* offsets;  // [kExMaxFields][256] first list entry of each distance
-    int* cursors;  // [kExMaxFields][256] scatter cursors
+    int* counts;       // this layer's cells per field
+    int* counts_next;  // the next layer's, cleared by ex_average_kernel
 };
 
-__device__ __forceinline__ unsigned splat4(unsigned b) { return b * 0x01010101u; }
+// word (wp, yp, zp) of a padded bitmask: wp = word + 1, yp = y + 1, zp = z + 1
+__device__ __forceinline__ long long pad_at(const ExField& F, int wp, int yp, int zp) {
+    return wp + (long long)(F.rw + 2) * (yp + (long long)(F.n1 + 2) * zp);
+}
 
-// ---- 1a. distance along x: one warp per row, three 32-cell chunks of ballot bits in registers
-// (the window reaches 32 cells either side, enough for layers <= 31)
-__global__ void __launch_bounds__(kDistThreads) ex_dist_x_kernel(const ExArgs a) {
+// the bits of word w of a row that are cells of the grid
+__device__ __forceinline__ unsigned row_mask(int n0, int w) {
+    const int rem = n0 - 32 * w;
+    return rem >= 32 ? 0xffffffffu : ((1u << rem) - 1u);
+}
+
+// ---- the valid masks as bitmasks, in two passes over all fields: the mask's bytes as a flat
+// bit stream (32 cells per word, 16-byte loads), then that stream cut into the padded rows.
+// The flat words go to the field's list buffer, which the first layer overwrites later.
+
+// bit q of the result: byte q of x is not zero
+__device__ __forceinline__ unsigned nonzero_bytes(unsigned x) {
+    const unsigned h = (((x & 0x7f7f7f7fu) + 0x7f7f7f7fu) | x) & 0x80808080u;
+    return ((h >> 7) & 1u) | ((h >> 14) & 2u) | ((h >> 21) & 4u) | ((h >> 28) & 8u);
+}
+
+__global__ void __launch_bounds__(kExThreads) ex_flat_kernel(const ExArgs a) {
     const ExField& F = a.f[blockIdx.y];
-    const int lane = threadIdx.x & 31;
-    const int row = blockIdx.x * (kDistThreads / 32) + (threadIdx.x >> 5);
-    const int rows = F.n1 * F.n2;
-    if (row >= rows) return;
-    const uint8_t* v = F.valid + (long long)row * F.n0;
-    uint8_t* out = F.da + (long long)row * F.pitch;
-    const unsigned cap = (unsigned)a.layers + 1u;
-    const int nch = (F.pitch + 31) / 32;  // chunks over the padded row (padding comes out capped)
-    auto ballot = [&](int ch) -> unsigned {
-        const int i = ch * 32 + lane;
-        const bool on = ch >= 0 && i < F.n0 && v[i] != 0;
-        return __ballot_sync(0xffffffffu, on);
-    };
-    unsigned prev = 0u, cur = ballot(0);
-    for (int ch = 0; ch < nch; ++ch) {
-        const unsigned next = ch + 1 < nch ? ballot(ch + 1) : 0u;
-        // left: bits 0..32+lane of prev|cur (cell at 32 + lane); right: cur|next from the cell up
-        const unsigned long long lo = ((unsigned long long)cur << 32) | prev;
-        const unsigned long long lmask = lane == 31 ? ~0ull : ((2ull << (32 + lane)) - 1ull);
-        const unsigned long long lm = lo & lmask;
-        unsigned d = cap;
-        if (lm) d = min(d, (unsigned)(32 + lane - (63 - __clzll((long long)lm))));
-        const unsigned long long hi = (((unsigned long long)next << 32) | cur) >> lane;
-        if (hi) d = min(d, (unsigned)(__ffsll((long long)hi) - 1));
-        const int i = ch * 32 + lane;
-        if (i < F.pitch) out[i] = (uint8_t)d;
-        prev = cur;
-        cur = next;
+    const long long n = (long long)F.n0 * F.n1 * F.n2;
+    const long long words = (n + 31) / 32;
+    unsigned* flat = reinterpret_cast<unsigned*>(F.list);
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < words;
+         t += (long long)gridDim.x * blockDim.x) {
+        unsigned word = 0u;
+        if (32 * t + 32 <= n) {
+            const uint4* v4 = reinterpret_cast<const uint4*>(F.valid) + 2 * t;
+            const uint4 p = v4[0], q = v4[1];
+            word = nonzero_bytes(p.x) | (nonzero_bytes(p.y) << 4) | (nonzero_bytes(p.z) << 8) |
+                   (nonzero_bytes(p.w) << 12) | (nonzero_bytes(q.x) << 16) | (nonzero_bytes(q.y) << 20) |
+                   (nonzero_bytes(q.z) << 24) | (nonzero_bytes(q.w) << 28);
+        } else {
+            for (int b = 0; 32 * t + b < n; ++b) word |= (F.valid[32 * t + b] != 0 ? 1u : 0u) << b;
+        }
+        flat[t] = word;
     }
 }
 
-// the same for layers > 31: each cell scans its row outwards
-__global__ void __launch_bounds__(kDistThreads) ex_dist_x_scan_kernel(const ExArgs a) {
+// every word of the first buffer (the padding as zeros), and the padding of the second, so that
+// a slot that held another field's layout before is fully defined
+__global__ void __launch_bounds__(kExThreads) ex_rows_kernel(const ExArgs a) {
     const ExField& F = a.f[blockIdx.y];
-    const long long n = (long long)F.pitch * F.n1 * F.n2;
-    const int cap = a.layers + 1;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
-         q += (long long)gridDim.x * blockDim.x) {
-        const long long row = q / F.pitch;
-        const int i = (int)(q - row * F.pitch);
-        const uint8_t* v = F.valid + row * F.n0;
-        int d = cap;
-        for (int t = 0; t < cap; ++t) {
-            if ((i - t >= 0 && i - t < F.n0 && v[i - t]) || (i + t < F.n0 && v[i + t])) {
-                d = t;
-                break;
-            }
+    const int pw = F.rw + 2;
+    const long long total = (long long)pw * (F.n1 + 2) * (F.n2 + 2);
+    const long long n = (long long)F.n0 * F.n1 * F.n2;
+    const long long words = (n + 31) / 32;
+    const unsigned* flat = reinterpret_cast<const unsigned*>(F.list);
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int wp = (int)(t % pw);
+        const long long r = t / pw;
+        const int yp = (int)(r % (F.n1 + 2)), zp = (int)(r / (F.n1 + 2));
+        if (wp < 1 || wp > F.rw || yp < 1 || yp > F.n1 || zp < 1 || zp > F.n2) {
+            F.s[t] = 0u;
+            F.s_next[t] = 0u;
+            continue;
         }
-        F.da[q] = (uint8_t)d;
+        // cells 32 (wp - 1) .. + 31 of row (yp - 1, zp - 1) in the flat stream
+        const long long c0 = 32ll * (wp - 1) + (long long)F.n0 * ((yp - 1) + (long long)F.n1 * (zp - 1));
+        const long long lo = c0 >> 5;
+        const unsigned sh = (unsigned)(c0 & 31);
+        const unsigned a0 = flat[lo], a1 = lo + 1 < words ? flat[lo + 1] : 0u;
+        F.s[t] = __funnelshift_r(a0, a1, sh) & row_mask(F.n0, wp - 1);
     }
 }
 
-// ---- 1b. one separable pass along y (AXIS 1) or z (AXIS 2): out = min_t max(|t|, in(c + t e))
-// over |t| <= layers, four cells per word.  The z pass also counts the cells of each distance.
-template <int AXIS>
-__global__ void __launch_bounds__(kDistThreads) ex_dist_pass_kernel(const ExArgs a) {
-    const ExField& F = a.f[blockIdx.y];
-    __shared__ int hist[256];
-    if (AXIS == 2) {
-        for (int q = threadIdx.x; q < 256; q += blockDim.x) hist[q] = 0;
-        __syncthreads();
-    }
-    const int words = F.pitch / 4;
-    const long long nw = (long long)words * F.n1 * F.n2;
-    const int m_extent = AXIS == 1 ? F.n1 : F.n2;
-    const long long stride = AXIS == 1 ? words : (long long)words * F.n1;  // in words
-    const unsigned* in = reinterpret_cast<const unsigned*>(AXIS == 1 ? F.da : F.db);
-    unsigned* out = reinterpret_cast<unsigned*>(AXIS == 1 ? F.db : F.da);
-    const int L = a.layers;
-    const unsigned cap4 = splat4((unsigned)L + 1u);
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nw;
-         q += (long long)gridDim.x * blockDim.x) {
-        const long long line = q / words;  // (j, k) of the word
-        const int m = AXIS == 1 ? (int)(line % F.n1) : (int)(line / F.n1);
-        unsigned best = in[q];
-        for (int t = 1; t <= L; ++t) {
-            const unsigned tt = splat4((unsigned)t);
-            if (m - t >= 0) best = __vminu4(best, __vmaxu4(in[q - t * stride], tt));
-            if (m + t < m_extent) best = __vminu4(best, __vmaxu4(in[q + t * stride], tt));
-        }
-        best = __vminu4(best, cap4);
-        out[q] = best;
-        if (AXIS == 2) {
-            const int i0 = (int)(q - line * words) * 4;
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const unsigned d = (best >> (8 * b)) & 0xffu;
-                if (i0 + b < F.n0 && d >= 1u && (int)d <= L) atomicAdd(&hist[d], 1);
-            }
-        }
-    }
-    if (AXIS == 2) {
-        __syncthreads();
-        for (int q = threadIdx.x; q <= L && q < 256; q += blockDim.x)
-            if (hist[q]) atomicAdd(&a.counts[blockIdx.y * 256 + q], hist[q]);
-    }
-}
-
-// The same pass for layers <= kTileMaxLayers through shared memory: a CTA takes 32 words (128
-// cells along x) by kTileRows positions along the pass axis at one position of the third axis,
-// stages its input with the halo of `layers` positions either side once, and reads the
-// candidates there (each input word is read from memory (kTileRows + 2 layers) / kTileRows
-// times instead of 2 layers + 1).  A tile whose input is all at the cap writes the cap.
-constexpr int kTileRows = 64;
-constexpr int kTileMaxLayers = 31;
-
-// two 16-bit lanes: max / min (native on this GPU, unlike the byte forms), and the byte word
-// of four distances split into two such pairs and joined back
-__device__ __forceinline__ unsigned max_u16x2(unsigned a, unsigned b) {
-    unsigned r;
-    asm("max.u16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
-    return r;
-}
-__device__ __forceinline__ unsigned min_u16x2(unsigned a, unsigned b) {
-    unsigned r;
-    asm("min.u16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
-    return r;
-}
-
-template <int AXIS>
-__global__ void __launch_bounds__(kDistThreads) ex_dist_tile_kernel(const ExArgs a, int max_other) {
-    extern __shared__ uint2 tile[];  // [kTileRows + 2 L][32]: cells {0, 1} and {2, 3} of a word
-    __shared__ int hist[kTileMaxLayers + 2];
-    const int f = blockIdx.z / max_other, o = blockIdx.z - f * max_other;
+// ---- 1. one layer's dilation over a tile of one field, and the list of the layer's cells
+__global__ void __launch_bounds__(kExThreads, 4) ex_dilate_kernel(const ExArgs a, int ztiles) {
+    __shared__ unsigned sm[kHZ][kHY][kHW];  // S over the tile and its halo
+    __shared__ unsigned zo[kTZ][kHY][kHW];  // OR over z
+    __shared__ unsigned yo[kTZ][kTY][kHW];  // then over y
+    __shared__ int wtot[kExThreads / 32];
+    __shared__ int base;
+    const int f = blockIdx.z / ztiles, zt = blockIdx.z - f * ztiles;
     if (f >= a.nf) return;
     const ExField& F = a.f[f];
-    const int words = F.pitch / 4;
-    const int extent = AXIS == 1 ? F.n1 : F.n2;
-    const int other = AXIS == 1 ? F.n2 : F.n1;
-    const int w0 = blockIdx.x * 32, m0 = blockIdx.y * kTileRows;
-    if (o >= other || w0 >= words || m0 >= extent) return;  // uniform over the CTA
-    const int L = a.layers;
-    const unsigned cap4 = splat4((unsigned)L + 1u);
-    const unsigned cap2 = ((unsigned)L + 1u) * 0x00010001u;
-    // word (w, m) of this field: AXIS 1 (y): m = j, o = k; AXIS 2 (z): m = k, o = j
-    auto at = [&](int w, int m) -> long long {
-        return AXIS == 1 ? ((long long)o * F.n1 + m) * words + w : ((long long)m * F.n1 + o) * words + w;
+    const int w0 = blockIdx.x * kTW, y0 = blockIdx.y * kTY, z0 = zt * kTZ;
+    if (w0 >= F.rw || y0 >= F.n1 || z0 >= F.n2) return;  // uniform over the CTA
+    const int tid = threadIdx.x;
+    const int pw = F.rw + 2, py = F.n1 + 2, pz = F.n2 + 2;
+    // padded coordinates of halo entry (hw, hy, hz): (w0 + hw, y0 + hy, z0 + hz); the entry's
+    // place in sm is its index e.  Every load of the thread is issued before the first store.
+    unsigned hv[kHaloLoads];
+#pragma unroll
+    for (int u = 0; u < kHaloLoads; ++u) {
+        const int e = tid + kExThreads * u;
+        const int hw = e % kHW, r = e / kHW, hy = r % kHY, hz = r / kHY;
+        const int wp = w0 + hw, yp = y0 + hy, zp = z0 + hz;
+        hv[u] = 0u;
+        if (e < kHaloWords && wp < pw && yp < py && zp < pz) hv[u] = F.s[pad_at(F, wp, yp, zp)];
+    }
+    unsigned* smf = &sm[0][0][0];
+    int any = 0;
+#pragma unroll
+    for (int u = 0; u < kHaloLoads; ++u) {
+        const int e = tid + kExThreads * u;
+        if (e < kHaloWords) {
+            smf[e] = hv[u];
+            any |= hv[u] != 0u;
+        }
+    }
+    // output m of the thread: word (w0 + tw, y0 + ty, z0 + tz) of the field
+    auto out_at = [&](int m, int& tw, int& ty, int& tz) -> bool {
+        const int e = tid + kExThreads * m;
+        tw = e % kTW;
+        ty = (e / kTW) % kTY;
+        tz = e / (kTW * kTY);
+        return w0 + tw < F.rw && y0 + ty < F.n1 && z0 + tz < F.n2;
     };
-    const unsigned* in = reinterpret_cast<const unsigned*>(AXIS == 1 ? F.da : F.db);
-    unsigned* out = reinterpret_cast<unsigned*>(AXIS == 1 ? F.db : F.da);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int rows = kTileRows + 2 * L;
-    int below = 0;
-    for (int r = warp; r < rows; r += kDistThreads / 32) {
-        const int m = m0 - L + r, w = w0 + lane;
-        const unsigned v = (m >= 0 && m < extent && w < words) ? in[at(w, m)] : cap4;
-        tile[r * 32 + lane] = make_uint2(__byte_perm(v, 0u, 0x4140), __byte_perm(v, 0u, 0x4342));
-        below |= v != cap4;
-    }
-    if (AXIS == 2)
-        for (int q = threadIdx.x; q <= L; q += blockDim.x) hist[q] = 0;
-    const bool any = __syncthreads_or(below) != 0;
-    const int w = w0 + lane;
-    for (int r = warp; r < kTileRows; r += kDistThreads / 32) {
-        const int m = m0 + r;
-        if (m >= extent || w >= words) continue;
-        unsigned best = cap4;
-        if (any) {
-            uint2 b = tile[(r + L) * 32 + lane];
-            for (int t = 1; t <= L; ++t) {
-                const unsigned tt = (unsigned)t * 0x00010001u;
-                const uint2 lo = tile[(r + L - t) * 32 + lane], hi = tile[(r + L + t) * 32 + lane];
-                b.x = min_u16x2(b.x, max_u16x2(min_u16x2(lo.x, hi.x), tt));
-                b.y = min_u16x2(b.y, max_u16x2(min_u16x2(lo.y, hi.y), tt));
-            }
-            b.x = min_u16x2(b.x, cap2);
-            b.y = min_u16x2(b.y, cap2);
-            best = __byte_perm(b.x, b.y, 0x6420);
-        }
-        out[at(w, m)] = best;
-        if (AXIS == 2 && any) {
+    // a tile with no set bit around it, or with every cell set, has no cell of this layer: S' = S
+    bool skip = !__syncthreads_or(any);
+    if (!skip) {
+        int full = 1;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const unsigned d = (best >> (8 * q)) & 0xffu;
-                if (w * 4 + q < F.n0 && d >= 1u && (int)d <= L) atomicAdd(&hist[d], 1);
-            }
+        for (int m = 0; m < kPerThread; ++m) {
+            int tw, ty, tz;
+            if (out_at(m, tw, ty, tz) && sm[tz + 1][ty + 1][tw + 1] != row_mask(F.n0, w0 + tw)) full = 0;
         }
+        skip = __syncthreads_and(full) != 0;
     }
-    if (AXIS == 2) {
-        __syncthreads();
-        for (int q = threadIdx.x; q <= L; q += blockDim.x)
-            if (q >= 1 && hist[q]) atomicAdd(&a.counts[f * 256 + q], hist[q]);
+    if (skip) {
+#pragma unroll
+        for (int m = 0; m < kPerThread; ++m) {
+            int tw, ty, tz;
+            if (out_at(m, tw, ty, tz))
+                F.s_next[pad_at(F, w0 + tw + 1, y0 + ty + 1, z0 + tz + 1)] = sm[tz + 1][ty + 1][tw + 1];
+        }
+        return;
     }
-}
-
-// ---- 2. list offsets per field and distance (one block)
-__global__ void ex_offsets_kernel(const ExArgs a) {
-    if (threadIdx.x != 0) return;
-    for (int f = 0; f < a.nf; ++f) {
+    for (int e = tid; e < kTZ * kHY * kHW; e += kExThreads) {
+        const int hw = e % kHW, r = e / kHW, hy = r % kHY, tz = r / kHY;
+        zo[tz][hy][hw] = sm[tz][hy][hw] | sm[tz + 1][hy][hw] | sm[tz + 2][hy][hw];
+    }
+    __syncthreads();
+    for (int e = tid; e < kTZ * kTY * kHW; e += kExThreads) {
+        const int hw = e % kHW, r = e / kHW, ty = r % kTY, tz = r / kTY;
+        yo[tz][ty][hw] = zo[tz][ty][hw] | zo[tz][ty + 1][hw] | zo[tz][ty + 2][hw];
+    }
+    __syncthreads();
+    // the layer's cells of output m: the dilation along x (a cell's left and right neighbours,
+    // across the word's edges), less S, inside the row
+    auto new_bits = [&](int tw, int ty, int tz) -> unsigned {
+        const unsigned c0 = yo[tz][ty][tw + 1], cm = yo[tz][ty][tw], cp = yo[tz][ty][tw + 2];
+        const unsigned dil = c0 | (c0 << 1) | (cm >> 31) | (c0 >> 1) | (cp << 31);
+        return dil & ~sm[tz + 1][ty + 1][tw + 1] & row_mask(F.n0, w0 + tw);
+    };
+    int cnt = 0;
+#pragma unroll
+    for (int m = 0; m < kPerThread; ++m) {
+        int tw, ty, tz;
+        if (!out_at(m, tw, ty, tz)) continue;
+        const unsigned nw = new_bits(tw, ty, tz);
+        F.s_next[pad_at(F, w0 + tw + 1, y0 + ty + 1, z0 + tz + 1)] = sm[tz + 1][ty + 1][tw + 1] | nw;
+        cnt += __popc(nw);
+    }
+    // the CTA's cells go to one range of the field's list: a scan of the threads' counts
+    const int lane = tid & 31, warp = tid >> 5;
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) wtot[warp] = incl;
+    __syncthreads();
+    if (tid == 0) {
         int run = 0;
-        for (int d = 1; d <= a.layers; ++d) {
-            a.offsets[f * 256 + d] = run;
-            a.cursors[f * 256 + d] = run;
-            run += a.counts[f * 256 + d];
+        for (int q = 0; q < kExThreads / 32; ++q) {
+            const int t = wtot[q];
+            wtot[q] = run;
+            run += t;
+        }
+        base = run ? atomicAdd(&a.counts[f], run) : 0;
+    }
+    __syncthreads();
+    int off = base + wtot[warp] + incl - cnt;
+    const long long ncell = (long long)F.n0 * F.n1 * F.n2;
+    (void)ncell;  // read by the index checks of the debug build
+#pragma unroll
+    for (int m = 0; m < kPerThread; ++m) {
+        int tw, ty, tz;
+        if (!out_at(m, tw, ty, tz)) continue;
+        unsigned bits = new_bits(tw, ty, tz);
+        const long long row0 = (long long)F.n0 * ((y0 + ty) + (long long)F.n1 * (z0 + tz)) + 32 * (w0 + tw);
+        while (bits) {
+            const int b = __ffs(bits) - 1;
+            bits &= bits - 1;
+            if (EL_IN(off, ncell, 20)) F.list[off] = (int)(row0 + b);
+            ++off;
         }
     }
 }
 
-// block-aggregated scatter of the cells of distance 1..layers into their distance's range: a
-// round takes kScatterWords words per thread; words with no cell in 1..layers (the valid region,
-// and the cells beyond reach) only cost their load
-constexpr int kScatterWords = 4;
-
-__global__ void __launch_bounds__(kDistThreads) ex_scatter_kernel(const ExArgs a) {
-    const ExField& F = a.f[blockIdx.y];
-    __shared__ int bcount[256], bbase[256];
-    const int L = a.layers;
-    const int words = F.pitch / 4;
-    const long long nw = (long long)words * F.n1 * F.n2;
-    const unsigned* dist = reinterpret_cast<const unsigned*>(F.da);
-    const long long per_round = (long long)blockDim.x * kScatterWords;
-    // the block's threads share `base`, so the barriers below are uniform within the block
-    for (long long base = (long long)blockIdx.x * per_round; base < nw; base += (long long)gridDim.x * per_round) {
-        for (int q = threadIdx.x; q <= L; q += blockDim.x) bcount[q] = 0;
-        __syncthreads();
-        unsigned wv[kScatterWords];
-        unsigned short rank[kScatterWords][4];
-#pragma unroll
-        for (int u = 0; u < kScatterWords; ++u) {
-            const long long q = base + threadIdx.x + (long long)u * blockDim.x;
-            wv[u] = 0u;  // distance 0 everywhere: nothing to list
-            if (q < nw) {
-                wv[u] = dist[q];
-                const int i0 = (int)(q % words) * 4;
-#pragma unroll
-                for (int b = 0; b < 4; ++b) {
-                    const int d = (int)((wv[u] >> (8 * b)) & 0xffu);
-                    rank[u][b] = 0;
-                    if (i0 + b < F.n0 && d >= 1 && d <= L) rank[u][b] = (unsigned short)atomicAdd(&bcount[d], 1);
-                }
-            }
-        }
-        __syncthreads();
-        for (int d = threadIdx.x; d <= L; d += blockDim.x)
-            if (d >= 1 && bcount[d]) bbase[d] = atomicAdd(&a.cursors[blockIdx.y * 256 + d], bcount[d]);
-        __syncthreads();
-#pragma unroll
-        for (int u = 0; u < kScatterWords; ++u) {
-            const long long q = base + threadIdx.x + (long long)u * blockDim.x;
-            if (q >= nw) continue;
-            const long long line = q / words;
-            const int i0 = (int)(q - line * words) * 4;
-            const long long cell0 = line * F.n0 + i0;  // (j, k) row start + i
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const int d = (int)((wv[u] >> (8 * b)) & 0xffu);
-                if (i0 + b < F.n0 && d >= 1 && d <= L &&
-                    EL_IN(bbase[d] + rank[u][b], (long long)F.n0 * F.n1 * F.n2, 20))
-                    F.list[bbase[d] + rank[u][b]] = (int)(cell0 + b);
-            }
-        }
-        __syncthreads();
-    }
-}
-
-// ---- 3. one layer: every cell of distance `dist` takes the mean of its neighbours of smaller
-// distance, summed in z, y, x order (extrapolation.cpp:24-33)
+// ---- 2. the layer's cells: the mean of the neighbours in S, summed in z, y, x order
+// (extrapolation.cpp:24-33)
 __device__ __forceinline__ float ex_add(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ double ex_add(double a, double b) { return __dadd_rn(a, b); }
 
 template <typename T>
-__global__ void __launch_bounds__(kDistThreads) ex_layer_kernel(const ExArgs a, int dist) {
+__global__ void __launch_bounds__(kExThreads) ex_average_kernel(const ExArgs a) {
     int total = 0;
     int start[kExMaxFields + 1];
     for (int f = 0; f < a.nf; ++f) {
         start[f] = total;
-        total += a.counts[f * 256 + dist];
+        total += a.counts[f];
     }
     start[a.nf] = total;
+    // the next layer's counts start from zero (its dilation runs after this kernel)
+    if (blockIdx.x == 0 && threadIdx.x < kExMaxFields) a.counts_next[threadIdx.x] = 0;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
         int f = 0;
         while (f + 1 < a.nf && q >= start[f + 1]) ++f;
         const ExField& F = a.f[f];
-        const int li = a.offsets[f * 256 + dist] + (q - start[f]);
-        if (!EL_IN(li, (long long)F.n0 * F.n1 * F.n2, 21)) continue;
+        const long long ncell = (long long)F.n0 * F.n1 * F.n2;
+        (void)ncell;
+        const int li = q - start[f];
+        if (!EL_IN(li, ncell, 21)) continue;
         const int c = F.list[li];
-        if (!EL_IN(c, (long long)F.n0 * F.n1 * F.n2, 22)) continue;
-        const int i = c % F.n0, r = c / F.n0;
-        const int j = r % F.n1, k = r / F.n1;
+        if (!EL_IN(c, ncell, 22)) continue;
+        const int x = c % F.n0, r = c / F.n0;
+        const int y = r % F.n1, z = r / F.n1;
+        // cells x - 1, x, x + 1 of a padded row: bits 0..2 of the window from the word holding
+        // cell x - 1 (padded word (x - 1 + 32) / 32)
+        const int lo = (x + 31) >> 5, sh = (x + 31) & 31;
         T* g = static_cast<T*>(F.g);
         T sum = T(0);
         int count = 0;
 #pragma unroll
-        for (int dk = -1; dk <= 1; ++dk) {
-            const int z = k + dk;
-            if (z < 0 || z >= F.n2) continue;
+        for (int dz = -1; dz <= 1; ++dz) {
 #pragma unroll
-            for (int dj = -1; dj <= 1; ++dj) {
-                const int y = j + dj;
-                if (y < 0 || y >= F.n1) continue;
-                const uint8_t* drow = F.da + ((long long)z * F.n1 + y) * F.pitch;
-                const T* grow = g + ((long long)z * F.n1 + y) * F.n0;
+            for (int dy = -1; dy <= 1; ++dy) {
+                const unsigned* row = F.s + pad_at(F, 0, y + 1 + dy, z + 1 + dz);
+                unsigned win = row[lo] >> sh;
+                if (sh > 29) win |= row[lo + 1] << (32 - sh);  // the cells straddle two words
+                if (!(win & 7u)) continue;
+                const T* grow = g + (long long)F.n0 * ((y + dy) + (long long)F.n1 * (z + dz));
 #pragma unroll
-                for (int di = -1; di <= 1; ++di) {
-                    const int x = i + di;
-                    if (x < 0 || x >= F.n0) continue;
-                    if ((int)drow[x] < dist) {
-                        sum = ex_add(sum, grow[x]);
+                for (int dx = -1; dx <= 1; ++dx) {
+                    if (win & (1u << (dx + 1))) {
+                        sum = ex_add(sum, grow[x + dx]);
                         ++count;
                     }
                 }
             }
         }
-        g[c] = sum / (T)count;  // count >= 1: a neighbour has distance dist - 1
+        g[c] = sum / (T)count;  // count >= 1: the cell has a neighbour in S
         if (F.write_back) F.valid[c] = 1;
     }
 }
 
 }  // namespace
 
-// Scratch of one field slot: two distance buffers with padded rows and the distance lists.
+// bytes of one padded bitmask of an n0 x n1 x n2 field
+size_t extrapolation_bits_bytes(int n0, int n1, int n2) {
+    return (size_t)((n0 + 31) / 32 + 2) * (size_t)(n1 + 2) * (size_t)(n2 + 2) * sizeof(unsigned);
+}
+
+// Scratch of one field slot: two padded bitmasks and the list of a layer's cells.
 static int ensure_ex_slot(el_ctx* ctx, int slot) {
-    if (ctx->ex_da[slot]) return EL_OK;
-    ctx->ex_da[slot] = (uint8_t*)ctx_alloc(ctx, ctx->ex_dist_bytes);
-    ctx->ex_db[slot] = (uint8_t*)ctx_alloc(ctx, ctx->ex_dist_bytes);
+    if (ctx->ex_bits[slot][0]) return EL_OK;
+    ctx->ex_bits[slot][0] = (unsigned*)ctx_alloc(ctx, ctx->ex_bits_bytes);
+    ctx->ex_bits[slot][1] = (unsigned*)ctx_alloc(ctx, ctx->ex_bits_bytes);
     ctx->ex_list[slot] = (int*)ctx_alloc(ctx, ctx->ex_list_bytes);
-    if (!ctx->ex_da[slot] || !ctx->ex_db[slot] || !ctx->ex_list[slot])
+    if (!ctx->ex_bits[slot][0] || !ctx->ex_bits[slot][1] || !ctx->ex_list[slot])
         return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "extrapolation scratch");
     return EL_OK;
 }
@@ -378,7 +329,7 @@ static int ensure_ex_slot(el_ctx* ctx, int slot) {
 // Allocates the scratch of `nfields` slots (outside any stream capture).
 int ensure_extrapolation(el_ctx* ctx, int nfields) {
     if (!ctx->ex_counts) {
-        ctx->ex_counts = (int*)ctx_alloc(ctx, 3 * kExMaxFields * 256 * sizeof(int));
+        ctx->ex_counts = (int*)ctx_alloc(ctx, 2 * kExMaxFields * sizeof(int));
         if (!ctx->ex_counts) return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "extrapolation counts");
     }
     for (int q = 0; q < nfields && q < kExMaxFields; ++q) {
@@ -396,68 +347,54 @@ int launch_extrapolate_fields(el_ctx* ctx, int nf, const int* fields, uint8_t* c
     if (nf < 1 || layers < 1) return 0;
     ExArgs a{};
     a.nf = nf;
-    a.layers = std::min(layers, 254);  // distances are bytes; layers + 1 is the cap
-    a.counts = ctx->ex_counts;
-    a.offsets = ctx->ex_counts + kExMaxFields * 256;
-    a.cursors = ctx->ex_counts + 2 * kExMaxFields * 256;
-    long long max_words = 0, max_rows = 0;
+    int max_rw = 0, max_n1 = 0, max_n2 = 0;
+    long long max_cells = 0, max_padded = 0;
     for (int q = 0; q < nf; ++q) {
         ExField& F = a.f[q];
         int n0, n1, n2;
         field_dims(ctx, fields[q], n0, n1, n2);
         F.g = ctx->field[fields[q]];
         F.valid = valid[q];
-        F.da = ctx->ex_da[q];
-        F.db = ctx->ex_db[q];
         F.list = ctx->ex_list[q];
         F.n0 = n0;
         F.n1 = n1;
         F.n2 = n2;
-        F.pitch = (n0 + 15) & ~15;
+        F.rw = (n0 + 31) / 32;
         F.write_back = write_back[q] ? 1 : 0;
-        max_words = std::max(max_words, (long long)(F.pitch / 4) * n1 * n2);
-        max_rows = std::max(max_rows, (long long)n1 * n2);
+        max_rw = std::max(max_rw, F.rw);
+        max_n1 = std::max(max_n1, n1);
+        max_n2 = std::max(max_n2, n2);
+        max_cells = std::max(max_cells, (long long)n0 * n1 * n2);
+        max_padded = std::max(max_padded, (long long)(F.rw + 2) * (n1 + 2) * (n2 + 2));
     }
-    int n = 0;
-    cudaMemsetAsync(ctx->ex_counts, 0, kExMaxFields * 256 * sizeof(int), ctx->stream);
-    const int wide = ctx->num_sms * 8;  // resident 256-thread blocks of the streaming passes
-    if (a.layers <= 31) {
-        const dim3 grid((unsigned)((max_rows + kDistThreads / 32 - 1) / (kDistThreads / 32)), nf);
-        ex_dist_x_kernel<<<grid, kDistThreads, 0, ctx->stream>>>(a);
-    } else {
-        ex_dist_x_scan_kernel<<<dim3(wide, nf), kDistThreads, 0, ctx->stream>>>(a);
-    }
-    const unsigned pass_blocks = (unsigned)std::min<long long>(wide, (max_words + kDistThreads - 1) / kDistThreads);
-    if (a.layers <= kTileMaxLayers) {
-        int max_words_row = 0, max_n1 = 0, max_n2 = 0;
+    auto set_layer = [&](int k) {  // layer k reads buffer (k - 1) & 1 and writes buffer k & 1
         for (int q = 0; q < nf; ++q) {
-            max_words_row = std::max(max_words_row, a.f[q].pitch / 4);
-            max_n1 = std::max(max_n1, a.f[q].n1);
-            max_n2 = std::max(max_n2, a.f[q].n2);
+            a.f[q].s = ctx->ex_bits[q][(k - 1) & 1];
+            a.f[q].s_next = ctx->ex_bits[q][k & 1];
         }
-        const int smem = (kTileRows + 2 * a.layers) * 32 * (int)sizeof(uint2);
-        const unsigned gx = (unsigned)((max_words_row + 31) / 32);
-        // y: tiles along j at each k; z: tiles along k at each j
-        ex_dist_tile_kernel<1><<<dim3(gx, (max_n1 + kTileRows - 1) / kTileRows, (unsigned)(nf * max_n2)),
-                                 kDistThreads, smem, ctx->stream>>>(a, max_n2);
-        ex_dist_tile_kernel<2><<<dim3(gx, (max_n2 + kTileRows - 1) / kTileRows, (unsigned)(nf * max_n1)),
-                                 kDistThreads, smem, ctx->stream>>>(a, max_n1);
-    } else {
-        ex_dist_pass_kernel<1><<<dim3(pass_blocks, nf), kDistThreads, 0, ctx->stream>>>(a);
-        ex_dist_pass_kernel<2><<<dim3(pass_blocks, nf), kDistThreads, 0, ctx->stream>>>(a);
-    }
-    ex_offsets_kernel<<<1, 32, 0, ctx->stream>>>(a);
-    const unsigned scatter_blocks =
-        (unsigned)std::min<long long>(wide, (max_words + kDistThreads * kScatterWords - 1) / (kDistThreads * kScatterWords));
-    ex_scatter_kernel<<<dim3(scatter_blocks, nf), kDistThreads, 0, ctx->stream>>>(a);
-    n += 5;
-    const int layer_blocks = ctx->num_sms * std::max(1, ctx->extrap_per_sm);
-    for (int d = 1; d <= a.layers; ++d) {
+        a.counts = ctx->ex_counts + (k & 1) * kExMaxFields;
+        a.counts_next = ctx->ex_counts + ((k + 1) & 1) * kExMaxFields;
+    };
+    set_layer(1);
+    cudaMemsetAsync(a.counts, 0, kExMaxFields * sizeof(int), ctx->stream);
+    const int wide = ctx->num_sms * 8;  // resident 256-thread blocks of the streaming passes
+    ex_flat_kernel<<<dim3((unsigned)std::min<long long>(wide, (max_cells / 32 + kExThreads) / kExThreads), nf),
+                     kExThreads, 0, ctx->stream>>>(a);
+    ex_rows_kernel<<<dim3((unsigned)std::min<long long>(wide, (max_padded + kExThreads - 1) / kExThreads), nf),
+                     kExThreads, 0, ctx->stream>>>(a);
+    int n = 2;
+    const int ztiles = (max_n2 + kTZ - 1) / kTZ;
+    const dim3 dgrid((unsigned)((max_rw + kTW - 1) / kTW), (unsigned)((max_n1 + kTY - 1) / kTY),
+                     (unsigned)(nf * ztiles));
+    const int avg_blocks = ctx->num_sms * std::max(1, ctx->extrap_per_sm);
+    for (int k = 1; k <= layers; ++k) {
+        set_layer(k);
+        ex_dilate_kernel<<<dgrid, kExThreads, 0, ctx->stream>>>(a, ztiles);
         if (ctx->dtype == EL_F64)
-            ex_layer_kernel<double><<<layer_blocks, kDistThreads, 0, ctx->stream>>>(a, d);
+            ex_average_kernel<double><<<avg_blocks, kExThreads, 0, ctx->stream>>>(a);
         else
-            ex_layer_kernel<float><<<layer_blocks, kDistThreads, 0, ctx->stream>>>(a, d);
-        ++n;
+            ex_average_kernel<float><<<avg_blocks, kExThreads, 0, ctx->stream>>>(a);
+        n += 2;
     }
     return n;
 }

@@ -217,13 +217,12 @@ struct el_ctx {
 
     // advection / extrapolation ping-pong buffers (same shapes as phi, u, v, w)
     void* tmp[4] = {};
-    // extrapolation scratch per field slot (el_extrap.cu): two distance buffers with rows padded
-    // to 16 bytes and the cells of each distance; counts / offsets / cursors per slot and distance
-    uint8_t* ex_da[4] = {};
-    uint8_t* ex_db[4] = {};
+    // extrapolation scratch per field slot (el_extrap.cu): two padded bitmasks of the valid
+    // cells and the list of a layer's cells; cells per slot of the current and the next layer
+    unsigned* ex_bits[4][2] = {};
     int* ex_list[4] = {};
     int* ex_counts = nullptr;
-    size_t ex_dist_bytes = 0, ex_list_bytes = 0;
+    size_t ex_bits_bytes = 0, ex_list_bytes = 0;
 
     // projection
     uint8_t* flags = nullptr;
@@ -347,6 +346,7 @@ void* ctx_alloc(el_ctx* ctx, size_t bytes);  // zero-filled, owned by the contex
 int ensure_projection(el_ctx* ctx);
 int ensure_solver(el_ctx* ctx, int solver);
 void field_dims(const el_ctx* ctx, int field, int& n0, int& n1, int& n2);
+size_t extrapolation_bits_bytes(int n0, int n1, int n2);
 // extrapolation (el_extrap.cu): scratch for `nfields` slots (outside capture), and up to four
 // fields extrapolated together; returns the kernels launched
 int ensure_extrapolation(el_ctx* ctx, int nfields);

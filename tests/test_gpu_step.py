@@ -121,11 +121,13 @@ def test_mixed_step_fp32_matches_oracle_to_solve_tolerance(el, orc):
 
 @pytest.mark.parametrize("shape,density,layers", [((23, 17, 30), 0.02, 10), ((40, 9, 12), 0.3, 3),
                                                   ((12, 33, 20), 0.0005, 40), ((16, 16, 16), 0.9, 1),
-                                                  ((18, 14, 11), 0.05, 0)])
+                                                  ((18, 14, 11), 0.05, 0), ((300, 37, 19), 0.002, 7),
+                                                  ((33, 70, 17), 0.01, 6), ((9, 6, 5), 0.01, 260)])
 def test_extrapolation_random_masks_bitexact(el, orc, shape, density, layers):
-    """Extrapolation by distance order against the oracle's layer loop on random masks and
-    non-cubic grids: few valid cells (long reach), dense masks, more than 31 layers (the row
-    scan of the distance pass), no layers at all."""
+    """The bitmask layer loop against the oracle's layer loop on random masks and non-cubic
+    grids: few valid cells (long reach), dense masks, rows of more than 256 cells and more than
+    32 rows (several dilation tiles along each axis, rows of 301 cells ending inside a word),
+    more layers than the grid is wide, no layers at all."""
     ni, nj, nk = shape
     rng = np.random.default_rng(ni * 1000 + layers)
     for dtype in DTYPES:
