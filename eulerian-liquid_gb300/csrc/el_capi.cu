@@ -199,6 +199,7 @@ EL_API int el_ctx_create(int ni, int nj, int nk, double dx, int dtype, int devic
         field_dims(ctx, f, n0, n1, n2);
         ctx->ex_bits_bytes = std::max(ctx->ex_bits_bytes, extrapolation_bits_bytes(n0, n1, n2));
         ctx->ex_list_bytes = std::max(ctx->ex_list_bytes, (size_t)n0 * n1 * n2 * sizeof(int));
+        ctx->ex_tile_count = std::max(ctx->ex_tile_count, extrapolation_tiles(n0, n1, n2));
     }
     ctx->dscal = (Scalars*)ctx_alloc(ctx, 4 * sizeof(Scalars));
     Geom g = stencil_geom(ni, nj, nk, ctx->num_sms);

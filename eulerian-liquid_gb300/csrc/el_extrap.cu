@@ -36,14 +36,22 @@ constexpr int kHaloWords = kHW * kHY * kHZ;
 constexpr int kHaloLoads = (kHaloWords + kExThreads - 1) / kExThreads;
 static_assert(kTileWords % kExThreads == 0, "whole outputs per thread");
 
+// what S holds on a dilation tile
+enum : uint8_t { kTileZero = 0, kTileMixed = 1, kTileFull = 2 };
+
 struct ExField {
-    void* g;          // the field (float or double), i-fastest n0 x n1 x n2
-    uint8_t* valid;   // its valid mask (written for the layers' cells when write_back)
-    unsigned* s;      // the valid set before the layer: padded bitmask
-    unsigned* s_next; // and after it
-    int* list;        // the layer's cells (linear indices)
+    void* g;            // the field (float or double), i-fastest n0 x n1 x n2
+    uint8_t* valid;     // its valid mask (written for the layers' cells when write_back)
+    unsigned* s;        // the valid set before the layer: padded bitmask
+    unsigned* s_next;   // and after it
+    int* list;          // the layer's cells (linear indices)
+    const uint8_t* st;  // per dilation tile: S before the layer (kTile*)
+    uint8_t* st_next;   // and after it
+    const uint8_t* ch;  // per dilation tile: the layer before changed S there
+    uint8_t* ch_next;   // this layer does
     int n0, n1, n2;
-    int rw;           // words per row, ceil(n0 / 32); a padded row holds rw + 2
+    int rw;             // words per row, ceil(n0 / 32); a padded row holds rw + 2
+    int ntx, nty, ntz;  // dilation tiles along x, y, z
     int write_back;
 };
 
@@ -137,6 +145,42 @@ __global__ void __launch_bounds__(kExThreads, 4) ex_dilate_kernel(const ExArgs a
     const int w0 = blockIdx.x * kTW, y0 = blockIdx.y * kTY, z0 = zt * kTZ;
     if (w0 >= F.rw || y0 >= F.n1 || z0 >= F.n2) return;  // uniform over the CTA
     const int tid = threadIdx.x;
+    const int tile = blockIdx.x + F.ntx * (blockIdx.y + F.nty * zt);
+    // output m of the thread: word (w0 + tw, y0 + ty, z0 + tz) of the field
+    auto out_at = [&](int m, int& tw, int& ty, int& tz) -> bool {
+        const int e = tid + kExThreads * m;
+        tw = e % kTW;
+        ty = (e / kTW) % kTY;
+        tz = e / (kTW * kTY);
+        return w0 + tw < F.rw && y0 + ty < F.n1 && z0 + tz < F.n2;
+    };
+    // a tile that S fills, or that S leaves empty with its neighbour tiles, has no cell of this
+    // layer and is not staged: S' = S there, and the buffer S' goes to holds S of two layers
+    // back, so its words are copied only if the layer before changed them
+    const uint8_t own = F.st[tile];
+    int busy = 0;
+    if (tid < 27) {
+        const int nx = (int)blockIdx.x + tid % 3 - 1, ny = (int)blockIdx.y + (tid / 3) % 3 - 1, nz = zt + tid / 9 - 1;
+        if (nx >= 0 && nx < F.ntx && ny >= 0 && ny < F.nty && nz >= 0 && nz < F.ntz)
+            busy = F.st[nx + F.ntx * (ny + F.nty * nz)] != kTileZero;
+    }
+    if (own == kTileFull || !__syncthreads_or(busy)) {
+        if (F.ch[tile]) {
+#pragma unroll
+            for (int m = 0; m < kPerThread; ++m) {
+                int tw, ty, tz;
+                if (out_at(m, tw, ty, tz)) {
+                    const long long q = pad_at(F, w0 + tw + 1, y0 + ty + 1, z0 + tz + 1);
+                    F.s_next[q] = F.s[q];
+                }
+            }
+        }
+        if (tid == 0) {
+            F.st_next[tile] = own;
+            F.ch_next[tile] = 0;
+        }
+        return;
+    }
     const int pw = F.rw + 2, py = F.n1 + 2, pz = F.n2 + 2;
     // padded coordinates of halo entry (hw, hy, hz): (w0 + hw, y0 + hy, z0 + hz); the entry's
     // place in sm is its index e.  Every load of the thread is issued before the first store.
@@ -159,31 +203,30 @@ __global__ void __launch_bounds__(kExThreads, 4) ex_dilate_kernel(const ExArgs a
             any |= hv[u] != 0u;
         }
     }
-    // output m of the thread: word (w0 + tw, y0 + ty, z0 + tz) of the field
-    auto out_at = [&](int m, int& tw, int& ty, int& tz) -> bool {
-        const int e = tid + kExThreads * m;
-        tw = e % kTW;
-        ty = (e / kTW) % kTY;
-        tz = e / (kTW * kTY);
-        return w0 + tw < F.rw && y0 + ty < F.n1 && z0 + tz < F.n2;
-    };
     // a tile with no set bit around it, or with every cell set, has no cell of this layer: S' = S
     bool skip = !__syncthreads_or(any);
-    if (!skip) {
-        int full = 1;
+    int full = 1;
 #pragma unroll
-        for (int m = 0; m < kPerThread; ++m) {
-            int tw, ty, tz;
-            if (out_at(m, tw, ty, tz) && sm[tz + 1][ty + 1][tw + 1] != row_mask(F.n0, w0 + tw)) full = 0;
-        }
-        skip = __syncthreads_and(full) != 0;
+    for (int m = 0; m < kPerThread; ++m) {
+        int tw, ty, tz;
+        if (out_at(m, tw, ty, tz) && sm[tz + 1][ty + 1][tw + 1] != row_mask(F.n0, w0 + tw)) full = 0;
     }
-    if (skip) {
+    const bool tile_full = __syncthreads_and(full) != 0;
+    if (skip || tile_full) {
+        int zero = 1;
 #pragma unroll
         for (int m = 0; m < kPerThread; ++m) {
             int tw, ty, tz;
-            if (out_at(m, tw, ty, tz))
-                F.s_next[pad_at(F, w0 + tw + 1, y0 + ty + 1, z0 + tz + 1)] = sm[tz + 1][ty + 1][tw + 1];
+            if (out_at(m, tw, ty, tz)) {
+                const unsigned v = sm[tz + 1][ty + 1][tw + 1];
+                F.s_next[pad_at(F, w0 + tw + 1, y0 + ty + 1, z0 + tz + 1)] = v;
+                zero &= v == 0u;
+            }
+        }
+        const bool tile_zero = __syncthreads_and(zero) != 0;
+        if (tid == 0) {
+            F.st_next[tile] = tile_full ? kTileFull : (tile_zero ? kTileZero : kTileMixed);
+            F.ch_next[tile] = 0;
         }
         return;
     }
@@ -204,14 +247,18 @@ __global__ void __launch_bounds__(kExThreads, 4) ex_dilate_kernel(const ExArgs a
         const unsigned dil = c0 | (c0 << 1) | (cm >> 31) | (c0 >> 1) | (cp << 31);
         return dil & ~sm[tz + 1][ty + 1][tw + 1] & row_mask(F.n0, w0 + tw);
     };
-    int cnt = 0;
+    int cnt = 0, zero = 1;
+    full = 1;
 #pragma unroll
     for (int m = 0; m < kPerThread; ++m) {
         int tw, ty, tz;
         if (!out_at(m, tw, ty, tz)) continue;
         const unsigned nw = new_bits(tw, ty, tz);
-        F.s_next[pad_at(F, w0 + tw + 1, y0 + ty + 1, z0 + tz + 1)] = sm[tz + 1][ty + 1][tw + 1] | nw;
+        const unsigned sn = sm[tz + 1][ty + 1][tw + 1] | nw;
+        F.s_next[pad_at(F, w0 + tw + 1, y0 + ty + 1, z0 + tz + 1)] = sn;
         cnt += __popc(nw);
+        zero &= sn == 0u;
+        full &= sn == row_mask(F.n0, w0 + tw);
     }
     // the CTA's cells go to one range of the field's list: a scan of the threads' counts
     const int lane = tid & 31, warp = tid >> 5;
@@ -222,7 +269,8 @@ __global__ void __launch_bounds__(kExThreads, 4) ex_dilate_kernel(const ExArgs a
         if (lane >= o) incl += t;
     }
     if (lane == 31) wtot[warp] = incl;
-    __syncthreads();
+    const bool next_zero = __syncthreads_and(zero) != 0;
+    const bool next_full = __syncthreads_and(full) != 0;
     if (tid == 0) {
         int run = 0;
         for (int q = 0; q < kExThreads / 32; ++q) {
@@ -231,6 +279,8 @@ __global__ void __launch_bounds__(kExThreads, 4) ex_dilate_kernel(const ExArgs a
             run += t;
         }
         base = run ? atomicAdd(&a.counts[f], run) : 0;
+        F.st_next[tile] = next_full ? kTileFull : (next_zero ? kTileZero : kTileMixed);
+        F.ch_next[tile] = run ? 1 : 0;
     }
     __syncthreads();
     int off = base + wtot[warp] + incl - cnt;
@@ -315,13 +365,21 @@ size_t extrapolation_bits_bytes(int n0, int n1, int n2) {
     return (size_t)((n0 + 31) / 32 + 2) * (size_t)(n1 + 2) * (size_t)(n2 + 2) * sizeof(unsigned);
 }
 
-// Scratch of one field slot: two padded bitmasks and the list of a layer's cells.
+// dilation tiles over an n0 x n1 x n2 field
+size_t extrapolation_tiles(int n0, int n1, int n2) {
+    return (size_t)(((n0 + 31) / 32 + kTW - 1) / kTW) * (size_t)((n1 + kTY - 1) / kTY) *
+           (size_t)((n2 + kTZ - 1) / kTZ);
+}
+
+// Scratch of one field slot: two padded bitmasks, the list of a layer's cells and four arrays
+// of tile states (S on each tile after an even / odd layer, and whether that layer changed it).
 static int ensure_ex_slot(el_ctx* ctx, int slot) {
     if (ctx->ex_bits[slot][0]) return EL_OK;
     ctx->ex_bits[slot][0] = (unsigned*)ctx_alloc(ctx, ctx->ex_bits_bytes);
     ctx->ex_bits[slot][1] = (unsigned*)ctx_alloc(ctx, ctx->ex_bits_bytes);
     ctx->ex_list[slot] = (int*)ctx_alloc(ctx, ctx->ex_list_bytes);
-    if (!ctx->ex_bits[slot][0] || !ctx->ex_bits[slot][1] || !ctx->ex_list[slot])
+    ctx->ex_tiles[slot] = (uint8_t*)ctx_alloc(ctx, 4 * ctx->ex_tile_count);
+    if (!ctx->ex_bits[slot][0] || !ctx->ex_bits[slot][1] || !ctx->ex_list[slot] || !ctx->ex_tiles[slot])
         return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "extrapolation scratch");
     return EL_OK;
 }
@@ -360,7 +418,13 @@ int launch_extrapolate_fields(el_ctx* ctx, int nf, const int* fields, uint8_t* c
         F.n1 = n1;
         F.n2 = n2;
         F.rw = (n0 + 31) / 32;
+        F.ntx = (F.rw + kTW - 1) / kTW;
+        F.nty = (n1 + kTY - 1) / kTY;
+        F.ntz = (n2 + kTZ - 1) / kTZ;
         F.write_back = write_back[q] ? 1 : 0;
+        // the tile states of S_0: unknown (mixed) and changed, so that the first layer stages
+        // every tile
+        cudaMemsetAsync(ctx->ex_tiles[q], 1, 4 * ctx->ex_tile_count, ctx->stream);
         max_rw = std::max(max_rw, F.rw);
         max_n1 = std::max(max_n1, n1);
         max_n2 = std::max(max_n2, n2);
@@ -368,9 +432,16 @@ int launch_extrapolate_fields(el_ctx* ctx, int nf, const int* fields, uint8_t* c
         max_padded = std::max(max_padded, (long long)(F.rw + 2) * (n1 + 2) * (n2 + 2));
     }
     auto set_layer = [&](int k) {  // layer k reads buffer (k - 1) & 1 and writes buffer k & 1
+        const size_t nt = ctx->ex_tile_count;
         for (int q = 0; q < nf; ++q) {
-            a.f[q].s = ctx->ex_bits[q][(k - 1) & 1];
-            a.f[q].s_next = ctx->ex_bits[q][k & 1];
+            ExField& F = a.f[q];
+            const int r = (k - 1) & 1, w = k & 1;
+            F.s = ctx->ex_bits[q][r];
+            F.s_next = ctx->ex_bits[q][w];
+            F.st = ctx->ex_tiles[q] + r * nt;
+            F.st_next = ctx->ex_tiles[q] + w * nt;
+            F.ch = ctx->ex_tiles[q] + (2 + r) * nt;
+            F.ch_next = ctx->ex_tiles[q] + (2 + w) * nt;
         }
         a.counts = ctx->ex_counts + (k & 1) * kExMaxFields;
         a.counts_next = ctx->ex_counts + ((k + 1) & 1) * kExMaxFields;

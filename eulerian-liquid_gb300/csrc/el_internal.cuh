@@ -221,8 +221,9 @@ struct el_ctx {
     // cells and the list of a layer's cells; cells per slot of the current and the next layer
     unsigned* ex_bits[4][2] = {};
     int* ex_list[4] = {};
+    uint8_t* ex_tiles[4] = {};  // the dilation's tile states
     int* ex_counts = nullptr;
-    size_t ex_bits_bytes = 0, ex_list_bytes = 0;
+    size_t ex_bits_bytes = 0, ex_list_bytes = 0, ex_tile_count = 0;
 
     // projection
     uint8_t* flags = nullptr;
@@ -347,6 +348,7 @@ int ensure_projection(el_ctx* ctx);
 int ensure_solver(el_ctx* ctx, int solver);
 void field_dims(const el_ctx* ctx, int field, int& n0, int& n1, int& n2);
 size_t extrapolation_bits_bytes(int n0, int n1, int n2);
+size_t extrapolation_tiles(int n0, int n1, int n2);
 // extrapolation (el_extrap.cu): scratch for `nfields` slots (outside capture), and up to four
 // fields extrapolated together; returns the kernels launched
 int ensure_extrapolation(el_ctx* ctx, int nfields);
