@@ -23,8 +23,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 # (seg_blocks_per_sm, stencil_blocks_per_sm, extrapolate_blocks_per_sm, advect_rows, advect_tiled,
 #  solver_tiles, coarse_fused, dependent_launch)
-DEFAULT = (6, 8, 12, 4, 1, 1, 0, 1)
-RANGES = ((1, 2, 3, 4, 6, 8), (2, 4, 8, 16), (4, 8, 12, 16), (2, 4, 8), (1, 0), (1, 0), (0, 1), (1, 0))
+DEFAULT = (8, 16, 12, 4, 1, 1, 0, 1)
+RANGES = ((1, 2, 3, 4, 6, 8), (2, 4, 8, 16), (4, 8, 12, 16), (2, 4, 8), (1, 0), (1, 0), (0, 1, 2), (1, 0))
 STATE_FIELDS = ("phi", "u", "v", "w", "valid_u", "valid_v", "valid_w")
 
 

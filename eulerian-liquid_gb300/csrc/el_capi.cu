@@ -273,7 +273,7 @@ EL_API int el_ctx_set_tuning(el_ctx* ctx, const el_tuning* t) {
         t->stencil_blocks_per_sm > 16 || t->extrapolate_blocks_per_sm < 1 || t->extrapolate_blocks_per_sm > 16 ||
         (t->advect_rows != 1 && t->advect_rows != 2 && t->advect_rows != 4 && t->advect_rows != 8) ||
         t->advect_tiled < 0 || t->advect_tiled > 2 || (t->solver_tiles != 0 && t->solver_tiles != 1) ||
-        (t->coarse_fused != 0 && t->coarse_fused != 1) || (t->dependent_launch != 0 && t->dependent_launch != 1))
+        t->coarse_fused < 0 || t->coarse_fused > 2 || (t->dependent_launch != 0 && t->dependent_launch != 1))
         return set_error(ctx, EL_ERR_INVALID_ARGUMENT, "tuning out of range");
     // the reduction partials are sized for 16 stencil blocks per SM (el_ctx_create)
     ctx->seg_per_sm = t->seg_blocks_per_sm;
@@ -920,7 +920,7 @@ EL_API int el_solve_pressure_noalloc(const el_grid* g, const float* phi, float* 
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return EL_ERR_CUDA;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return EL_ERR_CUDA;
     const Geom geom = stencil_geom(g->ni, g->nj, g->nk, sms);
-    const long long partials_needed = (long long)std::max(geom.blocks(), sms * 8) * 2 + 64;
+    const long long partials_needed = (long long)std::max(geom.blocks(), sms * 16) * 2 + 64;
     if (partials_needed > kNoAllocPartials) return EL_ERR_TOO_LARGE;
 
     // once per device, with that device current: the scratch array's device address

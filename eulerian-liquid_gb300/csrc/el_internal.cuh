@@ -201,7 +201,7 @@ struct el_ctx {
     // launch-shape tuning (el_ctx_set_tuning): resident blocks per SM of the segment kernels,
     // of the grid-wide stencil / element-wise kernels and of the extrapolation, and the rows of
     // the advection tile (32 x rows cells per block)
-    int seg_per_sm = 6, stencil_per_sm = 8, extrap_per_sm = 12, advect_rows = 4;
+    int seg_per_sm = 8, stencil_per_sm = 16, extrap_per_sm = 12, advect_rows = 4;
     int advect_tiled = 1;  // advection through the staged-tile kernels (2: boxes by plain loads only)
     int solver_tiles = 1;  // the mixed solver's finest level on the tile kernels (where supported)
     int coarse_fused = 0;  // the FP32 V-cycle's coarse levels in one cooperative launch (where supported)

@@ -1494,7 +1494,12 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
     // levels [coop_from, pre_end) and the bottom in one cooperative launch (the FP32 hierarchy)
     int coop_from = -1;
     if constexpr (kBottomType)
-        if (fused_bottom && coarse_fused_usable(ctx, L)) coop_from = std::max(from, 1);
+        if (fused_bottom && coarse_fused_usable(ctx, L)) {
+            // coarse_fused = 1: every level below the finest; 2: from the second one on (the
+            // first, the largest, keeps its launches)
+            const int c = std::max(from, ctx->coarse_fused);
+            if (c < pre_end) coop_from = c;
+        }
     const int down_end = coop_from >= 0 ? coop_from : pre_end;  // levels by per-level launches
     for (int l = from; l < down_end; ++l) {
         MGLevel<V>& F = mg[l];

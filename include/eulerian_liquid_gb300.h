@@ -133,8 +133,8 @@ int64_t el_ctx_kernel_launches(const el_ctx* ctx);
  * depend on them beyond the summation order of the device reductions.  A batch takes the
  * shapes its scenes have when it is created. */
 typedef struct el_tuning {
-    int seg_blocks_per_sm;       /* solver kernels over active row segments, 1..8 (default 6)   */
-    int stencil_blocks_per_sm;   /* matrix build, masks, element-wise kernels, 1..16 (default 8) */
+    int seg_blocks_per_sm;       /* solver kernels over active row segments, 1..8 (default 8)   */
+    int stencil_blocks_per_sm;   /* matrix build, masks, element-wise kernels, 1..16 (default 16)*/
     int extrapolate_blocks_per_sm; /* extrapolation tiles in flight per SM, 1..16 (default 12)  */
     int advect_rows;             /* per-sample advection: 32 x rows cells per block, 1, 2, 4 or 8 */
     int advect_tiled;            /* 1 (default): advection kernels that stage the velocity of a
@@ -148,7 +148,8 @@ typedef struct el_tuning {
                                     row-segment kernels everywhere                              */
     int coarse_fused;            /* 1: the mixed solver's multigrid levels below the finest, and
                                     the bottom pair, in one cooperative launch per V-cycle
-                                    (identical results); 0 (default): one launch per level pass */
+                                    (identical results); 2: the same from the second level below
+                                    the finest on; 0 (default): one launch per level pass      */
     int dependent_launch;        /* 1 (default): the mixed solver's chained kernels (finest-level
                                     tile kernels, coarse-level passes, the bottom) are launched as
                                     programmatic dependent launches, so that each is scheduled

@@ -23,11 +23,13 @@ def _scene(el, shape, seed):
     return sim
 
 
-@pytest.mark.parametrize("shape,tiles", [((96, 72, 80), 1), ((96, 72, 80), 0), ((70, 50, 60), 1)])
-def test_fused_coarse_cycle_is_bit_identical(el, orc, shape, tiles):
+@pytest.mark.parametrize("shape,tiles,level", [((96, 72, 80), 1, 1), ((96, 72, 80), 0, 1), ((70, 50, 60), 1, 1),
+                                              ((96, 72, 80), 1, 2), ((160, 120, 136), 1, 2)])
+def test_fused_coarse_cycle_is_bit_identical(el, orc, shape, tiles, level):
+    """level: the first level of the fused cycle (coarse_fused = 1 or 2)."""
     sims = [_scene(el, shape, 3), _scene(el, shape, 3)]
     out = []
-    for sim, fused in zip(sims, (1, 0)):
+    for sim, fused in zip(sims, (level, 0)):
         sim.set_tuning(solver_tiles=tiles, coarse_fused=fused)
         sim.profile_begin(1 << el.EL_KC_MG_COARSE)
         st = sim.solve_pressure(0.01, solver=el.SOLVER_MIXED, tol=1e-8, max_iter=400)
@@ -39,7 +41,7 @@ def test_fused_coarse_cycle_is_bit_identical(el, orc, shape, tiles):
     for f in f1:
         np.testing.assert_array_equal(f1[f], f0[f], err_msg=f)
     # one launch per V-cycle instead of four per level pass pair plus the bottom
-    assert prof1["launches"] < prof0["launches"] / 3, (prof1, prof0)
+    assert prof1["launches"] < prof0["launches"] / (3 if level == 1 else 1.3), (prof1, prof0)
     assert residual_rel(orc, sims[0].matrix(), f1["pressure"]) <= 5e-5
     for s in sims:
         s.close()
