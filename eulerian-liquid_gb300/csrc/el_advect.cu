@@ -591,7 +591,8 @@ __global__ void __launch_bounds__(kWX * kWY, sizeof(T) == 4 ? 2 : 1)
                                  const __grid_constant__ BoxMap pmap) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T* pbox = reinterpret_cast<T*>(align128(smem_raw));  // [z][y][x]
-    T* qbox = pbox + kWBoxN;                              // [s][row][floor index]
+    // [s][row][floor index]; in FP32 s = 0, 1 interleaved ({qa, qb} pairs), then the s = 2 plane
+    T* qbox = pbox + kWBoxN;
     const T* pb = pbox + 1;  // the box from node tile - 3 along x
     __shared__ uint64_t bar;
     const int x0 = blockIdx.x * kWX, y0 = blockIdx.y * kWY, z0 = blockIdx.z * kWZ;
@@ -626,8 +627,12 @@ __global__ void __launch_bounds__(kWX * kWY, sizeof(T) == 4 ? 2 : 1)
         const T* v = pb + row * kWBX + b;
         T qa, qb, qc;
         weno6_sq(v[0], v[1], v[2], v[3], v[4], v[5], qa, qb, qc);
-        qbox[e] = qa;
-        qbox[kWQ + e] = qb;
+        if constexpr (sizeof(T) == 4) {
+            reinterpret_cast<float2*>(qbox)[e] = make_float2(qa, qb);  // one 8-byte load for both
+        } else {
+            qbox[e] = qa;
+            qbox[kWQ + e] = qb;
+        }
         qbox[2 * kWQ + e] = qc;
     }
     __syncthreads();
@@ -652,7 +657,7 @@ __global__ void __launch_bounds__(kWX * kWY, sizeof(T) == 4 ? 2 : 1)
             const WenoAxis<T> wx = weno_axis(px.f);
             const WenoAxis<T> wy = weno_axis(py.f);
             T zl[6];
-#pragma unroll 1
+#pragma unroll
             for (int dk = 0; dk < 6; ++dk) {
                 const int row0 = (pz.a + dk) * kWBY + py.a;
                 T yl[6];
@@ -661,7 +666,16 @@ __global__ void __launch_bounds__(kWX * kWY, sizeof(T) == 4 ? 2 : 1)
                     const int row = row0 + dj;
                     const T* v = pb + row * kWBX + px.a;
                     const T* q = qbox + row * kWBases + px.a;
-                    yl[dj] = weno6_combine(wx, v[0], v[1], v[2], v[3], v[4], v[5], q[0], q[kWQ], q[2 * kWQ]);
+                    T qa, qb;
+                    if constexpr (sizeof(T) == 4) {
+                        const float2 qab = reinterpret_cast<const float2*>(qbox)[row * kWBases + px.a];
+                        qa = qab.x;
+                        qb = qab.y;
+                    } else {
+                        qa = q[0];
+                        qb = q[kWQ];
+                    }
+                    yl[dj] = weno6_combine(wx, v[0], v[1], v[2], v[3], v[4], v[5], qa, qb, q[2 * kWQ]);
                 }
                 const T zv = weno6_eval(wy, yl[0], yl[1], yl[2], yl[3], yl[4], yl[5]);
                 zl[0] = dk == 0 ? zv : zl[0];
