@@ -97,10 +97,11 @@ int ensure_projection(el_ctx* ctx) {
     if (ctx->flags) return EL_OK;
     const size_t n = (size_t)ctx->ni * ctx->nj * ctx->nk;
     ctx->flags = (uint8_t*)ctx_alloc(ctx, n);
+    ctx->built = (uint8_t*)ctx_alloc(ctx, n);  // zero: no row built yet (the outputs start zero)
     ctx->diag64 = (double*)ctx_alloc(ctx, n * 8);
     ctx->rhs64 = (double*)ctx_alloc(ctx, n * 8);
     for (int a = 0; a < 3; ++a) ctx->off[a] = ctx_alloc(ctx, n * ctx->esz);
-    if (!ctx->flags || !ctx->diag64 || !ctx->rhs64 || !ctx->off[0] || !ctx->off[1] || !ctx->off[2])
+    if (!ctx->flags || !ctx->built || !ctx->diag64 || !ctx->rhs64 || !ctx->off[0] || !ctx->off[1] || !ctx->off[2])
         return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "projection buffers");
     return EL_OK;
 }

@@ -26,7 +26,6 @@ constexpr int kIndexUnknown = 0x7fffffff;  // projection.cpp:6 UNKNOWN_INDEX = I
 // Cell flags written by the projection set-up kernel.
 constexpr uint8_t kFlagPressureValid = 1;  // is_pressure_valid (projection.cpp:8-12)
 constexpr uint8_t kFlagFluid = 2;          // pressure-valid and phi < 0
-constexpr uint8_t kFlagBuilt = 4;          // the matrix build's outputs at the cell may be nonzero
 
 struct Status {
     int code = EL_OK;
@@ -239,8 +238,10 @@ struct el_ctx {
     ushort4* A16 = nullptr;
     bool records_fresh = false;  // the last matrix build also wrote A32 / A16 (no packing pass needed)
     // the build leaves the zero rows of cells that were not fluid in the previous build either
-    // alone (kFlagBuilt); off where the outputs' contents are not known (scratch reused)
+    // alone (`built`: 1 where the build's outputs at the cell may be nonzero); off where the
+    // outputs' contents are not known (scratch reused)
     bool build_skip_zero = true;
+    uint8_t* built = nullptr;
     float *x32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *ap32 = nullptr;
     float* p32b = nullptr;
     float* r32b = nullptr;  // second residual buffer (the fused update writes r out of place)

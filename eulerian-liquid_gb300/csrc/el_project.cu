@@ -132,9 +132,11 @@ struct FaceView {
     const T* __restrict__ v;
     const T* __restrict__ w;
     int ni, nj, nk;
-    __device__ __forceinline__ T U(int i, int j, int k) const { return u[lin3(i, j, k, ni + 1, nj)]; }
-    __device__ __forceinline__ T V(int i, int j, int k) const { return v[lin3(i, j, k, ni, nj + 1)]; }
-    __device__ __forceinline__ T W(int i, int j, int k) const { return w[lin3(i, j, k, ni, nj)]; }
+    // read-only for the kernels that take a view: non-coherent loads, which the compiler may
+    // issue ahead of the kernel's byte stores (a byte pointer may alias anything)
+    __device__ __forceinline__ T U(int i, int j, int k) const { return __ldg(u + lin3(i, j, k, ni + 1, nj)); }
+    __device__ __forceinline__ T V(int i, int j, int k) const { return __ldg(v + lin3(i, j, k, ni, nj + 1)); }
+    __device__ __forceinline__ T W(int i, int j, int k) const { return __ldg(w + lin3(i, j, k, ni, nj)); }
 };
 
 // Cell flags (is_pressure_valid, projection.cpp:8-12; fluid = valid and phi < 0) and the
@@ -149,13 +151,15 @@ __global__ void flags_kernel(FaceView<T> wt, const T* __restrict__ phi, uint8_t*
     if (i < ni && j < nj) {
         // a contiguous chunk of planes per block: the neighbour planes come from L1
         const int k_end = min(nk, (int)(blockIdx.z + 1) * kz);
+#pragma unroll 4
         for (int k = blockIdx.z * kz; k < k_end; ++k) {
-            const bool pv = wt.U(i, j, k) > T(0) || wt.U(i + 1, j, k) > T(0) || wt.V(i, j, k) > T(0)
-                            || wt.V(i, j + 1, k) > T(0) || wt.W(i, j, k) > T(0) || wt.W(i, j, k + 1) > T(0);
+            const T w0 = wt.U(i, j, k), w1 = wt.U(i + 1, j, k), w2 = wt.V(i, j, k), w3 = wt.V(i, j + 1, k),
+                    w4 = wt.W(i, j, k), w5 = wt.W(i, j, k + 1);
             const long long c = lin3(i, j, k, ni, nj);
-            const bool fl = pv && phi[c] < T(0);
-            // the build's marker survives: it says what the build last wrote at the cell
-            flags[c] = (pv ? kFlagPressureValid : 0) | (fl ? kFlagFluid : 0) | (flags[c] & kFlagBuilt);
+            const T pc = __ldg(phi + c);
+            const bool pv = w0 > T(0) || w1 > T(0) || w2 > T(0) || w3 > T(0) || w4 > T(0) || w5 > T(0);
+            const bool fl = pv && pc < T(0);
+            flags[c] = (pv ? kFlagPressureValid : 0) | (fl ? kFlagFluid : 0);
             cnt[0] += fl ? 1.0 : 0.0;
         }
     }
@@ -176,9 +180,9 @@ struct CoeffOut {
 
 // build_matrix (projection.cpp:30-83), grid-shaped, plus |b|^2.
 template <typename T>
-__global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restrict__ phi, uint8_t* flags,
-                             CoeffOut<T> o, T dx, Scalars* s, double* partials, unsigned* counter, int kz,
-                             int skip_zero) {
+__global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restrict__ phi,
+                             const uint8_t* __restrict__ flags, uint8_t* __restrict__ built, CoeffOut<T> o, T dx,
+                             Scalars* s, double* partials, unsigned* counter, int kz) {
     const int ni = wt.ni, nj = wt.nj, nk = wt.nk;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -186,23 +190,27 @@ __global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restric
     const T scale = dx / dt;
     double bb[1] = {0.0};
     if (i < ni && j < nj) {
-        // a contiguous chunk of planes per block: the neighbour planes come from L1
+        // a contiguous chunk of planes per block: the neighbour planes come from L1; every load
+        // is a read-only one (the flags are not written here)
         const int k_end = min(nk, (int)(blockIdx.z + 1) * kz);
         for (int k = blockIdx.z * kz; k < k_end; ++k) {
             const long long c = lin3(i, j, k, ni, nj);
-            const uint8_t fc = flags[c];
+            const uint8_t fc = __ldg(flags + c);
             const bool fluid = (fc & kFlagFluid) != 0;
             // a row that is zero now and was zero after the previous build is left as it is
-            if (skip_zero && !fluid && !(fc & kFlagBuilt)) continue;
+            // (built: the marker of rows the build may have left nonzero, null where the outputs'
+            // contents are not known and every row is written)
+            const uint8_t bc = built ? built[c] : (uint8_t)1;
+            if (!fluid && !bc) continue;
             double d = 0.0, b = 0.0;
             double offv[3] = {0.0, 0.0, 0.0};
             if (fluid) {
-                const T pc = phi[c];
+                const T pc = __ldg(phi + c);
                 auto visit = [&](int x, int y, int z, T face_vel, T weight, bool forward, int axis) {
                     const bool inside = x >= 0 && y >= 0 && z >= 0 && x < ni && y < nj && z < nk;
                     const long long q = lin3(x, y, z, ni, nj);
-                    if (inside && (flags[q] & kFlagPressureValid)) {
-                        const T pn = phi[q];
+                    if (inside && (__ldg(flags + q) & kFlagPressureValid)) {
+                        const T pn = __ldg(phi + q);
                         if (pn < T(0)) {
                             d = dadd(d, (double)weight);
                             if (axis >= 0) offv[axis] = -(double)weight;
@@ -234,9 +242,7 @@ __global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restric
                 o.a16[c] = make_ushort4(__half_as_ushort(__float2half_ru(r.x)), __half_as_ushort(__float2half_rz(r.y)),
                                         __half_as_ushort(__float2half_rz(r.z)), __half_as_ushort(__float2half_rz(r.w)));
             }
-            // only this thread writes the byte; others read its low bits, which do not change
-            const uint8_t fn = fluid ? (uint8_t)(fc | kFlagBuilt) : (uint8_t)(fc & ~kFlagBuilt);
-            if (fn != fc) flags[c] = fn;
+            if (built && (fluid ? 1 : 0) != bc) built[c] = fluid ? 1 : 0;
             bb[0] += b * b;
         }
     }
@@ -413,9 +419,8 @@ static int launch_flags_build_t(el_ctx* ctx, bool inner32, bool build) {
     o.a32 = records ? ctx->A32 : nullptr;
     o.a16 = records ? ctx->A16 : nullptr;
     ctx->records_fresh = records;
-    build_kernel<T><<<g.grid, g.block, 0, ctx->stream>>>(vel, wt, phi, ctx->flags, o, (T)ctx->dx, ctx->dscal,
-                                                         ctx->partials, ctx->counter, g.kz,
-                                                         ctx->build_skip_zero ? 1 : 0);
+    build_kernel<T><<<g.grid, g.block, 0, ctx->stream>>>(vel, wt, phi, ctx->flags, ctx->build_skip_zero ? ctx->built : nullptr,
+                                                         o, (T)ctx->dx, ctx->dscal, ctx->partials, ctx->counter, g.kz);
     return 2;
 }
 
