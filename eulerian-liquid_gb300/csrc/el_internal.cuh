@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/eulerian_liquid_gb300.h"
+#include "el_f2d.cuh"
 
 namespace el {
 
@@ -397,6 +398,7 @@ inline Geom stencil_geom(int n0, int n1, int n2, int num_sms, int per_sm = 8) {
 __host__ __device__ inline long long lin3(int i, int j, int k, int n0, int n1) {
     return i + (long long)n0 * (j + (long long)n1 * k);
 }
+
 
 template <typename T>
 __device__ __forceinline__ T clampi(T v, T lo, T hi) {

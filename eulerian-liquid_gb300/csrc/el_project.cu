@@ -203,7 +203,7 @@ __global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restric
             const uint8_t bc = built ? built[c] : (uint8_t)1;
             if (!fluid && !bc) continue;
             double d = 0.0, b = 0.0;
-            double offv[3] = {0.0, 0.0, 0.0};
+            T offv[3] = {T(0), T(0), T(0)};  // exactly -weight: no rounding, so in the field type
             if (fluid) {
                 const T pc = __ldg(phi + c);
                 auto visit = [&](int x, int y, int z, T face_vel, T weight, bool forward, int axis) {
@@ -212,15 +212,15 @@ __global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restric
                     if (inside && (__ldg(flags + q) & kFlagPressureValid)) {
                         const T pn = __ldg(phi + q);
                         if (pn < T(0)) {
-                            d = dadd(d, (double)weight);
-                            if (axis >= 0) offv[axis] = -(double)weight;
+                            d = dadd(d, f2d(weight));
+                            if (axis >= 0) offv[axis] = -weight;
                         } else {
                             T theta = fraction_inside(pc, pn);
                             theta = theta < T(0.01) ? T(0.01) : theta;
-                            d = dadd(d, (double)(weight / theta));
+                            d = dadd(d, f2d(weight / theta));
                         }
                     }
-                    const double prod = (double)mul_rn(weight, face_vel);
+                    const double prod = f2d(mul_rn(weight, face_vel));
                     b = forward ? dsub(b, prod) : dadd(b, prod);
                 };
                 visit(i - 1, j, k, vel.U(i, j, k), wt.U(i, j, k), false, -1);
@@ -235,9 +235,9 @@ __global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restric
             o.diag64[c] = d;
             o.rhs64[c] = b;
 #pragma unroll
-            for (int a = 0; a < 3; ++a) o.off[a][c] = (T)offv[a];
+            for (int a = 0; a < 3; ++a) o.off[a][c] = offv[a];
             if (o.a32) {
-                const float4 r = make_float4((float)d, (float)(T)offv[0], (float)(T)offv[1], (float)(T)offv[2]);
+                const float4 r = make_float4((float)d, (float)offv[0], (float)offv[1], (float)offv[2]);
                 o.a32[c] = r;
                 o.a16[c] = make_ushort4(__half_as_ushort(__float2half_ru(r.x)), __half_as_ushort(__float2half_rz(r.y)),
                                         __half_as_ushort(__float2half_rz(r.z)), __half_as_ushort(__float2half_rz(r.w)));

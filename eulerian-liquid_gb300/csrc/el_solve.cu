@@ -397,7 +397,7 @@ template <typename OT>
 struct SplitLoad {
     SplitOp<OT> a;
     __device__ __forceinline__ Co<double> operator()(int q) const {
-        return Co<double>{a.d[q], (double)a.x[q], (double)a.y[q], (double)a.z[q]};
+        return Co<double>{a.d[q], f2d(a.x[q]), f2d(a.y[q]), f2d(a.z[q])};
     }
 };
 
@@ -665,7 +665,7 @@ __global__ void accumulate_kernel(LGeom g, SegArg seg, double* __restrict__ x64,
                                   const Scalars* si) {
     const double norm = si->norm;
     SEG_LOOP_BEGIN(seg, g)
-    x64[c] += norm * (double)x32[c];
+    x64[c] += norm * f2d(x32[c]);
     SEG_LOOP_END
 }
 
