@@ -122,6 +122,7 @@ struct MarchPlan {
     CUtensorMap centre[NCENTRE];
     CUtensorMap rec32, rec16, coarse_x;
     int per_sm[6] = {};  // resident CTAs per SM of each tile kernel
+    int planes = kMarchPlanes;  // planes per work item
 };
 
 // Makes `device` current for the length of one entry point and gives the caller's current
@@ -399,6 +400,32 @@ __host__ __device__ inline long long lin3(int i, int j, int k, int n0, int n1) {
     return i + (long long)n0 * (j + (long long)n1 * k);
 }
 
+
+// Round-to-nearest operations the compiler does not contract: an expression written with them
+// has one evaluation in every kernel.  (a * b + c * d may be contracted to fma(a, b, c * d) or
+// to fma(c, d, a * b), and different kernels may choose differently.)
+__device__ __forceinline__ float rn_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double rn_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float rn_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double rn_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float rn_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double rn_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float rn_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double rn_sub(double a, double b) { return __dsub_rn(a, b); }
+
+// The 7-point product d v0 + cxm vxm + cxp vxp + cym vym + cyp vyp + czm vzm + czp vzp in that
+// order, one rounding per multiply-add: the solver's kernels (segment, tile and bottom) share it
+template <typename V>
+__device__ __forceinline__ V stencil7(V d, V v0, V cxm, V vxm, V cxp, V vxp, V cym, V vym, V cyp, V vyp, V czm,
+                                      V vzm, V czp, V vzp) {
+    V t = rn_mul(d, v0);
+    t = rn_fma(cxm, vxm, t);
+    t = rn_fma(cxp, vxp, t);
+    t = rn_fma(cym, vym, t);
+    t = rn_fma(cyp, vyp, t);
+    t = rn_fma(czm, vzm, t);
+    return rn_fma(czp, vzp, t);
+}
 
 template <typename T>
 __device__ __forceinline__ T clampi(T v, T lo, T hi) {

@@ -72,10 +72,11 @@ struct Layout {
     static constexpr int nhalo = M == DIRSPMV ? 2 : (M == UPDZ ? 2 : 1);
     static constexpr int ncentre = M == UPDZ ? 2 : (M == ZERO2 || M == DIRSPMV ? 0 : 1);
     static constexpr bool coarse = M == PROLONG;
-    static constexpr int rec_bytes = M == DIRSPMV ? 16 : 8;
+    static constexpr bool f4 = M == DIRSPMV;  // float4 records (the PCG operator), else half4
+    static constexpr int rec_bytes = f4 ? 16 : 8;
     // the record box starts one (float4) or two (half4) cells left of the tile, the nearest
     // 16-byte boundary, and ends as far right of it
-    static constexpr int rec_x0 = M == DIRSPMV ? 1 : 2;
+    static constexpr int rec_x0 = f4 ? 1 : 2;
     static constexpr int rec_w = kTI + 2 * rec_x0;                // 34 / 36
     static constexpr int halo_bytes = kHX * kHY * 4;             // 2880
     static constexpr int rec_box_bytes = rec_w * kHY * rec_bytes; // 9792 / 5184
@@ -162,8 +163,8 @@ struct S7 {
     float d, cxm, cxp, cym, cyp, czm, czp;
 };
 __device__ __forceinline__ float apply7(const S7& st) {
-    return st.d * st.v0 + st.cxm * st.vxm + st.cxp * st.vxp + st.cym * st.vym + st.cyp * st.vyp + st.czm * st.vzm +
-           st.czp * st.vzp;
+    return stencil7(st.d, st.v0, st.cxm, st.vxm, st.cxp, st.vxp, st.cym, st.vym, st.cyp, st.vyp, st.czm, st.vzm,
+                    st.czp, st.vzp);
 }
 
 template <int M>
@@ -182,7 +183,8 @@ __device__ __forceinline__ bool dpos(const unsigned char* rec, int idx, int byte
 }
 
 template <int M>
-__global__ void __launch_bounds__(kThreads, Layout<M>::min_blocks) march_kernel(const __grid_constant__ Maps maps, const Args a) {
+__global__ void __launch_bounds__(kThreads, Layout<M>::min_blocks) march_kernel(const __grid_constant__ Maps maps,
+                                                                             const Args a) {
     using L = Layout<M>;
     Scalars* s = a.s;
     pdl_wait();
@@ -290,7 +292,7 @@ __global__ void __launch_bounds__(kThreads, Layout<M>::min_blocks) march_kernel(
                     if (dpos(Pp + L::off_rec, ridx, L::rec_bytes)) {
                         float raw = h0[hy * kHX + hx];
                         if (M == UPDZ) raw = raw - alpha * h1[hy * kHX + hx];
-                        out = mg_divf(w1 * raw, ld_rec(Pp + L::off_rec, ridx, L::rec_bytes).d);
+                        out = mg_divf(rn_mul(w1, raw), ld_rec(Pp + L::off_rec, ridx, L::rec_bytes).d);
                     }
                     mvp[e] = out;
                 }
@@ -408,7 +410,7 @@ __global__ void __launch_bounds__(kThreads, Layout<M>::min_blocks) march_kernel(
                         if (M == UPDZ || M == ZERO2) {
                             const float bc = M == UPDZ ? H(1, 0, hc) - alpha * H(1, 1, hc) : H(1, 0, hc);
                             float x2 = 0.f;
-                            if (dp0) x2 = st.v0 + mg_divf(w2 * (bc - apply7(st)), st.d);
+                            if (dp0) x2 = rn_add(st.v0, mg_divf(rn_mul(w2, rn_sub(bc, apply7(st))), st.d));
                             if (live && EL_IN(c, (long long)a.n0 * a.n1 * a.n2, 11)) {
                                 if (M == UPDZ) {
                                     // x += alpha p; r' out of place.  A tile also covers cells
@@ -428,11 +430,11 @@ __global__ void __launch_bounds__(kThreads, Layout<M>::min_blocks) march_kernel(
                         } else {
                             const float bc = Cn(0, row);
                             if (M == RESTRICT) {
-                                res[r] = dp0 ? bc - apply7(st) : 0.f;
+                                res[r] = dp0 ? rn_sub(bc, apply7(st)) : 0.f;
                             } else {
                                 const float omega = M == PROLONG ? w1 : w2;
                                 float xo = 0.f;
-                                if (dp0) xo = st.v0 + mg_divf(omega * (bc - apply7(st)), st.d);
+                                if (dp0) xo = rn_add(st.v0, mg_divf(rn_mul(omega, rn_sub(bc, apply7(st))), st.d));
                                 if (live && EL_IN(c, (long long)a.n0 * a.n1 * a.n2, 12)) {
                                     a.out0[c] = xo;
                                     if (M == LAST) part += bc * xo;
@@ -442,15 +444,18 @@ __global__ void __launch_bounds__(kThreads, Layout<M>::min_blocks) march_kernel(
                     }
                 }
                 if (M == RESTRICT) {
-                    // the residuals summed over 2x2x2 blocks onto the coarse rhs: the thread's two
-                    // rows are a j pair, the k pairs add in registers, the i pairs by shuffle
-                    racc0 = (k & 1) ? (racc0 + res[0]) + res[1] : res[0] + res[1];
+                    // the residuals summed over 2x2x2 blocks onto the coarse rhs in the segment
+                    // kernels' order: the i pairs first (by shuffle), then the block's four rows
+                    // (j, k) = (0, 0), (1, 0), (0, 1), (1, 1) -- the thread's two rows are a j pair,
+                    // the k pairs add in registers
+                    const float p0 = res[0] + __shfl_down_sync(kFull, res[0], 1);
+                    const float p1 = res[1] + __shfl_down_sync(kFull, res[1], 1);
+                    racc0 = (k & 1) ? (racc0 + p0) + p1 : p0 + p1;
                     if ((k & 1) || k + 1 == a.n2) {
-                        const float pr = racc0 + __shfl_down_sync(kFull, racc0, 1);
                         const int I = i0 / 2 + (lane >> 1), J = j0 / 2 + w, K = k >> 1;
                         if (!(lane & 1) && I < a.c0 && J < a.c1 &&
                             EL_IN(I + a.c0 * (J + a.c1 * K), (long long)a.c0 * a.c1 * a.c2, 13))
-                            a.out0[I + a.c0 * (J + a.c1 * K)] = pr;
+                            a.out0[I + a.c0 * (J + a.c1 * K)] = racc0;
                         racc0 = 0.f;
                     }
                 }
@@ -503,25 +508,28 @@ __global__ void __launch_bounds__(kThreads, Layout<M>::min_blocks) march_kernel(
 }
 
 // ---------------------------------------------------------------------------------------
-// work items: tiles of 32 x 16 cells x kMarchPlanes planes holding a cell with a positive
-// diagonal, in the order i-tile fastest, then j-tile, then plane chunk
+// work items: tiles of 32 x 16 cells x `planes` planes holding a cell with a positive diagonal,
+// in the order i-tile fastest, then j-tile, then plane chunk
 
-__global__ void march_flags_kernel(int n0, int n1, int n2, int nib, int njb, const ushort4* __restrict__ rec,
+__device__ __forceinline__ bool rec_active(const ushort4& r) { return __half2float(__ushort_as_half(r.x)) > 0.f; }
+__device__ __forceinline__ bool rec_active(const float4& r) { return r.x > 0.f; }
+
+template <typename R>
+__global__ void march_flags_kernel(int n0, int n1, int n2, int nib, int njb, int planes, const R* __restrict__ rec,
                                    uint8_t* __restrict__ flags) {
     const int item = blockIdx.x;
     const int ib = item % nib, jb = (item / nib) % njb, kc = item / (nib * njb);
     const int i = ib * kTI + (threadIdx.x & 31), j = jb * kTJ + (threadIdx.x >> 5);
-    const int k0 = kc * kMarchPlanes, k1 = min(n2, k0 + kMarchPlanes);
+    const int k0 = kc * planes, k1 = min(n2, k0 + planes);
     int act = 0;
     if (i < n0 && j < n1)
-        for (int k = k0; k < k1 && !act; ++k)
-            act = __half2float(__ushort_as_half(rec[i + n0 * (j + n1 * k)].x)) > 0.f;
+        for (int k = k0; k < k1 && !act; ++k) act = rec_active(rec[i + n0 * (j + n1 * k)]);
     act = __syncthreads_or(act);
     if (threadIdx.x == 0) flags[item] = act ? 1 : 0;
 }
 
 // ordered compaction of the flags (one block)
-__global__ void march_compact_kernel(int total, int nib, int njb, int n2, const uint8_t* __restrict__ flags,
+__global__ void march_compact_kernel(int total, int nib, int njb, int n2, int planes, const uint8_t* __restrict__ flags,
                                      int4* __restrict__ items, int* __restrict__ count) {
     __shared__ int scan[1024];
     const int t = threadIdx.x;
@@ -541,8 +549,8 @@ __global__ void march_compact_kernel(int total, int nib, int njb, int n2, const 
     for (int q = lo; q < hi; ++q)
         if (flags[q]) {
             const int ib = q % nib, jb = (q / nib) % njb, kc = q / (nib * njb);
-            const int k0 = kc * kMarchPlanes;
-            items[run++] = make_int4(ib * kTI, jb * kTJ, k0, min(n2, k0 + kMarchPlanes));
+            const int k0 = kc * planes;
+            items[run++] = make_int4(ib * kTI, jb * kTJ, k0, min(n2, k0 + planes));
         }
     if (t == blockDim.x - 1) *count = scan[t];
 }
@@ -560,25 +568,26 @@ int smem_bytes() {
 // dynamic shared memory, and the CTAs of the mode one SM holds (the grid is that many per SM,
 // or the number of tiles when smaller)
 template <int M>
-int set_smem(el_ctx* ctx) {
+int set_smem(el_ctx* ctx, MarchPlan& mp) {
     EL_CUDA_TRY(ctx, cudaFuncSetAttribute(march_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           smem_bytes<M>()));
     int per_sm = 0;
     EL_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_kernel<M>, kThreads, smem_bytes<M>()));
-    ctx->march.per_sm[M] = std::max(1, per_sm);
+    mp.per_sm[M] = std::max(1, per_sm);
     return EL_OK;
 }
 
 template <int M>
-int march_grid(el_ctx* ctx) {
-    const MarchPlan& mp = ctx->march;
+int march_grid(el_ctx* ctx, const MarchPlan& mp) {
     const long long total = (long long)mp.nib * mp.njb * mp.nkc;
     return (int)std::max<long long>(1, std::min<long long>(total, (long long)ctx->num_sms * mp.per_sm[M]));
 }
 
 template <int M>
 void launch(el_ctx* ctx, const Maps& maps, const Args& a) {
-    launch_dependent(ctx, march_kernel<M>, dim3(march_grid<M>(ctx)), dim3(kThreads), (size_t)smem_bytes<M>(), maps, a);
+    const MarchPlan& mp = ctx->march;
+    launch_dependent(ctx, march_kernel<M>, dim3(march_grid<M>(ctx, mp)), dim3(kThreads), (size_t)smem_bytes<M>(), maps,
+                     a);
 }
 
 Args base_args(el_ctx* ctx, Scalars* s) {
@@ -658,9 +667,9 @@ int march_setup(el_ctx* ctx) {
     ok = ok && tma_encode_3d(&mp.coarse_x, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, C.x, C.n0, C.n1, C.n2, C.n0, kCX, kCY);
     if (!ok) return EL_OK;  // the segment kernels stay in use
     int rc;
-    if ((rc = set_smem<DIRSPMV>(ctx)) != EL_OK || (rc = set_smem<UPDZ>(ctx)) != EL_OK ||
-        (rc = set_smem<ZERO2>(ctx)) != EL_OK || (rc = set_smem<RESTRICT>(ctx)) != EL_OK ||
-        (rc = set_smem<PROLONG>(ctx)) != EL_OK || (rc = set_smem<LAST>(ctx)) != EL_OK)
+    if ((rc = set_smem<DIRSPMV>(ctx, mp)) != EL_OK || (rc = set_smem<UPDZ>(ctx, mp)) != EL_OK ||
+        (rc = set_smem<ZERO2>(ctx, mp)) != EL_OK || (rc = set_smem<RESTRICT>(ctx, mp)) != EL_OK ||
+        (rc = set_smem<PROLONG>(ctx, mp)) != EL_OK || (rc = set_smem<LAST>(ctx, mp)) != EL_OK)
         return rc;
     mp.on = true;
     return EL_OK;
@@ -670,9 +679,10 @@ int march_setup(el_ctx* ctx) {
 int march_enqueue_items(el_ctx* ctx) {
     const MarchPlan& mp = ctx->march;
     const int total = mp.nib * mp.njb * mp.nkc;
-    march_flags_kernel<<<total, kTI * kTJ, 0, ctx->stream>>>(ctx->ni, ctx->nj, ctx->nk, mp.nib, mp.njb, ctx->A16,
-                                                            mp.flags);
-    march_compact_kernel<<<1, 1024, 0, ctx->stream>>>(total, mp.nib, mp.njb, ctx->nk, mp.flags, mp.items, mp.count);
+    march_flags_kernel<<<total, kTI * kTJ, 0, ctx->stream>>>(ctx->ni, ctx->nj, ctx->nk, mp.nib, mp.njb, mp.planes,
+                                                            ctx->A16, mp.flags);
+    march_compact_kernel<<<1, 1024, 0, ctx->stream>>>(total, mp.nib, mp.njb, ctx->nk, mp.planes, mp.flags, mp.items,
+                                                      mp.count);
     return 2;
 }
 

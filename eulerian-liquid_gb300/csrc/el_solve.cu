@@ -380,8 +380,8 @@ __device__ __forceinline__ St7<V> gather7(const LGeom& g, int c, int i, int j, i
 
 template <typename V>
 __device__ __forceinline__ V apply7(const St7<V>& st) {
-    return st.d * st.v0 + st.cxm * st.vxm + st.cxp * st.vxp + st.cym * st.vym + st.cyp * st.vyp + st.czm * st.vzm +
-           st.czp * st.vzp;
+    return stencil7(st.d, st.v0, st.cxm, st.vxm, st.cxp, st.vxp, st.cym, st.vym, st.cyp, st.vyp, st.czm, st.vzm,
+                    st.czp, st.vzp);
 }
 
 template <typename V, typename R>
@@ -752,14 +752,14 @@ __device__ __forceinline__ DotAcc<V> smooth_segments(const LGeom& g, const SegAr
     };
     auto valf = [&](V raw, const Co<V>& rec) -> V {
         if (!(rec.d > V(0))) return V(0);
-        return MODE == SM_ZERO2 ? mg_div(w_first * raw, rec.d) : raw;
+        return MODE == SM_ZERO2 ? mg_div(rn_mul(w_first, raw), rec.d) : raw;
     };
     SEG_LOOP_ALL_W_BEGIN(seg, g, wg, nw)
     const St7<V> st = gather7<V, true>(g, c, i, j, k, live, lane, recf, rawf, valf);
     if (live) {
         const V bc = ldv<COH>(b, c);
         V xo = V(0);
-        if (st.d > V(0)) xo = st.v0 + mg_div(omega * (bc - apply7(st)), st.d);
+        if (st.d > V(0)) xo = rn_add(st.v0, mg_div(rn_mul(omega, rn_sub(bc, apply7(st))), st.d));
         if (EL_IN(c, (long long)g.s2 * g.n2, 30)) x_out[c] = xo;
         if (DOT != DOT_NONE) part += (DotAcc<V>)bc * (DotAcc<V>)xo;
     }
@@ -826,7 +826,7 @@ __global__ void __launch_bounds__(kSegThreads, sizeof(V) == 4 ? 5 : 4) restrict_
                     const bool live = i < g.n0;
                     const int c = i + g.s1 * j + g.s2 * k;
                     const St7<V> st = gather7<V, false>(g, c, i, j, k, live, lane, recf, rawf, valf);
-                    if (live && st.d > V(0)) sum[h] += b[c] - apply7(st);
+                    if (live && st.d > V(0)) sum[h] += rn_sub(b[c], apply7(st));
                 }
         }
 #pragma unroll
@@ -874,7 +874,7 @@ __device__ __forceinline__ void restrict_quad_segments(const LGeom& g, const R* 
                 const bool live = i < g.n0;
                 const int c = i + g.s1 * j + g.s2 * k;
                 const St7<V> st = gather7<V, false>(g, c, i, j, k, live, lane, recf, rawf, valf);
-                if (live && st.d > V(0)) sum[h] = ldv<COH>(b, c) - apply7(st);
+                if (live && st.d > V(0)) sum[h] = rn_sub(ldv<COH>(b, c), apply7(st));
             }
         }
 #pragma unroll
@@ -930,7 +930,7 @@ __global__ void __launch_bounds__(kCoarsestMaxCells) coarsest_kernel(LGeom g, co
         sy[c] = (V)r.y;
         sz[c] = (V)r.z;
         sb[c] = b[c];
-        xa[c] = sd[c] > V(0) ? mg_div(omega * sb[c], sd[c]) : V(0);
+        xa[c] = sd[c] > V(0) ? mg_div(rn_mul(omega, sb[c]), sd[c]) : V(0);
     }
     __syncthreads();
     const int i = c % g.n0, j = (c / g.n0) % g.n1, k = c / (g.n0 * g.n1);
@@ -942,14 +942,14 @@ __global__ void __launch_bounds__(kCoarsestMaxCells) coarsest_kernel(LGeom g, co
             V xo = V(0);
             const V d = sd[c];
             if (d > V(0)) {
-                V a = d * cur[c];
-                if (i > 0) a += sx[c - 1] * cur[c - 1];
-                if (i < g.n0 - 1) a += sx[c] * cur[c + 1];
-                if (j > 0) a += sy[c - s1] * cur[c - s1];
-                if (j < g.n1 - 1) a += sy[c] * cur[c + s1];
-                if (k > 0) a += sz[c - s2] * cur[c - s2];
-                if (k < g.n2 - 1) a += sz[c] * cur[c + s2];
-                xo = cur[c] + mg_div(omega * (sb[c] - a), d);
+                V a = rn_mul(d, cur[c]);
+                if (i > 0) a = rn_fma(sx[c - 1], cur[c - 1], a);
+                if (i < g.n0 - 1) a = rn_fma(sx[c], cur[c + 1], a);
+                if (j > 0) a = rn_fma(sy[c - s1], cur[c - s1], a);
+                if (j < g.n1 - 1) a = rn_fma(sy[c], cur[c + s1], a);
+                if (k > 0) a = rn_fma(sz[c - s2], cur[c - s2], a);
+                if (k < g.n2 - 1) a = rn_fma(sz[c], cur[c + s2], a);
+                xo = rn_add(cur[c], mg_div(rn_mul(omega, rn_sub(sb[c], a)), d));
             }
             nxt[c] = xo;
         }
@@ -1058,7 +1058,7 @@ __device__ __forceinline__ void bottom_cycle(const LGeom& gf, const float4* __re
         const int c = fc[m];
         if (c < 0) continue;
         const float d = sr[c].x;
-        s1[c] = d > 0.f ? mg_div(w1 * sb[c], d) : 0.f;
+        s1[c] = d > 0.f ? mg_div(rn_mul(w1, sb[c]), d) : 0.f;
     }
     __syncthreads();
 #pragma unroll
@@ -1067,7 +1067,7 @@ __device__ __forceinline__ void bottom_cycle(const LGeom& gf, const float4* __re
         if (c < 0) continue;
         const St7<float> st = dense_st7(sr, s1, c, fin[m], gf);
         float xo = 0.f;
-        if (st.d > 0.f) xo = st.v0 + mg_div(w2 * (sb[c] - apply7(st)), st.d);
+        if (st.d > 0.f) xo = rn_add(st.v0, mg_div(rn_mul(w2, rn_sub(sb[c], apply7(st))), st.d));
         s2[c] = xo;
     }
     __syncthreads();
@@ -1078,7 +1078,7 @@ __device__ __forceinline__ void bottom_cycle(const LGeom& gf, const float4* __re
         const int c = fc[m];
         if (c < 0) continue;
         const St7<float> st = dense_st7(sr, s2, c, fin[m], gf);
-        s1[c] = st.d > 0.f ? sb[c] - apply7(st) : 0.f;
+        s1[c] = st.d > 0.f ? rn_sub(sb[c], apply7(st)) : 0.f;
     }
     __syncthreads();
     // the coarsest cell's record, rhs and neighbour bits in registers for all its sweeps
@@ -1105,7 +1105,7 @@ __device__ __forceinline__ void bottom_cycle(const LGeom& gf, const float4* __re
         if (cin & 4u) cym = cr[cq - gc.s1].z;
         if (cin & 16u) czm = cr[cq - gc.s2].w;
         // the coarsest level: damped Jacobi from zero, as coarsest_kernel
-        c1[cq] = cd > 0.f ? mg_div(omega * cbq, cd) : 0.f;
+        c1[cq] = cd > 0.f ? mg_div(rn_mul(omega, cbq), cd) : 0.f;
     }
     __syncthreads();
     float* cur = c1;
@@ -1115,14 +1115,14 @@ __device__ __forceinline__ void bottom_cycle(const LGeom& gf, const float4* __re
             float xo = 0.f;
             if (cd > 0.f) {
                 const float x0 = cur[cq];
-                float a = cd * x0;
-                if (cin & 1u) a += cxm * cur[cq - 1];
-                if (cin & 2u) a += cxp * cur[cq + 1];
-                if (cin & 4u) a += cym * cur[cq - gc.s1];
-                if (cin & 8u) a += cyp * cur[cq + gc.s1];
-                if (cin & 16u) a += czm * cur[cq - gc.s2];
-                if (cin & 32u) a += czp * cur[cq + gc.s2];
-                xo = x0 + mg_div(omega * (cbq - a), cd);
+                float a = rn_mul(cd, x0);
+                if (cin & 1u) a = rn_fma(cxm, cur[cq - 1], a);
+                if (cin & 2u) a = rn_fma(cxp, cur[cq + 1], a);
+                if (cin & 4u) a = rn_fma(cym, cur[cq - gc.s1], a);
+                if (cin & 8u) a = rn_fma(cyp, cur[cq + gc.s1], a);
+                if (cin & 16u) a = rn_fma(czm, cur[cq - gc.s2], a);
+                if (cin & 32u) a = rn_fma(czp, cur[cq + gc.s2], a);
+                xo = rn_add(x0, mg_div(rn_mul(omega, rn_sub(cbq, a)), cd));
             }
             nxt[cq] = xo;
         }
@@ -1146,7 +1146,7 @@ __device__ __forceinline__ void bottom_cycle(const LGeom& gf, const float4* __re
         if (c < 0) continue;
         const St7<float> st = dense_st7(sr, s1, c, fin[m], gf);
         float xo = 0.f;
-        if (st.d > 0.f) xo = st.v0 + mg_div(w1 * (sb[c] - apply7(st)), st.d);
+        if (st.d > 0.f) xo = rn_add(st.v0, mg_div(rn_mul(w1, rn_sub(sb[c], apply7(st))), st.d));
         s2[c] = xo;
     }
     __syncthreads();
@@ -1156,7 +1156,7 @@ __device__ __forceinline__ void bottom_cycle(const LGeom& gf, const float4* __re
         if (c < 0) continue;
         const St7<float> st = dense_st7(sr, s2, c, fin[m], gf);
         float xo = 0.f;
-        if (st.d > 0.f) xo = st.v0 + mg_div(w2 * (sb[c] - apply7(st)), st.d);
+        if (st.d > 0.f) xo = rn_add(st.v0, mg_div(rn_mul(w2, rn_sub(sb[c], apply7(st))), st.d));
         xf[c] = xo;
     }
 }

@@ -145,7 +145,7 @@ def test_trained_network_beats_zero_guess(el):
     ds = W.record(el, torch, specs, 6, (n, n, n), prm)
     assert len(ds) == 48
     net = W.WarmStartNet(torch, seed=0, lr=2e-3)
-    out = W.train(net, ds, epochs=12, batch=2, log=24)
+    out = W.train(net, ds, epochs=30, batch=2, log=24)
     hist = [h[1] for h in out["history"]]
     assert hist[-1] < 0.5 * hist[0], hist
     zero_it, warm_it = [], []
