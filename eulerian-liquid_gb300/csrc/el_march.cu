@@ -95,11 +95,12 @@ struct Layout {
     static constexpr int off_coarse = off_centre + ncentre * al(centre_bytes);
     static constexpr int off_mv = off_coarse + (coarse ? al(coarse_bytes) : 0);
     static constexpr int stage = al(off_mv + (mv ? mv_bytes : 0));
-    // six slots, five for ZERO2 (so that four of its CTAs fit an SM)
-    static constexpr int stages = M == ZERO2 ? 5 : 6;
+    // six slots; five for ZERO2 (four of its CTAs fit an SM); four for UPDZ (three CTAs per SM
+    // instead of two: 0.67 -> 0.70 of HBM; the same for DIRSPMV, RESTRICT or LAST measured slower)
+    static constexpr int stages = M == ZERO2 ? 5 : (M == UPDZ ? 4 : 6);
     static constexpr int smem = 128 + stages * stage + 128;  // barriers first; alignment slack
     // the CTAs an SM holds by shared memory, which the register budget must not lower
-    static constexpr int min_blocks = M == ZERO2 ? 4 : (M == DIRSPMV || M == UPDZ ? 2 : 3);
+    static constexpr int min_blocks = M == ZERO2 ? 4 : (M == DIRSPMV ? 2 : 3);
     static_assert(stages <= kMaxStages && 2 * kMaxStages * 8 <= 128, "barriers fit in front of the ring");
 };
 
