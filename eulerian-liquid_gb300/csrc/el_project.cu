@@ -11,6 +11,7 @@
 // rounds them, so the coefficients match the CPU restatement bit for bit.
 #include <cuda_fp16.h>
 
+#include "el_df.cuh"
 #include "el_internal.cuh"
 
 namespace el {
@@ -188,7 +189,10 @@ __global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restric
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const T dt = (T)s->dt;
     const T scale = dx / dt;
-    double bb[1] = {0.0};
+    // |b|^2: squares of the float-rounded b summed in FP32 per thread (a thread takes one column
+    // of kz cells; SqAcc keeps every square in range) and in FP64 over the grid -- FP64
+    // arithmetic per cell is what bounds this kernel
+    SqAcc bbs;
     if (i < ni && j < nj) {
         // a contiguous chunk of planes per block: the neighbour planes come from L1; every load
         // is a read-only one (the flags are not written here)
@@ -229,7 +233,7 @@ __global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restric
                 visit(i, j + 1, k, vel.V(i, j + 1, k), wt.V(i, j + 1, k), true, 1);
                 visit(i, j, k - 1, vel.W(i, j, k), wt.W(i, j, k), false, -1);
                 visit(i, j, k + 1, vel.W(i, j, k + 1), wt.W(i, j, k + 1), true, 2);
-                b = dmul(b, (double)scale);
+                b = dmul(b, f2d(scale));
             }
             if (!EL_IN(c, (long long)ni * nj * nk, 40)) continue;
             o.diag64[c] = d;
@@ -237,15 +241,16 @@ __global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restric
 #pragma unroll
             for (int a = 0; a < 3; ++a) o.off[a][c] = offv[a];
             if (o.a32) {
-                const float4 r = make_float4((float)d, (float)offv[0], (float)offv[1], (float)offv[2]);
+                const float4 r = make_float4(d2f(d), (float)offv[0], (float)offv[1], (float)offv[2]);
                 o.a32[c] = r;
                 o.a16[c] = make_ushort4(__half_as_ushort(__float2half_ru(r.x)), __half_as_ushort(__float2half_rz(r.y)),
                                         __half_as_ushort(__float2half_rz(r.z)), __half_as_ushort(__float2half_rz(r.w)));
             }
             if (built && (fluid ? 1 : 0) != bc) built[c] = fluid ? 1 : 0;
-            bb[0] += b * b;
+            bbs.add(d2f(b));
         }
     }
+    double bb[1] = {bbs.value()};
     double tot[1];
     if (grid_sum<1>(bb, partials, counter, tot)) s->bb = tot[0];
 }
@@ -315,13 +320,22 @@ __global__ void scan_write_kernel(const uint8_t* __restrict__ flags, long long n
     }
 }
 
+// a double into the field type (the float conversion on the integer pipe)
+template <typename T>
+__device__ __forceinline__ T to_field(double v) {
+    if constexpr (sizeof(T) == 4)
+        return d2f(v);
+    else
+        return v;
+}
+
 // build_grid_from_vector (projection.cpp:85-91): pressure = p on fluid cells, 0 elsewhere.
 template <typename T>
 __global__ void scatter_pressure_kernel(long long n, const double* __restrict__ x,
                                         const uint8_t* __restrict__ flags, T* __restrict__ p) {
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
          c += (long long)gridDim.x * blockDim.x)
-        p[c] = (flags[c] & kFlagFluid) ? (T)x[c] : T(0);
+        p[c] = (flags[c] & kFlagFluid) ? to_field<T>(x[c]) : T(0);
 }
 
 // update_velocity_using_pressure (projection.cpp:93-134): faces with index in [1, n) along

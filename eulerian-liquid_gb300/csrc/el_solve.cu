@@ -38,6 +38,7 @@
 
 #include <type_traits>
 
+#include "el_df.cuh"
 #include "el_internal.cuh"
 
 namespace el {
@@ -185,7 +186,7 @@ __global__ void seg_flags_diag_kernel(LGeom g, const double* __restrict__ diag, 
         int i, j, k;
         seg_cell((int)id, g, lane, i, j, k);
         bool act = false;
-        if (i < g.n0) act = diag[i + g.s1 * j + g.s2 * k] > 0;
+        if (i < g.n0) act = d_positive(diag[i + g.s1 * j + g.s2 * k]);
         const unsigned m = __ballot_sync(0xffffffffu, act);
         if (lane == 0) flags[id] = m ? 1 : 0;
     }
@@ -628,19 +629,50 @@ __global__ void guess_scale_kernel(LGeom g, SegArg seg, double* __restrict__ x, 
     }
 }
 
-// mixed solver: inner system r32 = r64 / |r64|, x32 = 0, inner thresholds.  The inner relative
-// tolerance is what the outer one still needs, halved, kept within [floor, 1/2] (FP32 cannot go
-// much below 1e-4 reliably): tau = clamp(0.5 tol |b| / |r|, floor, 0.5).
+// FP64 paths taken by few cells, kept out of line: the compiler would otherwise predicate them
+// into the common path, where each FP64 instruction costs an issue slot of the FP64 pipe (the
+// bound of these kernels) on every cell, switched off or not.
+__device__ __noinline__ float scale_fp64(double r, double inv) { return (float)(r * inv); }
+
+__device__ __noinline__ double residual_cell_fp64(double bc, double d, double x0, float cxm, double vxm, float cxp,
+                                                  double vxp, float cym, double xym, float cyp, double xyp,
+                                                  float czm, double xzm, float czp, double xzp) {
+    return bc - stencil7(d, x0, f2d(cxm), vxm, f2d(cxp), vxp, f2d(cym), xym, f2d(cyp), xyp, f2d(czm), xzm, f2d(czp),
+                         xzp);
+}
+
+// mixed solver: inner system r32 = r64 2^-k with 2^k the power of two at or below |r64| (the
+// scaling is exact both ways, and |r32| lies in [1, 2)), x32 = 0, inner thresholds.  The scale
+// comes from the exponent bits of |r|^2: square roots and divisions in FP64 by every thread cost
+// more FP64 issue than the cells' own work.  A cell's value is split into a float pair (integer
+// arithmetic) and scaled on the FP32 pipe.  |r|^2 outside [2^-200, 2^200] (or not finite) takes
+// the scale 1 / |r| in FP64.  The inner relative tolerance is what the outer one still needs,
+// halved, kept within [floor, 1/2] (FP32 cannot go much below 1e-4 reliably):
+// tau = clamp(0.5 tol |b| / |r|, floor, 0.5).
 __global__ void inner_init_kernel(LGeom g, SegArg seg, const double* __restrict__ r64, float* __restrict__ r32,
                                   float* __restrict__ x32, const Scalars* so, Scalars* si, double tol,
                                   double tau_floor, double* partials, unsigned* counter) {
-    const double want = so->rr > 0.0 ? 0.5 * tol * sqrt(so->bb / so->rr) : 0.5;
-    const double tau = fmin(0.5, fmax(tau_floor, want));
-    const double norm = sqrt(so->rr);
-    const double inv = norm > 0.0 ? 1.0 / norm : 0.0;
+    const double rr = so->rr;
+    const unsigned long long rb = (unsigned long long)__double_as_longlong(rr);
+    const int k = ((int)((rb >> 52) & 0x7ffu) - 1023) >> 1;
+    const bool pow2 = rb != 0ull && (rb >> 63) == 0ull && k >= -100 && k <= 100;
+    double norm, inv;
+    float invf;
+    if (pow2) {
+        norm = __longlong_as_double((long long)(1023 + k) << 52);
+        inv = __longlong_as_double((long long)(1023 - k) << 52);
+        invf = __int_as_float((127 - k) << 23);
+    } else {
+        norm = sqrt(rr);
+        inv = norm > 0.0 ? 1.0 / norm : 0.0;
+        invf = 0.f;
+    }
     float part = 0.f;
     SEG_LOOP_BEGIN(seg, g)
-    const float v = (float)(r64[c] * inv);
+    const double rc = r64[c];
+    bool ok = pow2;
+    const F2 q = df_split(rc, ok);
+    const float v = ok ? df_fma(q.h, invf, df_mul(q.l, invf)) : scale_fp64(rc, inv);
     r32[c] = v;
     x32[c] = 0.0f;
     part += v * v;
@@ -648,6 +680,8 @@ __global__ void inner_init_kernel(LGeom g, SegArg seg, const double* __restrict_
     double acc[1] = {(double)part};
     double tot[1];
     if (grid_sum<1>(acc, partials, counter, tot)) {
+        const double want = rr > 0.0 ? 0.5 * tol * sqrt(so->bb / rr) : 0.5;
+        const double tau = fmin(0.5, fmax(tau_floor, want));
         si->bb = tot[0];
         si->rr = tot[0];
         si->thresh = tau * tau * tot[0];
@@ -669,6 +703,17 @@ __global__ void accumulate_kernel(LGeom g, SegArg seg, double* __restrict__ x64,
     SEG_LOOP_END
 }
 
+// |r|^2 of a refinement residual into the scalars and the stopping test
+__device__ __forceinline__ void residual_done(Scalars* s, double rr) {
+    s->rr = rr;
+    if (!finite_d(rr)) {
+        s->bad = 1;
+        s->done = 1;
+    } else if (rr < s->thresh) {
+        s->done = 1;
+    }
+}
+
 // FP64 residual r = b - A x and |r|^2 (outer refinement step).
 template <typename OT>
 __global__ void __launch_bounds__(kSegThreads) residual_kernel(LGeom g, SegArg seg, SplitOp<OT> A,
@@ -682,21 +727,86 @@ __global__ void __launch_bounds__(kSegThreads) residual_kernel(LGeom g, SegArg s
     SEG_LOOP_ALL_BEGIN(seg, g)
     const St7<double> st = gather7<double, false>(g, c, i, j, k, live, lane, recf, rawf, valf);
     if (live) {
-        const double rc = st.d > 0.0 ? b[c] - apply7(st) : 0.0;
+        const double rc = d_positive(st.d) ? b[c] - apply7(st) : 0.0;
         r[c] = rc;
         acc[0] += rc * rc;
     }
     SEG_LOOP_END
     double tot[1];
-    if (grid_sum<1>(acc, partials, counter, tot)) {
-        s->rr = tot[0];
-        if (!finite_d(tot[0])) {
-            s->bad = 1;
-            s->done = 1;
-        } else if (tot[0] < s->thresh) {
-            s->done = 1;
+    if (grid_sum<1>(acc, partials, counter, tot)) residual_done(s, tot[0]);
+}
+
+// The mixed solver's refinement residual r = b - A x and |r|^2 for FP32 fields, whose couplings
+// are exact floats: double-float arithmetic on the FP32 pipe (el_df.cuh) in place of the FP64
+// operations, which bound the FP64 kernel above (nine a cell, its FP64 pipe 86 % busy).  b, the
+// diagonal and the iterate are split into float pairs by integer arithmetic; the pair of r is
+// within 2^-41 of the sum of its row's term magnitudes, and is stored as a double.  A warp in
+// which any operand lies outside the pairs' exponent range (el_df.cuh) takes the FP64
+// arithmetic of the kernel above for all its lanes.  |r|^2 is summed in FP32 per thread (each
+// takes a few dozen cells; SqAcc keeps every square in range) and in FP64 over the grid.
+__global__ void __launch_bounds__(kSegThreads, 4) residual_df_kernel(LGeom g, SegArg seg, SplitOp<float> A,
+                                                                  const double* __restrict__ b,
+                                                                  const double* __restrict__ x,
+                                                                  double* __restrict__ r, Scalars* s,
+                                                                  double* partials, unsigned* counter) {
+    SqAcc acc2;
+    SEG_LOOP_ALL_BEGIN(seg, g)
+    const bool iym = live && j > 0, iyp = live && j < g.n1 - 1;
+    const bool izm = live && k > 0, izp = live && k < g.n2 - 1;
+    const bool ixm = lane == 0 && live && i > 0;
+    const bool ixp = lane == 31 && live && i + 1 < g.n0;
+    // loads, all issued before any value is formed
+    const double d = live ? A.d[c] : 0.0;
+    const double bc = live ? b[c] : 0.0;
+    const float cxp = live ? A.x[c] : 0.f, cyp = live ? A.y[c] : 0.f, czp = live ? A.z[c] : 0.f;
+    const float cym = iym ? A.y[c - g.s1] : 0.f, czm = izm ? A.z[c - g.s2] : 0.f;
+    const float cxm_e = ixm ? A.x[c - 1] : 0.f;
+    const double x0 = live ? x[c] : 0.0;
+    const double xym = iym ? x[c - g.s1] : 0.0, xyp = iyp ? x[c + g.s1] : 0.0;
+    const double xzm = izm ? x[c - g.s2] : 0.0, xzp = izp ? x[c + g.s2] : 0.0;
+    const double xxm_e = ixm ? x[c - 1] : 0.0, xxp_e = ixp ? x[c + 1] : 0.0;
+    const bool act = live && d_positive(d);
+    const bool xp_in = live && i + 1 < g.n0;
+    const float cxm_s = __shfl_up_sync(kFull, cxp, 1);
+    const float cxm = lane == 0 ? cxm_e : cxm_s;
+    bool ok = true;
+    const F2 p0 = df_split(x0, ok);
+    const F2 pym = df_split(xym, ok), pyp = df_split(xyp, ok), pzm = df_split(xzm, ok), pzp = df_split(xzp, ok);
+    const F2 pxm_e = df_split(xxm_e, ok), pxp_e = df_split(xxp_e, ok);
+    const F2 pd = df_split(d, ok), pb = df_split(bc, ok);
+    F2 pxm, pxp;
+    pxm.h = __shfl_up_sync(kFull, p0.h, 1);
+    pxm.l = __shfl_up_sync(kFull, p0.l, 1);
+    pxp.h = __shfl_down_sync(kFull, p0.h, 1);
+    pxp.l = __shfl_down_sync(kFull, p0.l, 1);
+    if (lane == 0) pxm = pxm_e;
+    if (lane == 31) pxp = pxp_e;
+    if (!xp_in) pxp = F2{0.f, 0.f};
+    if (__all_sync(kFull, ok)) {
+        if (act) {
+            const F2 q = df_residual7(pb, pd, p0, cxm, pxm, cxp, pxp, cym, pym, cyp, pyp, czm, pzm, czp, pzp);
+            r[c] = __dadd_rn(f2d(q.h), f2d(q.l));
+            acc2.add(q.h);
+        } else if (live) {
+            r[c] = 0.0;
+        }
+    } else {
+        // the FP64 arithmetic of residual_kernel, for every lane of the warp
+        const double sxm = __shfl_up_sync(kFull, x0, 1), sxp = __shfl_down_sync(kFull, x0, 1);
+        if (live) {
+            const double vxm = lane == 0 ? xxm_e : sxm;
+            const double vxp = xp_in ? (lane == 31 ? xxp_e : sxp) : 0.0;
+            const double rc = act ? residual_cell_fp64(bc, d, x0, cxm, vxm, cxp, vxp, cym, xym, cyp, xyp, czm, xzm,
+                                                       czp, xzp)
+                                  : 0.0;
+            r[c] = rc;
+            acc2.add(d2f(rc));
         }
     }
+    SEG_LOOP_END
+    double acc[1] = {acc2.value()};
+    double tot[1];
+    if (grid_sum<1>(acc, partials, counter, tot)) residual_done(s, tot[0]);
 }
 
 
@@ -1785,6 +1895,19 @@ static void mg_restore_pointers(el_ctx* ctx) {
     if (!ctx->mg32.empty()) ctx->mg32[0].b = ctx->r32;
 }
 
+// The mixed solver's refinement residual: double-float arithmetic for FP32 fields (exact float
+// couplings), FP64 for FP64 fields.
+template <typename T>
+static void enqueue_refine_residual(el_ctx* ctx, const LGeom& g, const SplitOp<T>& A64, Scalars* s0) {
+    const int nb = seg_blocks(ctx, ctx->seg0.total);
+    if constexpr (std::is_same<T, float>::value)
+        residual_df_kernel<<<nb, kSegThreads, 0, ctx->stream>>>(g, seg_arg(ctx->seg0), A64, ctx->rhs64, ctx->x64,
+                                                                ctx->r64, s0, ctx->partials, ctx->counter);
+    else
+        residual_kernel<T><<<nb, kSegThreads, 0, ctx->stream>>>(g, seg_arg(ctx->seg0), A64, ctx->rhs64, ctx->x64,
+                                                                ctx->r64, s0, ctx->partials, ctx->counter);
+}
+
 // Solve A x64 = rhs64 (matrix already built, s0.bb set).  Fills stats.
 template <typename T>
 static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) {
@@ -1919,8 +2042,7 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
             {
                 // reads x, b, diag (f64), 3 couplings; writes r (f64)
                 ProfScope prof(ctx, EL_KC_RESIDUAL, na * (32 + 3 * sizeof(T)));
-                residual_kernel<T><<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
-                    g, seg_arg(ctx->seg0), A64, ctx->rhs64, ctx->x64, ctx->r64, s0, ctx->partials, ctx->counter);
+                enqueue_refine_residual(ctx, g, A64, s0);
             }
             ctx->launches += 2;
             ++outer;
@@ -2080,8 +2202,7 @@ static int enqueue_solve_device_t(el_ctx* ctx, const el_solve_params& prm, int k
     rc = end_while(ctx, parent_inner);
     accumulate_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
         g, seg_arg(ctx->seg0), ctx->x64, ctx->x32, s1);
-    residual_kernel<T><<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
-        g, seg_arg(ctx->seg0), A64, ctx->rhs64, ctx->x64, ctx->r64, s0, ctx->partials, ctx->counter);
+    enqueue_refine_residual(ctx, g, A64, s0);
     outer_cond_kernel<<<1, 1, 0, ctx->stream>>>(h_outer, s0, s1, max_outer, prm.max_iter, 1);
     const int rc2 = end_while(ctx, parent_outer);
     mg_restore_pointers(ctx);

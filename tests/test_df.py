@@ -1,0 +1,184 @@
+"""The double-float routines of the mixed solver's refinement residual (csrc/el_df.cuh) against
+exact rational arithmetic: the header compiled for the host (round-to-nearest float operations,
+no contraction), inputs and outputs passed as hexadecimal floats.
+
+* the split of a double into a float pair: h + l within 2^-46 of d, h the truncation of d to 24
+  significant bits, both of d's sign; below 2^-103 the nearest float and zero; the range flag
+  cleared exactly from 2^128 on (and for NaN);
+* the positivity test by integer comparison, for the special values;
+* the seven-point residual b - A x for Poisson-like rows whose terms cancel to a small residual:
+  within 2^-41 of the sum of the terms' magnitudes (the bound the header states), and the
+  typical error far below it.
+"""
+
+import math
+import os
+import random
+import shutil
+import struct
+import subprocess
+from fractions import Fraction
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+HEADER_DIR = os.path.join(HERE, "..", "eulerian-liquid_gb300", "csrc")
+
+DRIVER = r"""
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include "el_df.cuh"
+using namespace el;
+static double rd() { char b[64]; if (std::scanf("%63s", b) != 1) std::exit(2); return std::strtod(b, nullptr); }
+int main() {
+    char mode[16];
+    while (std::scanf("%15s", mode) == 1) {
+        if (!std::strcmp(mode, "split")) {
+            const double d = rd();
+            bool ok = true;
+            const F2 p = df_split(d, ok);
+            std::printf("%a %a %d\n", (double)p.h, (double)p.l, ok ? 1 : 0);
+        } else if (!std::strcmp(mode, "pos")) {
+            const double d = rd();
+            std::printf("%d\n", d_positive(d) ? 1 : 0);
+        } else {
+            double v[9];
+            float c[6];
+            for (double& q : v) q = rd();
+            for (float& q : c) q = (float)rd();
+            bool ok = true;
+            F2 p[9];
+            for (int q = 0; q < 9; ++q) p[q] = df_split(v[q], ok);
+            const F2 r = df_residual7(p[0], p[1], p[2], c[0], p[3], c[1], p[4], c[2], p[5], c[3], p[6], c[4], p[7],
+                                      c[5], p[8]);
+            std::printf("%a %a %d\n", (double)r.h, (double)r.l, ok ? 1 : 0);
+        }
+    }
+    return 0;
+}
+"""
+
+
+@pytest.fixture(scope="module")
+def run(tmp_path_factory):
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("no host compiler")
+    d = tmp_path_factory.mktemp("df")
+    src = d / "df.cpp"
+    src.write_text(DRIVER)
+    exe = d / "df"
+    subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I", HEADER_DIR, str(src), "-o", str(exe)],
+                   check=True)
+
+    def go(lines):
+        r = subprocess.run([str(exe)], input="\n".join(lines) + "\n", capture_output=True, text=True, timeout=120)
+        assert r.returncode == 0, r.stderr
+        return r.stdout.split("\n")[:len(lines)]
+
+    return go
+
+
+def f32(x):
+    return struct.unpack("<f", struct.pack("<f", x))[0]
+
+
+def trunc24(d):
+    """d truncated to 24 significant bits (toward zero)."""
+    m, e = math.frexp(abs(d))
+    t = math.ldexp(math.floor(math.ldexp(m, 24)), e - 24)
+    return math.copysign(t, d)
+
+
+def test_split(run):
+    rng = random.Random(5)
+    vals = [0.0, -0.0, 1.0, -1.0, 2.0 ** -103, -(2.0 ** -103), math.nextafter(2.0 ** -103, 0), 2.0 ** -104,
+            math.nextafter(2.0 ** 128, 0), -math.nextafter(2.0 ** 128, 0), 2.0 ** 128, 2.0 ** 127, 5e-324, 2.2e-308,
+            float("inf"), float("-inf"), float("nan"), 1e300, 1e-300]
+    for _ in range(4000):
+        vals.append(rng.choice((-1, 1)) * math.ldexp(rng.random() + 0.5, rng.randint(-160, 130)))
+    for _ in range(500):
+        vals.append(rng.choice((-1, 1)) * f32(rng.uniform(0.5, 1.0)) * 2.0 ** rng.randint(-20, 20))
+    out = run(["split " + v.hex() for v in vals])
+    for v, line in zip(vals, out):
+        h, l, ok = line.split()
+        h, l, ok = float.fromhex(h), float.fromhex(l), int(ok)
+        a = abs(v)
+        want_ok = not (a >= 2.0 ** 128 or math.isnan(v))
+        assert ok == want_ok, (v.hex(), ok)
+        if not ok:
+            continue
+        if v == 0.0:
+            assert h == 0.0 and l == 0.0
+            continue
+        if a < 2.0 ** -103:
+            # the nearest float and zero
+            assert h == f32(v) and l == 0.0, v.hex()
+            continue
+        assert h == trunc24(v), v.hex()
+        assert l == 0.0 or math.copysign(1.0, l) == math.copysign(1.0, v)
+        err = abs(Fraction(v) - Fraction(h) - Fraction(l))
+        assert err < Fraction(a) / 2 ** 46, v.hex()
+        assert f32(h) == h and f32(l) == l
+
+
+def test_positive(run):
+    vals = [0.0, -0.0, 1.0, -1.0, 5e-324, -5e-324, float("inf"), float("-inf"), float("nan"), -float("nan"),
+            1e308, -1e-308]
+    out = run(["pos " + v.hex() for v in vals])
+    for v, line in zip(vals, out):
+        assert int(line) == (1 if v > 0.0 else 0), v
+
+
+def _row(rng, scale, spread):
+    """A ghost-fluid Poisson row: couplings -w (floats, some zero), diagonal the double sum of
+    the weights plus an air term w / theta for some faces, x a smooth field of magnitude `scale`
+    with relative variation `spread`, b the exact A x plus a small residual."""
+    c = []
+    d = 0.0
+    for _ in range(6):
+        w = f32(rng.choice((1.0, rng.random(), rng.random() * 1e-3, 0.0)))
+        if rng.random() < 0.2:
+            d += float(f32(w / f32(max(0.01, rng.random()))))
+            c.append(0.0)
+        else:
+            d += w
+            c.append(-w)
+    d = d if d > 0 else 1.0
+    x0 = scale * (1 + spread * rng.uniform(-1, 1))
+    xs = [scale * (1 + spread * rng.uniform(-1, 1)) for _ in range(6)]
+    ax = Fraction(d) * Fraction(x0) + sum(Fraction(ci) * Fraction(xi) for ci, xi in zip(c, xs))
+    b = float(ax) + scale * rng.choice((0.0, 1e-6, 1e-10, 1.0)) * rng.uniform(-1, 1)
+    return [b, d, x0] + xs, c
+
+
+def test_residual7(run):
+    rng = random.Random(11)
+    rows = []
+    for _ in range(6000):
+        scale = rng.choice((1.0, 1e3, 1e-3, 37.5, 1e8, 1e-8))
+        rows.append(_row(rng, scale, rng.choice((1e-1, 1e-4, 1e-7, 0.0))))
+    lines = []
+    for v, c in rows:
+        b, d, x0, xxm, xxp, xym, xyp, xzm, xzp = v
+        cxm, cxp, cym, cyp, czm, czp = c
+        lines.append("res " + " ".join(q.hex() for q in (b, d, x0, xxm, xxp, xym, xyp, xzm, xzp)) + " " +
+                     " ".join(float(q).hex() for q in (cxm, cxp, cym, cyp, czm, czp)))
+    out = run(lines)
+    worst = Fraction(0)
+    for (v, c), line in zip(rows, out):
+        h, l, ok = line.split()
+        h, l = Fraction(float.fromhex(h)), Fraction(float.fromhex(l))
+        assert int(ok) == 1
+        b, d, x0, xxm, xxp, xym, xyp, xzm, xzp = (Fraction(q) for q in v)
+        cs = [Fraction(q) for q in c]
+        terms = [b, d * x0] + [ci * xi for ci, xi in zip(cs, (xxm, xxp, xym, xyp, xzm, xzp))]
+        exact = terms[0] - sum(terms[1:])
+        mag = sum(abs(t) for t in terms)
+        err = abs(h + l - exact)
+        assert err <= mag / 2 ** 41, (line, float(err / mag))
+        if mag:
+            worst = max(worst, err / mag)
+    # in practice the splits' truncation dominates: well inside the stated bound
+    assert worst < Fraction(1, 2 ** 44), float(worst)
