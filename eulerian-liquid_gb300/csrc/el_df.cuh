@@ -126,6 +126,54 @@ EL_F2D_HD F2 df_residual7(F2 b, F2 d, F2 x0, float cxm, F2 xxm, float cxp, F2 xx
     return r;
 }
 
+// The double sum of six floats added in order from zero, as fl(fl(fl(0 + t0) + t1) ...), when
+// no partial sum needs more than 53 significant bits: every nonzero term within 2^26 of the
+// largest in exponent (six terms below 2^(e_max + 1) sum below 2^(e_max + 4), in units of the
+// smallest term's last bit 2^(e_min - 23): 27 + e_max - e_min bits).  Each addition is then
+// exact, so the result is the exact sum, formed here in a 64-bit integer and packed as a
+// double; zero is +0, as the additions give.  Returns false otherwise (and for non-finite
+// terms), when the caller adds in FP64.  Integer arithmetic only.
+EL_F2D_HD bool exact_sum6(float t0, float t1, float t2, float t3, float t4, float t5, double& out) {
+    const float t[6] = {t0, t1, t2, t3, t4, t5};
+    uint32_t u[6];
+    uint32_t emax = 0u, emin = 255u, fin = 1u;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        std::memcpy(&u[q], &t[q], sizeof(uint32_t));
+        const uint32_t mag = u[q] & 0x7fffffffu;
+        uint32_t e = mag >> 23;
+        fin &= e != 255u ? 1u : 0u;
+        e = e ? e : 1u;  // a subnormal counts at exponent 1, without the leading one
+        if (mag) {
+            emax = e > emax ? e : emax;
+            emin = e < emin ? e : emin;
+        }
+    }
+    uint64_t bits = 0ull;
+    if (emax) {
+        if (!fin || emax - emin > 26u) return false;
+        int64_t S = 0;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const uint32_t mag = u[q] & 0x7fffffffu;
+            const uint32_t e = mag >> 23;
+            const uint32_t m = (mag & 0x7fffffu) | (e ? 0x800000u : 0u);
+            const int64_t v = (int64_t)((uint64_t)m << ((e ? e : 1u) - emin));
+            S += (u[q] >> 31) ? -v : v;
+        }
+        if (S != 0) {
+            const uint64_t sg = S < 0 ? 1ull : 0ull;
+            const uint64_t A = sg ? (uint64_t)(-S) : (uint64_t)S;  // below 2^53
+            const uint32_t ah = (uint32_t)(A >> 32);
+            const int p = ah ? 63 - clz32(ah) : 31 - clz32((uint32_t)A);
+            const uint64_t mant = (A << (52 - p)) & 0xfffffffffffffull;
+            bits = (sg << 63) | ((uint64_t)(p + (int)emin + 873) << 52) | mant;
+        }
+    }
+    std::memcpy(&out, &bits, sizeof(out));
+    return true;
+}
+
 // A sum of squares of floats in three FP32 accumulators by magnitude (below 2^-60, up to
 // 2^60, beyond), so that no square leaves the normal float range; the total in FP64.  For the
 // per-thread partial norms of kernels bound by FP64 issue.

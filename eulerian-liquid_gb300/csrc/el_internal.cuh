@@ -247,6 +247,7 @@ struct el_ctx {
     float *x32 = nullptr, *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *ap32 = nullptr;
     float* p32b = nullptr;
     float* r32b = nullptr;  // second residual buffer (the fused update writes r out of place)
+    float2* xs = nullptr;   // the mixed solver's FP64 iterate as float pairs (the double-float residual)
     el::MarchPlan march;    // finest-level tile kernels of the mixed solver
     el::Rec64* A64rec = nullptr;  // level-0 records of the FP64 multigrid
     el::SegList seg0;             // active segments of the finest level

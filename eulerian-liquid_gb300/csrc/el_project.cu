@@ -180,8 +180,37 @@ struct CoeffOut {
 };
 
 // build_matrix (projection.cpp:30-83), grid-shaped, plus |b|^2.
+// The diagonal: its terms added in the neighbours' order in double from zero (an absent
+// neighbour adds zero, which leaves the sum as it is).  FP32 fields: the exact integer sum where
+// no addition rounds (exact_sum6, nearly every row: the terms are weights of at most a few
+// powers of two apart), else the FP64 additions, out of line so that their instructions are not
+// issued, predicated off, for every row.
+__device__ __noinline__ double diag_sum_fp64(float t0, float t1, float t2, float t3, float t4, float t5) {
+    double d = dadd(0.0, f2d(t0));
+    d = dadd(d, f2d(t1));
+    d = dadd(d, f2d(t2));
+    d = dadd(d, f2d(t3));
+    d = dadd(d, f2d(t4));
+    return dadd(d, f2d(t5));
+}
+
 template <typename T>
-__global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restrict__ phi,
+__device__ __forceinline__ double diag_sum(const T (&t)[6]) {
+    if constexpr (sizeof(T) == 4) {
+        double d;
+        if (exact_sum6(t[0], t[1], t[2], t[3], t[4], t[5], d)) return d;
+        return diag_sum_fp64(t[0], t[1], t[2], t[3], t[4], t[5]);
+    } else {
+        double d = 0.0;
+#pragma unroll
+        for (int f = 0; f < 6; ++f) d = dadd(d, t[f]);
+        return d;
+    }
+}
+
+// four blocks of 256 per SM for FP32 fields (64 registers, no spills)
+template <typename T>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restrict__ phi,
                              const uint8_t* __restrict__ flags, uint8_t* __restrict__ built, CoeffOut<T> o, T dx,
                              Scalars* s, double* partials, unsigned* counter, int kz) {
     const int ni = wt.ni, nj = wt.nj, nk = wt.nk;
@@ -209,31 +238,46 @@ __global__ void build_kernel(FaceView<T> vel, FaceView<T> wt, const T* __restric
             double d = 0.0, b = 0.0;
             T offv[3] = {T(0), T(0), T(0)};  // exactly -weight: no rounding, so in the field type
             if (fluid) {
+                // every load of the row first (a neighbour outside the grid reads the cell itself
+                // and is masked), so that a thread waits for memory once per row
+                const long long s1 = ni, s2 = (long long)ni * nj;
+                const bool inb[6] = {i > 0, i + 1 < ni, j > 0, j + 1 < nj, k > 0, k + 1 < nk};
+                const long long off[6] = {-1, 1, -s1, s1, -s2, s2};
+                uint8_t nf[6];
+                T np[6];
+#pragma unroll
+                for (int f = 0; f < 6; ++f) {
+                    const long long q = inb[f] ? c + off[f] : c;
+                    nf[f] = __ldg(flags + q);
+                    np[f] = __ldg(phi + q);
+                }
                 const T pc = __ldg(phi + c);
-                auto visit = [&](int x, int y, int z, T face_vel, T weight, bool forward, int axis) {
-                    const bool inside = x >= 0 && y >= 0 && z >= 0 && x < ni && y < nj && z < nk;
-                    const long long q = lin3(x, y, z, ni, nj);
-                    if (inside && (__ldg(flags + q) & kFlagPressureValid)) {
-                        const T pn = __ldg(phi + q);
+                const T fv[6] = {vel.U(i, j, k), vel.U(i + 1, j, k), vel.V(i, j, k),
+                                 vel.V(i, j + 1, k), vel.W(i, j, k), vel.W(i, j, k + 1)};
+                const T fw[6] = {wt.U(i, j, k), wt.U(i + 1, j, k), wt.V(i, j, k),
+                                 wt.V(i, j + 1, k), wt.W(i, j, k), wt.W(i, j, k + 1)};
+                // the diagonal's terms (zero for a neighbour that adds none), summed below
+                T dterm[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+#pragma unroll
+                for (int f = 0; f < 6; ++f) {
+                    const T weight = fw[f];
+                    if (inb[f] && (nf[f] & kFlagPressureValid)) {
+                        const T pn = np[f];
                         if (pn < T(0)) {
-                            d = dadd(d, f2d(weight));
-                            if (axis >= 0) offv[axis] = -weight;
+                            dterm[f] = weight;
+                            if (f & 1) offv[f >> 1] = -weight;
                         } else {
                             T theta = fraction_inside(pc, pn);
                             theta = theta < T(0.01) ? T(0.01) : theta;
-                            d = dadd(d, f2d(weight / theta));
+                            dterm[f] = weight / theta;
                         }
                     }
-                    const double prod = f2d(mul_rn(weight, face_vel));
-                    b = forward ? dsub(b, prod) : dadd(b, prod);
-                };
-                visit(i - 1, j, k, vel.U(i, j, k), wt.U(i, j, k), false, -1);
-                visit(i + 1, j, k, vel.U(i + 1, j, k), wt.U(i + 1, j, k), true, 0);
-                visit(i, j - 1, k, vel.V(i, j, k), wt.V(i, j, k), false, -1);
-                visit(i, j + 1, k, vel.V(i, j + 1, k), wt.V(i, j + 1, k), true, 1);
-                visit(i, j, k - 1, vel.W(i, j, k), wt.W(i, j, k), false, -1);
-                visit(i, j, k + 1, vel.W(i, j, k + 1), wt.W(i, j, k + 1), true, 2);
+                    // b: + for the lower face, - for the upper one, in the neighbours' order
+                    const double prod = f2d(mul_rn(weight, fv[f]));
+                    b = (f & 1) ? dsub(b, prod) : dadd(b, prod);
+                }
                 b = dmul(b, f2d(scale));
+                d = diag_sum(dterm);
             }
             if (!EL_IN(c, (long long)ni * nj * nk, 40)) continue;
             o.diag64[c] = d;

@@ -556,11 +556,22 @@ __global__ void jacobi_rz_kernel(LGeom g, SegArg seg, const double* __restrict__
     if (grid_sum<1>(acc, partials, counter, tot)) s->rz = tot[0];
 }
 
+// The iterate as a float pair for the double-float residual (el_df.cuh), written with x by the
+// kernels that change it (xs: null where no double-float residual reads it).  Beyond the pairs'
+// range (|x| >= 2^128, an iterate no FP32 field can hold) the pair is infinite, so that the
+// residual turns non-finite and the solve reports it.
+__device__ __forceinline__ float2 x_pair(double x) {
+    bool ok = true;
+    const F2 p = df_split(x, ok);
+    return ok ? make_float2(p.h, p.l) : make_float2(d2f(x), 0.f);
+}
+
 // solve start (outer / plain): x = 0, r = b on the active segments, thresholds.
 __global__ void solve_init_kernel(LGeom g, SegArg seg, const double* __restrict__ b, double* __restrict__ x,
-                                  double* __restrict__ r, Scalars* s, double tol) {
+                                  float2* __restrict__ xs, double* __restrict__ r, Scalars* s, double tol) {
     SEG_LOOP_BEGIN(seg, g)
     x[c] = 0.0;
+    if (xs) xs[c] = make_float2(0.f, 0.f);
     r[c] = b[c];
     SEG_LOOP_END
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -606,13 +617,16 @@ __global__ void guess_alpha_kernel(LGeom g, SegArg seg, const double* __restrict
 }
 
 // x = alpha g, r = b - alpha A g = (1 - alpha) b + alpha r0, |r|^2 and the stopping test.
-__global__ void guess_scale_kernel(LGeom g, SegArg seg, double* __restrict__ x, const double* __restrict__ b,
-                                   double* __restrict__ r, Scalars* s, double* partials, unsigned* counter) {
+__global__ void guess_scale_kernel(LGeom g, SegArg seg, double* __restrict__ x, float2* __restrict__ xs,
+                                   const double* __restrict__ b, double* __restrict__ r, Scalars* s,
+                                   double* partials, unsigned* counter) {
     const double a = s->aux;
     double acc[1] = {0.0};
     SEG_LOOP_BEGIN(seg, g)
     // a == 0 (a useless or non-finite guess): exactly the zero start, whatever g held
-    x[c] = a != 0.0 ? a * x[c] : 0.0;
+    const double xc = a != 0.0 ? a * x[c] : 0.0;
+    x[c] = xc;
+    if (xs) xs[c] = x_pair(xc);
     const double rc = a != 0.0 ? (1.0 - a) * b[c] + a * r[c] : b[c];
     r[c] = rc;
     acc[0] += rc * rc;
@@ -694,12 +708,14 @@ __global__ void inner_init_kernel(LGeom g, SegArg seg, const double* __restrict_
     }
 }
 
-// mixed solver: x64 += |r| * x32
-__global__ void accumulate_kernel(LGeom g, SegArg seg, double* __restrict__ x64, const float* __restrict__ x32,
-                                  const Scalars* si) {
+// mixed solver: x64 += |r| * x32 (and its float pair)
+__global__ void accumulate_kernel(LGeom g, SegArg seg, double* __restrict__ x64, float2* __restrict__ xs,
+                                  const float* __restrict__ x32, const Scalars* si) {
     const double norm = si->norm;
     SEG_LOOP_BEGIN(seg, g)
-    x64[c] += norm * f2d(x32[c]);
+    const double xn = __fma_rn(norm, f2d(x32[c]), x64[c]);
+    x64[c] = xn;
+    if (xs) xs[c] = x_pair(xn);
     SEG_LOOP_END
 }
 
@@ -738,15 +754,17 @@ __global__ void __launch_bounds__(kSegThreads) residual_kernel(LGeom g, SegArg s
 
 // The mixed solver's refinement residual r = b - A x and |r|^2 for FP32 fields, whose couplings
 // are exact floats: double-float arithmetic on the FP32 pipe (el_df.cuh) in place of the FP64
-// operations, which bound the FP64 kernel above (nine a cell, its FP64 pipe 86 % busy).  b, the
-// diagonal and the iterate are split into float pairs by integer arithmetic; the pair of r is
+// operations, which bound the FP64 kernel above (nine a cell, its FP64 pipe 86 % busy).  The
+// iterate comes as float pairs (xs, written with x); b and the diagonal are split into pairs by
+// integer arithmetic; the pair of r is
 // within 2^-41 of the sum of its row's term magnitudes, and is stored as a double.  A warp in
 // which any operand lies outside the pairs' exponent range (el_df.cuh) takes the FP64
-// arithmetic of the kernel above for all its lanes.  |r|^2 is summed in FP32 per thread (each
+// arithmetic of the kernel above for all its lanes (the splits of b and the diagonal decide).  |r|^2 is summed in FP32 per thread (each
 // takes a few dozen cells; SqAcc keeps every square in range) and in FP64 over the grid.
 __global__ void __launch_bounds__(kSegThreads, 4) residual_df_kernel(LGeom g, SegArg seg, SplitOp<float> A,
                                                                   const double* __restrict__ b,
                                                                   const double* __restrict__ x,
+                                                                  const float2* __restrict__ xs,
                                                                   double* __restrict__ r, Scalars* s,
                                                                   double* partials, unsigned* counter) {
     SqAcc acc2;
@@ -761,18 +779,18 @@ __global__ void __launch_bounds__(kSegThreads, 4) residual_df_kernel(LGeom g, Se
     const float cxp = live ? A.x[c] : 0.f, cyp = live ? A.y[c] : 0.f, czp = live ? A.z[c] : 0.f;
     const float cym = iym ? A.y[c - g.s1] : 0.f, czm = izm ? A.z[c - g.s2] : 0.f;
     const float cxm_e = ixm ? A.x[c - 1] : 0.f;
-    const double x0 = live ? x[c] : 0.0;
-    const double xym = iym ? x[c - g.s1] : 0.0, xyp = iyp ? x[c + g.s1] : 0.0;
-    const double xzm = izm ? x[c - g.s2] : 0.0, xzp = izp ? x[c + g.s2] : 0.0;
-    const double xxm_e = ixm ? x[c - 1] : 0.0, xxp_e = ixp ? x[c + 1] : 0.0;
+    const float2 z2 = make_float2(0.f, 0.f);
+    const float2 q0 = live ? xs[c] : z2;
+    const float2 qym = iym ? xs[c - g.s1] : z2, qyp = iyp ? xs[c + g.s1] : z2;
+    const float2 qzm = izm ? xs[c - g.s2] : z2, qzp = izp ? xs[c + g.s2] : z2;
+    const float2 qxm_e = ixm ? xs[c - 1] : z2, qxp_e = ixp ? xs[c + 1] : z2;
     const bool act = live && d_positive(d);
     const bool xp_in = live && i + 1 < g.n0;
     const float cxm_s = __shfl_up_sync(kFull, cxp, 1);
     const float cxm = lane == 0 ? cxm_e : cxm_s;
+    const F2 p0{q0.x, q0.y}, pym{qym.x, qym.y}, pyp{qyp.x, qyp.y}, pzm{qzm.x, qzm.y}, pzp{qzp.x, qzp.y};
+    const F2 pxm_e{qxm_e.x, qxm_e.y}, pxp_e{qxp_e.x, qxp_e.y};
     bool ok = true;
-    const F2 p0 = df_split(x0, ok);
-    const F2 pym = df_split(xym, ok), pyp = df_split(xyp, ok), pzm = df_split(xzm, ok), pzp = df_split(xzp, ok);
-    const F2 pxm_e = df_split(xxm_e, ok), pxp_e = df_split(xxp_e, ok);
     const F2 pd = df_split(d, ok), pb = df_split(bc, ok);
     F2 pxm, pxp;
     pxm.h = __shfl_up_sync(kFull, p0.h, 1);
@@ -791,7 +809,11 @@ __global__ void __launch_bounds__(kSegThreads, 4) residual_df_kernel(LGeom g, Se
             r[c] = 0.0;
         }
     } else {
-        // the FP64 arithmetic of residual_kernel, for every lane of the warp
+        // the FP64 arithmetic of residual_kernel, for every lane of the warp, on the double iterate
+        const double x0 = live ? x[c] : 0.0;
+        const double xym = iym ? x[c - g.s1] : 0.0, xyp = iyp ? x[c + g.s1] : 0.0;
+        const double xzm = izm ? x[c - g.s2] : 0.0, xzp = izp ? x[c + g.s2] : 0.0;
+        const double xxm_e = ixm ? x[c - 1] : 0.0, xxp_e = ixp ? x[c + 1] : 0.0;
         const double sxm = __shfl_up_sync(kFull, x0, 1), sxp = __shfl_down_sync(kFull, x0, 1);
         if (live) {
             const double vxm = lane == 0 ? xxm_e : sxm;
@@ -1878,6 +1900,7 @@ static void reset_vectors(el_ctx* ctx) {
         if (v) cudaMemsetAsync(v, 0, n * 8, ctx->stream);
     for (float* v : {ctx->x32, ctx->r32, ctx->r32b, ctx->z32, ctx->p32, ctx->p32b, ctx->ap32})
         if (v) cudaMemsetAsync(v, 0, n * 4, ctx->stream);
+    if (ctx->xs) cudaMemsetAsync(ctx->xs, 0, n * 8, ctx->stream);
     for (auto& L : ctx->mg32) {
         const size_t m = (size_t)L.n0 * L.n1 * L.n2 * 4;
         for (float* v : {L.t, L.rec ? L.b : nullptr, L.rec ? L.x : nullptr})
@@ -1895,6 +1918,13 @@ static void mg_restore_pointers(el_ctx* ctx) {
     if (!ctx->mg32.empty()) ctx->mg32[0].b = ctx->r32;
 }
 
+// The float pair of the iterate, kept where the refinement residual is double-float: the mixed
+// solver on FP32 fields (exact float couplings); null otherwise.
+template <typename T>
+static float2* iterate_pairs(el_ctx* ctx, int solver) {
+    return (solver == EL_SOLVER_MIXED && std::is_same<T, float>::value) ? ctx->xs : nullptr;
+}
+
 // The mixed solver's refinement residual: double-float arithmetic for FP32 fields (exact float
 // couplings), FP64 for FP64 fields.
 template <typename T>
@@ -1902,7 +1932,7 @@ static void enqueue_refine_residual(el_ctx* ctx, const LGeom& g, const SplitOp<T
     const int nb = seg_blocks(ctx, ctx->seg0.total);
     if constexpr (std::is_same<T, float>::value)
         residual_df_kernel<<<nb, kSegThreads, 0, ctx->stream>>>(g, seg_arg(ctx->seg0), A64, ctx->rhs64, ctx->x64,
-                                                                ctx->r64, s0, ctx->partials, ctx->counter);
+                                                                ctx->xs, ctx->r64, s0, ctx->partials, ctx->counter);
     else
         residual_kernel<T><<<nb, kSegThreads, 0, ctx->stream>>>(g, seg_arg(ctx->seg0), A64, ctx->rhs64, ctx->x64,
                                                                 ctx->r64, s0, ctx->partials, ctx->counter);
@@ -1930,7 +1960,7 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
     {
         ProfScope prof(ctx, EL_KC_OTHER, na * 24);
         solve_init_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
-            g, seg_arg(ctx->seg0), ctx->rhs64, ctx->x64, ctx->r64, s0, prm.tol);
+            g, seg_arg(ctx->seg0), ctx->rhs64, ctx->x64, iterate_pairs<T>(ctx, prm.solver), ctx->r64, s0, prm.tol);
     }
     ctx->launches += 1;
     if (prm.initial_guess) {
@@ -1943,8 +1973,9 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
                                                                 ctx->r64, s0, ctx->partials, ctx->counter);
         guess_alpha_kernel<<<nb, kSegThreads, 0, ctx->stream>>>(g, seg_arg(ctx->seg0), ctx->x64, ctx->rhs64, ctx->r64,
                                                                 s0, ctx->partials, ctx->counter);
-        guess_scale_kernel<<<nb, kSegThreads, 0, ctx->stream>>>(g, seg_arg(ctx->seg0), ctx->x64, ctx->rhs64, ctx->r64,
-                                                                s0, ctx->partials, ctx->counter);
+        guess_scale_kernel<<<nb, kSegThreads, 0, ctx->stream>>>(g, seg_arg(ctx->seg0), ctx->x64,
+                                                                iterate_pairs<T>(ctx, prm.solver), ctx->rhs64,
+                                                                ctx->r64, s0, ctx->partials, ctx->counter);
         ctx->launches += 4;
     }
     st->outer_iterations = 1;
@@ -2037,7 +2068,7 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
             {
                 ProfScope prof(ctx, EL_KC_OTHER, na * 20);
                 accumulate_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
-                    g, seg_arg(ctx->seg0), ctx->x64, ctx->x32, s1);
+                    g, seg_arg(ctx->seg0), ctx->x64, iterate_pairs<T>(ctx, prm.solver), ctx->x32, s1);
             }
             {
                 // reads x, b, diag (f64), 3 couplings; writes r (f64)
@@ -2156,7 +2187,7 @@ static int enqueue_solve_device_t(el_ctx* ctx, const el_solve_params& prm, int k
         g, ctx->diag64, ctx->seg0.total, ctx->seg0.flags);
     nk += 1 + enqueue_compact(ctx, ctx->seg0, g);
     solve_init_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
-        g, seg_arg(ctx->seg0), ctx->rhs64, ctx->x64, ctx->r64, s0, prm.tol);
+        g, seg_arg(ctx->seg0), ctx->rhs64, ctx->x64, iterate_pairs<T>(ctx, EL_SOLVER_MIXED), ctx->r64, s0, prm.tol);
     if (!ctx->records_fresh) {
         pack32_kernel<T><<<grid1d(ctx, n), 256, 0, ctx->stream>>>(n, ctx->diag64, A64.x, A64.y, A64.z, ctx->A32,
                                                                   ctx->A16);
@@ -2201,7 +2232,7 @@ static int enqueue_solve_device_t(el_ctx* ctx, const el_solve_params& prm, int k
     inner_cond_kernel<<<1, 1, 0, ctx->stream>>>(h_inner, s0, s1, prm.max_iter, 1);
     rc = end_while(ctx, parent_inner);
     accumulate_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
-        g, seg_arg(ctx->seg0), ctx->x64, ctx->x32, s1);
+        g, seg_arg(ctx->seg0), ctx->x64, iterate_pairs<T>(ctx, EL_SOLVER_MIXED), ctx->x32, s1);
     enqueue_refine_residual(ctx, g, A64, s0);
     outer_cond_kernel<<<1, 1, 0, ctx->stream>>>(h_outer, s0, s1, max_outer, prm.max_iter, 1);
     const int rc2 = end_while(ctx, parent_outer);
@@ -2279,10 +2310,11 @@ int setup_solver_storage(el_ctx* ctx, int solver) {
         ctx->p32b = (float*)ctx_alloc(ctx, n * 4);
         ctx->ap32 = (float*)ctx_alloc(ctx, n * 4);
         ctx->r32b = (float*)ctx_alloc(ctx, n * 4);
+        ctx->xs = (float2*)ctx_alloc(ctx, n * sizeof(float2));
         ctx->A32 = (float4*)ctx_alloc(ctx, n * sizeof(float4));
         ctx->A16 = (ushort4*)ctx_alloc(ctx, n * sizeof(ushort4));
         if (!ctx->x32 || !ctx->r32 || !ctx->r32b || !ctx->z32 || !ctx->p32 || !ctx->p32b || !ctx->ap32 || !ctx->A32 ||
-            !ctx->A16)
+            !ctx->A16 || !ctx->xs)
             return set_error(ctx, EL_ERR_OUT_OF_MEMORY, "mixed solver vectors");
         int rc = build_hierarchy<float>(ctx, ctx->mg32, sizeof(float4));
         if (rc != EL_OK) return rc;

@@ -6,6 +6,8 @@ no contraction), inputs and outputs passed as hexadecimal floats.
   significant bits, both of d's sign; below 2^-103 the nearest float and zero; the range flag
   cleared exactly from 2^128 on (and for NaN);
 * the positivity test by integer comparison, for the special values;
+* the exact integer sum of six floats: bit-identical to the sequential double additions from zero
+  whenever it answers, and answering whenever the terms lie within 2^26 of one another;
 * the seven-point residual b - A x for Poisson-like rows whose terms cancel to a small residual:
   within 2^-41 of the sum of the terms' magnitudes (the bound the header states), and the
   typical error far below it.
@@ -39,6 +41,17 @@ int main() {
             bool ok = true;
             const F2 p = df_split(d, ok);
             std::printf("%a %a %d\n", (double)p.h, (double)p.l, ok ? 1 : 0);
+        } else if (!std::strcmp(mode, "sum6")) {
+            float t[6];
+            for (float& q : t) q = (float)rd();
+            double out = -1.0;
+            const bool ok = exact_sum6(t[0], t[1], t[2], t[3], t[4], t[5], out);
+            double seq = 0.0;
+            for (float q : t) seq = seq + (double)q;
+            unsigned long long a, b;
+            std::memcpy(&a, &out, 8);
+            std::memcpy(&b, &seq, 8);
+            std::printf("%d %d\n", ok ? 1 : 0, (ok && a != b) ? 1 : 0);
         } else if (!std::strcmp(mode, "pos")) {
             const double d = rd();
             std::printf("%d\n", d_positive(d) ? 1 : 0);
@@ -182,3 +195,35 @@ def test_residual7(run):
             worst = max(worst, err / mag)
     # in practice the splits' truncation dominates: well inside the stated bound
     assert worst < Fraction(1, 2 ** 44), float(worst)
+
+
+def test_exact_sum6(run):
+    rng = random.Random(3)
+    cases = []
+    for _ in range(20000):
+        base = rng.randint(-140, 120)
+        spread = rng.choice((0, 3, 10, 26, 27, 30, 60))
+        t = []
+        for _ in range(6):
+            r = rng.random()
+            if r < 0.15:
+                t.append(0.0 if rng.random() < 0.5 else -0.0)
+            else:
+                e = base - rng.randint(0, spread)
+                v = f32(math.ldexp(rng.uniform(1.0, 2.0), e))
+                t.append(v if rng.random() < 0.7 else -v)
+        cases.append(t)
+    cases += [[1.0] * 6, [0.0] * 6, [-0.0] * 6, [1.0, -1.0, 0.0, 0.0, 0.0, 0.0], [1e-45] * 6,
+              [float("inf"), 1.0, 0.0, 0.0, 0.0, 0.0], [3e38] * 6]
+    out = run(["sum6 " + " ".join(float(q).hex() for q in t) for t in cases])
+    answered = 0
+    for t, line in zip(cases, out):
+        ok, bad = (int(q) for q in line.split())
+        assert bad == 0, t
+        nz = [abs(q) for q in t if q != 0.0]
+        if nz and all(math.isfinite(q) for q in nz):
+            es = [max(math.frexp(q)[1], -125) for q in nz]
+            if max(es) - min(es) <= 26:
+                assert ok == 1, t
+        answered += ok
+    assert answered > len(cases) // 2
