@@ -134,9 +134,7 @@ __device__ __forceinline__ void velocity_at(const Mac<T>& m, T x, T y, T z, T dx
 // trace_rk2 (ode.h:30-35) or Ralston RK3 (c = 0, 1/2, 3/4; b = 2/9, 1/3, 4/9); h is the
 // signed step (-dt for a backtrace).
 template <typename T, int TRACE>
-__device__ __forceinline__ void backtrace(const Mac<T>& m, T& x, T& y, T& z, T h, T dx, T inv) {
-    T ax, ay, az;
-    velocity_at(m, x, y, z, dx, inv, ax, ay, az);
+__device__ __forceinline__ void backtrace_from(const Mac<T>& m, T ax, T ay, T az, T& x, T& y, T& z, T h, T dx, T inv) {
     const T h2 = T(0.5) * h;
     T bx, by, bz;
     velocity_at(m, x + h2 * ax, y + h2 * ay, z + h2 * az, dx, inv, bx, by, bz);
@@ -153,6 +151,27 @@ __device__ __forceinline__ void backtrace(const Mac<T>& m, T& x, T& y, T& z, T h
         y = y + w1 * ay + w2 * by + w3 * cy;
         z = z + w1 * az + w2 * bz + w3 * cz;
     }
+}
+
+template <typename T, int TRACE>
+__device__ __forceinline__ void backtrace(const Mac<T>& m, T& x, T& y, T& z, T h, T dx, T inv) {
+    T ax, ay, az;
+    velocity_at(m, x, y, z, dx, inv, ax, ay, az);
+    backtrace_from<T, TRACE>(m, ax, ay, az, x, y, z, h, dx, inv);
+}
+
+// The velocity at the centre of cell (i, j, k), the first stage of a level-set backtrace: the
+// trilinear read there has fractions 1/2 along a component's own axis and 0 along the others,
+// so each component is the mean of its two faces (a zero fraction leaves its first value).
+// Exact fractions where index_fraction of the rounded cell position may carry a rounding error
+// of an ulp or so.  The faces of a cell are inside every grid (no clamping).
+template <typename T>
+__device__ __forceinline__ void cell_velocity(const Mac<T>& m, int i, int j, int k, T& vx, T& vy, T& vz) {
+    const long long cu = lin3(i, j, k, m.u.n0, m.u.n1), cv = lin3(i, j, k, m.v.n0, m.v.n1);
+    const long long cw = lin3(i, j, k, m.w.n0, m.w.n1);
+    vx = lerp1(__ldg(m.u.d + cu), __ldg(m.u.d + cu + 1), T(0.5));
+    vy = lerp1(__ldg(m.v.d + cv), __ldg(m.v.d + cv + m.v.n0), T(0.5));
+    vz = lerp1(__ldg(m.w.d + cw), __ldg(m.w.d + cw + (long long)m.w.n0 * m.w.n1), T(0.5));
 }
 
 // out(x) = src(trace(x, -dt)) for every sample of src's grid (cell centres or one face
@@ -281,12 +300,11 @@ __device__ __forceinline__ void velocity_at_staged(const Mac<T>& m, const Staged
     if (!staged_lerp<T, CHECK>(s.w.box, xc, yc, zf, vz) && CHECK) vz = sample_trilinear(m.w, x, y, z, dx, inv);
 }
 
-// backtrace with the staged velocity: the same stages and arithmetic as backtrace()
+// backtrace with the staged velocity: the same stages and arithmetic as backtrace(), from the
+// first stage's velocity (ax, ay, az) at (x, y, z)
 template <typename T, int TRACE, bool CHECK = true>
-__device__ __forceinline__ void backtrace_staged(const Mac<T>& m, const StagedMac<T>& sm, T& x, T& y, T& z, T h, T dx,
-                                                 T inv) {
-    T ax, ay, az;
-    velocity_at_staged<T, CHECK>(m, sm, x, y, z, dx, inv, ax, ay, az);
+__device__ __forceinline__ void backtrace_staged_from(const Mac<T>& m, const StagedMac<T>& sm, T ax, T ay, T az, T& x,
+                                                      T& y, T& z, T h, T dx, T inv) {
     const T h2 = T(0.5) * h;
     T bx, by, bz;
     velocity_at_staged<T, CHECK>(m, sm, x + h2 * ax, y + h2 * ay, z + h2 * az, dx, inv, bx, by, bz);
@@ -302,6 +320,48 @@ __device__ __forceinline__ void backtrace_staged(const Mac<T>& m, const StagedMa
         x = x + w1 * ax + w2 * bx + w3 * cx;
         y = y + w1 * ay + w2 * by + w3 * cy;
         z = z + w1 * az + w2 * bz + w3 * cz;
+    }
+}
+
+template <typename T, int TRACE, bool CHECK = true>
+__device__ __forceinline__ void backtrace_staged(const Mac<T>& m, const StagedMac<T>& sm, T& x, T& y, T& z, T h, T dx,
+                                                 T inv) {
+    T ax, ay, az;
+    velocity_at_staged<T, CHECK>(m, sm, x, y, z, dx, inv, ax, ay, az);
+    backtrace_staged_from<T, TRACE, CHECK>(m, sm, ax, ay, az, x, y, z, h, dx, inv);
+}
+
+// The velocity at the centre of a face of component c, the first stage of its backtrace: the
+// trilinear read there has fractions 0 and 1/2 only, so it is the face's own value and the
+// four-point means of the two other components, in the trilinear read's order (x, then y, then
+// z; a zero fraction leaves its first value).  Exact fractions where index_fraction of the
+// rounded face position may carry a rounding error of an ulp or so.  Every point lies in the
+// staged boxes (their halos are at least one entry), which hold the clamped grid.
+template <typename T>
+__device__ __forceinline__ T box_at(const Staged<T>& b, int I, int J, int K) {
+    return b.box[(K * kBoxY + J) * kBoxX + I];
+}
+
+template <typename T>
+__device__ __forceinline__ T mid4(T a, T b, T c, T d) {
+    return lerp1(lerp1(a, b, T(0.5)), lerp1(c, d, T(0.5)), T(0.5));
+}
+
+template <typename T>
+__device__ __forceinline__ void face_velocity(const StagedMac<T>& s, int c, int i, int j, int k, T& vx, T& vy, T& vz) {
+    const int I = i - s.u.bx0, J = j - s.u.by0, K = k - s.u.bz0;
+    if (c == 0) {
+        vx = box_at(s.u, I, J, K);
+        vy = mid4(box_at(s.v, I - 1, J, K), box_at(s.v, I, J, K), box_at(s.v, I - 1, J + 1, K), box_at(s.v, I, J + 1, K));
+        vz = mid4(box_at(s.w, I - 1, J, K), box_at(s.w, I, J, K), box_at(s.w, I - 1, J, K + 1), box_at(s.w, I, J, K + 1));
+    } else if (c == 1) {
+        vx = mid4(box_at(s.u, I, J - 1, K), box_at(s.u, I + 1, J - 1, K), box_at(s.u, I, J, K), box_at(s.u, I + 1, J, K));
+        vy = box_at(s.v, I, J, K);
+        vz = mid4(box_at(s.w, I, J - 1, K), box_at(s.w, I, J, K), box_at(s.w, I, J - 1, K + 1), box_at(s.w, I, J, K + 1));
+    } else {
+        vx = mid4(box_at(s.u, I, J, K - 1), box_at(s.u, I + 1, J, K - 1), box_at(s.u, I, J, K), box_at(s.u, I + 1, J, K));
+        vy = mid4(box_at(s.v, I, J, K - 1), box_at(s.v, I, J + 1, K - 1), box_at(s.v, I, J, K), box_at(s.v, I, J + 1, K));
+        vz = box_at(s.w, I, J, K);
     }
 }
 
@@ -489,7 +549,9 @@ __device__ __forceinline__ void velocity_tile(const Mac<T>& mac, const StagedMac
             T x = (i + T(0.5)) * dx + g.ox;
             T y = (j + T(0.5)) * dx + g.oy;
             T z = (k + T(0.5)) * dx + g.oz;
-            backtrace_staged<T, TRACE, CHECK>(mac, sm, x, y, z, h, dx, inv_dx);
+            T ax, ay, az;
+            face_velocity(sm, c, i, j, k, ax, ay, az);
+            backtrace_staged_from<T, TRACE, CHECK>(mac, sm, ax, ay, az, x, y, z, h, dx, inv_dx);
             const long long oc = lin3(i, j, k, g.n0, g.n1);
             const T r = sample_staged<T, CHECK>(g, b, x, y, z, dx, inv_dx);
             if (EL_IN(oc, (long long)g.n0 * g.n1 * g.n2, 2)) o[oc] = r;
@@ -551,10 +613,12 @@ __global__ void __launch_bounds__(kTileX * kTileY) advect_phi_tiled_kernel(GridV
         T x = (i + T(0.5)) * dx + src.ox;
         T y = (j + T(0.5)) * dx + src.oy;
         T z = (k + T(0.5)) * dx + src.oz;
+        T ax, ay, az;
+        cell_velocity(mac, i, j, k, ax, ay, az);
         if (inside)
-            backtrace_staged<T, TRACE, false>(mac, sm, x, y, z, h, dx, inv_dx);
+            backtrace_staged_from<T, TRACE, false>(mac, sm, ax, ay, az, x, y, z, h, dx, inv_dx);
         else
-            backtrace_staged<T, TRACE, true>(mac, sm, x, y, z, h, dx, inv_dx);
+            backtrace_staged_from<T, TRACE, true>(mac, sm, ax, ay, az, x, y, z, h, dx, inv_dx);
         T r;
         if constexpr (SAMPLE == EL_SAMPLE_WENO6)
             r = sample_weno6(src, x, y, z, dx, inv_dx);
@@ -646,7 +710,9 @@ __global__ void __launch_bounds__(kWX * kWY, sizeof(T) == 4 ? 2 : 1)
         T x = (i + T(0.5)) * dx + src.ox;
         T y = (j + T(0.5)) * dx + src.oy;
         T z = (k + T(0.5)) * dx + src.oz;
-        backtrace<T, TRACE>(mac, x, y, z, h, dx, inv_dx);
+        T ax, ay, az;
+        cell_velocity(mac, i, j, k, ax, ay, az);
+        backtrace_from<T, TRACE>(mac, ax, ay, az, x, y, z, h, dx, inv_dx);
         // stencil origin (floor - 2) relative to the box, per axis
         const AxisPos<T> px = axis_pos(x, src.ox, x0 - 1, dx, inv_dx);
         const AxisPos<T> py = axis_pos(y, src.oy, y0 - 1, dx, inv_dx);
