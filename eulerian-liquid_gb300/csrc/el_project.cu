@@ -385,31 +385,41 @@ __global__ void scatter_pressure_kernel(long long n, const double* __restrict__ 
 // update_velocity_using_pressure (projection.cpp:93-134): faces with index in [1, n) along
 // their normal and [1, n-1) along the two tangential axes, as the reference's loops.
 template <typename T>
-__global__ void update_velocity_kernel(int ni, int nj, int nk, T* __restrict__ f, int comp,
-                                       const T* __restrict__ p, const T* __restrict__ phi, T dx,
-                                       const Scalars* s, double dt_value, int kz) {
+__device__ __forceinline__ void update_face(int ni, int nj, int comp, int i, int j, int k, T* __restrict__ f,
+                                            const T* __restrict__ p, const T* __restrict__ phi, T dt, T dx) {
+    const long long b = lin3(i, j, k, ni, nj);
+    const long long a = comp == 0 ? b - 1 : (comp == 1 ? b - ni : b - (long long)ni * nj);
+    const T pb = __ldg(phi + b), pa = __ldg(phi + a);
+    if (pb < T(0) || pa < T(0)) {
+        T theta = T(1);
+        if (pb >= T(0) || pa >= T(0)) theta = fraction_inside(pa, pb);
+        theta = theta < T(0.01) ? T(0.01) : theta;
+        const T num = mul_rn(dt, __ldg(p + b) - __ldg(p + a));
+        const T den = mul_rn(dx, theta);
+        const long long fi = lin3(i, j, k, ni + (comp == 0), nj + (comp == 1));
+        f[fi] = f[fi] - num / den;
+    }
+}
+
+// The three components in one launch: a thread takes the faces u, v and w at (i, j, k) down a
+// column, each within its component's range, so that the pressure and the level set are read
+// once for all three (their neighbouring cells' values come from L1).
+template <typename T>
+__global__ void update_velocity3_kernel(int ni, int nj, int nk, T* __restrict__ u, T* __restrict__ v,
+                                        T* __restrict__ w, const T* __restrict__ p, const T* __restrict__ phi, T dx,
+                                        const Scalars* s, double dt_value, int kz) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int ei = comp == 0 ? ni : ni - 1, ej = comp == 1 ? nj : nj - 1, ek = comp == 2 ? nk : nk - 1;
-    if (i >= ei || j >= ej) return;
+    if (i >= ni || j >= nj) return;
     const T dt = (T)(s ? s->dt : dt_value);
-    const int f0 = ni + (comp == 0), f1 = nj + (comp == 1);
-    // a column of kz faces per thread (independent: the loads of several are in flight)
-#pragma unroll 4
+#pragma unroll 2
     for (int kk = 0; kk < kz; ++kk) {
         const int k = blockIdx.z * kz + kk + 1;
-        if (k >= ek) break;
-        const long long b = lin3(i, j, k, ni, nj);
-        const long long a = comp == 0 ? b - 1 : (comp == 1 ? b - ni : b - (long long)ni * nj);
-        if (phi[b] < T(0) || phi[a] < T(0)) {
-            T theta = T(1);
-            if (phi[b] >= T(0) || phi[a] >= T(0)) theta = fraction_inside(phi[a], phi[b]);
-            theta = theta < T(0.01) ? T(0.01) : theta;
-            const T num = mul_rn(dt, p[b] - p[a]);
-            const T den = mul_rn(dx, theta);
-            const long long fi = lin3(i, j, k, f0, f1);
-            f[fi] = f[fi] - num / den;
-        }
+        if (k >= nk) break;
+        // u: i in [1, ni), j in [1, nj - 1), k in [1, nk - 1); v and w likewise
+        if (j < nj - 1 && k < nk - 1) update_face(ni, nj, 0, i, j, k, u, p, phi, dt, dx);
+        if (i < ni - 1 && k < nk - 1) update_face(ni, nj, 1, i, j, k, v, p, phi, dt, dx);
+        if (i < ni - 1 && j < nj - 1) update_face(ni, nj, 2, i, j, k, w, p, phi, dt, dx);
     }
 }
 
@@ -511,21 +521,14 @@ int launch_scatter_pressure(el_ctx* ctx) {
 template <typename T>
 static int launch_update_velocity_t(el_ctx* ctx, const Scalars* s, double dtv) {
     const int ni = ctx->ni, nj = ctx->nj, nk = ctx->nk;
+    if (ni <= 1 || nj <= 1 || nk <= 1) return 0;
     dim3 block(32, 8, 1);
     constexpr int kz = 8;
-    const T* p = (const T*)ctx->field[EL_FIELD_PRESSURE];
-    const T* phi = (const T*)ctx->field[EL_FIELD_PHI];
-    const T dx = (T)ctx->dx;
-    int launched = 0;
-    for (int comp = 0; comp < 3; ++comp) {
-        const int ei = comp == 0 ? ni : ni - 1, ej = comp == 1 ? nj : nj - 1, ek = comp == 2 ? nk : nk - 1;
-        if (ei <= 1 || ej <= 1 || ek <= 1) continue;
-        dim3 grid = plane_grid(ei - 1, ej - 1, (ek - 1 + kz - 1) / kz, block);
-        update_velocity_kernel<T><<<grid, block, 0, ctx->stream>>>(
-            ni, nj, nk, (T*)ctx->field[EL_FIELD_U + comp], comp, p, phi, dx, s, dtv, kz);
-        ++launched;
-    }
-    return launched;
+    dim3 grid = plane_grid(ni - 1, nj - 1, (nk - 1 + kz - 1) / kz, block);
+    update_velocity3_kernel<T><<<grid, block, 0, ctx->stream>>>(
+        ni, nj, nk, (T*)ctx->field[EL_FIELD_U], (T*)ctx->field[EL_FIELD_V], (T*)ctx->field[EL_FIELD_W],
+        (const T*)ctx->field[EL_FIELD_PRESSURE], (const T*)ctx->field[EL_FIELD_PHI], (T)ctx->dx, s, dtv, kz);
+    return 1;
 }
 
 int launch_update_velocity(el_ctx* ctx, const Scalars* s, double dtv) {

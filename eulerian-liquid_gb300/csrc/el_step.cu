@@ -16,36 +16,51 @@ __device__ __forceinline__ float add_rn2(float a, float b) { return __fadd_rn(a,
 __device__ __forceinline__ double add_rn2(double a, double b) { return __dadd_rn(a, b); }
 
 // ---------------------------------------------------------------------------------------
-// add_gravity + find_valid_velocity + set_invalid_velocity_zero, fused per face component
+// add_gravity + find_valid_velocity + set_invalid_velocity_zero, fused per face
 // (simulator.cpp:90-93, 125-158, 169-178).  The phi test applies on faces with index in
 // [1, n) along the normal and [1, n-1) along the tangential axes, as the reference's loops.
+// The three components in one launch: a thread takes the faces u, v and w at (i, j, k) down a
+// column, so that the level set is read once for all three (its values for the neighbouring
+// faces come from L1).
 template <typename T>
-__global__ void masks_kernel(int ni, int nj, int nk, int comp, T* __restrict__ f, const T* __restrict__ wt,
-                             const T* __restrict__ phi, uint8_t* __restrict__ valid, int apply_gravity,
-                             T gravity, const Scalars* s, double dt_value, int zero_invalid, int kz) {
-    const int f0 = ni + (comp == 0), f1 = nj + (comp == 1), f2 = nk + (comp == 2);
+__device__ __forceinline__ void mask_face(int ni, int nj, int nk, int comp, int i, int j, int k, T* __restrict__ f,
+                                          const T* __restrict__ wt, const T* __restrict__ phi,
+                                          uint8_t* __restrict__ valid, bool gravity, T gdt, bool zero_invalid) {
+    const int f0 = ni + (comp == 0), f1 = nj + (comp == 1);
+    const int ei = comp == 0 ? ni : ni - 1, ej = comp == 1 ? nj : nj - 1, ek = comp == 2 ? nk : nk - 1;
+    const long long fi = lin3(i, j, k, f0, f1);
+    T val = f[fi];
+    if (gravity) val = val - gdt;
+    bool ok = __ldg(wt + fi) != T(0);
+    if (ok && i >= 1 && j >= 1 && k >= 1 && i < ei && j < ej && k < ek) {
+        const long long b = lin3(i, j, k, ni, nj);
+        const long long a = comp == 0 ? b - 1 : (comp == 1 ? b - ni : b - (long long)ni * nj);
+        if (__ldg(phi + a) >= T(0) && __ldg(phi + b) >= T(0)) ok = false;
+    }
+    valid[fi] = ok ? 1 : 0;
+    if (zero_invalid && !ok) val = T(0);
+    if (gravity || (zero_invalid && !ok)) f[fi] = val;
+}
+
+template <typename T>
+__global__ void masks3_kernel(int ni, int nj, int nk, T* __restrict__ u, T* __restrict__ v, T* __restrict__ w,
+                              const T* __restrict__ wu, const T* __restrict__ wv, const T* __restrict__ ww,
+                              const T* __restrict__ phi, uint8_t* __restrict__ mu, uint8_t* __restrict__ mv,
+                              uint8_t* __restrict__ mw, int apply_gravity, T gravity, const Scalars* s,
+                              double dt_value, int zero_invalid, int kz) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= f0 || j >= f1) return;
+    if (i > ni || j > nj) return;
     const T dt = apply_gravity ? (T)(s ? s->dt : dt_value) : T(0);
-    const int ei = comp == 0 ? ni : ni - 1, ej = comp == 1 ? nj : nj - 1, ek = comp == 2 ? nk : nk - 1;
-    // a column of kz faces per thread (independent: the loads of several are in flight)
-#pragma unroll 4
+    const T gdt = mul_rn2(gravity, dt);  // the product each face subtracts (one rounding)
+    const bool zero = zero_invalid != 0;
+#pragma unroll 2
     for (int kk = 0; kk < kz; ++kk) {
         const int k = blockIdx.z * kz + kk;
-        if (k >= f2) break;
-        const long long fi = lin3(i, j, k, f0, f1);
-        T val = f[fi];
-        if (apply_gravity) val = val - mul_rn2(gravity, dt);
-        bool ok = wt[fi] != T(0);
-        if (ok && i >= 1 && j >= 1 && k >= 1 && i < ei && j < ej && k < ek) {
-            const long long b = lin3(i, j, k, ni, nj);
-            const long long a = comp == 0 ? b - 1 : (comp == 1 ? b - ni : b - (long long)ni * nj);
-            if (phi[a] >= T(0) && phi[b] >= T(0)) ok = false;
-        }
-        valid[fi] = ok ? 1 : 0;
-        if (zero_invalid && !ok) val = T(0);
-        if (apply_gravity || (zero_invalid && !ok)) f[fi] = val;
+        if (k > nk) break;
+        if (j < nj && k < nk) mask_face(ni, nj, nk, 0, i, j, k, u, wu, phi, mu, false, gdt, zero);
+        if (i < ni && k < nk) mask_face(ni, nj, nk, 1, i, j, k, v, wv, phi, mv, apply_gravity != 0, gdt, zero);
+        if (i < ni && j < nj) mask_face(ni, nj, nk, 2, i, j, k, w, ww, phi, mw, false, gdt, zero);
     }
 }
 
@@ -213,16 +228,18 @@ template <typename T>
 static int launch_masks_t(el_ctx* ctx, bool gravity, double g, const Scalars* s, double dtv, bool zero) {
     dim3 block(32, 8, 1);
     constexpr int kz = 8;
-    for (int comp = 0; comp < 3; ++comp) {
-        int n0, n1, n2;
-        field_dims(ctx, EL_FIELD_U + comp, n0, n1, n2);
-        masks_kernel<T><<<pgrid(n0, n1, (n2 + kz - 1) / kz, block), block, 0, ctx->stream>>>(
-            ctx->ni, ctx->nj, ctx->nk, comp, (T*)ctx->field[EL_FIELD_U + comp],
-            (const T*)ctx->field[EL_FIELD_WEIGHT_U + comp], (const T*)ctx->field[EL_FIELD_PHI],
-            (uint8_t*)ctx->field[EL_FIELD_VALID_U + comp], (gravity && comp == 1) ? 1 : 0, (T)g, s, dtv,
-            zero ? 1 : 0, kz);
+    T* f[3];
+    const T* wt[3];
+    uint8_t* m[3];
+    for (int c = 0; c < 3; ++c) {
+        f[c] = (T*)ctx->field[EL_FIELD_U + c];
+        wt[c] = (const T*)ctx->field[EL_FIELD_WEIGHT_U + c];
+        m[c] = (uint8_t*)ctx->field[EL_FIELD_VALID_U + c];
     }
-    return 3;
+    masks3_kernel<T><<<pgrid(ctx->ni + 1, ctx->nj + 1, (ctx->nk + 1 + kz - 1) / kz, block), block, 0, ctx->stream>>>(
+        ctx->ni, ctx->nj, ctx->nk, f[0], f[1], f[2], wt[0], wt[1], wt[2], (const T*)ctx->field[EL_FIELD_PHI], m[0], m[1],
+        m[2], gravity ? 1 : 0, (T)g, s, dtv, zero ? 1 : 0, kz);
+    return 1;
 }
 
 int launch_masks(el_ctx* ctx, bool gravity, double g, const Scalars* s, double dtv, bool zero) {
