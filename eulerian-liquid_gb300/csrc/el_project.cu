@@ -384,26 +384,23 @@ __global__ void scatter_pressure_kernel(long long n, const double* __restrict__ 
 
 // update_velocity_using_pressure (projection.cpp:93-134): faces with index in [1, n) along
 // their normal and [1, n-1) along the two tangential axes, as the reference's loops.
+// one face given the level set and pressure of its two cells (a: below, b: above)
 template <typename T>
-__device__ __forceinline__ void update_face(int ni, int nj, int comp, int i, int j, int k, T* __restrict__ f,
-                                            const T* __restrict__ p, const T* __restrict__ phi, T dt, T dx) {
-    const long long b = lin3(i, j, k, ni, nj);
-    const long long a = comp == 0 ? b - 1 : (comp == 1 ? b - ni : b - (long long)ni * nj);
-    const T pb = __ldg(phi + b), pa = __ldg(phi + a);
+__device__ __forceinline__ void update_face(T pa, T pb, T qa, T qb, long long fi, T* __restrict__ f, T dt, T dx) {
     if (pb < T(0) || pa < T(0)) {
         T theta = T(1);
         if (pb >= T(0) || pa >= T(0)) theta = fraction_inside(pa, pb);
         theta = theta < T(0.01) ? T(0.01) : theta;
-        const T num = mul_rn(dt, __ldg(p + b) - __ldg(p + a));
+        const T num = mul_rn(dt, qb - qa);
         const T den = mul_rn(dx, theta);
-        const long long fi = lin3(i, j, k, ni + (comp == 0), nj + (comp == 1));
         f[fi] = f[fi] - num / den;
     }
 }
 
 // The three components in one launch: a thread takes the faces u, v and w at (i, j, k) down a
 // column, each within its component's range, so that the pressure and the level set are read
-// once for all three (their neighbouring cells' values come from L1).
+// once for all three (their neighbouring cells' values come from L1); the loads of a cell's
+// faces are issued together.
 template <typename T>
 __global__ void update_velocity3_kernel(int ni, int nj, int nk, T* __restrict__ u, T* __restrict__ v,
                                         T* __restrict__ w, const T* __restrict__ p, const T* __restrict__ phi, T dx,
@@ -412,14 +409,21 @@ __global__ void update_velocity3_kernel(int ni, int nj, int nk, T* __restrict__ 
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (i >= ni || j >= nj) return;
     const T dt = (T)(s ? s->dt : dt_value);
+    const long long plane = (long long)ni * nj;
 #pragma unroll 2
     for (int kk = 0; kk < kz; ++kk) {
         const int k = blockIdx.z * kz + kk + 1;
         if (k >= nk) break;
         // u: i in [1, ni), j in [1, nj - 1), k in [1, nk - 1); v and w likewise
-        if (j < nj - 1 && k < nk - 1) update_face(ni, nj, 0, i, j, k, u, p, phi, dt, dx);
-        if (i < ni - 1 && k < nk - 1) update_face(ni, nj, 1, i, j, k, v, p, phi, dt, dx);
-        if (i < ni - 1 && j < nj - 1) update_face(ni, nj, 2, i, j, k, w, p, phi, dt, dx);
+        const bool hu = j < nj - 1 && k < nk - 1, hv = i < ni - 1 && k < nk - 1, hw = i < ni - 1 && j < nj - 1;
+        const long long b = lin3(i, j, k, ni, nj);
+        const T pc = __ldg(phi + b), qc = __ldg(p + b);
+        const T pxm = hu ? __ldg(phi + b - 1) : T(0), qxm = hu ? __ldg(p + b - 1) : T(0);
+        const T pym = hv ? __ldg(phi + b - ni) : T(0), qym = hv ? __ldg(p + b - ni) : T(0);
+        const T pzm = hw ? __ldg(phi + b - plane) : T(0), qzm = hw ? __ldg(p + b - plane) : T(0);
+        if (hu) update_face(pxm, pc, qxm, qc, lin3(i, j, k, ni + 1, nj), u, dt, dx);
+        if (hv) update_face(pym, pc, qym, qc, lin3(i, j, k, ni, nj + 1), v, dt, dx);
+        if (hw) update_face(pzm, pc, qzm, qc, lin3(i, j, k, ni, nj), w, dt, dx);
     }
 }
 

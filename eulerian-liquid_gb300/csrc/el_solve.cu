@@ -182,13 +182,23 @@ __global__ void seg_flags_diag_kernel(LGeom g, const double* __restrict__ diag, 
     const int lane = threadIdx.x & 31;
     const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long id = w0; id < total; id += nw) {
-        int i, j, k;
-        seg_cell((int)id, g, lane, i, j, k);
-        bool act = false;
-        if (i < g.n0) act = d_positive(diag[i + g.s1 * j + g.s2 * k]);
-        const unsigned m = __ballot_sync(0xffffffffu, act);
-        if (lane == 0) flags[id] = m ? 1 : 0;
+    // four segments a warp per pass, their loads in flight together
+    constexpr int U = 4;
+    for (long long id0 = w0; id0 < total; id0 += U * nw) {
+        bool act[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long long id = id0 + u * nw;
+            int i, j, k;
+            seg_cell((int)id, g, lane, i, j, k);
+            act[u] = id < total && i < g.n0 && d_positive(diag[i + g.s1 * j + g.s2 * k]);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long long id = id0 + u * nw;
+            const unsigned m = __ballot_sync(0xffffffffu, act[u]);
+            if (lane == 0 && id < total) flags[id] = m ? 1 : 0;
+        }
     }
 }
 

@@ -22,21 +22,14 @@ __device__ __forceinline__ double add_rn2(double a, double b) { return __dadd_rn
 // The three components in one launch: a thread takes the faces u, v and w at (i, j, k) down a
 // column, so that the level set is read once for all three (its values for the neighbouring
 // faces come from L1).
+// One face after its loads: gravity, the mask (weight nonzero and, on the faces the phi test
+// covers, not both cells outside the liquid), the invalid value zeroed.
 template <typename T>
-__device__ __forceinline__ void mask_face(int ni, int nj, int nk, int comp, int i, int j, int k, T* __restrict__ f,
-                                          const T* __restrict__ wt, const T* __restrict__ phi,
+__device__ __forceinline__ void mask_face(T val, T wt, bool tested, T pa, T pb, long long fi, T* __restrict__ f,
                                           uint8_t* __restrict__ valid, bool gravity, T gdt, bool zero_invalid) {
-    const int f0 = ni + (comp == 0), f1 = nj + (comp == 1);
-    const int ei = comp == 0 ? ni : ni - 1, ej = comp == 1 ? nj : nj - 1, ek = comp == 2 ? nk : nk - 1;
-    const long long fi = lin3(i, j, k, f0, f1);
-    T val = f[fi];
     if (gravity) val = val - gdt;
-    bool ok = __ldg(wt + fi) != T(0);
-    if (ok && i >= 1 && j >= 1 && k >= 1 && i < ei && j < ej && k < ek) {
-        const long long b = lin3(i, j, k, ni, nj);
-        const long long a = comp == 0 ? b - 1 : (comp == 1 ? b - ni : b - (long long)ni * nj);
-        if (__ldg(phi + a) >= T(0) && __ldg(phi + b) >= T(0)) ok = false;
-    }
+    bool ok = wt != T(0);
+    if (ok && tested && pa >= T(0) && pb >= T(0)) ok = false;
     valid[fi] = ok ? 1 : 0;
     if (zero_invalid && !ok) val = T(0);
     if (gravity || (zero_invalid && !ok)) f[fi] = val;
@@ -54,13 +47,29 @@ __global__ void masks3_kernel(int ni, int nj, int nk, T* __restrict__ u, T* __re
     const T dt = apply_gravity ? (T)(s ? s->dt : dt_value) : T(0);
     const T gdt = mul_rn2(gravity, dt);  // the product each face subtracts (one rounding)
     const bool zero = zero_invalid != 0;
+    const long long plane = (long long)ni * nj;
 #pragma unroll 2
     for (int kk = 0; kk < kz; ++kk) {
         const int k = blockIdx.z * kz + kk;
         if (k > nk) break;
-        if (j < nj && k < nk) mask_face(ni, nj, nk, 0, i, j, k, u, wu, phi, mu, false, gdt, zero);
-        if (i < ni && k < nk) mask_face(ni, nj, nk, 1, i, j, k, v, wv, phi, mv, apply_gravity != 0, gdt, zero);
-        if (i < ni && j < nj) mask_face(ni, nj, nk, 2, i, j, k, w, ww, phi, mw, false, gdt, zero);
+        // the faces u, v, w at (i, j, k) that exist, and which of them the phi test covers
+        // (index in [1, n) along the normal, [1, n - 1) along the tangential axes)
+        const bool hu = j < nj && k < nk, hv = i < ni && k < nk, hw = i < ni && j < nj;
+        const bool low = i >= 1 && j >= 1 && k >= 1;
+        const bool tu = low && i < ni && j < nj - 1 && k < nk - 1;
+        const bool tv = low && i < ni - 1 && j < nj && k < nk - 1;
+        const bool tw = low && i < ni - 1 && j < nj - 1 && k < nk;
+        const long long fu = lin3(i, j, k, ni + 1, nj), fv = lin3(i, j, k, ni, nj + 1), fw = lin3(i, j, k, ni, nj);
+        const long long b = fw;  // the cell (i, j, k), inside the grid wherever a test reads it
+        // every load first
+        const T u0 = hu ? u[fu] : T(0), v0 = hv ? v[fv] : T(0), w0 = hw ? w[fw] : T(0);
+        const T wu0 = hu ? __ldg(wu + fu) : T(0), wv0 = hv ? __ldg(wv + fv) : T(0), ww0 = hw ? __ldg(ww + fw) : T(0);
+        const T pc = (tu || tv || tw) ? __ldg(phi + b) : T(0);
+        const T pxm = tu ? __ldg(phi + b - 1) : T(0), pym = tv ? __ldg(phi + b - ni) : T(0);
+        const T pzm = tw ? __ldg(phi + b - plane) : T(0);
+        if (hu) mask_face(u0, wu0, tu, pxm, pc, fu, u, mu, false, gdt, zero);
+        if (hv) mask_face(v0, wv0, tv, pym, pc, fv, v, mv, apply_gravity != 0, gdt, zero);
+        if (hw) mask_face(w0, ww0, tw, pzm, pc, fw, w, mw, false, gdt, zero);
     }
 }
 
