@@ -658,6 +658,12 @@ __global__ void guess_scale_kernel(LGeom g, SegArg seg, double* __restrict__ x, 
 // bound of these kernels) on every cell, switched off or not.
 __device__ __noinline__ float scale_fp64(double r, double inv) { return (float)(r * inv); }
 
+// |r| and 1 / |r| from |r|^2
+__device__ __noinline__ double2 scale_from_norm(double rr) {
+    const double norm = sqrt(rr);
+    return make_double2(norm, norm > 0.0 ? 1.0 / norm : 0.0);
+}
+
 __device__ __noinline__ double residual_cell_fp64(double bc, double d, double x0, float cxm, double vxm, float cxp,
                                                   double vxp, float cym, double xym, float cyp, double xyp,
                                                   float czm, double xzm, float czp, double xzp) {
@@ -687,20 +693,41 @@ __global__ void inner_init_kernel(LGeom g, SegArg seg, const double* __restrict_
         inv = __longlong_as_double((long long)(1023 - k) << 52);
         invf = __int_as_float((127 - k) << 23);
     } else {
-        norm = sqrt(rr);
-        inv = norm > 0.0 ? 1.0 / norm : 0.0;
+        const double2 ni = scale_from_norm(rr);
+        norm = ni.x;
+        inv = ni.y;
         invf = 0.f;
     }
     float part = 0.f;
-    SEG_LOOP_BEGIN(seg, g)
-    const double rc = r64[c];
-    bool ok = pow2;
-    const F2 q = df_split(rc, ok);
-    const float v = ok ? df_fma(q.h, invf, df_mul(q.l, invf)) : scale_fp64(rc, inv);
-    r32[c] = v;
-    x32[c] = 0.0f;
-    part += v * v;
-    SEG_LOOP_END
+    // four segments a warp per pass, their loads in flight together (one load a cell)
+    const int lane = threadIdx.x & 31;
+    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const int nseg = *seg.count;
+    constexpr int U = 4;
+    for (int q0 = wg; q0 < nseg; q0 += U * nw) {
+        int cc[U];
+        bool lv[U];
+        double rc[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int qs = q0 + u * nw;
+            const int4 sd = qs < nseg ? seg.desc[qs] : make_int4(0, g.n0, 0, 0);
+            cc[u] = sd.x + lane;
+            lv[u] = qs < nseg && sd.y + lane < g.n0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) rc[u] = lv[u] ? r64[cc[u]] : 0.0;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (!lv[u]) continue;
+            bool ok = pow2;
+            const F2 q = df_split(rc[u], ok);
+            const float v = ok ? df_fma(q.h, invf, df_mul(q.l, invf)) : scale_fp64(rc[u], inv);
+            r32[cc[u]] = v;
+            x32[cc[u]] = 0.0f;
+            part += v * v;
+        }
+    }
     double acc[1] = {(double)part};
     double tot[1];
     if (grid_sum<1>(acc, partials, counter, tot)) {

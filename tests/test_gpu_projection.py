@@ -75,6 +75,42 @@ def test_assign_indices_and_build_matrix_bitexact(el, orc, dtype, n):
 
 
 @pytest.mark.parametrize("dtype", DTYPES)
+def test_build_matrix_wide_weight_range_bitexact(el, orc, dtype):
+    """Face weights spread over forty binades (1, 2^-10, 2^-30, 2^-40 times U(0.1, 1), and zero):
+    a row's diagonal terms then lie too far apart in exponent for the build's exact integer sum
+    in many rows, which take the FP64 additions instead; every row, and the rhs's double sums
+    of products of such weights, still equal the oracle's build."""
+    n = 20
+    spec = _spec(n)
+    phi, _, wts = scene_fields(orc, spec, dtype)
+    rng = np.random.default_rng(31)
+    wide = []
+    for a in wts:
+        scale = rng.choice([1.0, 2.0 ** -10, 2.0 ** -30, 2.0 ** -40, 0.0], size=a.shape,
+                           p=[0.55, 0.15, 0.1, 0.1, 0.1])
+        wide.append((rng.uniform(0.1, 1.0, a.shape) * scale).astype(dtype))
+    u, v, w = _velocity(orc, wts, dtype, 5)
+    sim = make_sim(el, n, dtype, spec)
+    for f, a in zip(("weight_u", "weight_v", "weight_w", "u", "v", "w"), (*wide, u, v, w)):
+        sim.upload(f, a)
+    dt = 0.013
+    got = sim.build_matrix(dt)
+    want = orc.build_matrix(phi, u, v, w, *wide, sim.dx, dt)
+    for g, r, name in zip(got, want, ("diag", "offx", "offy", "offz", "rhs")):
+        np.testing.assert_array_equal(g, r, err_msg=name)
+    # the build the mixed solver runs (which also writes its FP32 / FP16 records) gives the same
+    # system; the solve itself may stall on so ill-conditioned a matrix, which is not the point
+    try:
+        sim.solve_pressure(dt, solver=el.SOLVER_MIXED, tol=1e-3, max_iter=50)
+    except RuntimeError:
+        pass
+    got = sim.matrix()
+    for g, r, name in zip(got, want, ("diag", "offx", "offy", "offz", "rhs")):
+        np.testing.assert_array_equal(g, r, err_msg=name)
+    sim.close()
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
 def test_rebuild_after_the_fluid_moves_bitexact(el, orc, dtype):
     """Consecutive builds where the fluid region shrinks, moves and grows again: the build only
     rewrites rows that are or were nonzero, and every row (the zero ones included) still equals
