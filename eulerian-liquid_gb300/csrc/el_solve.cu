@@ -220,25 +220,36 @@ __global__ void seg_count_kernel(const uint8_t* __restrict__ flags, long long to
     }
 }
 
+// Exclusive scan of the chunk counts in one block of 1024 threads: each thread sums a span of
+// chunks, the span sums are scanned by warp shuffles (within a warp, then over the 32 warp
+// totals), and each thread rewrites its span with running offsets.
 __global__ void seg_scan_kernel(int* __restrict__ chunk, int nchunks, int* __restrict__ total_out) {
-    __shared__ int span[1024];
+    __shared__ int wsum[32];
     const int per = (nchunks + blockDim.x - 1) / blockDim.x;
     const int lo = threadIdx.x * per, hi = min(nchunks, lo + per);
     int s = 0;
     for (int q = lo; q < hi; ++q) s += chunk[q];
-    span[threadIdx.x] = s;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int x = s;  // inclusive scan within the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(kFull, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        int run = 0;
-        for (int t = 0; t < (int)blockDim.x; ++t) {
-            const int v = span[t];
-            span[t] = run;
-            run += v;
+    if (w == 0) {
+        int v = lane < nw ? wsum[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(kFull, v, o);
+            if (lane >= o) v += y;
         }
-        *total_out = run;
+        wsum[lane] = v;  // inclusive over the warps
     }
     __syncthreads();
-    int run = span[threadIdx.x];
+    int run = x - s + (w > 0 ? wsum[w - 1] : 0);
+    if (threadIdx.x == blockDim.x - 1) *total_out = run + s;
     for (int q = lo; q < hi; ++q) {
         const int v = chunk[q];
         chunk[q] = run;
@@ -246,15 +257,28 @@ __global__ void seg_scan_kernel(int* __restrict__ chunk, int nchunks, int* __res
     }
 }
 
+// The descriptors of a chunk's active segments, in order: each warp of the block takes an equal
+// run of the chunk's flags, counts its active ones, and writes them after the counts of the
+// warps before it.
 __global__ void seg_write_kernel(LGeom g, const uint8_t* __restrict__ flags, long long total,
                                  const int* __restrict__ chunk, int4* __restrict__ desc) {
-    const long long base = (long long)blockIdx.x * kSegChunk;
-    const int lane = threadIdx.x;
+    __shared__ int wcount[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int span = kSegChunk / nw;
+    const long long wb = (long long)blockIdx.x * kSegChunk + (long long)w * span;
+    int cnt = 0;
+    for (int q = 0; q < span; q += 32) {
+        const long long id = wb + q + lane;
+        cnt += __popc(__ballot_sync(kFull, id < total && flags[id]));
+    }
+    if (lane == 0) wcount[w] = cnt;
+    __syncthreads();
     int run = chunk[blockIdx.x];
-    for (int q = 0; q < kSegChunk; q += 32) {
-        const long long id = base + q + lane;
+    for (int v = 0; v < w; ++v) run += wcount[v];
+    for (int q = 0; q < span; q += 32) {
+        const long long id = wb + q + lane;
         const bool f = id < total && flags[id];
-        const unsigned m = __ballot_sync(0xffffffffu, f);
+        const unsigned m = __ballot_sync(kFull, f);
         if (f) {
             int i0, j, k;
             seg_cell((int)id, g, 0, i0, j, k);
@@ -1516,7 +1540,7 @@ static int enqueue_compact(el_ctx* ctx, SegList& l, const LGeom& g) {
     const int nchunks = (int)((l.total + kSegChunk - 1) / kSegChunk);
     seg_count_kernel<<<nchunks, 256, 0, ctx->stream>>>(l.flags, l.total, l.chunk);
     seg_scan_kernel<<<1, 1024, 0, ctx->stream>>>(l.chunk, nchunks, l.count);
-    seg_write_kernel<<<nchunks, 32, 0, ctx->stream>>>(g, l.flags, l.total, l.chunk, l.desc);
+    seg_write_kernel<<<nchunks, 256, 0, ctx->stream>>>(g, l.flags, l.total, l.chunk, l.desc);
     return 3;
 }
 
