@@ -410,7 +410,7 @@ __global__ void update_velocity3_kernel(int ni, int nj, int nk, T* __restrict__ 
     if (i >= ni || j >= nj) return;
     const T dt = (T)(s ? s->dt : dt_value);
     const long long plane = (long long)ni * nj;
-#pragma unroll 2
+#pragma unroll
     for (int kk = 0; kk < kz; ++kk) {
         const int k = blockIdx.z * kz + kk + 1;
         if (k >= nk) break;

@@ -48,7 +48,7 @@ __global__ void masks3_kernel(int ni, int nj, int nk, T* __restrict__ u, T* __re
     const T gdt = mul_rn2(gravity, dt);  // the product each face subtracts (one rounding)
     const bool zero = zero_invalid != 0;
     const long long plane = (long long)ni * nj;
-#pragma unroll 2
+#pragma unroll
     for (int kk = 0; kk < kz; ++kk) {
         const int k = blockIdx.z * kz + kk;
         if (k > nk) break;
