@@ -148,7 +148,7 @@ __global__ void flags_kernel(FaceView<T> wt, const T* __restrict__ phi, uint8_t*
     const int ni = wt.ni, nj = wt.nj, nk = wt.nk;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    double cnt[1] = {0.0};
+    int count = 0;  // an integer: one FP64 addition a cell was most of this kernel's FP64 pipe time
     if (i < ni && j < nj) {
         // a contiguous chunk of planes per block: the neighbour planes come from L1
         const int k_end = min(nk, (int)(blockIdx.z + 1) * kz);
@@ -161,9 +161,10 @@ __global__ void flags_kernel(FaceView<T> wt, const T* __restrict__ phi, uint8_t*
             const bool pv = w0 > T(0) || w1 > T(0) || w2 > T(0) || w3 > T(0) || w4 > T(0) || w5 > T(0);
             const bool fl = pv && pc < T(0);
             flags[c] = (pv ? kFlagPressureValid : 0) | (fl ? kFlagFluid : 0);
-            cnt[0] += fl ? 1.0 : 0.0;
+            count += fl ? 1 : 0;
         }
     }
+    double cnt[1] = {(double)count};
     double tot[1];
     if (grid_sum<1>(cnt, partials, counter, tot)) s->count = (int)tot[0];
 }
