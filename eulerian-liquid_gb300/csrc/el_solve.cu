@@ -1992,8 +1992,9 @@ template <typename T>
 static void enqueue_refine_residual(el_ctx* ctx, const LGeom& g, const SplitOp<T>& A64, Scalars* s0) {
     const int nb = seg_blocks(ctx, ctx->seg0.total);
     if constexpr (std::is_same<T, float>::value)
-        residual_df_kernel<<<nb, kSegThreads, 0, ctx->stream>>>(g, seg_arg(ctx->seg0), A64, ctx->rhs64, ctx->x64,
-                                                                ctx->xs, ctx->r64, s0, ctx->partials, ctx->counter);
+        // the resident four CTAs per SM (its launch bounds) in one wave: 102 -> 94 us at 256^3
+        residual_df_kernel<<<std::min(nb, ctx->num_sms * 4), kSegThreads, 0, ctx->stream>>>(
+            g, seg_arg(ctx->seg0), A64, ctx->rhs64, ctx->x64, ctx->xs, ctx->r64, s0, ctx->partials, ctx->counter);
     else
         residual_kernel<T><<<nb, kSegThreads, 0, ctx->stream>>>(g, seg_arg(ctx->seg0), A64, ctx->rhs64, ctx->x64,
                                                                 ctx->r64, s0, ctx->partials, ctx->counter);
