@@ -13,6 +13,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <unordered_map>
 #include <utility>
 #include <vector>
 
@@ -286,6 +287,8 @@ struct el_ctx {
     // while profiling: cells covered by the active segments of each multigrid level of the
     // current solve (read back once per solve), for the byte counts of the segment kernels
     std::vector<double> prof_active;
+    // resident CTAs per SM of the kernels launched through one_wave(), by kernel
+    std::unordered_map<const void*, int> resident;
 };
 
 namespace el {
@@ -305,6 +308,24 @@ cudaError_t launch_dependent(const el_ctx* ctx, void (*kernel)(KArgs...), dim3 g
     cfg.attrs = attr;
     cfg.numAttrs = ctx->dependent_launch ? 1 : 0;
     return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+// A grid of `want` blocks of `threads` (no dynamic shared memory) capped at one wave of the
+// kernel's resident CTAs, for grid-stride kernels whose work per warp does not depend on the
+// grid: a second, partial wave only lengthens the tail.
+template <typename... KArgs>
+int one_wave(el_ctx* ctx, void (*kernel)(KArgs...), int threads, int want) {
+    const void* key = reinterpret_cast<const void*>(kernel);
+    auto it = ctx->resident.find(key);
+    int per_sm = 0;
+    if (it == ctx->resident.end()) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        ctx->resident.emplace(key, per_sm);
+    } else {
+        per_sm = it->second;
+    }
+    return std::max(1, std::min(want, ctx->num_sms * per_sm));
 }
 }  // namespace el
 

@@ -1613,7 +1613,8 @@ static void launch_smooth(el_ctx* ctx, const MGLevel<V>& F, const SegList& seg, 
                           V* x_out, Scalars* s) {
     const LGeom g = make_geom(F.n0, F.n1, F.n2);
     const LGeom gc = C ? make_geom(C->n0, C->n1, C->n2) : g;
-    launch_dependent(ctx, smooth_kernel<V, R, MODE, DOT>, dim3(seg_blocks(ctx, seg.total)), dim3(kSegThreads), 0, g,
+    const int blocks = one_wave(ctx, smooth_kernel<V, R, MODE, DOT>, kSegThreads, seg_blocks(ctx, seg.total));
+    launch_dependent(ctx, smooth_kernel<V, R, MODE, DOT>, dim3(blocks), dim3(kSegThreads), 0, g,
                      seg_arg(seg), (const R*)F.rec, (const V*)F.b, x_in, gc, C ? (const V*)C->x : (const V*)nullptr,
                      x_out, s, ctx->partials, ctx->counter);
 }
@@ -1714,7 +1715,9 @@ static int enqueue_vcycle(el_ctx* ctx, std::vector<MGLevel<V>>& mg, const SegLis
                 restrict_kernel<V, R0><<<restrict_blocks(ctx, C.seg.total), kSegThreads, 0, ctx->stream>>>(
                     gf, (const R0*)F.rec, F.b, F.x, gc, seg_arg(C.seg), C.b, s);
             else
-                launch_dependent(ctx, restrict_quad_kernel<V, RC>, dim3(seg_blocks(ctx, 4 * C.seg.total)),
+                launch_dependent(ctx, restrict_quad_kernel<V, RC>,
+                                 dim3(one_wave(ctx, restrict_quad_kernel<V, RC>, kSegThreads,
+                                               seg_blocks(ctx, 4 * C.seg.total))),
                                  dim3(kSegThreads), 0, gf, (const RC*)F.rec, (const V*)F.b, (const V*)F.x, gc,
                                  seg_arg(C.seg), C.b, (const Scalars*)s);
         }
