@@ -179,25 +179,29 @@ __global__ void seg_flags_rec_kernel(LGeom g, const R* __restrict__ rec, long lo
 
 __global__ void seg_flags_diag_kernel(LGeom g, const double* __restrict__ diag, long long total,
                                       uint8_t* __restrict__ flags) {
+    // a warp per row (j, k): one index division a row, not one a segment, and up to eight of
+    // the row's segments in flight together; segment id = row * nsr + segment of the row
+    (void)total;
     const int lane = threadIdx.x & 31;
     const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-    // four segments a warp per pass, their loads in flight together
-    constexpr int U = 4;
-    for (long long id0 = w0; id0 < total; id0 += U * nw) {
-        bool act[U];
+    const long long nrows = (long long)g.n1 * g.n2;
+    constexpr int U = 8;
+    for (long long row = w0; row < nrows; row += nw) {
+        const int j = (int)(row % g.n1), k = (int)(row / g.n1);
+        const double* drow = diag + (long long)g.s1 * j + (long long)g.s2 * k;
+        for (int s0 = 0; s0 < g.nsr; s0 += U) {
+            bool act[U];
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const long long id = id0 + u * nw;
-            int i, j, k;
-            seg_cell((int)id, g, lane, i, j, k);
-            act[u] = id < total && i < g.n0 && d_positive(diag[i + g.s1 * j + g.s2 * k]);
-        }
+            for (int u = 0; u < U; ++u) {
+                const int i = (s0 + u) * 32 + lane;
+                act[u] = s0 + u < g.nsr && i < g.n0 && d_positive(drow[i]);
+            }
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const long long id = id0 + u * nw;
-            const unsigned m = __ballot_sync(0xffffffffu, act[u]);
-            if (lane == 0 && id < total) flags[id] = m ? 1 : 0;
+            for (int u = 0; u < U; ++u) {
+                const unsigned m = __ballot_sync(0xffffffffu, act[u]);
+                if (lane == 0 && s0 + u < g.nsr) flags[row * g.nsr + s0 + u] = m ? 1 : 0;
+            }
         }
     }
 }
