@@ -727,21 +727,34 @@ __global__ void __launch_bounds__(kWX * kWY, sizeof(T) == 4 ? 2 : 1)
             for (int dk = 0; dk < 6; ++dk) {
                 const int row0 = (pz.a + dk) * kWBY + py.a;
                 T yl[6];
+                if constexpr (sizeof(T) == 4) {
+                    // FP32: the x-passes of rows dj and dj + 1 together in packed float2
+                    // arithmetic (two lanes per FMA instruction, each lane rounded as a scalar
+                    // FMA), the same expressions as weno6_combine
 #pragma unroll
-                for (int dj = 0; dj < 6; ++dj) {
-                    const int row = row0 + dj;
-                    const T* v = pb + row * kWBX + px.a;
-                    const T* q = qbox + row * kWBases + px.a;
-                    T qa, qb;
-                    if constexpr (sizeof(T) == 4) {
-                        const float2 qab = reinterpret_cast<const float2*>(qbox)[row * kWBases + px.a];
-                        qa = qab.x;
-                        qb = qab.y;
-                    } else {
-                        qa = q[0];
-                        qb = q[kWQ];
+                    for (int dj = 0; dj < 6; dj += 2) {
+                        const int row = row0 + dj;
+                        const float* va = pb + row * kWBX + px.a;
+                        const float* vb = va + kWBX;
+                        const float2 qa2 = reinterpret_cast<const float2*>(qbox)[row * kWBases + px.a];
+                        const float2 qb2 = reinterpret_cast<const float2*>(qbox)[(row + 1) * kWBases + px.a];
+                        const float* qc = qbox + 2 * kWQ + row * kWBases + px.a;
+                        float2 v[6];
+#pragma unroll
+                        for (int m = 0; m < 6; ++m) v[m] = make_float2(va[m], vb[m]);
+                        const float2 r = weno6_combine2(wx, v, make_float2(qa2.x, qb2.x), make_float2(qa2.y, qb2.y),
+                                                        make_float2(qc[0], qc[kWBases]));
+                        yl[dj] = r.x;
+                        yl[dj + 1] = r.y;
                     }
-                    yl[dj] = weno6_combine(wx, v[0], v[1], v[2], v[3], v[4], v[5], qa, qb, q[2 * kWQ]);
+                } else {
+#pragma unroll
+                    for (int dj = 0; dj < 6; ++dj) {
+                        const int row = row0 + dj;
+                        const T* v = pb + row * kWBX + px.a;
+                        const T* q = qbox + row * kWBases + px.a;
+                        yl[dj] = weno6_combine(wx, v[0], v[1], v[2], v[3], v[4], v[5], q[0], q[kWQ], q[2 * kWQ]);
+                    }
                 }
                 const T zv = weno6_eval(wy, yl[0], yl[1], yl[2], yl[3], yl[4], yl[5]);
                 zl[0] = dk == 0 ? zv : zl[0];

@@ -682,6 +682,26 @@ __device__ __forceinline__ T weno6_combine(const WenoAxis<T>& w, T v0, T v1, T v
     }
 }
 
+// weno6_combine for two FP32 passes at once (lanes .x and .y) in packed float2 arithmetic:
+// the candidates as FMA chains from the first product, the nonlinear combination
+// (aa pa + ab pb + ac pc) / (aa + ab + ac), each lane rounded as its scalar operations
+__device__ __forceinline__ float2 weno6_combine2(const WenoAxis<float>& w, const float2 (&v)[6], float2 qa, float2 qb,
+                                                 float2 qc) {
+    auto b2 = [](float x) { return make_float2(x, x); };
+    float2 p[3];
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+        float2 t = __fmul2_rn(b2(w.L[s][0]), v[s]);
+        t = __ffma2_rn(b2(w.L[s][1]), v[s + 1], t);
+        t = __ffma2_rn(b2(w.L[s][2]), v[s + 2], t);
+        p[s] = __ffma2_rn(b2(w.L[s][3]), v[s + 3], t);
+    }
+    const float2 aa = __fmul2_rn(b2(w.C[0]), qa), ab = __fmul2_rn(b2(w.C[1]), qb), ac = __fmul2_rn(b2(w.C[2]), qc);
+    const float2 num = __ffma2_rn(ac, p[2], __ffma2_rn(ab, p[1], __fmul2_rn(aa, p[0])));
+    const float2 den = __fadd2_rn(__fadd2_rn(aa, ab), ac);
+    return make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y));
+}
+
 template <typename T>
 __device__ __forceinline__ T weno6_eval(const WenoAxis<T>& w, T v0, T v1, T v2, T v3, T v4, T v5) {
     T qa, qb, qc;
