@@ -686,18 +686,36 @@ __global__ void __launch_bounds__(kWX * kWY, sizeof(T) == 4 ? 2 : 1)
         }
     }
     __syncthreads();
-    for (int e = tid; e < kWQ; e += kWX * kWY) {
-        const int row = e / kWBases, b = e - row * kWBases;
-        const T* v = pb + row * kWBX + b;
-        T qa, qb, qc;
-        weno6_sq(v[0], v[1], v[2], v[3], v[4], v[5], qa, qb, qc);
-        if constexpr (sizeof(T) == 4) {
-            reinterpret_cast<float2*>(qbox)[e] = make_float2(qa, qb);  // one 8-byte load for both
-        } else {
+    if constexpr (sizeof(T) == 4) {
+        // two (row, floor index) entries a thread per pass in packed float2 arithmetic
+        constexpr int kStep = kWX * kWY;
+        for (int e0 = tid; e0 < kWQ; e0 += 2 * kStep) {
+            const int e1 = e0 + kStep < kWQ ? e0 + kStep : e0;  // the tail repeats its first entry
+            const int r0 = e0 / kWBases, r1 = e1 / kWBases;
+            const float* va = pb + r0 * kWBX + (e0 - r0 * kWBases);
+            const float* vb = pb + r1 * kWBX + (e1 - r1 * kWBases);
+            float2 v[6];
+#pragma unroll
+            for (int m = 0; m < 6; ++m) v[m] = make_float2(va[m], vb[m]);
+            float2 qa, qb, qc;
+            weno6_sq2(v, qa, qb, qc);
+            reinterpret_cast<float2*>(qbox)[e0] = make_float2(qa.x, qb.x);  // one 8-byte load for both
+            qbox[2 * kWQ + e0] = qc.x;
+            if (e1 != e0) {
+                reinterpret_cast<float2*>(qbox)[e1] = make_float2(qa.y, qb.y);
+                qbox[2 * kWQ + e1] = qc.y;
+            }
+        }
+    } else {
+        for (int e = tid; e < kWQ; e += kWX * kWY) {
+            const int row = e / kWBases, b = e - row * kWBases;
+            const T* v = pb + row * kWBX + b;
+            T qa, qb, qc;
+            weno6_sq(v[0], v[1], v[2], v[3], v[4], v[5], qa, qb, qc);
             qbox[e] = qa;
             qbox[kWQ + e] = qb;
+            qbox[2 * kWQ + e] = qc;
         }
-        qbox[2 * kWQ + e] = qc;
     }
     __syncthreads();
     const int i = x0 + threadIdx.x, j = y0 + threadIdx.y;
@@ -723,38 +741,53 @@ __global__ void __launch_bounds__(kWX * kWY, sizeof(T) == 4 ? 2 : 1)
             const WenoAxis<T> wx = weno_axis(px.f);
             const WenoAxis<T> wy = weno_axis(py.f);
             T zl[6];
+            if constexpr (sizeof(T) == 4) {
+                // FP32: packed float2 arithmetic (two lanes per instruction, each rounded as its
+                // scalar operation): the x-passes of rows dj and dj + 1, and the y-passes of
+                // planes dk and dk + 1, together; the expressions of weno6_combine / weno6_eval
+#pragma unroll
+                for (int dk = 0; dk < 6; dk += 2) {
+                    float2 yl2[6];  // .x: plane dk, .y: plane dk + 1
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int row0 = (pz.a + dk + h) * kWBY + py.a;
+#pragma unroll
+                        for (int dj = 0; dj < 6; dj += 2) {
+                            const int row = row0 + dj;
+                            const float* va = pb + row * kWBX + px.a;
+                            const float* vb = va + kWBX;
+                            const float2 qa2 = reinterpret_cast<const float2*>(qbox)[row * kWBases + px.a];
+                            const float2 qb2 = reinterpret_cast<const float2*>(qbox)[(row + 1) * kWBases + px.a];
+                            const float* qc = qbox + 2 * kWQ + row * kWBases + px.a;
+                            float2 v[6];
+#pragma unroll
+                            for (int m = 0; m < 6; ++m) v[m] = make_float2(va[m], vb[m]);
+                            const float2 rr = weno6_combine2(wx, v, make_float2(qa2.x, qb2.x),
+                                                             make_float2(qa2.y, qb2.y), make_float2(qc[0], qc[kWBases]));
+                            if (h == 0) {
+                                yl2[dj].x = rr.x;
+                                yl2[dj + 1].x = rr.y;
+                            } else {
+                                yl2[dj].y = rr.x;
+                                yl2[dj + 1].y = rr.y;
+                            }
+                        }
+                    }
+                    const float2 zv = weno6_eval2(wy, yl2);
+                    zl[dk] = zv.x;
+                    zl[dk + 1] = zv.y;
+                }
+            } else {
 #pragma unroll
             for (int dk = 0; dk < 6; ++dk) {
                 const int row0 = (pz.a + dk) * kWBY + py.a;
                 T yl[6];
-                if constexpr (sizeof(T) == 4) {
-                    // FP32: the x-passes of rows dj and dj + 1 together in packed float2
-                    // arithmetic (two lanes per FMA instruction, each lane rounded as a scalar
-                    // FMA), the same expressions as weno6_combine
 #pragma unroll
-                    for (int dj = 0; dj < 6; dj += 2) {
-                        const int row = row0 + dj;
-                        const float* va = pb + row * kWBX + px.a;
-                        const float* vb = va + kWBX;
-                        const float2 qa2 = reinterpret_cast<const float2*>(qbox)[row * kWBases + px.a];
-                        const float2 qb2 = reinterpret_cast<const float2*>(qbox)[(row + 1) * kWBases + px.a];
-                        const float* qc = qbox + 2 * kWQ + row * kWBases + px.a;
-                        float2 v[6];
-#pragma unroll
-                        for (int m = 0; m < 6; ++m) v[m] = make_float2(va[m], vb[m]);
-                        const float2 r = weno6_combine2(wx, v, make_float2(qa2.x, qb2.x), make_float2(qa2.y, qb2.y),
-                                                        make_float2(qc[0], qc[kWBases]));
-                        yl[dj] = r.x;
-                        yl[dj + 1] = r.y;
-                    }
-                } else {
-#pragma unroll
-                    for (int dj = 0; dj < 6; ++dj) {
-                        const int row = row0 + dj;
-                        const T* v = pb + row * kWBX + px.a;
-                        const T* q = qbox + row * kWBases + px.a;
-                        yl[dj] = weno6_combine(wx, v[0], v[1], v[2], v[3], v[4], v[5], q[0], q[kWQ], q[2 * kWQ]);
-                    }
+                for (int dj = 0; dj < 6; ++dj) {
+                    const int row = row0 + dj;
+                    const T* v = pb + row * kWBX + px.a;
+                    const T* q = qbox + row * kWBases + px.a;
+                    yl[dj] = weno6_combine(wx, v[0], v[1], v[2], v[3], v[4], v[5], q[0], q[kWQ], q[2 * kWQ]);
                 }
                 const T zv = weno6_eval(wy, yl[0], yl[1], yl[2], yl[3], yl[4], yl[5]);
                 zl[0] = dk == 0 ? zv : zl[0];
@@ -763,6 +796,7 @@ __global__ void __launch_bounds__(kWX * kWY, sizeof(T) == 4 ? 2 : 1)
                 zl[3] = dk == 3 ? zv : zl[3];
                 zl[4] = dk == 4 ? zv : zl[4];
                 zl[5] = dk == 5 ? zv : zl[5];
+            }
             }
             r = weno6_eval(weno_axis(pz.f), zl[0], zl[1], zl[2], zl[3], zl[4], zl[5]);
         } else {

@@ -702,6 +702,38 @@ __device__ __forceinline__ float2 weno6_combine2(const WenoAxis<float>& w, const
     return make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y));
 }
 
+// weno6_sq for two FP32 passes at once in packed float2 arithmetic (the reciprocals per lane)
+__device__ __forceinline__ void weno6_sq2(const float2 (&v)[6], float2& qa, float2& qb, float2& qc) {
+    auto b2 = [](float x) { return make_float2(x, x); };
+    float2 d[6];
+#pragma unroll
+    for (int m = 1; m < 6; ++m) d[m] = __fadd2_rn(v[m], make_float2(-v[m - 1].x, -v[m - 1].y));  // exact negation
+    const float2 k = b2(1.0f / 180.0f);
+    auto form = [&](float2 a, float2 b, float2 c, float ca, float cb, float cc, float cbb, float cbc, float ccc) {
+        // (a (ca a + cb b + cc c) + b (cbb b + cbc c) + ccc c c) k
+        const float2 t1 = __ffma2_rn(b2(cc), c, __ffma2_rn(b2(cb), b, __fmul2_rn(b2(ca), a)));
+        const float2 t2 = __ffma2_rn(b2(cbc), c, __fmul2_rn(b2(cbb), b));
+        float2 t = __ffma2_rn(b, t2, __fmul2_rn(a, t1));
+        t = __ffma2_rn(__fmul2_rn(b2(ccc), c), c, t);
+        return __fmul2_rn(t, k);
+    };
+    const float2 ia = form(d[1], d[2], d[3], 244.f, -1171.f, 683.f, 1561.f, -1951.f, 814.f);
+    const float2 ib = form(d[2], d[3], d[4], 244.f, -781.f, 293.f, 961.f, -781.f, 244.f);
+    const float2 ic = form(d[3], d[4], d[5], 814.f, -1951.f, 683.f, 1561.f, -1171.f, 244.f);
+    const float2 eps = b2(1e-6f);
+    const float2 sa = __fadd2_rn(eps, ia), sb = __fadd2_rn(eps, ib), sc = __fadd2_rn(eps, ic);
+    const float2 sa2 = __fmul2_rn(sa, sa), sb2 = __fmul2_rn(sb, sb), sc2 = __fmul2_rn(sc, sc);
+    qa = make_float2(__fdividef(1.f, sa2.x), __fdividef(1.f, sa2.y));
+    qb = make_float2(__fdividef(1.f, sb2.x), __fdividef(1.f, sb2.y));
+    qc = make_float2(__fdividef(1.f, sc2.x), __fdividef(1.f, sc2.y));
+}
+
+__device__ __forceinline__ float2 weno6_eval2(const WenoAxis<float>& w, const float2 (&v)[6]) {
+    float2 qa, qb, qc;
+    weno6_sq2(v, qa, qb, qc);
+    return weno6_combine2(w, v, qa, qb, qc);
+}
+
 template <typename T>
 __device__ __forceinline__ T weno6_eval(const WenoAxis<T>& w, T v0, T v1, T v2, T v3, T v4, T v5) {
     T qa, qb, qc;
