@@ -75,6 +75,29 @@ __device__ __forceinline__ void axis_index(T pos, T origin, T dx, T inv_dx, int&
     floor_index(t, idx, frac);
 }
 
+// axis_index of one coordinate against two origins; FP32 in packed float2 arithmetic, the same
+// operations as axis_index and floor_index lane by lane
+template <typename T>
+__device__ __forceinline__ void axis_index_pair(T pos, T o1, T o2, T dx, T inv_dx, int& i1, T& f1, int& i2, T& f2) {
+    if constexpr (sizeof(T) == 4) {
+        const float h = 0.5f * dx;
+        const float2 t = __fmul2_rn(__fadd2_rn(__fadd2_rn(make_float2(pos, pos), make_float2(-o1, -o2)),
+                                               make_float2(-h, -h)),
+                                    make_float2(inv_dx, inv_dx));
+        const float big = 12582912.0f;  // 1.5 * 2^23, as floor_index
+        const float2 r = __fadd2_rd(t, make_float2(big, big));
+        const float2 fl = __fadd2_rn(r, make_float2(-big, -big));
+        const float2 f = __fadd2_rn(t, make_float2(-fl.x, -fl.y));
+        i1 = (int)((unsigned)__float_as_int(r.x) - 0x4B400000u);
+        i2 = (int)((unsigned)__float_as_int(r.y) - 0x4B400000u);
+        f1 = f.x;
+        f2 = f.y;
+    } else {
+        axis_index(pos, o1, dx, inv_dx, i1, f1);
+        axis_index(pos, o2, dx, inv_dx, i2, f2);
+    }
+}
+
 // the 8 points of a trilinear read at floor indices (i, j, k) are inside the grid (then clamping
 // changes none of them)
 template <typename T>
@@ -94,13 +117,26 @@ __device__ __forceinline__ Tri8<T> tri_load(const GridView<T>& g, int i, int j, 
     return Tri8<T>{{__ldg(p), __ldg(p + 1), __ldg(p + sy), __ldg(p + sy + 1), __ldg(p + sz), __ldg(p + sz + 1),
                     __ldg(p + sz + sy), __ldg(p + sz + sy + 1)}};
 }
+// the trilinear combination of 8 loaded points: x, then y, then z lerps; FP32 with the z = 0 and
+// z = 1 halves side by side in packed float2 arithmetic (each lane rounded as its scalar lerp)
 template <typename T>
 __device__ __forceinline__ T tri_mix(const Tri8<T>& v, T fx, T fy, T fz) {
-    TriIdx<T> t;
-    t.fx = fx;
-    t.fy = fy;
-    t.fz = fz;
-    return tri_combine(t, v.c[0], v.c[1], v.c[2], v.c[3], v.c[4], v.c[5], v.c[6], v.c[7]);
+    if constexpr (sizeof(T) == 4) {
+        auto lerp2 = [](float2 a, float2 b, float f) {
+            const float g = 1.f - f;
+            return __ffma2_rn(make_float2(f, f), b, __fmul2_rn(make_float2(g, g), a));
+        };
+        const float2 x0 = lerp2(make_float2(v.c[0], v.c[4]), make_float2(v.c[1], v.c[5]), fx);
+        const float2 x1 = lerp2(make_float2(v.c[2], v.c[6]), make_float2(v.c[3], v.c[7]), fx);
+        const float2 y = lerp2(x0, x1, fy);
+        return lerp1(y.x, y.y, fz);
+    } else {
+        TriIdx<T> t;
+        t.fx = fx;
+        t.fy = fy;
+        t.fz = fz;
+        return tri_combine(t, v.c[0], v.c[1], v.c[2], v.c[3], v.c[4], v.c[5], v.c[6], v.c[7]);
+    }
 }
 
 // u, v, w at one position from global memory: the three components share six axis coordinates
@@ -112,12 +148,9 @@ __device__ __forceinline__ void velocity_at(const Mac<T>& m, T x, T y, T z, T dx
                                             T& vz) {
     int ixf, ixc, jyf, jyc, kzf, kzc;
     T fxf, fxc, fyf, fyc, fzf, fzc;
-    axis_index(x, m.u.ox, dx, inv, ixf, fxf);
-    axis_index(x, m.v.ox, dx, inv, ixc, fxc);
-    axis_index(y, m.v.oy, dx, inv, jyf, fyf);
-    axis_index(y, m.u.oy, dx, inv, jyc, fyc);
-    axis_index(z, m.w.oz, dx, inv, kzf, fzf);
-    axis_index(z, m.u.oz, dx, inv, kzc, fzc);
+    axis_index_pair(x, m.u.ox, m.v.ox, dx, inv, ixf, fxf, ixc, fxc);
+    axis_index_pair(y, m.v.oy, m.u.oy, dx, inv, jyf, fyf, jyc, fyc);
+    axis_index_pair(z, m.w.oz, m.u.oz, dx, inv, kzf, fzf, kzc, fzc);
     if (tri_inside(m.u, ixf, jyc, kzc) && tri_inside(m.v, ixc, jyf, kzc) && tri_inside(m.w, ixc, jyc, kzf)) {
         const Tri8<T> a = tri_load(m.u, ixf, jyc, kzc), b = tri_load(m.v, ixc, jyf, kzc),
                       c = tri_load(m.w, ixc, jyc, kzf);
@@ -247,9 +280,33 @@ __device__ __forceinline__ AxisPos<T> axis_pos(T pos, T origin, int box0, T dx, 
 template <typename T>
 __device__ __forceinline__ T lerp_combine(T fx, T fy, T fz, T c000, T c100, T c010, T c110, T c001, T c101, T c011,
                                           T c111) {
-    const T lo = lerp1(lerp1(c000, c100, fx), lerp1(c010, c110, fx), fy);
-    const T hi = lerp1(lerp1(c001, c101, fx), lerp1(c011, c111, fx), fy);
-    return lerp1(lo, hi, fz);
+    if constexpr (sizeof(T) == 4) {
+        // FP32: the z = 0 and z = 1 halves side by side in packed float2 arithmetic (the same
+        // lerps, x then y, each lane rounded as its scalar operations), then the z lerp
+        auto lerp2 = [](float2 a, float2 b, float f) {
+            const float g = 1.f - f;
+            return __ffma2_rn(make_float2(f, f), b, __fmul2_rn(make_float2(g, g), a));
+        };
+        const float2 x0 = lerp2(make_float2(c000, c001), make_float2(c100, c101), fx);
+        const float2 x1 = lerp2(make_float2(c010, c011), make_float2(c110, c111), fx);
+        const float2 y = lerp2(x0, x1, fy);
+        return lerp1(y.x, y.y, fz);
+    } else {
+        const T lo = lerp1(lerp1(c000, c100, fx), lerp1(c010, c110, fx), fy);
+        const T hi = lerp1(lerp1(c001, c101, fx), lerp1(c011, c111, fx), fy);
+        return lerp1(lo, hi, fz);
+    }
+}
+
+// axis_pos of one coordinate against two origins (FP32: in packed float2 arithmetic, the same
+// operations as cell_coord and floor_index lane by lane)
+template <typename T>
+__device__ __forceinline__ void axis_pos_pair(T pos, T o1, T o2, int box0, T dx, T inv_dx, AxisPos<T>& p1,
+                                              AxisPos<T>& p2) {
+    int i1, i2;
+    axis_index_pair(pos, o1, o2, dx, inv_dx, i1, p1.f, i2, p2.f);
+    p1.a = (int)((unsigned)i1 - (unsigned)box0);
+    p2.a = (int)((unsigned)i2 - (unsigned)box0);
 }
 
 // trilinear sample from a staged box at box-relative (x, y, z); false when the 8 points are not
@@ -292,9 +349,10 @@ struct StagedMac {
 template <typename T, bool CHECK = true>
 __device__ __forceinline__ void velocity_at_staged(const Mac<T>& m, const StagedMac<T>& s, T x, T y, T z, T dx, T inv,
                                                    T& vx, T& vy, T& vz) {
-    const AxisPos<T> xf = axis_pos(x, m.u.ox, s.u.bx0, dx, inv), xc = axis_pos(x, m.v.ox, s.u.bx0, dx, inv);
-    const AxisPos<T> yf = axis_pos(y, m.v.oy, s.u.by0, dx, inv), yc = axis_pos(y, m.u.oy, s.u.by0, dx, inv);
-    const AxisPos<T> zf = axis_pos(z, m.w.oz, s.u.bz0, dx, inv), zc = axis_pos(z, m.u.oz, s.u.bz0, dx, inv);
+    AxisPos<T> xf, xc, yf, yc, zf, zc;
+    axis_pos_pair(x, m.u.ox, m.v.ox, s.u.bx0, dx, inv, xf, xc);
+    axis_pos_pair(y, m.v.oy, m.u.oy, s.u.by0, dx, inv, yf, yc);
+    axis_pos_pair(z, m.w.oz, m.u.oz, s.u.bz0, dx, inv, zf, zc);
     if (!staged_lerp<T, CHECK>(s.u.box, xf, yc, zc, vx) && CHECK) vx = sample_trilinear(m.u, x, y, z, dx, inv);
     if (!staged_lerp<T, CHECK>(s.v.box, xc, yf, zc, vy) && CHECK) vy = sample_trilinear(m.v, x, y, z, dx, inv);
     if (!staged_lerp<T, CHECK>(s.w.box, xc, yc, zf, vz) && CHECK) vz = sample_trilinear(m.w, x, y, z, dx, inv);
