@@ -326,17 +326,21 @@ __global__ void __launch_bounds__(kThreads, Layout<M>::min_blocks) march_kernel(
                 };
                 auto R = [&](int pl, int idx) -> Rc { return ld_rec(P[pl] + L::off_rec, idx, L::rec_bytes); };
                 float res[2];  // RESTRICT: the two rows' residuals
+                // the stencils of the thread's two rows first, then their arithmetic in packed
+                // float2 operations (lane r = row 2w + r; each lane rounded as the scalar
+                // operations of stencil7 and the sweeps, so the results are those of the scalar
+                // expressions)
+                S7 sts[2];
+                float bcs[2];
 #pragma unroll
                 for (int r = 0; r < 2; ++r) {
                     const int row = 2 * w + r;
-                    const int j = j0 + row;
-                    const bool live = i < a.n0 && j < a.n1;
                     const int hc = (row + 1) * kHX + lane + 4;               // in a staged value box
                     const int rc = (row + 1) * L::rec_w + lane + L::rec_x0;  // in the staged record box
                     // records of the stencil: the cell's own ({d, +x, +y, +z}), and the -x, -y,
                     // -z neighbours' (their +x/+y/+z couplings are the cell's -x/-y/-z ones)
                     const Rc r0 = R(1, rc);
-                    S7 st;
+                    S7& st = sts[r];
                     st.d = r0.d;
                     st.cxp = r0.x;
                     st.cyp = r0.y;
@@ -347,102 +351,116 @@ __global__ void __launch_bounds__(kThreads, Layout<M>::min_blocks) march_kernel(
                     // stencil points: centre, -x, +x, -y, +y (plane k), -z (k - 1), +z (k + 1)
                     const int vo[7] = {0, -1, 1, -kHX, kHX, 0, 0};
                     const int pq[7] = {1, 1, 1, 1, 1, 0, 2};
-                    const int c = i + a.n0 * (j + a.n1 * k);
+                    float v[7];
                     if (M == DIRSPMV) {
-                        // p' = z + beta p at every stencil point; Ap' and p'.Ap' at the cell
-                        float v[7];
+                        // p' = z + beta p at every stencil point
 #pragma unroll
                         for (int q = 0; q < 7; ++q) {
                             const float zq = H(pq[q], 0, hc + vo[q]);
                             v[q] = a.first ? zq : zq + beta * H(pq[q], 1, hc + vo[q]);
                         }
-                        st.v0 = v[0];
-                        st.vxm = v[1];
-                        st.vxp = v[2];
-                        st.vym = v[3];
-                        st.vyp = v[4];
-                        st.vzm = v[5];
-                        st.vzp = v[6];
-                        float pc = 0.f, apc = 0.f;
-                        if (st.d > 0.f) {
-                            pc = st.v0;
-                            apc = apply7(st);
+                        bcs[r] = 0.f;
+                    } else if constexpr (L::mv) {
+                        // ZERO2 / UPDZ read the stencil's first-sweep values x1 = w1 b / D from
+                        // the planes' masked values, with b = r' = r - alpha Ap (UPDZ) or b (ZERO2)
+                        const int e0 = (row + 1) * kMVW + lane + 1;
+                        const int mo[7] = {0, -1, 1, -kMVW, kMVW, 0, 0};
+#pragma unroll
+                        for (int q = 0; q < 7; ++q) v[q] = MV(pq[q], e0 + mo[q]);
+                        bcs[r] = M == UPDZ ? H(1, 0, hc) - alpha * H(1, 1, hc) : H(1, 0, hc);
+                    } else {
+                        // RESTRICT / PROLONG / LAST read the level's stored values as they are: a
+                        // neighbour outside the system holds a finite value (zero where the kernels
+                        // wrote it) and meets a zero coupling
+#pragma unroll
+                        for (int q = 0; q < 7; ++q) {
+                            float raw = H(pq[q], 0, hc + vo[q]);
+                            if (M == PROLONG) {
+                                // + the coarse parent's correction; each ring slot holds the
+                                // coarse plane of its fine plane
+                                const int fi = lane + (q == 1 ? -1 : (q == 2 ? 1 : 0));
+                                const int fj = row + (q == 3 ? -1 : (q == 4 ? 1 : 0));
+                                const int cx = (fi >> 1) + 4, cy = (fj >> 1) + 1;
+                                raw += reinterpret_cast<const float*>(P[pq[q]] + L::off_coarse)[cy * kCX + cx];
+                            }
+                            v[q] = raw;
                         }
+                        bcs[r] = Cn(0, row);
+                    }
+                    st.v0 = v[0];
+                    st.vxm = v[1];
+                    st.vxp = v[2];
+                    st.vym = v[3];
+                    st.vyp = v[4];
+                    st.vzm = v[5];
+                    st.vzp = v[6];
+                }
+                auto f2 = [](float x, float y) { return make_float2(x, y); };
+                // the 7-point product d v0 + cxm vxm + ... in stencil7's order
+                float2 a7 = __fmul2_rn(f2(sts[0].d, sts[1].d), f2(sts[0].v0, sts[1].v0));
+                a7 = __ffma2_rn(f2(sts[0].cxm, sts[1].cxm), f2(sts[0].vxm, sts[1].vxm), a7);
+                a7 = __ffma2_rn(f2(sts[0].cxp, sts[1].cxp), f2(sts[0].vxp, sts[1].vxp), a7);
+                a7 = __ffma2_rn(f2(sts[0].cym, sts[1].cym), f2(sts[0].vym, sts[1].vym), a7);
+                a7 = __ffma2_rn(f2(sts[0].cyp, sts[1].cyp), f2(sts[0].vyp, sts[1].vyp), a7);
+                a7 = __ffma2_rn(f2(sts[0].czm, sts[1].czm), f2(sts[0].vzm, sts[1].vzm), a7);
+                a7 = __ffma2_rn(f2(sts[0].czp, sts[1].czp), f2(sts[0].vzp, sts[1].vzp), a7);
+                // a sweep x = v0 + omega (b - A v) / D in the scalar sweeps' operations, per lane
+                auto sweep2 = [&](float omega) {
+                    const float2 dr = __fmul2_rn(f2(omega, omega), __fadd2_rn(f2(bcs[0], bcs[1]), f2(-a7.x, -a7.y)));
+                    return __fadd2_rn(f2(sts[0].v0, sts[1].v0), f2(mg_divf(dr.x, sts[0].d), mg_divf(dr.y, sts[1].d)));
+                };
+                float2 sw = f2(0.f, 0.f);
+                if (M == UPDZ || M == ZERO2) sw = sweep2(w2);
+                if (M == PROLONG) sw = sweep2(w1);
+                if (M == LAST) sw = sweep2(w2);
+#pragma unroll
+                for (int r = 0; r < 2; ++r) {
+                    const int row = 2 * w + r;
+                    const int j = j0 + row;
+                    const bool live = i < a.n0 && j < a.n1;
+                    const int hc = (row + 1) * kHX + lane + 4;
+                    const int c = i + a.n0 * (j + a.n1 * k);
+                    const S7& st = sts[r];
+                    const bool dp0 = st.d > 0.f;
+                    const float a7r = r == 0 ? a7.x : a7.y;
+                    const float swr = r == 0 ? sw.x : sw.y;
+                    const float bc = bcs[r];
+                    if (M == DIRSPMV) {
+                        // Ap' and p'.Ap' at the cell
+                        const float pc = dp0 ? st.v0 : 0.f, apc = dp0 ? a7r : 0.f;
                         if (live && EL_IN(c, (long long)a.n0 * a.n1 * a.n2, 10)) {
                             a.out0[c] = pc;
                             a.out1[c] = apc;
                             part += pc * apc;
                         }
-                    } else {
-                        // ZERO2 / UPDZ read the stencil's first-sweep values x1 = w1 b / D from
-                        // the planes' masked values, with b = r' = r - alpha Ap (UPDZ) or b (ZERO2);
-                        // RESTRICT / PROLONG / LAST read the level's stored values as they are: a
-                        // neighbour outside the system holds a finite value (zero where the kernels
-                        // wrote it) and meets a zero coupling
-                        float v[7];
-                        if constexpr (L::mv) {
-                            const int e0 = (row + 1) * kMVW + lane + 1;
-                            const int mo[7] = {0, -1, 1, -kMVW, kMVW, 0, 0};
-#pragma unroll
-                            for (int q = 0; q < 7; ++q) v[q] = MV(pq[q], e0 + mo[q]);
-                        } else {
-#pragma unroll
-                            for (int q = 0; q < 7; ++q) {
-                                float raw = H(pq[q], 0, hc + vo[q]);
-                                if (M == PROLONG) {
-                                    // + the coarse parent's correction; each ring slot holds the
-                                    // coarse plane of its fine plane
-                                    const int fi = lane + (q == 1 ? -1 : (q == 2 ? 1 : 0));
-                                    const int fj = row + (q == 3 ? -1 : (q == 4 ? 1 : 0));
-                                    const int cx = (fi >> 1) + 4, cy = (fj >> 1) + 1;
-                                    raw += reinterpret_cast<const float*>(P[pq[q]] + L::off_coarse)[cy * kCX + cx];
-                                }
-                                v[q] = raw;
+                    } else if (M == UPDZ || M == ZERO2) {
+                        const float x2 = dp0 ? swr : 0.f;
+                        if (live && EL_IN(c, (long long)a.n0 * a.n1 * a.n2, 11)) {
+                            if (M == UPDZ) {
+                                // x += alpha p; r' out of place.  A tile also covers cells
+                                // outside the system (diagonal 0), whose r may still hold an
+                                // earlier solve's values: their r' is 0 and they stay out of
+                                // |r'|^2, as in the segment kernels (where r is 0 on every
+                                // such cell of an active segment).
+                                const float rn = dp0 ? bc : 0.f;
+                                a.out0[c] = Cn(0, row) + alpha * Cn(1, row);
+                                a.out1[c] = rn;
+                                part += rn * rn;
+                                a.out2[c] = x2;
+                            } else {
+                                a.out0[c] = x2;
                             }
                         }
-                        st.v0 = v[0];
-                        st.vxm = v[1];
-                        st.vxp = v[2];
-                        st.vym = v[3];
-                        st.vyp = v[4];
-                        st.vzm = v[5];
-                        st.vzp = v[6];
-                        const bool dp0 = r0.d > 0.f;
-                        if (M == UPDZ || M == ZERO2) {
-                            const float bc = M == UPDZ ? H(1, 0, hc) - alpha * H(1, 1, hc) : H(1, 0, hc);
-                            float x2 = 0.f;
-                            if (dp0) x2 = rn_add(st.v0, mg_divf(rn_mul(w2, rn_sub(bc, apply7(st))), st.d));
-                            if (live && EL_IN(c, (long long)a.n0 * a.n1 * a.n2, 11)) {
-                                if (M == UPDZ) {
-                                    // x += alpha p; r' out of place.  A tile also covers cells
-                                    // outside the system (diagonal 0), whose r may still hold an
-                                    // earlier solve's values: their r' is 0 and they stay out of
-                                    // |r'|^2, as in the segment kernels (where r is 0 on every
-                                    // such cell of an active segment).
-                                    const float rn = dp0 ? bc : 0.f;
-                                    a.out0[c] = Cn(0, row) + alpha * Cn(1, row);
-                                    a.out1[c] = rn;
-                                    part += rn * rn;
-                                    a.out2[c] = x2;
-                                } else {
-                                    a.out0[c] = x2;
-                                }
-                            }
-                        } else {
-                            const float bc = Cn(0, row);
-                            if (M == RESTRICT) {
-                                res[r] = dp0 ? rn_sub(bc, apply7(st)) : 0.f;
-                            } else {
-                                const float omega = M == PROLONG ? w1 : w2;
-                                float xo = 0.f;
-                                if (dp0) xo = rn_add(st.v0, mg_divf(rn_mul(omega, rn_sub(bc, apply7(st))), st.d));
-                                if (live && EL_IN(c, (long long)a.n0 * a.n1 * a.n2, 12)) {
-                                    a.out0[c] = xo;
-                                    if (M == LAST) part += bc * xo;
-                                }
-                            }
+                    } else if (M == RESTRICT) {
+                        res[r] = dp0 ? rn_sub(bc, a7r) : 0.f;
+                    } else {
+                        const float xo = dp0 ? swr : 0.f;
+                        if (live && EL_IN(c, (long long)a.n0 * a.n1 * a.n2, 12)) {
+                            a.out0[c] = xo;
+                            if (M == LAST) part += bc * xo;
                         }
                     }
+                    (void)hc;
                 }
                 if (M == RESTRICT) {
                     // the residuals summed over 2x2x2 blocks onto the coarse rhs in the segment
