@@ -43,8 +43,9 @@ EL_F2D_HD float df_fma(float a, float b, float c) { return std::fmaf(a, b, c); }
 // d = h + l: h holds the top 24 significant bits of d and l the next 23, both truncated, so
 // |d - (h + l)| < 2^-46 |d|; h and l carry d's sign.  Integer arithmetic and one float
 // subtraction.  Below 2^-103 (where l would leave the normal float range) the pair is the
-// float nearest d and zero: an absolute error below 2^-126 (2^-24 relative at most), far under
-// any residual the solver acts on unless the whole system is scaled below 1e-30.  Zero gives
+// float nearest d and zero: an absolute error below 2^-126 (2^-24 relative at most); the
+// residual kernel shifts its system by a power of two that brings |b| near 1, so only values
+// some 2^100 below the system's scale come this close.  Zero gives
 // (0, 0).  ok is cleared for |d| at or above 2^128 (infinities and NaN among them), which the
 // float pair cannot hold: the caller then takes FP64 arithmetic.
 EL_F2D_HD F2 df_split(double d, bool& ok) {
@@ -71,6 +72,30 @@ EL_F2D_HD F2 df_split(double d, bool& ok) {
         r.h = d2f(d);
         r.l = 0.f;
     }
+    return r;
+}
+
+// d 2^k for a power-of-two shift k by integer arithmetic on the exponent field: exact while the
+// result is a normal double; zero stays zero; a result below the normal range flushes to zero
+// (the shifts here bring values near 1, so only values 2^-1000 or so below the largest reach
+// that), one above it, or an infinite or NaN input, is NaN.
+EL_F2D_HD double d_shift(double d, int k) {
+    uint64_t bits;
+    std::memcpy(&bits, &d, sizeof(bits));
+    const int e = (int)((bits >> 52) & 0x7ffu);
+    const int ne = e + k;
+    uint64_t out;
+    if (e == 0) {
+        out = bits & 0x8000000000000000ull;  // zero (or subnormal: flushed), sign kept
+    } else if (e == 0x7ff || ne >= 0x7ff) {
+        out = 0x7ff8000000000000ull;
+    } else if (ne <= 0) {
+        out = bits & 0x8000000000000000ull;
+    } else {
+        out = (bits & ~(0x7ffull << 52)) | ((uint64_t)ne << 52);
+    }
+    double r;
+    std::memcpy(&r, &out, sizeof(r));
     return r;
 }
 

@@ -54,6 +54,8 @@ struct Scalars {
     int inner_total; // mixed solver: inner iterations summed over the sweeps
     int inner_passes;// device-driven mixed solver: passes of its PCG loop
     int fault;       // a bounded device wait gave up (the solve reports EL_ERR_TIMEOUT)
+    int df_shift;    // mixed solver: the power of two 2^df_shift that brings |b| near 1 in the
+                     // double-float residual (scale invariance for its float pairs)
 };
 
 // Per-scene running totals of a batch (el_batch_stats on the device).

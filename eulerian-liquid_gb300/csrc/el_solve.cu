@@ -595,13 +595,16 @@ __global__ void jacobi_rz_kernel(LGeom g, SegArg seg, const double* __restrict__
 }
 
 // The iterate as a float pair for the double-float residual (el_df.cuh), written with x by the
-// kernels that change it (xs: null where no double-float residual reads it).  Beyond the pairs'
+// kernels that change it (xs: null where no double-float residual reads it), shifted by the
+// solve's power of two 2^df_shift (set from |b| by solve_init_kernel), which keeps the pairs
+// of the whole system near 1 whatever its scale.  Beyond the pairs'
 // range (|x| >= 2^128, an iterate no FP32 field can hold) the pair is infinite, so that the
 // residual turns non-finite and the solve reports it.
-__device__ __forceinline__ float2 x_pair(double x) {
+__device__ __forceinline__ float2 x_pair(double x, int shift) {
+    const double xs = d_shift(x, shift);
     bool ok = true;
-    const F2 p = df_split(x, ok);
-    return ok ? make_float2(p.h, p.l) : make_float2(d2f(x), 0.f);
+    const F2 p = df_split(xs, ok);
+    return ok ? make_float2(p.h, p.l) : make_float2(d2f(xs), 0.f);
 }
 
 // solve start (outer / plain): x = 0, r = b on the active segments, thresholds.
@@ -614,6 +617,10 @@ __global__ void solve_init_kernel(LGeom g, SegArg seg, const double* __restrict_
     SEG_LOOP_END
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         const double bb = s->bb;
+        // 2^df_shift |b| in [1, 2): the exponent of |b|^2 halved (0 for a zero or non-finite b)
+        const unsigned long long bbits = (unsigned long long)__double_as_longlong(bb);
+        const int eb = (int)((bbits >> 52) & 0x7ffu);
+        s->df_shift = (eb == 0 || eb == 0x7ff) ? 0 : -((eb - 1023) >> 1);
         s->thresh = tol * tol * bb;
         s->rr = bb;
         s->iter = 0;
@@ -664,7 +671,7 @@ __global__ void guess_scale_kernel(LGeom g, SegArg seg, double* __restrict__ x, 
     // a == 0 (a useless or non-finite guess): exactly the zero start, whatever g held
     const double xc = a != 0.0 ? a * x[c] : 0.0;
     x[c] = xc;
-    if (xs) xs[c] = x_pair(xc);
+    if (xs) xs[c] = x_pair(xc, s->df_shift);
     const double rc = a != 0.0 ? (1.0 - a) * b[c] + a * r[c] : b[c];
     r[c] = rc;
     acc[0] += rc * rc;
@@ -702,9 +709,10 @@ __device__ __noinline__ double residual_cell_fp64(double bc, double d, double x0
 // mixed solver: inner system r32 = r64 2^-k with 2^k the power of two at or below |r64| (the
 // scaling is exact both ways, and |r32| lies in [1, 2)), x32 = 0, inner thresholds.  The scale
 // comes from the exponent bits of |r|^2: square roots and divisions in FP64 by every thread cost
-// more FP64 issue than the cells' own work.  A cell's value is split into a float pair (integer
-// arithmetic) and scaled on the FP32 pipe.  |r|^2 outside [2^-200, 2^200] (or not finite) takes
-// the scale 1 / |r| in FP64.  The inner relative tolerance is what the outer one still needs,
+// more FP64 issue than the cells' own work.  A cell's value is shifted by the exponent field and
+// rounded to float by integer arithmetic (d_shift, d2f): the inner system of a system scaled by
+// a power of two is the same floats.  A zero, subnormal or non-finite |r|^2 takes the scale
+// 1 / |r| in FP64.  The inner relative tolerance is what the outer one still needs,
 // halved, kept within [floor, 1/2] (FP32 cannot go much below 1e-4 reliably):
 // tau = clamp(0.5 tol |b| / |r|, floor, 0.5).
 __global__ void inner_init_kernel(LGeom g, SegArg seg, const double* __restrict__ r64, float* __restrict__ r32,
@@ -712,19 +720,18 @@ __global__ void inner_init_kernel(LGeom g, SegArg seg, const double* __restrict_
                                   double tau_floor, double* partials, unsigned* counter) {
     const double rr = so->rr;
     const unsigned long long rb = (unsigned long long)__double_as_longlong(rr);
-    const int k = ((int)((rb >> 52) & 0x7ffu) - 1023) >> 1;
-    const bool pow2 = rb != 0ull && (rb >> 63) == 0ull && k >= -100 && k <= 100;
+    const int erb = (int)((rb >> 52) & 0x7ffu);
+    const int k = (erb - 1023) >> 1;
+    // every positive normal |r|^2 gives a shift within the doubles' range (|k| <= 511)
+    const bool pow2 = rb != 0ull && (rb >> 63) == 0ull && erb != 0 && erb != 0x7ff;
     double norm, inv;
-    float invf;
     if (pow2) {
         norm = __longlong_as_double((long long)(1023 + k) << 52);
-        inv = __longlong_as_double((long long)(1023 - k) << 52);
-        invf = __int_as_float((127 - k) << 23);
+        inv = 0.0;
     } else {
         const double2 ni = scale_from_norm(rr);
         norm = ni.x;
         inv = ni.y;
-        invf = 0.f;
     }
     float part = 0.f;
     // four segments a warp per pass, their loads in flight together (one load a cell)
@@ -748,9 +755,8 @@ __global__ void inner_init_kernel(LGeom g, SegArg seg, const double* __restrict_
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             if (!lv[u]) continue;
-            bool ok = pow2;
-            const F2 q = df_split(rc[u], ok);
-            const float v = ok ? df_fma(q.h, invf, df_mul(q.l, invf)) : scale_fp64(rc[u], inv);
+            // r 2^-k by the exponent field, then rounded to float: exact scaling, integer pipe
+            const float v = pow2 ? d2f(d_shift(rc[u], -k)) : scale_fp64(rc[u], inv);
             r32[cc[u]] = v;
             x32[cc[u]] = 0.0f;
             part += v * v;
@@ -775,12 +781,13 @@ __global__ void inner_init_kernel(LGeom g, SegArg seg, const double* __restrict_
 
 // mixed solver: x64 += |r| * x32 (and its float pair)
 __global__ void accumulate_kernel(LGeom g, SegArg seg, double* __restrict__ x64, float2* __restrict__ xs,
-                                  const float* __restrict__ x32, const Scalars* si) {
+                                  const float* __restrict__ x32, const Scalars* si, const Scalars* so) {
     const double norm = si->norm;
+    const int shift = so->df_shift;
     SEG_LOOP_BEGIN(seg, g)
     const double xn = __fma_rn(norm, f2d(x32[c]), x64[c]);
     x64[c] = xn;
-    if (xs) xs[c] = x_pair(xn);
+    if (xs) xs[c] = x_pair(xn, shift);
     SEG_LOOP_END
 }
 
@@ -821,7 +828,9 @@ __global__ void __launch_bounds__(kSegThreads) residual_kernel(LGeom g, SegArg s
 // are exact floats: double-float arithmetic on the FP32 pipe (el_df.cuh) in place of the FP64
 // operations, which bound the FP64 kernel above (nine a cell, its FP64 pipe 86 % busy).  The
 // iterate comes as float pairs (xs, written with x); b and the diagonal are split into pairs by
-// integer arithmetic; the pair of r is
+// integer arithmetic, b and the iterate shifted by the solve's power of two 2^df_shift (|b| near
+// 1: the pairs' exponent range then holds the system at any scale, and the shift is undone
+// exactly on r and |r|^2); the pair of r is
 // within 2^-41 of the sum of its row's term magnitudes, and is stored as a double.  A warp in
 // which any operand lies outside the pairs' exponent range (el_df.cuh) takes the FP64
 // arithmetic of the kernel above for all its lanes (the splits of b and the diagonal decide).  |r|^2 is summed in FP32 per thread (each
@@ -833,6 +842,8 @@ __global__ void __launch_bounds__(kSegThreads, 4) residual_df_kernel(LGeom g, Se
                                                                   double* __restrict__ r, Scalars* s,
                                                                   double* partials, unsigned* counter) {
     SqAcc acc2;
+    // the pairs hold b and x times 2^k (x_pair); the residual pair is r 2^k, shifted back
+    const int sk = s->df_shift;
     SEG_LOOP_ALL_BEGIN(seg, g)
     const bool iym = live && j > 0, iyp = live && j < g.n1 - 1;
     const bool izm = live && k > 0, izp = live && k < g.n2 - 1;
@@ -856,7 +867,7 @@ __global__ void __launch_bounds__(kSegThreads, 4) residual_df_kernel(LGeom g, Se
     const F2 p0{q0.x, q0.y}, pym{qym.x, qym.y}, pyp{qyp.x, qyp.y}, pzm{qzm.x, qzm.y}, pzp{qzp.x, qzp.y};
     const F2 pxm_e{qxm_e.x, qxm_e.y}, pxp_e{qxp_e.x, qxp_e.y};
     bool ok = true;
-    const F2 pd = df_split(d, ok), pb = df_split(bc, ok);
+    const F2 pd = df_split(d, ok), pb = df_split(d_shift(bc, sk), ok);
     F2 pxm, pxp;
     pxm.h = __shfl_up_sync(kFull, p0.h, 1);
     pxm.l = __shfl_up_sync(kFull, p0.l, 1);
@@ -868,7 +879,7 @@ __global__ void __launch_bounds__(kSegThreads, 4) residual_df_kernel(LGeom g, Se
     if (__all_sync(kFull, ok)) {
         if (act) {
             const F2 q = df_residual7(pb, pd, p0, cxm, pxm, cxp, pxp, cym, pym, cyp, pyp, czm, pzm, czp, pzp);
-            r[c] = __dadd_rn(f2d(q.h), f2d(q.l));
+            r[c] = d_shift(__dadd_rn(f2d(q.h), f2d(q.l)), -sk);
             acc2.add(q.h);
         } else if (live) {
             r[c] = 0.0;
@@ -887,13 +898,13 @@ __global__ void __launch_bounds__(kSegThreads, 4) residual_df_kernel(LGeom g, Se
                                                        czp, xzp)
                                   : 0.0;
             r[c] = rc;
-            acc2.add(d2f(rc));
+            acc2.add(d2f(d_shift(rc, sk)));
         }
     }
     SEG_LOOP_END
     double acc[1] = {acc2.value()};
     double tot[1];
-    if (grid_sum<1>(acc, partials, counter, tot)) residual_done(s, tot[0]);
+    if (grid_sum<1>(acc, partials, counter, tot)) residual_done(s, d_shift(tot[0], -2 * sk));
 }
 
 
@@ -2137,7 +2148,7 @@ static int solve_t(el_ctx* ctx, const el_solve_params& prm, el_solve_stats* st) 
             {
                 ProfScope prof(ctx, EL_KC_OTHER, na * 20);
                 accumulate_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
-                    g, seg_arg(ctx->seg0), ctx->x64, iterate_pairs<T>(ctx, prm.solver), ctx->x32, s1);
+                    g, seg_arg(ctx->seg0), ctx->x64, iterate_pairs<T>(ctx, prm.solver), ctx->x32, s1, s0);
             }
             {
                 // reads x, b, diag (f64), 3 couplings; writes r (f64)
@@ -2301,7 +2312,7 @@ static int enqueue_solve_device_t(el_ctx* ctx, const el_solve_params& prm, int k
     inner_cond_kernel<<<1, 1, 0, ctx->stream>>>(h_inner, s0, s1, prm.max_iter, 1);
     rc = end_while(ctx, parent_inner);
     accumulate_kernel<<<seg_blocks(ctx, ctx->seg0.total), kSegThreads, 0, ctx->stream>>>(
-        g, seg_arg(ctx->seg0), ctx->x64, iterate_pairs<T>(ctx, EL_SOLVER_MIXED), ctx->x32, s1);
+        g, seg_arg(ctx->seg0), ctx->x64, iterate_pairs<T>(ctx, EL_SOLVER_MIXED), ctx->x32, s1, s0);
     enqueue_refine_residual(ctx, g, A64, s0);
     outer_cond_kernel<<<1, 1, 0, ctx->stream>>>(h_outer, s0, s1, max_outer, prm.max_iter, 1);
     const int rc2 = end_while(ctx, parent_outer);

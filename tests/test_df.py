@@ -52,6 +52,10 @@ int main() {
             std::memcpy(&a, &out, 8);
             std::memcpy(&b, &seq, 8);
             std::printf("%d %d\n", ok ? 1 : 0, (ok && a != b) ? 1 : 0);
+        } else if (!std::strcmp(mode, "shift")) {
+            const double d = rd();
+            const int k = (int)rd();
+            std::printf("%a\n", d_shift(d, k));
         } else if (!std::strcmp(mode, "pos")) {
             const double d = rd();
             std::printf("%d\n", d_positive(d) ? 1 : 0);
@@ -227,3 +231,33 @@ def test_exact_sum6(run):
                 assert ok == 1, t
         answered += ok
     assert answered > len(cases) // 2
+
+
+def test_shift(run):
+    """d 2^k by the exponent field: exact for normal results, zero below the normal range
+    (subnormal inputs flushed), NaN beyond it or for infinite and NaN inputs."""
+    rng = random.Random(9)
+    cases = [(0.0, 5), (-0.0, -5), (1.0, 0), (1.5, 10), (-3.25, -1000), (1.0, 1023), (1.0, 1024),
+             (1.0, -1022), (1.0, -1023), (5e-324, 3), (float("inf"), 1), (float("nan"), 0)]
+    for _ in range(3000):
+        cases.append((rng.choice((-1, 1)) * math.ldexp(rng.random() + 0.5, rng.randint(-1000, 1000)),
+                      rng.randint(-300, 300)))
+    out = run(["shift " + d.hex() + " " + float(k).hex() for d, k in cases])
+    for (d, k), line in zip(cases, out):
+        got = float.fromhex(line)
+        if d == 0.0 or (math.isfinite(d) and abs(d) < 2.0 ** -1022):
+            assert got == 0.0 and math.copysign(1.0, got) == math.copysign(1.0, d), (d, k, got)
+            continue
+        if not math.isfinite(d):
+            assert math.isnan(got)
+            continue
+        try:
+            want = math.ldexp(d, k)
+        except OverflowError:
+            want = math.inf
+        if math.isinf(want):
+            assert math.isnan(got), (d, k, got)
+        elif abs(want) < 2.0 ** -1022:
+            assert got == 0.0, (d, k, got)
+        else:
+            assert got == want, (d, k, got)

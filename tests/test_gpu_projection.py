@@ -110,6 +110,33 @@ def test_build_matrix_wide_weight_range_bitexact(el, orc, dtype):
     sim.close()
 
 
+@pytest.mark.parametrize("m", [-100, 93])
+def test_mixed_solve_is_scale_equivariant(el, orc, m):
+    """FP32 fields with velocities scaled by 2^m (m = -100: |u| below 1e-30, pressures down to
+    1e-32; m = 93: near 1e28; both keep every scaled velocity a normal float, so the scaled
+    system is exactly the unscaled one times 2^m):
+    the mixed solve still reaches the tolerance, and its pressure is the unscaled solve's times
+    2^m -- the double-float residual holds b and x shifted by a power of two near |b| = 1, so
+    neither a tiny nor a huge system leaves its pairs' exponent range, and every rounding of the
+    solve scales with the system."""
+    n = 24
+    spec = _spec(n)
+    _, _, wts = scene_fields(orc, spec, np.float32)
+    u, v, w = _velocity(orc, wts, np.float32, 7)
+    out = []
+    for e in (0, m):
+        sim = make_sim(el, n, np.float32, spec)
+        for f, a in (("u", u), ("v", v), ("w", w)):
+            sim.upload(f, np.ldexp(a, e).astype(np.float32))
+        st = sim.solve_pressure(0.01, solver=el.SOLVER_MIXED, tol=1e-6)
+        assert st["status"] == 0 and st["relres"] < 1e-6, (e, st)
+        out.append((st, sim.download("pressure").astype(np.float64)))
+        sim.close()
+    (st0, p0), (st1, p1) = out
+    assert st1["iterations"] == st0["iterations"], (st0, st1)
+    np.testing.assert_allclose(p1, np.ldexp(p0, m), rtol=1e-6, atol=0)
+
+
 @pytest.mark.parametrize("dtype", DTYPES)
 def test_rebuild_after_the_fluid_moves_bitexact(el, orc, dtype):
     """Consecutive builds where the fluid region shrinks, moves and grows again: the build only
